@@ -1,0 +1,112 @@
+"""Build and load the native solver library ``csrc/libgbfdtd.so`` (sm_103a CUDA + C ABI).
+
+The library is compiled in-tree with nvcc. There is no fallback: if the library cannot be
+built or loaded, :func:`lib` raises, so a model never runs anywhere but the GPU kernels.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, 'csrc')
+LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
+SOURCES = ['gbfdtd.cu', 'fdtd_kernels.cuh']
+HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-shared']
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _nvcc():
+    for cand in (os.environ.get('NVCC'), '/usr/local/cuda/bin/nvcc', 'nvcc'):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return 'nvcc'
+
+
+def _stale():
+    if not os.path.exists(LIBPATH):
+        return True
+    t = os.path.getmtime(LIBPATH)
+    deps = [os.path.join(CSRC, s) for s in SOURCES] + [HEADER]
+    return any(os.path.getmtime(p) > t for p in deps if os.path.exists(p))
+
+
+def build(force=False, verbose=False):
+    """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources."""
+    if not force and not _stale():
+        return LIBPATH
+    cmd = [_nvcc()] + ARCH + NVCC_FLAGS + [os.path.join(CSRC, 'gbfdtd.cu'), '-o', LIBPATH + '.tmp']
+    if verbose:
+        print(' '.join(cmd))
+    subprocess.run(cmd, check=True, cwd=CSRC)
+    os.replace(LIBPATH + '.tmp', LIBPATH)
+    return LIBPATH
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [('nx', ctypes.c_int32), ('ny', ctypes.c_int32), ('nz', ctypes.c_int32),
+                ('iterations', ctypes.c_int32), ('nmat', ctypes.c_int32),
+                ('maxpoles', ctypes.c_int32), ('pml_formulation', ctypes.c_int32),
+                ('pml_order', ctypes.c_int32), ('pml_thickness', ctypes.c_int32 * 6),
+                ('dx', ctypes.c_float), ('dy', ctypes.c_float), ('dz', ctypes.c_float),
+                ('nsrc', ctypes.c_int32), ('nrx', ctypes.c_int32), ('nsnap', ctypes.c_int32),
+                ('reserved', ctypes.c_int32 * 4)]
+
+
+GBF_RUN_GRAPH = 1
+GBF_RUN_CHECK = 2
+
+_P = ctypes.c_void_p
+_SIGS = {
+    'gbf_create': (ctypes.c_int, [ctypes.POINTER(GridDesc), ctypes.POINTER(_P)]),
+    'gbf_destroy': (None, [_P]),
+    'gbf_upload_materials': (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    'gbf_upload_pml': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
+    'gbf_upload_sources': (ctypes.c_int, [_P, _P, _P, _P]),
+    'gbf_set_receivers': (ctypes.c_int, [_P, _P]),
+    'gbf_set_snapshots': (ctypes.c_int, [_P, _P]),
+    'gbf_reset': (ctypes.c_int, [_P]),
+    'gbf_run': (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32]),
+    'gbf_current_iteration': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
+    'gbf_synchronize': (ctypes.c_int, [_P]),
+    'gbf_download_rx': (ctypes.c_int, [_P, _P]),
+    'gbf_download_fields': (ctypes.c_int, [_P, _P]),
+    'gbf_upload_fields': (ctypes.c_int, [_P, _P]),
+    'gbf_download_dispersive': (ctypes.c_int, [_P, _P]),
+    'gbf_download_snapshot': (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    'gbf_profile': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                   ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    'gbf_device_bytes': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    'gbf_version': (ctypes.c_char_p, []),
+}
+
+
+def exported_symbols():
+    """Names the C ABI exports (the functions declared in include/gbfdtd.h)."""
+    return sorted(_SIGS)
+
+
+def load(path=LIBPATH):
+    """Load the library without building (raises OSError if it is absent)."""
+    lib_ = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib_, name)
+        f.restype = res
+        f.argtypes = args
+    return lib_
+
+
+def lib():
+    """The loaded native library, built on first use when nvcc is available."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if _stale():
+                build()
+            _lib = load()
+    return _lib

@@ -1,0 +1,655 @@
+"""Processing of input commands into an :class:`FDTDGrid`.
+
+Single-use commands follow ``gprMax/input_cmds_singleuse.py:41-336``, multi-use commands
+``input_cmds_multiuse.py:45-851`` and geometry commands ``input_cmds_geometry.py:51-1527`` for
+the commands this solver core supports. Parameter checks raise :class:`CmdInputError` with the
+reference's messages. Transmission lines and the fractal/surface/grass commands are rejected
+with an explicit error.
+"""
+import decimal as d
+import inspect
+import os
+
+import numpy as np
+from scipy import interpolate
+
+from .constants import c, floattype
+from .exceptions import CmdInputError
+from .materials import Material
+from .pml import CFS, CFSParameter, PML
+from .receivers import Rx, allocate_outputs
+from .snapshots import Snapshot
+from .sources import HertzianDipole, MagneticDipole, VoltageSource
+from .utilities import round_value
+from .waveforms import Waveform
+from . import geometry as geo
+
+
+def _log(G, msg):
+    if G.messages:
+        print(msg)
+
+
+def process_singlecmds(singlecmds, G):
+    """Domain, discretisation, dt, iterations and PML settings (``input_cmds_singleuse.py:41-336``)."""
+    cmd = '#messages'
+    if singlecmds[cmd] is not None:
+        tmp = singlecmds[cmd].split()
+        if len(tmp) != 1:
+            raise CmdInputError(cmd + ' requires exactly one parameter')
+        if singlecmds[cmd].lower() == 'y':
+            G.messages = True
+        elif singlecmds[cmd].lower() == 'n':
+            G.messages = False
+        else:
+            raise CmdInputError(cmd + ' requires input values of either y or n')
+
+    cmd = '#title'
+    if singlecmds[cmd] is not None:
+        G.title = singlecmds[cmd]
+        _log(G, 'Model title: {}'.format(G.title))
+
+    cmd = '#num_threads'
+    if singlecmds[cmd] is not None:
+        tmp = tuple(int(x) for x in singlecmds[cmd].split())
+        if len(tmp) != 1:
+            raise CmdInputError(cmd + ' requires exactly one parameter to specify the number of threads to use')
+        if tmp[0] < 1:
+            raise CmdInputError(cmd + ' requires the value to be an integer not less than one')
+        G.nthreads = tmp[0]
+
+    cmd = '#dx_dy_dz'
+    tmp = [float(x) for x in singlecmds[cmd].split()]
+    if len(tmp) != 3:
+        raise CmdInputError(cmd + ' requires exactly three parameters')
+    for v, ax in zip(tmp, 'xyz'):
+        if v <= 0:
+            raise CmdInputError(cmd + ' requires the {}-direction spatial step to be greater than zero'.format(ax))
+    G.dx, G.dy, G.dz = tmp
+
+    cmd = '#domain'
+    tmp = [float(x) for x in singlecmds[cmd].split()]
+    if len(tmp) != 3:
+        raise CmdInputError(cmd + ' requires exactly three parameters')
+    G.nx = round_value(tmp[0] / G.dx)
+    G.ny = round_value(tmp[1] / G.dy)
+    G.nz = round_value(tmp[2] / G.dz)
+    if G.nx == 0 or G.ny == 0 or G.nz == 0:
+        raise CmdInputError(cmd + ' requires at least one cell in every dimension')
+
+    # CFL time step (3D, or 2D with the invariant direction's PML switched off)
+    if G.nx == 1:
+        G.dt = 1 / (c * np.sqrt((1 / G.dy) * (1 / G.dy) + (1 / G.dz) * (1 / G.dz)))
+        G.mode = '2D TMx'
+        G.pmlthickness['x0'] = 0
+        G.pmlthickness['xmax'] = 0
+    elif G.ny == 1:
+        G.dt = 1 / (c * np.sqrt((1 / G.dx) * (1 / G.dx) + (1 / G.dz) * (1 / G.dz)))
+        G.mode = '2D TMy'
+        G.pmlthickness['y0'] = 0
+        G.pmlthickness['ymax'] = 0
+    elif G.nz == 1:
+        G.dt = 1 / (c * np.sqrt((1 / G.dx) * (1 / G.dx) + (1 / G.dy) * (1 / G.dy)))
+        G.mode = '2D TMz'
+        G.pmlthickness['z0'] = 0
+        G.pmlthickness['zmax'] = 0
+    else:
+        G.dt = 1 / (c * np.sqrt((1 / G.dx) * (1 / G.dx) + (1 / G.dy) * (1 / G.dy)
+                                + (1 / G.dz) * (1 / G.dz)))
+        G.mode = '3D'
+    # round down with one digit less than the decimal context precision
+    G.dt = round_value(G.dt, decimalplaces=d.getcontext().prec - 1)
+
+    cmd = '#time_step_stability_factor'
+    if singlecmds[cmd] is not None:
+        tmp = tuple(float(x) for x in singlecmds[cmd].split())
+        if len(tmp) != 1:
+            raise CmdInputError(cmd + ' requires exactly one parameter')
+        if tmp[0] <= 0 or tmp[0] > 1:
+            raise CmdInputError(cmd + ' requires the value of the time step stability factor to be between zero and one')
+        G.dt = G.dt * tmp[0]
+
+    cmd = '#time_window'
+    tmp = singlecmds[cmd].split()
+    if len(tmp) != 1:
+        raise CmdInputError(cmd + ' requires exactly one parameter to specify the time window. Either in seconds or number of iterations.')
+    tmp = tmp[0].lower()
+    try:
+        tmp = int(tmp)
+        G.timewindow = (tmp - 1) * G.dt
+        G.iterations = tmp
+    except ValueError:
+        tmp = float(tmp)
+        if tmp > 0:
+            G.timewindow = tmp
+            G.iterations = int(np.ceil(tmp / G.dt)) + 1
+        else:
+            raise CmdInputError(cmd + ' must have a value greater than zero')
+    _log(G, 'Time window: {:g} secs ({} iterations)'.format(G.timewindow, G.iterations))
+
+    cmd = '#pml_cells'
+    if singlecmds[cmd] is not None:
+        tmp = singlecmds[cmd].split()
+        if len(tmp) != 1 and len(tmp) != 6:
+            raise CmdInputError(cmd + ' requires either one or six parameter(s)')
+        if len(tmp) == 1:
+            for key in G.pmlthickness.keys():
+                G.pmlthickness[key] = int(tmp[0])
+        else:
+            for key, v in zip(('x0', 'y0', 'z0', 'xmax', 'ymax', 'zmax'), tmp):
+                G.pmlthickness[key] = int(v)
+    if (2 * G.pmlthickness['x0'] >= G.nx or 2 * G.pmlthickness['y0'] >= G.ny
+            or 2 * G.pmlthickness['z0'] >= G.nz or 2 * G.pmlthickness['xmax'] >= G.nx
+            or 2 * G.pmlthickness['ymax'] >= G.ny or 2 * G.pmlthickness['zmax'] >= G.nz):
+        raise CmdInputError(cmd + ' has too many cells for the domain size')
+
+    cmd = '#pml_formulation'
+    if singlecmds[cmd] is not None:
+        tmp = singlecmds[cmd].split()
+        if len(tmp) != 1:
+            raise CmdInputError(cmd + ' requires exactly one parameter')
+        if singlecmds[cmd].upper() in PML.formulations:
+            G.pmlformulation = singlecmds[cmd].upper()
+        else:
+            raise CmdInputError(cmd + ' PML formulation is not found')
+
+    for cmd, target in (('#src_steps', G.srcsteps), ('#rx_steps', G.rxsteps)):
+        if singlecmds[cmd] is not None:
+            tmp = singlecmds[cmd].split()
+            if len(tmp) != 3:
+                raise CmdInputError(cmd + ' requires exactly three parameters')
+            target[0] = round_value(float(tmp[0]) / G.dx)
+            target[1] = round_value(float(tmp[1]) / G.dy)
+            target[2] = round_value(float(tmp[2]) / G.dz)
+
+    cmd = '#excitation_file'
+    if singlecmds[cmd] is not None:
+        _excitation_file(singlecmds[cmd], G)
+
+    cmd = '#output_dir'
+    if singlecmds[cmd] is not None:
+        G.outputdirectory = singlecmds[cmd]
+
+
+def _excitation_file(params, G):
+    """User waveforms from a text file, interpolated with scipy (``input_cmds_singleuse.py:264-331``)."""
+    tmp = params.split()
+    if len(tmp) != 1 and len(tmp) != 3:
+        raise CmdInputError('#excitation_file requires either one or three parameter(s)')
+    excitationfile = tmp[0]
+    if len(tmp) > 1:
+        kwargs = {'kind': tmp[1], 'fill_value': tmp[2]}
+    else:
+        spec = inspect.getfullargspec(interpolate.interp1d)
+        kwargs = dict(zip(reversed(spec.args), reversed(spec.defaults)))
+    if not os.path.isfile(excitationfile):
+        excitationfile = os.path.abspath(os.path.join(G.inputdirectory, excitationfile))
+    with open(excitationfile, 'r') as f:
+        waveformIDs = f.readline().split()
+    waveformvalues = np.loadtxt(excitationfile, skiprows=1, dtype=floattype)
+    if waveformIDs[0].lower() == 'time':
+        waveformIDs = waveformIDs[1:]
+        waveformtime = waveformvalues[:, 0]
+        waveformvalues = waveformvalues[:, 1:]
+    else:
+        waveformtime = np.arange(0, G.timewindow + G.dt, G.dt)
+    for n, wid in enumerate(waveformIDs):
+        if any(x.ID == wid for x in G.waveforms):
+            raise CmdInputError('Waveform with ID {} already exists'.format(wid))
+        w = Waveform()
+        w.ID = wid
+        w.type = 'user'
+        vals = waveformvalues[:] if len(waveformvalues.shape) == 1 else waveformvalues[:, n]
+        if len(vals) > len(waveformtime):
+            vals = vals[:len(waveformtime)]
+        elif len(vals) < len(waveformtime):
+            padded = np.zeros(len(waveformtime))
+            padded[:len(vals)] = vals
+            vals = padded
+        w.userfunc = interpolate.interp1d(waveformtime, vals, **kwargs)
+        G.waveforms.append(w)
+
+
+def _err(cmdname, tmp, msg):
+    return CmdInputError("'" + cmdname + ': ' + ' '.join(tmp) + "'" + msg)
+
+
+def _check_coords(G, cmdname, tmp, x, y, z, name=''):
+    try:
+        G.within_bounds(x=x, y=y, z=z)
+    except ValueError as err:
+        raise CmdInputError("'{}: {} ' {} {}-coordinate is not within the model domain".format(
+            cmdname, ' '.join(tmp), name, err.args[0]))
+
+
+def _in_pml_warning(G, cmdname, tmp, x, y, z):
+    if (x < G.pmlthickness['x0'] or x > G.nx - G.pmlthickness['xmax'] or y < G.pmlthickness['y0']
+            or y > G.ny - G.pmlthickness['ymax'] or z < G.pmlthickness['z0']
+            or z > G.nz - G.pmlthickness['zmax']):
+        _log(G, "WARNING: '" + cmdname + ': ' + ' '.join(tmp) + "'"
+             + ' sources and receivers should not normally be positioned within the PML.')
+
+
+def _check_polarisation(G, cmdname, tmp, pol):
+    if pol not in ('x', 'y', 'z'):
+        raise _err(cmdname, tmp, ' polarisation must be x, y, or z')
+    if '2D TMx' in G.mode and pol in ('y', 'z'):
+        raise _err(cmdname, tmp, ' polarisation must be x in 2D TMx mode')
+    if '2D TMy' in G.mode and pol in ('x', 'z'):
+        raise _err(cmdname, tmp, ' polarisation must be y in 2D TMy mode')
+    if '2D TMz' in G.mode and pol in ('x', 'y'):
+        raise _err(cmdname, tmp, ' polarisation must be z in 2D TMz mode')
+
+
+def _start_stop(G, cmdname, tmp, src, first):
+    if len(tmp) > first:
+        start = float(tmp[first])
+        stop = float(tmp[first + 1])
+        if start < 0:
+            raise _err(cmdname, tmp, ' delay of the initiation of the source should not be less than zero')
+        if stop < 0:
+            raise _err(cmdname, tmp, ' time to remove the source should not be less than zero')
+        if stop - start <= 0:
+            raise _err(cmdname, tmp, ' duration of the source should not be zero or less')
+        src.start = start
+        src.stop = G.timewindow if stop > G.timewindow else stop
+    else:
+        src.start = 0
+        src.stop = G.timewindow
+
+
+def _simple_source(G, cmdname, cmdinstance, cls, minparams):
+    tmp = cmdinstance.split()
+    if len(tmp) < minparams:
+        raise _err(cmdname, tmp, ' requires at least {} parameters'.format(
+            {5: 'five', 6: 'six'}[minparams]))
+    pol = tmp[0].lower()
+    _check_polarisation(G, cmdname, tmp, pol)
+    x = G.calculate_coord('x', tmp[1])
+    y = G.calculate_coord('y', tmp[2])
+    z = G.calculate_coord('z', tmp[3])
+    _check_coords(G, cmdname, tmp, x, y, z)
+    _in_pml_warning(G, cmdname, tmp, x, y, z)
+    src = cls()
+    src.polarisation = pol
+    src.xcoord, src.ycoord, src.zcoord = x, y, z
+    src.xcoordorigin, src.ycoordorigin, src.zcoordorigin = x, y, z
+    src.ID = cls.__name__ + '(' + str(x) + ',' + str(y) + ',' + str(z) + ')'
+    return tmp, src
+
+
+def process_multicmds(multicmds, G):
+    """Waveforms, sources, receivers, snapshots, materials, dispersion and CFS terms."""
+    cmdname = '#waveform'
+    for cmdinstance in multicmds[cmdname]:
+        tmp = cmdinstance.split()
+        if len(tmp) != 4:
+            raise _err(cmdname, tmp, ' requires exactly four parameters')
+        if tmp[0].lower() not in Waveform.types:
+            raise _err(cmdname, tmp, ' must have one of the following types {}'.format(','.join(Waveform.types)))
+        if float(tmp[2]) <= 0:
+            raise _err(cmdname, tmp, ' requires an excitation frequency value of greater than zero')
+        if any(x.ID == tmp[3] for x in G.waveforms):
+            raise _err(cmdname, tmp, ' with ID {} already exists'.format(tmp[3]))
+        w = Waveform()
+        w.ID = tmp[3]
+        w.type = tmp[0].lower()
+        w.amp = float(tmp[1])
+        w.freq = float(tmp[2])
+        G.waveforms.append(w)
+
+    cmdname = '#voltage_source'
+    for cmdinstance in multicmds[cmdname]:
+        tmp, v = _simple_source(G, cmdname, cmdinstance, VoltageSource, 6)
+        resistance = float(tmp[4])
+        if resistance < 0:
+            raise _err(cmdname, tmp, ' requires a source resistance of zero or greater')
+        if not any(x.ID == tmp[5] for x in G.waveforms):
+            raise _err(cmdname, tmp, ' there is no waveform with the identifier {}'.format(tmp[5]))
+        v.resistance = resistance
+        v.waveformID = tmp[5]
+        _start_stop(G, cmdname, tmp, v, 6)
+        v.calculate_waveform_values(G)
+        G.voltagesources.append(v)
+
+    cmdname = '#hertzian_dipole'
+    for cmdinstance in multicmds[cmdname]:
+        tmp, h = _simple_source(G, cmdname, cmdinstance, HertzianDipole, 5)
+        if not any(x.ID == tmp[4] for x in G.waveforms):
+            raise _err(cmdname, tmp, ' there is no waveform with the identifier {}'.format(tmp[4]))
+        h.dl = {'x': G.dx, 'y': G.dy, 'z': G.dz}[h.polarisation]
+        h.waveformID = tmp[4]
+        _start_stop(G, cmdname, tmp, h, 5)
+        h.calculate_waveform_values(G)
+        G.hertziandipoles.append(h)
+
+    cmdname = '#magnetic_dipole'
+    for cmdinstance in multicmds[cmdname]:
+        tmp, m = _simple_source(G, cmdname, cmdinstance, MagneticDipole, 5)
+        if not any(x.ID == tmp[4] for x in G.waveforms):
+            raise _err(cmdname, tmp, ' there is no waveform with the identifier {}'.format(tmp[4]))
+        m.waveformID = tmp[4]
+        _start_stop(G, cmdname, tmp, m, 5)
+        m.calculate_waveform_values(G)
+        G.magneticdipoles.append(m)
+
+    if multicmds['#transmission_line']:
+        raise CmdInputError('#transmission_line is not supported by the GB300 solver core')
+
+    cmdname = '#rx'
+    for cmdinstance in multicmds[cmdname]:
+        tmp = cmdinstance.split()
+        if len(tmp) != 3 and len(tmp) < 5:
+            raise _err(cmdname, tmp, ' has an incorrect number of parameters')
+        x = round_value(float(tmp[0]) / G.dx)
+        y = round_value(float(tmp[1]) / G.dy)
+        z = round_value(float(tmp[2]) / G.dz)
+        _check_coords(G, cmdname, tmp, x, y, z)
+        _in_pml_warning(G, cmdname, tmp, x, y, z)
+        r = Rx()
+        r.xcoord, r.ycoord, r.zcoord = x, y, z
+        r.xcoordorigin, r.ycoordorigin, r.zcoordorigin = x, y, z
+        if len(tmp) == 3:
+            r.ID = 'Rx(' + str(x) + ',' + str(y) + ',' + str(z) + ')'
+            allocate_outputs(r, Rx.defaultoutputs, G.iterations)
+        else:
+            r.ID = tmp[3]
+            for field in tmp[4:]:
+                if field not in Rx.allowableoutputs:
+                    raise _err(cmdname, tmp, ' contains an output type that is not allowable. '
+                               'Allowable outputs in current context are {}'.format(Rx.allowableoutputs))
+                allocate_outputs(r, [field], G.iterations)
+        G.rxs.append(r)
+
+    cmdname = '#rx_array'
+    for cmdinstance in multicmds[cmdname]:
+        tmp = cmdinstance.split()
+        if len(tmp) != 9:
+            raise _err(cmdname, tmp, ' requires exactly nine parameters')
+        xs, ys, zs = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[0:3]))
+        xf, yf, zf = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[3:6]))
+        sx, sy, sz = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[6:9]))
+        _check_coords(G, cmdname, tmp, xs, ys, zs, name='lower')
+        _check_coords(G, cmdname, tmp, xf, yf, zf, name='upper')
+        if xs > xf or ys > yf or zs > zf:
+            raise _err(cmdname, tmp, ' the lower coordinates should be less than the upper coordinates')
+        if sx < 0 or sy < 0 or sz < 0:
+            raise _err(cmdname, tmp, ' the step size should not be less than zero')
+        steps = []
+        for s in (sx, sy, sz):
+            if s < 1:
+                if s == 0:
+                    s = 1
+                else:
+                    raise _err(cmdname, tmp, ' the step size should not be less than the spatial discretisation')
+            steps.append(s)
+        for x in range(xs, xf + 1, steps[0]):
+            for y in range(ys, yf + 1, steps[1]):
+                for z in range(zs, zf + 1, steps[2]):
+                    r = Rx()
+                    r.xcoord, r.ycoord, r.zcoord = x, y, z
+                    r.xcoordorigin, r.ycoordorigin, r.zcoordorigin = x, y, z
+                    r.ID = 'Rx(' + str(x) + ',' + str(y) + ',' + str(z) + ')'
+                    allocate_outputs(r, Rx.defaultoutputs, G.iterations)
+                    G.rxs.append(r)
+
+    cmdname = '#snapshot'
+    for cmdinstance in multicmds[cmdname]:
+        tmp = cmdinstance.split()
+        if len(tmp) != 11:
+            raise _err(cmdname, tmp, ' requires exactly eleven parameters')
+        xs, ys, zs = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[0:3]))
+        xf, yf, zf = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[3:6]))
+        sdx, sdy, sdz = (G.calculate_coord(a, v) for a, v in zip('xyz', tmp[6:9]))
+        try:
+            time = int(tmp[9])
+        except ValueError:
+            time = float(tmp[9])
+            if time > 0:
+                time = round_value((time / G.dt)) + 1
+            else:
+                raise _err(cmdname, tmp, ' time value must be greater than zero')
+        _check_coords(G, cmdname, tmp, xs, ys, zs, name='lower')
+        _check_coords(G, cmdname, tmp, xf, yf, zf, name='upper')
+        if xs >= xf or ys >= yf or zs >= zf:
+            raise _err(cmdname, tmp, ' the lower coordinates should be less than the upper coordinates')
+        if sdx < 0 or sdy < 0 or sdz < 0:
+            raise _err(cmdname, tmp, ' the step size should not be less than zero')
+        if sdx < 1 or sdy < 1 or sdz < 1:
+            raise _err(cmdname, tmp, ' the step size should not be less than the spatial discretisation')
+        if time <= 0 or time > G.iterations:
+            raise _err(cmdname, tmp, ' time value is not valid')
+        G.snapshots.append(Snapshot(xs, ys, zs, xf, yf, zf, sdx, sdy, sdz, time, tmp[10]))
+
+    cmdname = '#material'
+    for cmdinstance in multicmds[cmdname]:
+        tmp = cmdinstance.split()
+        if len(tmp) != 5:
+            raise _err(cmdname, tmp, ' requires exactly five parameters')
+        if float(tmp[0]) < 1:
+            raise _err(cmdname, tmp, ' requires a positive value of one or greater for static (DC) permittivity')
+        if tmp[1] != 'inf':
+            se = float(tmp[1])
+            if se < 0:
+                raise _err(cmdname, tmp, ' requires a positive value for conductivity')
+        else:
+            se = float('inf')
+        if float(tmp[2]) < 1:
+            raise _err(cmdname, tmp, ' requires a positive value of one or greater for permeability')
+        if float(tmp[3]) < 0:
+            raise _err(cmdname, tmp, ' requires a positive value for magnetic conductivity')
+        if any(x.ID == tmp[4] for x in G.materials):
+            raise _err(cmdname, tmp, ' with ID {} already exists'.format(tmp[4]))
+        m = Material(len(G.materials), tmp[4])
+        m.er = float(tmp[0])
+        m.se = se
+        m.mr = float(tmp[2])
+        m.sm = float(tmp[3])
+        if m.se == float('inf'):
+            m.averagable = False
+        G.materials.append(m)
+
+    for cmdname, kind, per in (('#add_dispersion_debye', 'debye', 2),
+                               ('#add_dispersion_lorentz', 'lorentz', 3),
+                               ('#add_dispersion_drude', 'drude', 2)):
+        for cmdinstance in multicmds[cmdname]:
+            tmp = cmdinstance.split()
+            need = 4 if kind == 'debye' else 5
+            if len(tmp) < need:
+                raise _err(cmdname, tmp, ' requires at least {} parameters'.format(
+                    'four' if need == 4 else 'five'))
+            if int(tmp[0]) < 0:
+                raise _err(cmdname, tmp, ' requires a positive value for number of poles')
+            poles = int(tmp[0])
+            span = 2 * poles if kind in ('debye', 'drude') else 3 * poles
+            if kind == 'drude':
+                span = 3 * poles   # the reference slices materials after 3 values per pole
+            requested = tmp[span + 1:] if kind != 'debye' else tmp[(2 * poles) + 1:]
+            materials = [y for x in requested for y in G.materials if y.ID == x]
+            if len(materials) != len(requested):
+                notfound = [x for x in requested if x not in materials]
+                raise _err(cmdname, tmp, ' material(s) {} do not exist'.format(notfound))
+            for material in materials:
+                material.type = kind
+                material.poles = poles
+                material.averagable = False
+                if kind == 'debye':
+                    for pole in range(1, 2 * poles, 2):
+                        if float(tmp[pole]) > 0:
+                            material.deltaer.append(float(tmp[pole]))
+                            material.tau.append(float(tmp[pole + 1]))
+                        else:
+                            raise _err(cmdname, tmp, ' requires positive values for the permittivity difference.')
+                elif kind == 'lorentz':
+                    for pole in range(1, 3 * poles, 3):
+                        if float(tmp[pole]) > 0 and float(tmp[pole + 1]) > G.dt and float(tmp[pole + 2]) > G.dt:
+                            material.deltaer.append(float(tmp[pole]))
+                            material.tau.append(float(tmp[pole + 1]))
+                            material.alpha.append(float(tmp[pole + 2]))
+                        else:
+                            raise _err(cmdname, tmp, ' requires positive values for the permittivity difference and frequencies, and associated times that are greater than the time step for the model.')
+                else:
+                    for pole in range(1, 2 * poles, 2):
+                        if float(tmp[pole]) > 0 and float(tmp[pole + 1]) > G.dt:
+                            material.tau.append(float(tmp[pole]))
+                            material.alpha.append(float(tmp[pole + 1]))
+                        else:
+                            raise _err(cmdname, tmp, ' requires positive values for the frequencies, and associated times that are greater than the time step for the model.')
+                if material.poles > G.maxpoles:
+                    G.maxpoles = material.poles
+
+    if multicmds['#soil_peplinski']:
+        raise CmdInputError('#soil_peplinski is not supported by the GB300 solver core')
+
+    cmdname = '#pml_cfs'
+    if multicmds[cmdname]:
+        if len(multicmds[cmdname]) > 2:
+            raise CmdInputError("'" + cmdname + "' can only be used up to two times, for up to a 2nd order PML")
+        for cmdinstance in multicmds[cmdname]:
+            tmp = cmdinstance.split()
+            if len(tmp) != 12:
+                raise _err(cmdname, tmp, ' requires exactly twelve parameters')
+            profiles = CFSParameter.scalingprofiles.keys()
+            if tmp[0] not in profiles or tmp[4] not in profiles or tmp[8] not in profiles:
+                raise _err(cmdname, tmp, ' must have scaling type {}'.format(','.join(profiles)))
+            dirs = CFSParameter.scalingdirections
+            if tmp[1] not in dirs or tmp[5] not in dirs or tmp[9] not in dirs:
+                raise _err(cmdname, tmp, ' must have scaling type {}'.format(','.join(dirs)))
+            if (float(tmp[2]) < 0 or float(tmp[3]) < 0 or float(tmp[6]) < 0 or float(tmp[7]) < 0
+                    or float(tmp[10]) < 0):
+                raise _err(cmdname, tmp, ' minimum and maximum scaling values must be positive')
+            if float(tmp[6]) < 1 and G.pmlformulation == 'HORIPML':
+                raise _err(cmdname, tmp, ' minimum scaling value for kappa must be greater than or equal to one')
+            cfs = CFS()
+            cfs.alpha = CFSParameter(ID='alpha', scalingprofile=tmp[0], scalingdirection=tmp[1],
+                                     min=float(tmp[2]), max=float(tmp[3]))
+            cfs.kappa = CFSParameter(ID='kappa', scalingprofile=tmp[4], scalingdirection=tmp[5],
+                                     min=float(tmp[6]), max=float(tmp[7]))
+            cfs.sigma = CFSParameter(ID='sigma', scalingprofile=tmp[8], scalingdirection=tmp[9],
+                                     min=float(tmp[10]),
+                                     max=None if tmp[11] == 'None' else float(tmp[11]))
+            G.cfs.append(cfs)
+
+
+def _lookup_materials(G, tmp, requested):
+    materials = [y for x in requested for y in G.materials if y.ID == x]
+    if len(materials) != len(requested):
+        notfound = [x for x in requested if x not in materials]
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' material(s) {} do not exist'.format(notfound))
+    return materials
+
+
+def _volume_material(G, tmp, materials, averageflag):
+    """Material numbers and smoothing flag of a volume primitive (isotropic or uniaxial)."""
+    if len(materials) == 1:
+        averaging = materials[0].averagable and averageflag
+        n = materials[0].numID
+        return n, n, n, n, averaging
+    requiredID = materials[0].ID + '+' + materials[1].ID + '+' + materials[2].ID
+    found = [x for x in G.materials if x.ID == requiredID]
+    if found:
+        numID = found[0].numID
+    else:
+        numID = len(G.materials)
+        m = Material(numID, requiredID)
+        m.type = 'dielectric-smoothed'
+        m.er = np.mean((materials[0].er, materials[1].er, materials[2].er), axis=0)
+        m.se = np.mean((materials[0].se, materials[1].se, materials[2].se), axis=0)
+        m.mr = np.mean((materials[0].mr, materials[1].mr, materials[2].mr), axis=0)
+        m.sm = np.mean((materials[0].sm, materials[1].sm, materials[2].sm), axis=0)
+        G.materials.append(m)
+    return numID, materials[0].numID, materials[1].numID, materials[2].numID, False
+
+
+def _average_option(G, tmp, n_iso, opt_index):
+    if len(tmp) == n_iso:
+        return [tmp[n_iso - 1]], G.averagevolumeobjects
+    if len(tmp) == n_iso + 1:
+        flag = tmp[opt_index].lower()
+        if flag == 'y':
+            return [tmp[n_iso - 1]], True
+        if flag == 'n':
+            return [tmp[n_iso - 1]], False
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires averaging to be either y or n')
+    if len(tmp) == n_iso + 2:
+        return tmp[n_iso - 1:], False
+    raise CmdInputError("'" + ' '.join(tmp) + "'" + ' too many parameters have been given')
+
+
+def process_geometrycmds(geometry, G):
+    """Build geometry primitives in the order given (``input_cmds_geometry.py:51``)."""
+    for line in geometry:
+        tmp = line.split()
+        name = tmp[0]
+        if name == '#box:':
+            if len(tmp) < 8:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least seven parameters')
+            requested, avg = _average_option(G, tmp, 8, 8)
+            xs = round_value(float(tmp[1]) / G.dx)
+            xf = round_value(float(tmp[4]) / G.dx)
+            ys = round_value(float(tmp[2]) / G.dy)
+            yf = round_value(float(tmp[5]) / G.dy)
+            zs = round_value(float(tmp[3]) / G.dz)
+            zf = round_value(float(tmp[6]) / G.dz)
+            for v, n, ax in ((xs, G.nx, 'x'), (xf, G.nx, 'x'), (ys, G.ny, 'y'), (yf, G.ny, 'y'),
+                             (zs, G.nz, 'z'), (zf, G.nz, 'z')):
+                if v < 0 or v > n:
+                    raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the {}-coordinate is not within the model domain'.format(ax))
+            if xs >= xf or ys >= yf or zs >= zf:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the lower coordinates should be less than the upper coordinates')
+            mats = _lookup_materials(G, tmp, requested)
+            numID, nx_, ny_, nz_, averaging = _volume_material(G, tmp, mats, avg)
+            geo.build_box(G, xs, xf, ys, yf, zs, zf, numID, nx_, ny_, nz_, averaging)
+        elif name == '#sphere:':
+            if len(tmp) < 6:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least five parameters')
+            requested, avg = _average_option(G, tmp, 6, 6)
+            xc = round_value(float(tmp[1]) / G.dx)
+            yc = round_value(float(tmp[2]) / G.dy)
+            zc = round_value(float(tmp[3]) / G.dz)
+            r = float(tmp[4])
+            mats = _lookup_materials(G, tmp, requested)
+            numID, nx_, ny_, nz_, averaging = _volume_material(G, tmp, mats, avg)
+            geo.build_sphere(G, xc, yc, zc, r, numID, nx_, ny_, nz_, averaging)
+        elif name == '#cylinder:':
+            if len(tmp) < 9:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least eight parameters')
+            requested, avg = _average_option(G, tmp, 9, 9)
+            # face centres snap to the nearest grid node
+            x1 = round_value(float(tmp[1]) / G.dx) * G.dx
+            y1 = round_value(float(tmp[2]) / G.dy) * G.dy
+            z1 = round_value(float(tmp[3]) / G.dz) * G.dz
+            x2 = round_value(float(tmp[4]) / G.dx) * G.dx
+            y2 = round_value(float(tmp[5]) / G.dy) * G.dy
+            z2 = round_value(float(tmp[6]) / G.dz) * G.dz
+            r = float(tmp[7])
+            if r <= 0:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the radius {:g} should be a positive value.'.format(r))
+            mats = _lookup_materials(G, tmp, requested)
+            numID, nx_, ny_, nz_, averaging = _volume_material(G, tmp, mats, avg)
+            geo.build_cylinder(G, x1, y1, z1, x2, y2, z2, r, numID, nx_, ny_, nz_, averaging)
+        elif name == '#edge:':
+            if len(tmp) != 8:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires exactly seven parameters')
+            xs = round_value(float(tmp[1]) / G.dx)
+            xf = round_value(float(tmp[4]) / G.dx)
+            ys = round_value(float(tmp[2]) / G.dy)
+            yf = round_value(float(tmp[5]) / G.dy)
+            zs = round_value(float(tmp[3]) / G.dz)
+            zf = round_value(float(tmp[6]) / G.dz)
+            mats = _lookup_materials(G, tmp, [tmp[7]])
+            geo.build_edge(G, xs, ys, zs, xf, yf, zf, mats[0].numID)
+        elif name == '#plate:':
+            if len(tmp) < 8:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least seven parameters')
+            requested = tmp[7:]
+            xs = round_value(float(tmp[1]) / G.dx)
+            xf = round_value(float(tmp[4]) / G.dx)
+            ys = round_value(float(tmp[2]) / G.dy)
+            yf = round_value(float(tmp[5]) / G.dy)
+            zs = round_value(float(tmp[3]) / G.dz)
+            zf = round_value(float(tmp[6]) / G.dz)
+            mats = _lookup_materials(G, tmp, requested)
+            geo.build_plate(G, xs, xf, ys, yf, zs, zf, [m.numID for m in mats])
+        else:
+            raise CmdInputError('{} is not supported by the GB300 solver core'.format(name.rstrip(':')))

@@ -1,0 +1,606 @@
+// gbfdtd.cu — context, device memory, time loop and C ABI of libgbfdtd.so (see include/gbfdtd.h).
+//
+// Device layout (one allocation per array, all C order with k fastest):
+//   fields   6 x fp32 [nx+1][ny+1][nz+1]         E then H
+//   ID       uint32 [6][nx+1][ny+1][nz+1]
+//   T        float2 [3][P][nx+1][ny+1][nz+1]     dispersive state (P = maxpoles)
+//   Phi      per slab, E and H, first and second tangential component, fp32 [order][...]
+//            with layouts x:[p][j][k], y:[i][p][k], z:[i][j][p] (p = profile index)
+//   rxs      fp32 [9][iterations][nrx]
+// The iteration number lives in device memory and is advanced by the last kernel of each
+// step, so a step is a fixed launch sequence that a CUDA graph can replay.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfdtd.h"
+#include "fdtd_kernels.cuh"
+
+using namespace gbf;
+
+struct gbf_ctx {
+  gbf_grid_desc d;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long ncomp = 0;
+  float* fields = nullptr;     // 6 * ncomp
+  uint32_t* ID = nullptr;      // 6 * ncomp
+  float* cE = nullptr;
+  float* cH = nullptr;
+  float2* cD = nullptr;
+  float2* T = nullptr;
+  float* pml_mem = nullptr;    // all Phi arrays
+  float* pml_coef = nullptr;   // 6 slabs x (E,H) x [4][order][T]
+  Src* srcs = nullptr;         // device: E sources in domain, H sources, E sources out of domain
+  float* waves = nullptr;
+  int* rx_coords = nullptr;
+  float* rxs = nullptr;
+  int* d_it = nullptr;
+  std::vector<float*> snaps;
+  std::vector<int> snapdef;    // nsnap x 10
+  int it = 0;                  // host copy of the iteration counter
+  bool materials = false;
+  size_t bytes = 0;
+  StepParams sp{};
+  RxParams rp{};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_steps = 0;
+};
+
+static std::string g_create_err;
+
+static void invalidate_graph(gbf_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+}
+
+static int fail(gbf_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf; else g_create_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA,          \
+                  "%s failed: %s", #call, cudaGetErrorString(e_));                        \
+  } while (0)
+
+static int dev_alloc(gbf_ctx* ctx, void** p, size_t n) {
+  if (n == 0) n = 16;
+  cudaError_t e = cudaMalloc(p, n);
+  if (e != cudaSuccess)
+    return fail(ctx, GBF_ENOMEM, "cudaMalloc of %zu bytes failed: %s", n, cudaGetErrorString(e));
+  ctx->bytes += n;
+  CK(cudaMemsetAsync(*p, 0, n, ctx->stream));
+  return GBF_OK;
+}
+
+static int pml_kind(const gbf_grid_desc& d) {
+  bool any = false;
+  for (int s = 0; s < 6; ++s) any |= d.pml_thickness[s] > 0;
+  if (!any) return PML_NONE;
+  if (d.pml_formulation == GBF_PML_HORIPML) return d.pml_order == 1 ? PML_HORI1 : PML_HORI2;
+  return d.pml_order == 1 ? PML_MRI1 : PML_MRI2;
+}
+
+extern "C" {
+
+const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
+
+int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n) {
+  if (!buf || n == 0) return GBF_EINVAL;
+  const std::string& s = ctx ? ctx->err : g_create_err;
+  snprintf(buf, n, "%s", s.c_str());
+  return GBF_OK;
+}
+
+void gbf_destroy(gbf_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  void* ptrs[] = {ctx->fields, ctx->ID, ctx->cE, ctx->cH, ctx->cD, ctx->T, ctx->pml_mem,
+                  ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (float* p : ctx->snaps)
+    if (p) cudaFree(p);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
+  if (!desc || !out) return fail(nullptr, GBF_EINVAL, "gbf_create: NULL argument");
+  *out = nullptr;
+  const gbf_grid_desc& d = *desc;
+  if (d.nx < 2 || d.ny < 2 || d.nz < 2)
+    return fail(nullptr, GBF_EINVAL, "gbf_create: 2D grids (a dimension of one cell) are not supported yet (nx=%d ny=%d nz=%d)", d.nx, d.ny, d.nz);
+  if (d.iterations < 1 || d.nmat < 1 || d.maxpoles < 0 || d.maxpoles > kMaxPoles)
+    return fail(nullptr, GBF_EINVAL, "gbf_create: bad iterations/nmat/maxpoles (%d/%d/%d; poles <= %d)", d.iterations, d.nmat, d.maxpoles, kMaxPoles);
+  if (d.pml_order < 1 || d.pml_order > 2 || (d.pml_formulation != 0 && d.pml_formulation != 1))
+    return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
+  if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
+    return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
+  const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
+  if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
+    return fail(nullptr, GBF_EINVAL, "gbf_create: more than 2^31 nodes per component");
+  const int n3[3] = {d.nx, d.ny, d.nz};
+  for (int s = 0; s < 6; ++s) {
+    const int t = d.pml_thickness[s];
+    if (t < 0 || 2 * t >= n3[s % 3])
+      return fail(nullptr, GBF_EINVAL, "gbf_create: PML slab %d thickness %d too large for the domain", s, t);
+  }
+  gbf_ctx* ctx = new gbf_ctx();
+  ctx->d = d;
+  ctx->ncomp = npts;
+  cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    fail(nullptr, GBF_ECUDA, "gbf_create: CUDA unavailable: %s", cudaGetErrorString(e));
+    delete ctx;
+    return GBF_ECUDA;
+  }
+  int rc = GBF_OK;
+  auto A = [&](void** p, size_t n) { if (rc == GBF_OK) rc = dev_alloc(ctx, p, n); };
+  A((void**)&ctx->fields, sizeof(float) * 6 * npts);
+  A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
+  A((void**)&ctx->cE, sizeof(float) * 5 * d.nmat);
+  A((void**)&ctx->cH, sizeof(float) * 5 * d.nmat);
+  if (d.maxpoles > 0) {
+    A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
+    A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * npts);
+  }
+  // PML state: per slab 4 Phi arrays of order * T * nu * nv
+  long long phi_total = 0;
+  for (int s = 0; s < 6; ++s) {
+    const int t = d.pml_thickness[s];
+    if (!t) continue;
+    const int ax = s % 3;
+    const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
+    phi_total += 4LL * d.pml_order * t * nu * nv;
+  }
+  A((void**)&ctx->pml_mem, sizeof(float) * phi_total);
+  int tmax = 1;
+  for (int s = 0; s < 6; ++s) tmax = d.pml_thickness[s] > tmax ? d.pml_thickness[s] : tmax;
+  A((void**)&ctx->pml_coef, sizeof(float) * 6 * 2 * 4 * d.pml_order * tmax);
+  A((void**)&ctx->srcs, sizeof(Src) * (d.nsrc + 1));
+  A((void**)&ctx->waves, sizeof(float) * (size_t)(d.nsrc + 1) * d.iterations);
+  A((void**)&ctx->rx_coords, sizeof(int) * 3 * (d.nrx + 1));
+  A((void**)&ctx->rxs, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
+  A((void**)&ctx->d_it, sizeof(int));
+  if (rc != GBF_OK) {
+    g_create_err = ctx->err;
+    gbf_destroy(ctx);
+    return rc;
+  }
+
+  // kernel parameters
+  StepParams& p = ctx->sp;
+  for (int c = 0; c < 3; ++c) {
+    p.E[c] = ctx->fields + c * npts;
+    p.H[c] = ctx->fields + (3 + c) * npts;
+  }
+  p.ID = ctx->ID;
+  p.ncomp = npts;
+  p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
+  p.sy = d.nz + 1;
+  p.sx = (d.ny + 1) * (d.nz + 1);
+  p.cE = ctx->cE; p.cH = ctx->cH; p.cD = ctx->cD; p.T = ctx->T; p.P = d.maxpoles;
+  p.d_it = ctx->d_it;
+  p.chunk = 16;
+  p.nslab = 0;
+  float* phi = ctx->pml_mem;
+  const float dd[3] = {d.dx, d.dy, d.dz};
+  for (int s = 0; s < 6; ++s) {
+    const int t = d.pml_thickness[s];
+    if (!t) continue;
+    Slab& sl = p.slab[p.nslab++];
+    sl.axis = s % 3;
+    sl.minus = s < 3;
+    sl.T = t;
+    sl.n_axis = n3[sl.axis];
+    sl.nu = sl.axis == 0 ? d.ny : d.nx;
+    sl.nv = sl.axis == 2 ? d.ny : d.nz;
+    sl.d = dd[sl.axis];
+    sl.ocount = (long long)t * sl.nu * sl.nv;
+    const long long per = (long long)d.pml_order * sl.ocount;
+    sl.phiE1 = phi; phi += per;
+    sl.phiE2 = phi; phi += per;
+    sl.phiH1 = phi; phi += per;
+    sl.phiH2 = phi; phi += per;
+    sl.eR = ctx->pml_coef + (size_t)(s * 2 + 0) * 4 * d.pml_order * tmax;
+    sl.hR = ctx->pml_coef + (size_t)(s * 2 + 1) * 4 * d.pml_order * tmax;
+  }
+  p.nsrcE = p.nsrcH = 0;
+  p.srcE = p.srcH = ctx->srcs;
+  RxParams& r = ctx->rp;
+  r.coords = ctx->rx_coords;
+  r.out = ctx->rxs;
+  r.nrx = d.nrx;
+  r.iterations = d.iterations;
+  r.dx = d.dx; r.dy = d.dy; r.dz = d.dz;
+  r.nsrcOut = 0;
+  r.srcOut = ctx->srcs;
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    fail(nullptr, GBF_ECUDA, "gbf_create: %s", cudaGetErrorString(e));
+    gbf_destroy(ctx);
+    return GBF_ECUDA;
+  }
+  *out = ctx;
+  return GBF_OK;
+}
+
+int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
+                         const float* coeffH, const float* coeffD) {
+  if (!ctx) return GBF_EINVAL;
+  if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
+  const int nmat = ctx->d.nmat;
+  // every ID must index the tables
+  const size_t n = 6 * (size_t)ctx->ncomp;
+  for (size_t q = 0; q < n; ++q)
+    if (ID[q] >= (uint32_t)nmat)
+      return fail(ctx, GBF_EINVAL, "gbf_upload_materials: ID[%zu] = %u >= nmat %d", q, ID[q], nmat);
+  CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cE, coeffE, sizeof(float) * 5 * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cH, coeffH, sizeof(float) * 5 * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->d.maxpoles > 0)
+    CK(cudaMemcpyAsync(ctx->cD, coeffD, sizeof(float2) * 3 * ctx->d.maxpoles * nmat,
+                       cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->materials = true;
+  return GBF_OK;
+}
+
+int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]) {
+  if (!ctx) return GBF_EINVAL;
+  if (slab < 0 || slab >= 6 || !rows) return fail(ctx, GBF_EINVAL, "gbf_upload_pml: bad slab %d", slab);
+  const int t = ctx->d.pml_thickness[slab];
+  if (!t) return fail(ctx, GBF_EINVAL, "gbf_upload_pml: slab %d has zero thickness", slab);
+  int tmax = 1;
+  for (int s = 0; s < 6; ++s) tmax = ctx->d.pml_thickness[s] > tmax ? ctx->d.pml_thickness[s] : tmax;
+  const int order = ctx->d.pml_order;
+  for (int h = 0; h < 2; ++h) {
+    float* base = ctx->pml_coef + (size_t)(slab * 2 + h) * 4 * order * tmax;
+    for (int q = 0; q < 4; ++q) {
+      const float* src = rows[h * 4 + q];
+      if (!src) return fail(ctx, GBF_EINVAL, "gbf_upload_pml: NULL row");
+      // rows are [order][thickness]; device rows [q][order][T] with T == thickness
+      CK(cudaMemcpyAsync(base + (size_t)q * order * t, src, sizeof(float) * order * t,
+                         cudaMemcpyHostToDevice, ctx->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, const float* waves) {
+  if (!ctx) return GBF_EINVAL;
+  const gbf_grid_desc& d = ctx->d;
+  if (d.nsrc == 0) return GBF_OK;
+  if (!info || !scale || !waves) return fail(ctx, GBF_EINVAL, "gbf_upload_sources: NULL array");
+  std::vector<Src> inE, inH, outE;
+  for (int s = 0; s < d.nsrc; ++s) {
+    const int32_t* q = info + 8 * s;
+    Src v{};
+    v.kind = q[0]; v.comp = q[1]; v.i = q[2]; v.j = q[3]; v.k = q[4];
+    v.first = q[5]; v.last = q[6];
+    v.s0 = scale[2 * s]; v.s1 = scale[2 * s + 1];
+    v.w = ctx->waves + (size_t)s * d.iterations;
+    if (v.kind < 0 || v.kind > 3 || v.comp < 0 || v.comp > 5 || v.i < 0 || v.i > d.nx ||
+        v.j < 0 || v.j > d.ny || v.k < 0 || v.k > d.nz)
+      return fail(ctx, GBF_EINVAL, "gbf_upload_sources: source %d out of range", s);
+    if ((v.kind == GBF_SRC_MAGNETIC) != (v.comp >= 3))
+      return fail(ctx, GBF_EINVAL, "gbf_upload_sources: source %d kind/component mismatch", s);
+    if (v.kind == GBF_SRC_MAGNETIC) inH.push_back(v);
+    else if (v.i < d.nx && v.j < d.ny && v.k < d.nz) inE.push_back(v);
+    else outE.push_back(v);
+  }
+  std::vector<Src> all;
+  all.insert(all.end(), inE.begin(), inE.end());
+  all.insert(all.end(), inH.begin(), inH.end());
+  all.insert(all.end(), outE.begin(), outE.end());
+  CK(cudaMemcpyAsync(ctx->srcs, all.data(), sizeof(Src) * all.size(), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->waves, waves, sizeof(float) * (size_t)d.nsrc * d.iterations,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  invalidate_graph(ctx);
+  ctx->sp.nsrcE = (int)inE.size();
+  ctx->sp.srcE = ctx->srcs;
+  ctx->sp.nsrcH = (int)inH.size();
+  ctx->sp.srcH = ctx->srcs + inE.size();
+  ctx->rp.nsrcOut = (int)outE.size();
+  ctx->rp.srcOut = ctx->srcs + inE.size() + inH.size();
+  return GBF_OK;
+}
+
+int gbf_set_receivers(gbf_ctx* ctx, const int32_t* coords) {
+  if (!ctx) return GBF_EINVAL;
+  const gbf_grid_desc& d = ctx->d;
+  if (d.nrx == 0) return GBF_OK;
+  if (!coords) return fail(ctx, GBF_EINVAL, "gbf_set_receivers: NULL coords");
+  for (int n = 0; n < d.nrx; ++n) {
+    const int x = coords[3 * n], y = coords[3 * n + 1], z = coords[3 * n + 2];
+    if (x < 0 || x > d.nx || y < 0 || y > d.ny || z < 0 || z > d.nz)
+      return fail(ctx, GBF_EINVAL, "gbf_set_receivers: receiver %d at (%d,%d,%d) outside the grid", n, x, y, z);
+  }
+  CK(cudaMemcpyAsync(ctx->rx_coords, coords, sizeof(int) * 3 * d.nrx, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_set_snapshots(gbf_ctx* ctx, const int32_t* defs) {
+  if (!ctx) return GBF_EINVAL;
+  const gbf_grid_desc& d = ctx->d;
+  if (d.nsnap == 0) return GBF_OK;
+  if (!defs) return fail(ctx, GBF_EINVAL, "gbf_set_snapshots: NULL defs");
+  for (float* p : ctx->snaps) if (p) cudaFree(p);
+  ctx->snaps.assign(d.nsnap, nullptr);
+  ctx->snapdef.assign(defs, defs + 10 * d.nsnap);
+  for (int s = 0; s < d.nsnap; ++s) {
+    const int32_t* q = defs + 10 * s;
+    const int xs = q[0], ys = q[1], zs = q[2], sdx = q[3], sdy = q[4], sdz = q[5];
+    const int snx = q[6], sny = q[7], snz = q[8], time = q[9];
+    if (sdx < 1 || sdy < 1 || sdz < 1 || snx < 1 || sny < 1 || snz < 1 ||
+        xs < 0 || ys < 0 || zs < 0 || xs + snx * sdx > d.nx || ys + sny * sdy > d.ny ||
+        zs + snz * sdz > d.nz || time < 1 || time > d.iterations)
+      return fail(ctx, GBF_EINVAL, "gbf_set_snapshots: snapshot %d out of range", s);
+    int rc = dev_alloc(ctx, (void**)&ctx->snaps[s], sizeof(float) * 6 * (size_t)snx * sny * snz);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_reset(gbf_ctx* ctx) {
+  if (!ctx) return GBF_EINVAL;
+  const gbf_grid_desc& d = ctx->d;
+  CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * 6 * ctx->ncomp, ctx->stream));
+  if (ctx->T) CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)d.maxpoles * ctx->ncomp, ctx->stream));
+  long long phi_total = 0;
+  for (int s = 0; s < ctx->sp.nslab; ++s) phi_total += 4LL * d.pml_order * ctx->sp.slab[s].ocount;
+  if (phi_total) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * phi_total, ctx->stream));
+  CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
+  CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->it = 0;
+  return GBF_OK;
+}
+
+}  // extern "C"
+
+// ---- launch helpers ------------------------------------------------------------------
+typedef void (*HKern)(StepParams);
+typedef void (*EKern)(StepParams);
+
+static HKern pick_h(int pk) {
+  switch (pk) {
+    case PML_HORI1: return h_half_step<PML_HORI1>;
+    case PML_HORI2: return h_half_step<PML_HORI2>;
+    case PML_MRI1: return h_half_step<PML_MRI1>;
+    case PML_MRI2: return h_half_step<PML_MRI2>;
+    default: return h_half_step<PML_NONE>;
+  }
+}
+
+template <int PK>
+static EKern pick_e_np(int np) {
+  switch (np) {
+    case 1: return e_half_step<PK, 1>;
+    case 2: return e_half_step<PK, 2>;
+    case 3: return e_half_step<PK, 3>;
+    case 4: return e_half_step<PK, 4>;
+    default: return e_half_step<PK, 0>;
+  }
+}
+
+static EKern pick_e(int pk, int np) {
+  switch (pk) {
+    case PML_HORI1: return pick_e_np<PML_HORI1>(np);
+    case PML_HORI2: return pick_e_np<PML_HORI2>(np);
+    case PML_MRI1: return pick_e_np<PML_MRI1>(np);
+    case PML_MRI2: return pick_e_np<PML_MRI2>(np);
+    default: return pick_e_np<PML_NONE>(np);
+  }
+}
+
+static void launch_h(gbf_ctx* ctx) {
+  const StepParams& p = ctx->sp;
+  dim3 block(kBX, kBY);
+  dim3 grid((p.nz + 1 + kBX - 1) / kBX, (p.ny + 1 + kBY - 1) / kBY, (p.nx + 1 + p.chunk - 1) / p.chunk);
+  pick_h(pml_kind(ctx->d))<<<grid, block, 0, ctx->stream>>>(p);
+}
+
+static void launch_e(gbf_ctx* ctx) {
+  const StepParams& p = ctx->sp;
+  dim3 block(kBX, kBY);
+  dim3 grid((p.nz + kBX - 1) / kBX, (p.ny + kBY - 1) / kBY, (p.nx + p.chunk - 1) / p.chunk);
+  pick_e(pml_kind(ctx->d), ctx->d.maxpoles)<<<grid, block, 0, ctx->stream>>>(p);
+}
+
+static void launch_end(gbf_ctx* ctx) {
+  end_of_step<<<1, 256, 0, ctx->stream>>>(ctx->sp, ctx->rp, ctx->d_it);
+}
+
+static void launch_step(gbf_ctx* ctx) {
+  launch_h(ctx);
+  launch_e(ctx);
+  launch_end(ctx);
+}
+
+static int launch_snapshot(gbf_ctx* ctx, int s) {
+  const int* q = &ctx->snapdef[10 * s];
+  SnapParams sp;
+  sp.xs = q[0]; sp.ys = q[1]; sp.zs = q[2]; sp.sdx = q[3]; sp.sdy = q[4]; sp.sdz = q[5];
+  sp.snx = q[6]; sp.sny = q[7]; sp.snz = q[8];
+  sp.out = ctx->snaps[s];
+  long long n = (long long)sp.snx * sp.sny * sp.snz;
+  int blocks = (int)((n + 255) / 256);
+  if (blocks > 4096) blocks = 4096;
+  snapshot_store<<<blocks, 256, 0, ctx->stream>>>(ctx->sp, sp);
+  CK(cudaGetLastError());
+  return GBF_OK;
+}
+
+static const int kGraphSteps = 16;
+
+static int ensure_graph(gbf_ctx* ctx) {
+  if (ctx->gexec) return GBF_OK;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < kGraphSteps; ++s) launch_step(ctx);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (e != cudaSuccess) return fail(ctx, GBF_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  ctx->graph = g;
+  CK(cudaGraphInstantiate(&ctx->gexec, g, 0));
+  ctx->graph_steps = kGraphSteps;
+  return GBF_OK;
+}
+
+extern "C" {
+
+int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
+  if (!ctx) return GBF_EINVAL;
+  if (!ctx->materials) return fail(ctx, GBF_ESTATE, "gbf_run: materials not uploaded");
+  if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
+    return fail(ctx, GBF_EINVAL, "gbf_run: %d steps from iteration %d exceed %d iterations", nsteps, ctx->it, ctx->d.iterations);
+  if (flags & GBF_RUN_GRAPH) {
+    int rc = ensure_graph(ctx);
+    if (rc) return rc;
+  }
+  int done = 0;
+  while (done < nsteps) {
+    const int it = ctx->it;
+    // snapshots due at the start of this iteration (time == it + 1)
+    for (int s = 0; s < ctx->d.nsnap; ++s)
+      if (ctx->snapdef[10 * s + 9] == it + 1) {
+        int rc = launch_snapshot(ctx, s);
+        if (rc) return rc;
+      }
+    // steps until the next snapshot (a graph chunk never crosses one)
+    int span = nsteps - done;
+    for (int s = 0; s < ctx->d.nsnap; ++s) {
+      const int t = ctx->snapdef[10 * s + 9] - 1;
+      if (t > it && t - it < span) span = t - it;
+    }
+    int n = span;
+    if ((flags & GBF_RUN_GRAPH) && ctx->gexec) {
+      while (n >= ctx->graph_steps) {
+        CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
+        n -= ctx->graph_steps;
+      }
+    }
+    for (int s = 0; s < n; ++s) launch_step(ctx);
+    CK(cudaGetLastError());
+    ctx->it += span;
+    done += span;
+  }
+  if (flags & GBF_RUN_CHECK) {
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return GBF_OK;
+}
+
+int gbf_current_iteration(gbf_ctx* ctx, int32_t* it) {
+  if (!ctx || !it) return GBF_EINVAL;
+  *it = ctx->it;
+  return GBF_OK;
+}
+
+int gbf_synchronize(gbf_ctx* ctx) {
+  if (!ctx) return GBF_EINVAL;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_download_rx(gbf_ctx* ctx, float* rxs) {
+  if (!ctx || !rxs) return GBF_EINVAL;
+  const size_t n = 9 * (size_t)ctx->d.iterations * ctx->d.nrx;
+  if (n) CK(cudaMemcpyAsync(rxs, ctx->rxs, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_download_fields(gbf_ctx* ctx, float* fields) {
+  if (!ctx || !fields) return GBF_EINVAL;
+  CK(cudaMemcpyAsync(fields, ctx->fields, sizeof(float) * 6 * ctx->ncomp, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
+  if (!ctx || !fields) return GBF_EINVAL;
+  CK(cudaMemcpyAsync(ctx->fields, fields, sizeof(float) * 6 * ctx->ncomp, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_download_dispersive(gbf_ctx* ctx, float* T) {
+  if (!ctx || !T) return GBF_EINVAL;
+  if (!ctx->T) return fail(ctx, GBF_ESTATE, "gbf_download_dispersive: model has no dispersive state");
+  CK(cudaMemcpyAsync(T, ctx->T, sizeof(float2) * 3 * (size_t)ctx->d.maxpoles * ctx->ncomp,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_download_snapshot(gbf_ctx* ctx, int s, float* out) {
+  if (!ctx || !out) return GBF_EINVAL;
+  if (s < 0 || s >= ctx->d.nsnap) return fail(ctx, GBF_EINVAL, "gbf_download_snapshot: bad index %d", s);
+  const int* q = &ctx->snapdef[10 * s];
+  const size_t n = 6 * (size_t)q[6] * q[7] * q[8];
+  CK(cudaMemcpyAsync(out, ctx->snaps[s], sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GBF_OK;
+}
+
+int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_total) {
+  if (!ctx || !ms_h || !ms_e || !ms_total) return GBF_EINVAL;
+  if (!ctx->materials) return fail(ctx, GBF_ESTATE, "gbf_profile: materials not uploaded");
+  if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
+    return fail(ctx, GBF_EINVAL, "gbf_profile: too many steps");
+  std::vector<cudaEvent_t> ev(3 * nsteps + 1);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaEventRecord(ev[0], ctx->stream));
+  for (int s = 0; s < nsteps; ++s) {
+    launch_h(ctx);
+    CK(cudaEventRecord(ev[3 * s + 1], ctx->stream));
+    launch_e(ctx);
+    CK(cudaEventRecord(ev[3 * s + 2], ctx->stream));
+    launch_end(ctx);
+    CK(cudaEventRecord(ev[3 * s + 3], ctx->stream));
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  float th = 0, te = 0, tt = 0, t;
+  for (int s = 0; s < nsteps; ++s) {
+    CK(cudaEventElapsedTime(&t, ev[3 * s], ev[3 * s + 1])); th += t;
+    CK(cudaEventElapsedTime(&t, ev[3 * s + 1], ev[3 * s + 2])); te += t;
+  }
+  if (nsteps) CK(cudaEventElapsedTime(&tt, ev[0], ev[3 * nsteps]));
+  for (auto& e : ev) cudaEventDestroy(e);
+  ctx->it += nsteps;
+  *ms_h += th; *ms_e += te; *ms_total += tt;
+  return GBF_OK;
+}
+
+int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes) {
+  if (!ctx || !bytes) return GBF_EINVAL;
+  *bytes = ctx->bytes;
+  return GBF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,253 @@
+"""Voxelisation of geometry primitives into the solid, rigid and ID arrays.
+
+Semantics follow ``gprMax/geometry_primitives_ext.pyx``: a primitive built without dielectric
+smoothing writes the solid array, marks its cells rigid and writes the 12 edge IDs of each
+cell (``build_voxel`` :314-377; ``build_box`` :618-691 writes whole index ranges instead);
+with smoothing it only writes the solid array and clears the rigid flags, and the edge IDs are
+derived later by :mod:`gprmax_gb300.yee_build`. Cell selection for spheres and cylinders uses
+the reference's fp32 geometry inputs (``build_sphere`` :873, ``build_cylinder`` :692).
+All writes here are whole-array numpy operations; one primitive writes one material, so the
+order of its cells does not matter.
+"""
+import numpy as np
+
+from .utilities import round_value
+
+# rigidE holds 12 edge flags per cell, rigidH 6 (``yee_cell_setget_rigid_ext.pyx:24-157``)
+
+
+def _set_cells(G, I, J, K, numID, numIDx, numIDy, numIDz, averaging):
+    """``build_voxel`` applied to every cell (I, J, K)."""
+    G.solid[I, J, K] = numID
+    if averaging:
+        G.rigidE[:, I, J, K] = 0
+        G.rigidH[:, I, J, K] = 0
+        return
+    G.rigidE[:, I, J, K] = 1
+    G.rigidH[:, I, J, K] = 1
+    ID = G.ID
+    for comp, val in ((0, numIDx), (3, numIDx)):
+        ID[comp, I, J, K] = val
+        ID[comp, I, J + 1, K + 1] = val
+        ID[comp, I, J + 1, K] = val
+        ID[comp, I, J, K + 1] = val
+    for comp, val in ((1, numIDy), (4, numIDy)):
+        ID[comp, I, J, K] = val
+        ID[comp, I + 1, J, K + 1] = val
+        ID[comp, I + 1, J, K] = val
+        ID[comp, I, J, K + 1] = val
+    for comp, val in ((2, numIDz), (5, numIDz)):
+        ID[comp, I, J, K] = val
+        ID[comp, I + 1, J + 1, K] = val
+        ID[comp, I + 1, J, K] = val
+        ID[comp, I, J + 1, K] = val
+
+
+def build_voxels_mask(G, mask, origin, numID, numIDx, numIDy, numIDz, averaging):
+    """Build every cell where ``mask`` (a box starting at ``origin``) is true."""
+    I, J, K = np.nonzero(mask)
+    I = I + origin[0]
+    J = J + origin[1]
+    K = K + origin[2]
+    if I.size:
+        _set_cells(G, I, J, K, numID, numIDx, numIDy, numIDz, averaging)
+
+
+def build_box(G, xs, xf, ys, yf, zs, zf, numID, numIDx, numIDy, numIDz, averaging):
+    """Axis-aligned box of cells [xs, xf) x [ys, yf) x [zs, zf) (``build_box`` :618-691)."""
+    G.solid[xs:xf, ys:yf, zs:zf] = numID
+    if averaging:
+        G.rigidE[:, xs:xf, ys:yf, zs:zf] = 0
+        G.rigidH[:, xs:xf, ys:yf, zs:zf] = 0
+        return
+    G.rigidE[:, xs:xf, ys:yf, zs:zf] = 1
+    G.rigidH[:, xs:xf, ys:yf, zs:zf] = 1
+    ID = G.ID
+    ID[0, xs:xf, ys:yf + 1, zs:zf + 1] = numIDx
+    ID[1, xs:xf + 1, ys:yf, zs:zf + 1] = numIDy
+    ID[2, xs:xf + 1, ys:yf + 1, zs:zf] = numIDz
+    ID[3, xs:xf + 1, ys:yf, zs:zf] = numIDx
+    ID[4, xs:xf, ys:yf + 1, zs:zf] = numIDy
+    ID[5, xs:xf, ys:yf, zs:zf + 1] = numIDz
+
+
+def _clip(lo, hi, n):
+    return max(lo, 0), min(hi, n)
+
+
+def build_sphere(G, xc, yc, zc, r, numID, numIDx, numIDy, numIDz, averaging):
+    """Cells whose centre lies within ``r`` of node (xc, yc, zc) (``build_sphere`` :873-928)."""
+    dx, dy, dz, rf = (np.float32(G.dx), np.float32(G.dy), np.float32(G.dz), np.float32(r))
+    xs = round_value(((xc * dx) - rf) / dx) - 1
+    xf = round_value(((xc * dx) + rf) / dx) + 1
+    ys = round_value(((yc * dy) - rf) / dy) - 1
+    yf = round_value(((yc * dy) + rf) / dy) + 1
+    zs = round_value(((zc * dz) - rf) / dz) - 1
+    zf = round_value(((zc * dz) + rf) / dz) + 1
+    xs, xf = _clip(xs, xf, G.nx)
+    ys, yf = _clip(ys, yf, G.ny)
+    zs, zf = _clip(zs, zf, G.nz)
+    if xs >= xf or ys >= yf or zs >= zf:
+        return
+    i = np.arange(xs, xf, dtype=np.float64)[:, None, None]
+    j = np.arange(ys, yf, dtype=np.float64)[None, :, None]
+    k = np.arange(zs, zf, dtype=np.float64)[None, None, :]
+    # fp32 squares of the cell sizes, promoted to double as in the compiled reference
+    dx2, dy2, dz2 = (np.float64(dx * dx), np.float64(dy * dy), np.float64(dz * dz))
+    dist = np.sqrt((i + 0.5 - xc) ** 2 * dx2 + (j + 0.5 - yc) ** 2 * dy2
+                   + (k + 0.5 - zc) ** 2 * dz2)
+    build_voxels_mask(G, dist <= np.float64(rf), (xs, ys, zs), numID, numIDx, numIDy, numIDz,
+                      averaging)
+
+
+def build_cylinder(G, x1, y1, z1, x2, y2, z2, r, numID, numIDx, numIDy, numIDz, averaging):
+    """Cylinder between face centres (x1,y1,z1) and (x2,y2,z2) (``build_cylinder`` :692-871)."""
+    f32 = np.float32
+    x1, y1, z1, x2, y2, z2, r = (f32(x1), f32(y1), f32(z1), f32(x2), f32(y2), f32(z2), f32(r))
+    dx, dy, dz = f32(G.dx), f32(G.dy), f32(G.dz)
+    x_align = y_align = z_align = False
+    if round_value(y1 / dy) == round_value(y2 / dy) and round_value(z1 / dz) == round_value(z2 / dz):
+        x_align = True
+    elif round_value(x1 / dx) == round_value(x2 / dx) and round_value(z1 / dz) == round_value(z2 / dz):
+        y_align = True
+    elif round_value(x1 / dx) == round_value(x2 / dx) and round_value(y1 / dy) == round_value(y2 / dy):
+        z_align = True
+
+    def bounds(a1, a2, d, aligned):
+        lo, hi = (a1, a2) if a1 < a2 else (a2, a1)
+        if aligned:
+            return round_value(lo / d), round_value(hi / d)
+        return round_value((lo - r) / d) - 1, round_value((hi + r) / d) + 1
+    xs, xf = _clip(*bounds(x1, x2, dx, x_align), G.nx)
+    ys, yf = _clip(*bounds(y1, y2, dy, y_align), G.ny)
+    zs, zf = _clip(*bounds(z1, z2, dz, z_align), G.nz)
+    if xs >= xf or ys >= yf or zs >= zf:
+        return
+
+    def centre(n0, n1, d, a):
+        # (n * d) in fp32, plus 0.5 * d and minus the face centre in double
+        n = np.arange(n0, n1)
+        return (n.astype(f32) * d).astype(np.float64) + 0.5 * np.float64(d) - np.float64(a)
+
+    cx = centre(xs, xf, dx, x1)
+    cy = centre(ys, yf, dy, y1)
+    cz = centre(zs, zf, dz, z1)
+    shape = (xf - xs, yf - ys, zf - zs)
+    if x_align:
+        m2 = np.sqrt(cy[:, None] ** 2 + cz[None, :] ** 2) <= np.float64(r)
+        mask = np.broadcast_to(m2[None, :, :], shape)
+    elif y_align:
+        m2 = np.sqrt(cx[:, None] ** 2 + cz[None, :] ** 2) <= np.float64(r)
+        mask = np.broadcast_to(m2[:, None, :], shape)
+    elif z_align:
+        m2 = np.sqrt(cx[:, None] ** 2 + cy[None, :] ** 2) <= np.float64(r)
+        mask = np.broadcast_to(m2[:, :, None], shape)
+    else:
+        mask = _oblique_cylinder_mask(xs, xf, ys, yf, zs, zf, dx, dy, dz, x1, y1, z1, x2, y2, z2, r)
+    build_voxels_mask(G, mask, (xs, ys, zs), numID, numIDx, numIDy, numIDz, averaging)
+
+
+def _oblique_cylinder_mask(xs, xf, ys, yf, zs, zf, dx, dy, dz, x1, y1, z1, x2, y2, z2, r):
+    """Point-to-axis distance test of a cylinder not aligned with an axis (fp32 vectors)."""
+    f32 = np.float32
+    f1f2 = np.array([x2 - x1, y2 - y1, z2 - z1], dtype=f32)
+    f2f1 = np.array([x1 - x2, y1 - y2, z1 - z2], dtype=f32)
+    f1f2mag = np.sqrt((f1f2 * f1f2).sum(axis=0))
+    f2f1mag = np.sqrt((f2f1 * f2f1).sum(axis=0))
+    out = np.zeros((xf - xs, yf - ys, zf - zs), dtype=bool)
+    with np.errstate(invalid='ignore'):
+        for i in range(xs, xf):
+            for j in range(ys, yf):
+                for k in range(zs, zf):
+                    px = i * dx + 0.5 * dx
+                    py = j * dy + 0.5 * dy
+                    pz = k * dz + 0.5 * dz
+                    f1pt = np.array([px - x1, py - y1, pz - z1], dtype=f32)
+                    f2pt = np.array([px - x2, py - y2, pz - z2], dtype=f32)
+                    f1ptmag = np.sqrt((f1pt * f1pt).sum(axis=0))
+                    f2ptmag = np.sqrt((f2pt * f2pt).sum(axis=0))
+                    if f1ptmag == 0 or f2ptmag == 0:
+                        out[i - xs, j - ys, k - zs] = True
+                        continue
+                    factor1 = np.float32(np.dot(f1f2, f1pt) / (f1f2mag * f1ptmag))
+                    factor2 = np.float32(np.dot(f2f1, f2pt) / (f2f1mag * f2ptmag))
+                    theta1 = np.arccos(factor1)
+                    theta2 = np.arccos(factor2)
+                    theta1 = f32(0) if np.isnan(theta1) else f32(theta1)
+                    theta2 = f32(0) if np.isnan(theta2) else f32(theta2)
+                    distance1 = f32(f1ptmag * np.sin(theta1))
+                    distance2 = f32(f2ptmag * np.sin(theta2))
+                    if ((distance1 <= r or distance2 <= r) and theta1 <= np.pi / 2
+                            and theta2 <= np.pi / 2):
+                        out[i - xs, j - ys, k - zs] = True
+    return out
+
+
+def build_edge(G, xs, ys, zs, xf, yf, zf, numID):
+    """Single-material line of edges (``input_cmds_geometry.py`` #edge; ``build_edge_*``)."""
+    if xs != xf:
+        for i in range(xs, xf):
+            _rigid_edge(G, 0, i, ys, zs)
+            G.ID[0, i, ys, zs] = numID
+    elif ys != yf:
+        for j in range(ys, yf):
+            _rigid_edge(G, 1, xs, j, zs)
+            G.ID[1, xs, j, zs] = numID
+    elif zs != zf:
+        for k in range(zs, zf):
+            _rigid_edge(G, 2, xs, ys, k)
+            G.ID[2, xs, ys, k] = numID
+
+
+def _rigid_edge(G, comp, i, j, k):
+    """``set_rigid_Ex/Ey/Ez`` (``yee_cell_setget_rigid_ext.pyx:72-97``)."""
+    r = G.rigidE
+    if comp == 0:
+        r[0, i, j, k] = 1
+        if j != 0:
+            r[1, i, j - 1, k] = 1
+        if k != 0:
+            r[3, i, j, k - 1] = 1
+        if j != 0 and k != 0:
+            r[2, i, j - 1, k - 1] = 1
+    elif comp == 1:
+        r[4, i, j, k] = 1
+        if i != 0:
+            r[7, i - 1, j, k] = 1
+        if k != 0:
+            r[5, i, j, k - 1] = 1
+        if i != 0 and k != 0:
+            r[6, i - 1, j, k - 1] = 1
+    else:
+        r[8, i, j, k] = 1
+        if i != 0:
+            r[9, i - 1, j, k] = 1
+        if j != 0:
+            r[11, i, j - 1, k] = 1
+        if i != 0 and j != 0:
+            r[10, i - 1, j - 1, k] = 1
+
+
+def build_plate(G, xs, xf, ys, yf, zs, zf, numIDs):
+    """Zero-thickness plate of E edges on one grid plane (#plate; ``build_face_*`` :230-312).
+    ``numIDs`` holds one or two material numbers (isotropic or anisotropic)."""
+    a = numIDs[0]
+    b = numIDs[-1]
+    if xs == xf:
+        for j in range(ys, yf):
+            for k in range(zs, zf):
+                for (jj, kk, comp, val) in ((j, k, 1, a), (j, k, 2, b), (j, k + 1, 1, a), (j + 1, k, 2, b)):
+                    _rigid_edge(G, comp, xs, jj, kk)
+                    G.ID[comp, xs, jj, kk] = val
+    elif ys == yf:
+        for i in range(xs, xf):
+            for k in range(zs, zf):
+                for (ii, kk, comp, val) in ((i, k, 0, a), (i, k, 2, b), (i, k + 1, 0, a), (i + 1, k, 2, b)):
+                    _rigid_edge(G, comp, ii, ys, kk)
+                    G.ID[comp, ii, ys, kk] = val
+    elif zs == zf:
+        for i in range(xs, xf):
+            for j in range(ys, yf):
+                for (ii, jj, comp, val) in ((i, j, 0, a), (i, j, 1, b), (i, j + 1, 0, a), (i + 1, j, 1, b)):
+                    _rigid_edge(G, comp, ii, jj, zs)
+                    G.ID[comp, ii, jj, zs] = val

@@ -1,0 +1,210 @@
+"""GB300 solver driver: the drop-in for the reference's ``solve_cpu``/``solve_gpu``.
+
+``solve_gb300(currentmodelrun, modelend, G)`` reads the same grid object the reference's
+solvers read (``model_build_run.py:369-373``), runs every iteration on the GPU through the C
+ABI of ``libgbfdtd.so`` and fills ``G.rxs[*].outputs`` and the snapshots, so the output writer
+is unchanged. :class:`DeviceModel` is the reusable form: build once, run, read back, reset.
+"""
+import ctypes
+import time
+
+import numpy as np
+
+from . import _native
+from .exceptions import SolverError
+from .receivers import OUTPUT_INDEX
+
+PML_SLABS = ['x0', 'y0', 'z0', 'xmax', 'ymax', 'zmax']
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p(0)
+
+
+def source_list(G):
+    """Sources in the reference's application order: E sources (voltage sources, then
+    Hertzian dipoles; ``model_build_run.py:459-461``), then magnetic dipoles."""
+    return list(G.voltagesources) + list(G.hertziandipoles) + list(G.magneticdipoles)
+
+
+def source_tables(G):
+    """int32 [n][8] info, fp32 [n][2] scales and fp32 [n][iterations] waveform tables."""
+    srcs = source_list(G)
+    n = len(srcs)
+    info = np.zeros((max(n, 1), 8), dtype=np.int32)
+    scale = np.zeros((max(n, 1), 2), dtype=np.float32)
+    waves = np.zeros((max(n, 1), G.iterations), dtype=np.float32)
+    for s, src in enumerate(srcs):
+        kind, comp, sc, table = src.kernel_record(G)
+        first, last = src.active_range()
+        info[s] = (kind, comp, src.xcoord, src.ycoord, src.zcoord, first, last, 0)
+        scale[s] = sc
+        waves[s] = table
+    return info, scale, waves
+
+
+class DeviceModel:
+    """One model resident on the GPU (fields, IDs, coefficients, PML and dispersive state)."""
+
+    def __init__(self, G):
+        self.G = G
+        self.lib = _native.lib()
+        self.ctx = ctypes.c_void_p(0)
+        d = _native.GridDesc()
+        d.nx, d.ny, d.nz = G.nx, G.ny, G.nz
+        d.iterations = G.iterations
+        d.nmat = len(G.materials)
+        d.maxpoles = G.maxpoles
+        d.pml_formulation = 0 if G.pmlformulation == 'HORIPML' else 1
+        d.pml_order = max(len(G.cfs), 1)
+        thick = {pml.ID: pml.thickness for pml in G.pmls}
+        for s, key in enumerate(PML_SLABS):
+            d.pml_thickness[s] = thick.get(key, 0)
+        d.dx, d.dy, d.dz = np.float32(G.dx), np.float32(G.dy), np.float32(G.dz)
+        d.nsrc = len(source_list(G))
+        d.nrx = len(G.rxs)
+        d.nsnap = len(G.snapshots)
+        self.desc = d
+        self._check(self.lib.gbf_create(ctypes.byref(d), ctypes.byref(self.ctx)), create=True)
+        try:
+            self._upload()
+        except Exception:
+            self.close()
+            raise
+
+    def _check(self, rc, create=False):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(1024)
+            self.lib.gbf_last_error(None if create else self.ctx, buf, 1024)
+            raise SolverError('libgbfdtd error {}: {}'.format(rc, buf.value.decode()))
+
+    def _upload(self):
+        G = self.G
+        ID = np.ascontiguousarray(G.ID, dtype=np.uint32)
+        cE = np.ascontiguousarray(G.updatecoeffsE, dtype=np.float32)
+        cH = np.ascontiguousarray(G.updatecoeffsH, dtype=np.float32)
+        cD = None
+        if G.maxpoles > 0:
+            cD = np.ascontiguousarray(G.updatecoeffsdispersive, dtype=np.complex64)
+        self._check(self.lib.gbf_upload_materials(self.ctx, _ptr(ID), _ptr(cE), _ptr(cH), _ptr(cD)))
+        for pml in G.pmls:
+            rows = [np.ascontiguousarray(getattr(pml, n), dtype=np.float32)
+                    for n in ('ERA', 'ERB', 'ERE', 'ERF', 'HRA', 'HRB', 'HRE', 'HRF')]
+            arr = (ctypes.c_void_p * 8)(*[r.ctypes.data for r in rows])
+            self._check(self.lib.gbf_upload_pml(self.ctx, PML_SLABS.index(pml.ID), arr))
+            self._keep = rows
+        if self.desc.nsrc:
+            info, scale, waves = source_tables(G)
+            self._check(self.lib.gbf_upload_sources(self.ctx, _ptr(info), _ptr(scale), _ptr(waves)))
+        if G.rxs:
+            coords = np.array([[r.xcoord, r.ycoord, r.zcoord] for r in G.rxs], dtype=np.int32)
+            self._check(self.lib.gbf_set_receivers(self.ctx, _ptr(coords)))
+        if G.snapshots:
+            defs = np.array([[s.xs, s.ys, s.zs, s.dx, s.dy, s.dz, s.nx, s.ny, s.nz, s.time]
+                             for s in G.snapshots], dtype=np.int32)
+            self._check(self.lib.gbf_set_snapshots(self.ctx, _ptr(defs)))
+        self.reset()
+
+    def reset(self):
+        self._check(self.lib.gbf_reset(self.ctx))
+
+    def run(self, nsteps=None, graph=True):
+        """Advance ``nsteps`` iterations (default: all remaining) on the device stream."""
+        if nsteps is None:
+            nsteps = self.G.iterations - self.iteration()
+        flags = _native.GBF_RUN_GRAPH if graph else 0
+        self._check(self.lib.gbf_run(self.ctx, int(nsteps), flags))
+
+    def synchronize(self):
+        self._check(self.lib.gbf_synchronize(self.ctx))
+
+    def iteration(self):
+        it = ctypes.c_int32(0)
+        self._check(self.lib.gbf_current_iteration(self.ctx, ctypes.byref(it)))
+        return it.value
+
+    def receivers(self):
+        """fp32 [9][iterations][nrx] receiver samples."""
+        out = np.zeros((9, self.G.iterations, max(len(self.G.rxs), 1)), dtype=np.float32)
+        if self.G.rxs:
+            self._check(self.lib.gbf_download_rx(self.ctx, _ptr(out)))
+        return out[:, :, :len(self.G.rxs)]
+
+    def fields(self):
+        """fp32 [6][nx+1][ny+1][nz+1] (Ex, Ey, Ez, Hx, Hy, Hz)."""
+        G = self.G
+        out = np.zeros((6, G.nx + 1, G.ny + 1, G.nz + 1), dtype=np.float32)
+        self._check(self.lib.gbf_download_fields(self.ctx, _ptr(out)))
+        return out
+
+    def set_fields(self, fields):
+        f = np.ascontiguousarray(fields, dtype=np.float32)
+        self._check(self.lib.gbf_upload_fields(self.ctx, _ptr(f)))
+
+    def dispersive(self):
+        """complex64 [3][maxpoles][nx+1][ny+1][nz+1] (Tx, Ty, Tz)."""
+        G = self.G
+        out = np.zeros((3, G.maxpoles, G.nx + 1, G.ny + 1, G.nz + 1), dtype=np.complex64)
+        self._check(self.lib.gbf_download_dispersive(self.ctx, _ptr(out)))
+        return out
+
+    def snapshot(self, s):
+        snap = self.G.snapshots[s]
+        out = np.zeros((6, snap.nx, snap.ny, snap.nz), dtype=np.float32)
+        self._check(self.lib.gbf_download_snapshot(self.ctx, s, _ptr(out)))
+        return out
+
+    def profile(self, nsteps):
+        """Device milliseconds of the H kernels, E kernels and whole steps over ``nsteps``."""
+        h, e, t = ctypes.c_float(0), ctypes.c_float(0), ctypes.c_float(0)
+        self._check(self.lib.gbf_profile(self.ctx, int(nsteps), ctypes.byref(h), ctypes.byref(e),
+                                         ctypes.byref(t)))
+        return h.value, e.value, t.value
+
+    def device_bytes(self):
+        b = ctypes.c_size_t(0)
+        self._check(self.lib.gbf_device_bytes(self.ctx, ctypes.byref(b)))
+        return b.value
+
+    def close(self):
+        if self.ctx and self.ctx.value:
+            self.lib.gbf_destroy(self.ctx)
+        self.ctx = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def store_results(self, fields=True):
+        """Copy receiver outputs, snapshots and (optionally) final fields into ``G``."""
+        G = self.G
+        rx = self.receivers()
+        for n, r in enumerate(G.rxs):
+            for name in r.outputs:
+                r.outputs[name] = rx[OUTPUT_INDEX[name], :, n].copy()
+        for s, snap in enumerate(G.snapshots):
+            f = self.snapshot(s)
+            snap.set_fields(*f)
+        if fields:
+            f = self.fields()
+            G.Ex, G.Ey, G.Ez, G.Hx, G.Hy, G.Hz = (f[c] for c in range(6))
+            if G.maxpoles > 0:
+                T = self.dispersive()
+                G.Tx, G.Ty, G.Tz = T[0], T[1], T[2]
+
+
+def solve_gb300(currentmodelrun, modelend, G, fields=True):
+    """Run all iterations of ``G`` on the GPU; returns (tsolve seconds, device bytes)."""
+    dm = DeviceModel(G)
+    try:
+        t0 = time.perf_counter()
+        dm.run()
+        dm.synchronize()
+        tsolve = time.perf_counter() - t0
+        dm.store_results(fields=fields)
+        mem = dm.device_bytes()
+    finally:
+        dm.close()
+    return tsolve, mem

@@ -1,0 +1,161 @@
+/*
+ * gbfdtd.h — C ABI of the GB300 FDTD solver core for gprMax models (libgbfdtd.so).
+ *
+ * The library replaces the time-stepping part of gprMax v3.1.7: the loop of solve_cpu /
+ * solve_gpu (gprMax/model_build_run.py:408-474 and :477-716) and the kernels it calls
+ * (gprMax/fields_updates_ext.pyx, gprMax/pml_updates/pml_updates_*_ext.pyx,
+ * gprMax/sources.py update_* methods, gprMax/fields_outputs.py store_outputs,
+ * gprMax/snapshots.py Snapshot.store). The host builds the model exactly as the reference
+ * does (material IDs, fp32 update coefficients, PML coefficient rows, source waveform tables)
+ * and hands the arrays over through this interface; every array crosses as a plain host
+ * pointer with the reference's C-order layout.
+ *
+ * Conventions
+ *  - Every call returns GBF_OK (0) or a negative GBF_E* status; the message of the last
+ *    failure on a context is available from gbf_last_error. Nothing calls exit() or traps.
+ *  - Host buffers are owned by the caller and copied; device memory is owned by the context.
+ *  - One context per host thread; calls on one context are not re-entrant. The context owns
+ *    one CUDA stream on which all of its work runs.
+ *  - Grid sizes nx, ny, nz are cell counts; field and ID arrays have (nx+1)(ny+1)(nz+1) nodes
+ *    per component, C order with k (z) fastest, exactly as gprMax/grid.py:157-178.
+ */
+#ifndef GBFDTD_H
+#define GBFDTD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBF_OK 0
+#define GBF_EINVAL (-1)      /* bad argument, size or layout */
+#define GBF_ECUDA (-2)       /* CUDA runtime error (message has the CUDA error string) */
+#define GBF_ENOMEM (-3)      /* device allocation failed */
+#define GBF_ESTATE (-4)      /* call out of order (e.g. run before materials were uploaded) */
+#define GBF_ENONFINITE (-5)  /* the NaN/Inf probe found a non-finite receiver sample */
+
+/* PML formulations (gprMax/pml.py:156-159) */
+#define GBF_PML_HORIPML 0
+#define GBF_PML_MRIPML 1
+
+/* source kinds (gprMax/sources.py) */
+#define GBF_SRC_HERTZIAN 0          /* E -= ((srce*w[it])*s0)*s1        sources.py:163-193 */
+#define GBF_SRC_VOLTAGE_RESISTIVE 1 /* E -= (srce*w[it])*s0             sources.py:81-120  */
+#define GBF_SRC_VOLTAGE_HARD 2      /* E = (-w[it])/s0 while active     sources.py:81-120  */
+#define GBF_SRC_MAGNETIC 3          /* H -= (srcm*w[it])*s0             sources.py:202-232 */
+
+/* gbf_run flags */
+#define GBF_RUN_GRAPH 1u     /* replay the step sequence from a captured CUDA graph */
+#define GBF_RUN_CHECK 2u     /* after the run, test receiver samples for NaN/Inf */
+
+/* Model description. Mirrors the attributes of gprMax's FDTDGrid that the time loop reads. */
+typedef struct gbf_grid_desc {
+    int32_t nx, ny, nz;          /* cells (grid.py: G.nx, G.ny, G.nz) */
+    int32_t iterations;          /* time steps (input_cmds_singleuse.py:184-207) */
+    int32_t nmat;                /* rows of the coefficient tables (len(G.materials)) */
+    int32_t maxpoles;            /* dispersive poles per material, 0 = none (Material.maxpoles) */
+    int32_t pml_formulation;     /* GBF_PML_* (G.pmlformulation) */
+    int32_t pml_order;           /* CFS terms per slab, 1 or 2 (len(G.cfs)) */
+    int32_t pml_thickness[6];    /* cells for x0, y0, z0, xmax, ymax, zmax (G.pmlthickness) */
+    float dx, dy, dz;            /* cell sizes as fp32 (the PML kernels' `float d`) */
+    int32_t nsrc;                /* sources (voltage sources, then Hertzian, then magnetic) */
+    int32_t nrx;                 /* receivers */
+    int32_t nsnap;               /* snapshots */
+    int32_t reserved[4];         /* must be zero */
+} gbf_grid_desc;
+
+typedef struct gbf_ctx gbf_ctx;
+
+/* Create a context on the current CUDA device and allocate all device state.
+ * Replaces: the array set-up of solve_gpu (model_build_run.py:505-583; grid.py:251-272;
+ * pml.py:298-364). */
+int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out);
+
+/* Destroy a context and free its device memory. Safe on NULL. */
+void gbf_destroy(gbf_ctx* ctx);
+
+/* Copy the material IDs and coefficient tables.
+ *   ID       uint32 [6][nx+1][ny+1][nz+1]   component order Ex, Ey, Ez, Hx, Hy, Hz (grid.py:168)
+ *   coeffE   fp32   [nmat][5]  CA, CBx, CBy, CBz, srce   (materials.py:200-201)
+ *   coeffH   fp32   [nmat][5]  DA, DBx, DBy, DBz, srcm
+ *   coeffD   complex64 as fp32 pairs [nmat][3*maxpoles] (e0*eqt2, eqt, zt) per pole, or NULL
+ *            when maxpoles == 0 (materials.py:204-208)
+ * Replaces: the __constant__ coefficient upload of solve_gpu (model_build_run.py:512-529). */
+int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
+                         const float* coeffH, const float* coeffD);
+
+/* Copy one PML slab's coefficient rows, each fp32 [pml_order][thickness], E then H:
+ * ERA, ERB, ERE, ERF, HRA, HRB, HRE, HRF (pml.py:221-274). `slab` indexes x0, y0, z0, xmax,
+ * ymax, zmax; slabs with zero thickness take no call. Replaces: PML.gpu_initialise_arrays
+ * (pml.py:306-319). */
+int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]);
+
+/* Copy the source list. Per source: info int32[8] = kind (GBF_SRC_*), component (0-2 for E,
+ * 3-5 for H), i, j, k, first and last active iteration (inclusive), 0; scale fp32[2]; waves
+ * fp32 [nsrc][iterations] (whole-step table for Hertzian and resistive sources, half-step for
+ * hard voltage sources and magnetic dipoles). Order matters: within one iteration E sources
+ * apply in list order after the PML (model_build_run.py:459-461).
+ * Replaces: gpu_initialise_src_arrays (sources.py:235-283). */
+int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale,
+                       const float* waves);
+
+/* Receiver positions int32 [nrx][3]. Outputs per receiver are Ex, Ey, Ez, Hx, Hy, Hz, Ix,
+ * Iy, Iz. Replaces: gpu_initialise_rx_arrays (receivers.py:45-68). */
+int gbf_set_receivers(gbf_ctx* ctx, const int32_t* coords);
+
+/* Snapshot definitions int32 [nsnap][10] = xs, ys, zs, dx, dy, dz (cells), nx, ny, nz, time.
+ * Snapshot s is taken at the start of iteration time-1 (model_build_run.py:429-431). */
+int gbf_set_snapshots(gbf_ctx* ctx, const int32_t* defs);
+
+/* Zero the fields, PML and dispersive state and restart at iteration 0. */
+int gbf_reset(gbf_ctx* ctx);
+
+/* Advance `nsteps` iterations from the current one (flags: GBF_RUN_*). Each iteration runs
+ * the H half-step (update, PML, magnetic sources), the E half-step (update or dispersive
+ * update, PML, E sources, dispersive second part) and stores receiver samples, in the order of
+ * solve_cpu (model_build_run.py:424-470). Asynchronous on the context stream unless
+ * GBF_RUN_CHECK is set. */
+int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
+
+/* Iteration the next gbf_run call starts at. */
+int gbf_current_iteration(gbf_ctx* ctx, int32_t* it);
+
+/* Block until all work on the context stream is complete. */
+int gbf_synchronize(gbf_ctx* ctx);
+
+/* Receiver samples fp32 [9][iterations][nrx] (Ex, Ey, Ez, Hx, Hy, Hz, Ix, Iy, Iz).
+ * Replaces: gpu_get_rx_array (receivers.py:71-88). */
+int gbf_download_rx(gbf_ctx* ctx, float* rxs);
+
+/* Fields fp32 [6][nx+1][ny+1][nz+1] (Ex, Ey, Ez, Hx, Hy, Hz): download / upload. */
+int gbf_download_fields(gbf_ctx* ctx, float* fields);
+int gbf_upload_fields(gbf_ctx* ctx, const float* fields);
+
+/* Dispersive state complex64 as fp32 pairs [3][maxpoles][nx+1][ny+1][nz+1] (Tx, Ty, Tz). */
+int gbf_download_dispersive(gbf_ctx* ctx, float* T);
+
+/* Snapshot s: fp32 [6][snx][sny][snz] cell-averaged Ex, Ey, Ez, Hx, Hy, Hz
+ * (snapshots_ext.pyx:24-71). */
+int gbf_download_snapshot(gbf_ctx* ctx, int s, float* out);
+
+/* Time `nsteps` iterations on the context stream with CUDA events around every launch; adds
+ * the summed device milliseconds of the H and E half-step kernels and of the whole sequence. */
+int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_total);
+
+/* Bytes of device memory the context holds. */
+int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes);
+
+/* Copy the message of the last failure on `ctx` (or of the last gbf_create failure when ctx
+ * is NULL) into buf. */
+int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n);
+
+/* Library version string. */
+const char* gbf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFDTD_H */
