@@ -1,0 +1,345 @@
+"""Benchmark: FDTD throughput (Mcells/s) of the GB300 solver core on the dispersive-soil model.
+
+Workload (the configuration the headline metric is quoted on): a 400 x 400 x 200 grid at
+2 mm, air above z = 150 cells and a 50-material single-pole Debye soil below, binned from a
+seeded fractal field, with a buried PEC cylinder, a 10-cell CFS PML on all faces, an
+x-polarised Hertzian dipole and a receiver 10 mm above the surface; Ricker 1.5 GHz, fp32
+fields, complex64 dispersive state. Synthetic, seeded inputs; no external data.
+
+Metric: Mcells/s = nx*ny*nz*steps / t / 1e6 (the reference's definition; t covers the time
+loop only). A step is one full Yee iteration (H half-step, E half-step with the dispersive
+update, PML, sources, receiver store).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line. The device-timed ``value`` uses CUDA events on the solver's stream
+around K steps (inputs resident; the working set, about 2.5 GB, is far larger than L2).
+``e2e`` is the same metric through the public API with host buffers: model upload to the
+GPU, K steps and the read-back of the receiver traces inside the timed region.
+``roofline`` is for the dominant kernel (the E half-step) from per-launch CUDA events.
+``cpu_baseline`` times the reference's own compiled CPU kernels (``oracle/_ref``) on all host
+cores on a bounded sample of the same workload (the oracle's C port when those are absent).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+
+METRIC = 'Mcells/s'
+WORKLOAD = 'dispersive_soil_400x400x200_debye50_pml10'
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            p = json.load(f)
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def slab_cells(G):
+    """Cells covered by each PML slab (a cell in k slabs counts k times)."""
+    n = 0
+    for p in G.pmls:
+        n += p.nx * p.ny * p.nz
+    return n
+
+
+def algorithmic_bytes(G):
+    """Bytes per launch that each half-step must move at minimum (fp32 fields, uint32 IDs,
+    complex64 dispersive state), per cell: H half-step reads E, H, 3 IDs and writes H
+    (48 B); E half-step the same plus 48 B per pole (T read and written); PML adds, per
+    slab cell and CFS order, two Phi values read and written (16 B) in each half-step."""
+    cells = G.nx * G.ny * G.nz
+    order = max(len(G.cfs), 1)
+    pml = slab_cells(G) * 16 * order
+    h = cells * 48 + pml
+    e = cells * (48 + 48 * G.maxpoles) + pml
+    return h, e
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples taken while the timed region runs."""
+
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.device), '--query-gpu=' + self.QUERY,
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(',')])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled'], 'samples': 0}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace('.', '').isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for n, v in zip(names, r[5:9]):
+                    if v.lower() == 'active':
+                        reasons.add(n)
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': max(mx) if mx else None,
+                'reasons': sorted(reasons), 'samples': len(self.rows)}
+
+
+def build_workload(iterations, grid=None):
+    from gprmax_gb300 import workloads
+    if grid:
+        nx, ny, nz = grid
+        G = workloads.dispersive_soil(nx=nx, ny=ny, nz=nz, surface=int(nz * 0.75))
+    else:
+        G = workloads.dispersive_soil()
+    if iterations > G.iterations:
+        # longer time window; per-step work is unchanged
+        G.iterations = iterations
+        for src in G.hertziandipoles + G.voltagesources + G.magneticdipoles:
+            src.stop = (iterations - 1) * G.dt
+            src.calculate_waveform_values(G)
+        for r in G.rxs:
+            for k in r.outputs:
+                r.outputs[k] = np.zeros(iterations, dtype=np.float32)
+    return G
+
+
+def cpu_baseline(G, budget_s=20.0, max_steps=60):
+    """Bounded CPU run of the same model: reference kernels on all host cores."""
+    import ref_cpu
+    cores = os.cpu_count() or 1
+    solver, kind = ref_cpu.make_solver(G, cores)
+    t0 = time.perf_counter()
+    solver.step()
+    t1 = time.perf_counter()
+    per = max(t1 - t0, 1e-3)
+    n = int(max(2, min(max_steps, budget_s / per)))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        solver.step()
+    t = time.perf_counter() - t0
+    cells = G.nx * G.ny * G.nz
+    return {'value': cells * n / t / 1e6, 'unit': METRIC, 'cores': cores, 'kind': kind,
+            'sample': '{} steps (after 1 warm-up step) of the full {}x{}x{} model, {} OpenMP '
+                      'threads'.format(n, G.nx, G.ny, G.nz, cores)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    return world, rank, local, dist
+
+
+def barrier_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device='cuda')
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_gb300(args):
+    world, rank, local, dist = dist_setup(args.gpus)
+    from gprmax_gb300 import _native
+    from gprmax_gb300.solver import DeviceModel
+    _native.lib()
+    K, W = args.steps, args.warmup
+    G = build_workload(max(3117, K + W + args.profile_steps + 1), args.grid)
+    cells = G.nx * G.ny * G.nz
+    # warm the CUDA context with a tiny model (not timed)
+    from gprmax_gb300.workloads import freespace_dipole
+    if not args.no_warm_context:
+        tiny = DeviceModel(freespace_dipole(n=20, timewindow='10', pml=4))
+        tiny.run()
+        tiny.synchronize()
+        tiny.close()
+
+    # --- end to end through the public API: upload from host, K steps, read back traces
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    dm = DeviceModel(G)
+    dm.run(K)
+    rx = dm.receivers()
+    t_e2e = time.perf_counter() - t0
+    h2d = (G.ID.nbytes + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
+           + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)
+           + sum(8 * getattr(p, 'ERA').nbytes for p in G.pmls)
+           + len(G.hertziandipoles + G.voltagesources + G.magneticdipoles) * G.iterations * 4)
+    d2h = rx.nbytes
+    t_e2e = barrier_max(dist, t_e2e)
+
+    # --- device-timed: warm-up, then K steps between events on the solver stream
+    dm.reset()
+    dm.run(W)
+    dm.synchronize()
+    if dist is not None:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        ms = dm.run_timed(K)
+    ms = barrier_max(dist, ms)
+    # --- per-kernel launch times for the roofline
+    ms_h, ms_e, ms_t = dm.profile(max(args.profile_steps, 1))
+    checksum = float(np.abs(dm.receivers()).sum())
+    dm.close()
+    value = world * cells * K / (ms / 1e3) / 1e6
+    bytes_h, bytes_e = algorithmic_bytes(G)
+    peak, peak_kind = load_peaks()
+    npf = max(args.profile_steps, 1)
+    t_e = ms_e / npf / 1e3
+    t_h = ms_h / npf / 1e3
+    achieved = bytes_e / t_e / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, 'profiles', 'e_half_step_soil_traffic.json')
+    if os.path.exists(tf):
+        try:
+            with open(tf) as f:
+                traffic = json.load(f).get('dram_bytes_per_launch')
+        except Exception:
+            traffic = None
+    if rank != 0:
+        return
+    out = {
+        'metric': METRIC, 'value': round(value, 1), 'unit': METRIC, 'n_gpus': world,
+        'steps': K, 'warmup': W, 'ms_per_step': ms / K, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (seeded fractal Debye soil)',
+        'config': {'workload': WORKLOAD if not args.grid else 'dispersive_soil_{}x{}x{}'.format(*args.grid), 'grid': [G.nx, G.ny, G.nz], 'dx_m': G.dx,
+                   'materials': len(G.materials), 'poles': G.maxpoles, 'pml_cells': 10,
+                   'cells': cells, 'l2': 'working set {:.2f} GB > L2 (129 MB), no flush'.format(
+                       dm_bytes(G) / 1e9), 'replicas': world},
+        'e2e': {'value': round(world * cells * K / t_e2e / 1e6, 1), 'unit': METRIC,
+                'h2d_bytes_per_step': int(h2d / K), 'd2h_bytes_per_step': int(d2h / K),
+                'what': 'DeviceModel(G) upload from host + {} steps + receiver read-back'.format(K)},
+        'gpu_launches': 3 * K,
+        'roofline': {'bound': 'hbm', 'kernel': 'e_half_step', 'achieved': round(achieved, 1),
+                     'peak': peak, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
+                     'traffic': traffic, 'peak_source': peak_kind,
+                     'bytes_per_launch': bytes_e, 'ms_per_launch': t_e * 1e3},
+        'kernels': {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
+                                    'GBps': round(bytes_h / t_h / 1e9, 1)},
+                    'e_half_step': {'ms': t_e * 1e3, 'bytes': bytes_e,
+                                    'GBps': round(achieved, 1)},
+                    'step_ms_profiled': ms_t / npf},
+        'clocks': clk.summary(),
+        'checksum_rx_abs_sum': checksum,
+    }
+    if args.cpu_baseline:
+        out['cpu_baseline'] = cpu_baseline(G, budget_s=args.cpu_budget)
+    print(json.dumps(out), flush=True)
+
+
+def dm_bytes(G):
+    return G.memory_estimate()
+
+
+def run_reference(args):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    import ref_cpu
+    K, W = args.steps, args.warmup
+    G = build_workload(3117)
+    cores = os.cpu_count() or 1
+    solver, kind = ref_cpu.make_solver(G, cores)
+    t0 = time.perf_counter()
+    for _ in range(max(W, 1)):
+        solver.step()
+    per = (time.perf_counter() - t0) / max(W, 1)
+    n = K
+    note = ''
+    if per * K > args.ref_budget:
+        n = max(2, int(args.ref_budget / per))
+        note = ' (bounded to {} of the {} requested steps to stay within {:.0f} s)'.format(n, K, args.ref_budget)
+    t0 = time.perf_counter()
+    for _ in range(n):
+        solver.step()
+    t = time.perf_counter() - t0
+    cells = G.nx * G.ny * G.nz
+    value = cells * n / t / 1e6
+    sample = '{} steps after {} warm-up of the full {}x{}x{} model, {} OpenMP threads{}'.format(
+        n, max(W, 1), G.nx, G.ny, G.nz, cores, note)
+    out = {'metric': METRIC, 'value': round(value, 2), 'unit': METRIC, 'n_gpus': world,
+           'steps': n, 'warmup': max(W, 1), 'ms_per_step': t / n * 1e3, 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+           'data': 'synthetic (seeded fractal Debye soil)', 'impl': 'reference',
+           'config': {'workload': WORKLOAD if not args.grid else 'dispersive_soil_{}x{}x{}'.format(*args.grid), 'grid': [G.nx, G.ny, G.nz], 'cells': cells},
+           'cpu_baseline': {'value': round(value, 2), 'unit': METRIC, 'cores': cores,
+                            'kind': kind, 'sample': sample},
+           'e2e': {'value': round(value, 2), 'unit': METRIC, 'h2d_bytes_per_step': 0,
+                   'd2h_bytes_per_step': 0},
+           'gpu_launches': 0}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=1000)
+    ap.add_argument('--warmup', type=int, default=20)
+    ap.add_argument('--impl', choices=['gb300', 'reference'], default='gb300')
+    ap.add_argument('--profile-steps', type=int, default=50)
+    ap.add_argument('--no-cpu-baseline', dest='cpu_baseline', action='store_false')
+    ap.add_argument('--cpu-budget', type=float, default=20.0)
+    ap.add_argument('--ref-budget', type=float, default=150.0)
+    ap.add_argument('--grid', type=int, nargs=3, default=None,
+                    help='smaller soil grid (profiling runs); default 400 400 200')
+    ap.add_argument('--no-warm-context', action='store_true',
+                    help='skip the small context warm-up model (launch counting for ncu)')
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -14,7 +14,9 @@ LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
 SOURCES = ['gbfdtd.cu', 'fdtd_kernels.cuh']
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-shared']
+# --fmad=false: every product and sum is rounded as written, which makes the GPU results
+# bit-identical to the reference's CPU kernels compiled without floating-point contraction
+NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '--fmad=false', '-Xcompiler', '-fPIC', '-shared']
 
 _lock = threading.Lock()
 _lib = None
@@ -71,6 +73,7 @@ _SIGS = {
     'gbf_set_snapshots': (ctypes.c_int, [_P, _P]),
     'gbf_reset': (ctypes.c_int, [_P]),
     'gbf_run': (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32]),
+    'gbf_run_timed': (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]),
     'gbf_current_iteration': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     'gbf_synchronize': (ctypes.c_int, [_P]),
     'gbf_download_rx': (ctypes.c_int, [_P, _P]),

@@ -362,7 +362,7 @@ e_half_step(const StepParams p) {
   const int k = blockIdx.x * kBX + threadIdx.x;
   const int j = blockIdx.y * kBY + threadIdx.y;
   if (k >= p.nz || j >= p.ny) return;
-  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const int nx = p.nx;
   const int i0 = blockIdx.z * p.chunk;
   const int i1 = min(i0 + p.chunk, nx);
   const float* __restrict__ Hx = p.H[0];

@@ -514,6 +514,22 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
   return GBF_OK;
 }
 
+int gbf_run_timed(gbf_ctx* ctx, int nsteps, uint32_t flags, float* ms) {
+  if (!ctx || !ms) return GBF_EINVAL;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->stream));
+  int rc = gbf_run(ctx, nsteps, flags & ~GBF_RUN_CHECK);
+  if (rc) { cudaEventDestroy(a); cudaEventDestroy(b); return rc; }
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  CK(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return GBF_OK;
+}
+
 int gbf_current_iteration(gbf_ctx* ctx, int32_t* it) {
   if (!ctx || !it) return GBF_EINVAL;
   *it = ctx->it;

@@ -251,3 +251,48 @@ def build_plate(G, xs, xf, ys, yf, zs, zf, numIDs):
                 for (ii, jj, comp, val) in ((i, j, 0, a), (i, j, 1, b), (i, j + 1, 0, a), (i + 1, j, 1, b)):
                     _rigid_edge(G, comp, ii, jj, zs)
                     G.ID[comp, ii, jj, zs] = val
+
+
+# Edge offsets written by ``build_voxel`` for one cell, per component (E and H alike):
+# x-directed components take (0,0,0), (0,1,1), (0,1,0), (0,0,1) and so on.
+_VOXEL_EDGE_OFFSETS = {
+    0: ((0, 0, 0), (0, 1, 1), (0, 1, 0), (0, 0, 1)),
+    1: ((0, 0, 0), (1, 0, 1), (1, 0, 0), (0, 0, 1)),
+    2: ((0, 0, 0), (1, 1, 0), (1, 0, 0), (0, 1, 0)),
+}
+
+
+def build_voxels_array(G, origin, numids, averaging):
+    """``build_voxels_from_array`` (``geometry_primitives_ext.pyx:930-980``) for a block of
+    per-cell material numbers (negative = leave the cell alone), clipped to the domain.
+
+    Cells sharing an edge write it in the reference's (i, j, k) loop order, so the edge ends
+    with the material of the last such cell; the writes below are issued in that order.
+    """
+    xs, ys, zs = origin
+    n = numids[:max(0, min(numids.shape[0], G.nx - xs)), :max(0, min(numids.shape[1], G.ny - ys)),
+               :max(0, min(numids.shape[2], G.nz - zs))]
+    built = n >= 0
+    if not built.any():
+        return
+    X = slice(xs, xs + n.shape[0])
+    Y = slice(ys, ys + n.shape[1])
+    Z = slice(zs, zs + n.shape[2])
+    solid = G.solid[X, Y, Z]
+    solid[built] = n[built]
+    for r in (G.rigidE, G.rigidH):
+        view = r[:, X, Y, Z]
+        view[:, built] = 0 if averaging else 1
+    if averaging:
+        return
+    sx, sy, sz = n.shape
+    for comp in range(3):
+        offs = _VOXEL_EDGE_OFFSETS[comp]
+        # a cell with a larger (i, j, k) writes later; offsets ordered by how late the writing
+        # cell comes relative to the edge: the edge at cell + o is written by cell = edge - o
+        order = sorted(offs, key=lambda o: (-o[0], -o[1], -o[2]))
+        for o in order:
+            for c in (comp, comp + 3):
+                target = G.ID[c, xs + o[0]:xs + o[0] + sx, ys + o[1]:ys + o[1] + sy,
+                              zs + o[2]:zs + o[2] + sz]
+                target[built] = n[built]

@@ -17,10 +17,13 @@ from . import cmds
 from .yee_build import build_electric_components, build_magnetic_components
 
 
-def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=None):
+def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=None,
+               geometry_hook=None):
     """Build a model from input-file lines up to the coefficient tables (before solving).
 
     Follows the build sequence of ``run_model`` (``model_build_run.py:110-292``).
+    ``geometry_hook(G)``, when given, runs before the geometry commands (used to place
+    programmatic voxel blocks, as ``#fractal_box`` would).
     """
     G = G or FDTDGrid()
     if usernamespace is None:
@@ -32,11 +35,15 @@ def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=Non
     processed = process_python_include_code(lines, usernamespace, inputfilename)
     singlecmds, multicmds, geometry = check_cmd_names(processed)
     G.materials = builtin_materials()
+    if messages is not None:
+        G.messages = messages
     cmds.process_singlecmds(singlecmds, G)
     if messages is not None:
         G.messages = messages
     cmds.process_multicmds(multicmds, G)
     G.initialise_geometry_arrays()
+    if geometry_hook is not None:
+        geometry_hook(G)
     cmds.process_geometrycmds(geometry, G)
     finish_build(G)
     return G

@@ -115,6 +115,13 @@ class DeviceModel:
         flags = _native.GBF_RUN_GRAPH if graph else 0
         self._check(self.lib.gbf_run(self.ctx, int(nsteps), flags))
 
+    def run_timed(self, nsteps, graph=True):
+        """Run ``nsteps`` iterations; device milliseconds from CUDA events on the solver stream."""
+        ms = ctypes.c_float(0)
+        flags = _native.GBF_RUN_GRAPH if graph else 0
+        self._check(self.lib.gbf_run_timed(self.ctx, int(nsteps), flags, ctypes.byref(ms)))
+        return ms.value
+
     def synchronize(self):
         self._check(self.lib.gbf_synchronize(self.ctx))
 

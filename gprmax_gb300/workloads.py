@@ -1,0 +1,104 @@
+"""Synthetic models with the shapes, sizes and value distributions of the benchmark
+configurations (no external data is involved; every draw is seeded).
+
+* :func:`freespace_dipole`    100^3 free-space Hertzian dipole, 10-cell CFS PML, Ricker 1.5 GHz
+* :func:`dispersive_soil`     400x400x200 heterogeneous 50-material Debye soil with a PEC
+                              cylinder, x-dipole and receiver above the surface
+* :func:`throughput_cube`     N^3 grid with a seeded dielectric block in the central half
+The soil is binned from a fractal field made with the reference's fractal-volume recipe
+(``gprMax/fractals.py:141-194``): FFT of seeded Gaussian noise, scaled by 1/r^D about the
+spectrum centre, inverse FFT, then ``np.digitize`` into equal-width bins.
+"""
+import numpy as np
+
+from .geometry import build_voxels_array
+from .grid import FDTDGrid
+from .materials import Material
+from .model import build_grid, finish_build
+
+
+def fractal_volume(shape, dimension, seed, nbins):
+    """Bin indices 0..nbins-1 of a seeded fractal field of the given shape."""
+    nx, ny, nz = shape
+    weighting = np.array([1.0, 1.0, 1.0]) * (np.amin(np.array(shape)) / np.array(shape, dtype=np.float64))
+    v1 = np.array([weighting[0] * nx / 2, weighting[1] * ny / 2, weighting[2] * nz / 2])
+    rng = np.random.default_rng(seed=seed)
+    A = rng.standard_normal(size=shape)
+    A = np.fft.fftshift(np.fft.fftn(A))
+    i = (weighting[0] * np.arange(nx) - v1[0])[:, None, None]
+    j = (weighting[1] * np.arange(ny) - v1[1])[None, :, None]
+    k = (weighting[2] * np.arange(nz) - v1[2])[None, None, :]
+    rr = np.sqrt(i ** 2 + j ** 2 + k ** 2)
+    B = rr ** dimension
+    B[B == 0] = 0.9
+    A /= B
+    A = np.fft.ifftshift(A)
+    A[0, 0, 0] = 0
+    vol = np.real(np.fft.ifftn(A)).astype(np.float32)
+    bins = np.linspace(np.amin(vol), np.amax(vol), nbins)
+    return np.digitize(vol, bins, right=True).astype(np.int64)
+
+
+def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
+    """Free-space z-dipole at the centre, receiver 10 cells along x (1 mm cells)."""
+    d = 0.001
+    c = n * d / 2
+    lines = ['#domain: {0:g} {0:g} {0:g}'.format(n * d), '#dx_dy_dz: 0.001 0.001 0.001',
+             '#time_window: {}'.format(timewindow), '#pml_cells: {}'.format(pml),
+             '#waveform: ricker 1 1.5e9 w',
+             '#hertzian_dipole: z {0:g} {0:g} {0:g} w'.format(c),
+             '#rx: {:g} {:g} {:g} rx1 Ez Hx Hy'.format(c + 10 * d, c, c)]
+    return build_grid([l + '\n' for l in lines], messages=messages)
+
+
+def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
+                    timewindow='12e-9', cylinder=True, messages=False):
+    """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
+
+    Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
+    sigma ~ logU[1e-4,1e-2] S/m. A PEC cylinder of radius 20 mm runs along y at depth 60 mm;
+    an x-polarised dipole and a receiver 40 mm apart sit 10 mm above the surface.
+    """
+    rng = np.random.default_rng(seed)
+    es = rng.uniform(5, 20, nmat)
+    einf = rng.uniform(3, 6, nmat)
+    tau = 10 ** rng.uniform(-10, -8, nmat)
+    sig = 10 ** rng.uniform(-4, -2, nmat)
+    zsurf = surface * dx
+    xc = nx * dx / 2
+    yc = ny * dx / 2
+    lines = ['#domain: {:g} {:g} {:g}'.format(nx * dx, ny * dx, nz * dx),
+             '#dx_dy_dz: {0:g} {0:g} {0:g}'.format(dx), '#time_window: {}'.format(timewindow),
+             '#pml_cells: 10', '#waveform: ricker 1 1.5e9 w',
+             '#hertzian_dipole: x {:g} {:g} {:g} w'.format(xc - 0.02, yc, zsurf + 0.01),
+             '#rx: {:g} {:g} {:g}'.format(xc + 0.02, yc, zsurf + 0.01)]
+    for m in range(nmat):
+        lines.append('#material: {!r} {!r} 1 0 soil{}'.format(float(einf[m]), float(sig[m]), m))
+        lines.append('#add_dispersion_debye: 1 {!r} {!r} soil{}'.format(
+            float(es[m] - einf[m]), float(tau[m]), m))
+    if cylinder:
+        lines.append('#cylinder: {0:g} 0 {1:g} {0:g} {2:g} {1:g} 0.02 pec'.format(
+            xc, zsurf - 0.06, ny * dx))
+    first_soil = 2
+
+    def soil(G):
+        bins = fractal_volume((nx, ny, surface), 1.5, seed, nmat)
+        build_voxels_array(G, (0, 0, 0), bins + first_soil, averaging=False)
+    return build_grid([l + '\n' for l in lines], messages=messages, geometry_hook=soil)
+
+
+def throughput_cube(n, iterations=2000, seed=0, pml=10, messages=False):
+    """N^3 cube at 1 mm with a seeded dielectric block filling the central half."""
+    rng = np.random.default_rng(seed)
+    er = rng.uniform(2, 20)
+    se = rng.uniform(0, 0.01)
+    d = 0.001
+    L = n * d
+    c = L / 2
+    lines = ['#domain: {0:g} {0:g} {0:g}'.format(L), '#dx_dy_dz: 0.001 0.001 0.001',
+             '#time_window: {}'.format(iterations), '#pml_cells: {}'.format(pml),
+             '#waveform: ricker 1 1.5e9 w', '#material: {!r} {!r} 1 0 block'.format(er, se),
+             '#box: {0:g} {0:g} {0:g} {1:g} {1:g} {1:g} block'.format(L / 4, 3 * L / 4),
+             '#hertzian_dipole: z {0:g} {0:g} {1:g} w'.format(c, L / 4 - 5 * d),
+             '#rx: {0:g} {0:g} {1:g}'.format(c + 5 * d, L / 4 - 5 * d)]
+    return build_grid([l + '\n' for l in lines], messages=messages)

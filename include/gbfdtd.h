@@ -144,6 +144,10 @@ int gbf_download_snapshot(gbf_ctx* ctx, int s, float* out);
  * the summed device milliseconds of the H and E half-step kernels and of the whole sequence. */
 int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_total);
 
+/* Run `nsteps` iterations like gbf_run, bracketed by CUDA events recorded on the context
+ * stream; blocks until done and returns the elapsed device milliseconds in *ms. */
+int gbf_run_timed(gbf_ctx* ctx, int nsteps, uint32_t flags, float* ms);
+
 /* Bytes of device memory the context holds. */
 int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes);
 

@@ -1,0 +1,99 @@
+"""Small input models shared by the parity tests (each runs in well under a second)."""
+
+BASE = """#domain: {dom}
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: {steps}
+"""
+
+MODELS = {
+    # free space, default CFS PML (HORIPML order 1), z-dipole
+    'fs_hori1': BASE.format(dom='0.030 0.030 0.030', steps=150) + """#pml_cells: 6
+#waveform: ricker 1 1.5e9 w
+#hertzian_dipole: z 0.015 0.015 0.015 w
+#rx: 0.020 0.015 0.015
+#rx: 0.012 0.018 0.011 r2 Ex Ey Ez Hx Hy Hz Ix Iy Iz
+""",
+    # PML off
+    'pml_off': BASE.format(dom='0.024 0.022 0.020', steps=120) + """#pml_cells: 0
+#waveform: gaussiandot 1 1e9 w
+#hertzian_dipole: y 0.012 0.011 0.010 w
+#rx: 0.016 0.011 0.010
+""",
+    # HORIPML order 2 with unequal slabs
+    'hori2': BASE.format(dom='0.032 0.028 0.026', steps=140) + """#pml_cells: 5 4 6 6 5 4
+#pml_cfs: constant forward 0 0 constant forward 1 1 sextic forward 0 0.5836
+#pml_cfs: constant forward 0.05 0.05 cubic forward 1 8 quadratic forward 0 5.8357
+#waveform: gaussiandotnorm 1 2e9 w
+#hertzian_dipole: x 0.016 0.014 0.013 w
+#rx: 0.020 0.016 0.012
+""",
+    # MRIPML order 1 and 2
+    'mri1': BASE.format(dom='0.028 0.030 0.026', steps=130) + """#pml_cells: 6
+#pml_formulation: MRIPML
+#pml_cfs: constant forward 0.05 0.05 quartic forward 1 8 quartic forward 0 11.67
+#waveform: ricker 1 2e9 w
+#hertzian_dipole: z 0.014 0.015 0.013 w
+#rx: 0.018 0.013 0.015
+""",
+    'mri2': BASE.format(dom='0.028 0.026 0.030', steps=130) + """#pml_cells: 5
+#pml_formulation: MRIPML
+#pml_cfs: constant forward 0 0 constant forward 1 1 sextic forward 0 0.5836
+#pml_cfs: constant forward 0.05 0.05 cubic forward 1 8 quadratic forward 0 5.8357
+#waveform: ricker 1 2e9 w
+#hertzian_dipole: y 0.014 0.013 0.015 w
+#rx: 0.010 0.016 0.017
+""",
+    # single-pole Debye block with smoothing at its faces
+    'debye1': BASE.format(dom='0.030 0.028 0.026', steps=150) + """#pml_cells: 6
+#material: 4.9 0.001 1 0 water
+#add_dispersion_debye: 1 75.2 9.231e-12 water
+#material: 6 0.002 1 0 sand
+#box: 0.004 0.004 0.004 0.026 0.024 0.012 water
+#sphere: 0.015 0.014 0.018 0.004 sand
+#waveform: ricker 1 1.5e9 w
+#hertzian_dipole: z 0.015 0.014 0.016 w
+#rx: 0.019 0.014 0.016
+""",
+    # multi-pole Debye, Lorentz, Drude, all source kinds, anisotropic box, currents
+    'mixed': BASE.format(dom='0.040 0.036 0.032', steps=100) + """#pml_cells: 6 5 4 5 6 4
+#pml_formulation: MRIPML
+#pml_cfs: constant forward 0 0 constant forward 1 1 sextic forward 0 0.5836
+#pml_cfs: constant forward 0.05 0.05 cubic forward 1 8 quadratic forward 0 5.8357
+#material: 4 0.01 1 0 half
+#material: 6 0.001 1 0 soil
+#material: 3 0 1 0 lor
+#material: 2 0 1 0 dru
+#material: 5 0 1 0 ax
+#material: 7 0 1 0 ay
+#material: 9 0 1 0 az
+#add_dispersion_lorentz: 1 2.5 1e9 1e8 lor
+#add_dispersion_drude: 1 1e9 1e8 0 dru
+#add_dispersion_debye: 2 3 1e-9 2 1e-10 soil
+#waveform: ricker 1 1.5e9 w
+#waveform: gaussiandot 1 2e9 w2
+#hertzian_dipole: z 0.020 0.018 0.016 w
+#voltage_source: y 0.015 0.012 0.020 50 w2
+#voltage_source: x 0.022 0.020 0.012 0 w 1e-11 5e-11
+#magnetic_dipole: x 0.025 0.014 0.018 w2
+#rx: 0.024 0.018 0.016
+#rx: 0.010 0.010 0.010 r2 Ex Hz Ix Iy Iz
+#box: 0 0 0 0.040 0.036 0.010 half
+#sphere: 0.020 0.018 0.016 0.006 soil
+#cylinder: 0.010 0.005 0.020 0.010 0.030 0.020 0.004 lor
+#cylinder: 0.030 0.010 0.005 0.030 0.010 0.028 0.003 dru n
+#box: 0.005 0.005 0.024 0.012 0.012 0.030 pec
+#box: 0.026 0.024 0.020 0.034 0.030 0.028 ax ay az
+#snapshot: 0.004 0.004 0.004 0.036 0.032 0.028 0.002 0.002 0.002 60 snap1
+""",
+    # sources on the upper domain faces and a receiver on a face (boundary index paths)
+    'faces': BASE.format(dom='0.020 0.018 0.016', steps=90) + """#pml_cells: 0
+#waveform: gaussiandot 1 2e9 w
+#hertzian_dipole: z 0.020 0.009 0.008 w
+#hertzian_dipole: x 0.010 0.018 0.008 w
+#voltage_source: y 0.010 0.009 0.016 0 w
+#magnetic_dipole: z 0.010 0.009 0.016 w
+#hertzian_dipole: z 0.010 0.009 0.008 w
+#rx: 0.010 0.009 0.000
+#rx: 0.011 0.010 0.009
+""",
+}
