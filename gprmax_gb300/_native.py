@@ -56,7 +56,7 @@ class GridDesc(ctypes.Structure):
                 ('pml_order', ctypes.c_int32), ('pml_thickness', ctypes.c_int32 * 6),
                 ('dx', ctypes.c_float), ('dy', ctypes.c_float), ('dz', ctypes.c_float),
                 ('nsrc', ctypes.c_int32), ('nrx', ctypes.c_int32), ('nsnap', ctypes.c_int32),
-                ('reserved', ctypes.c_int32 * 4)]
+                ('options', ctypes.c_int32), ('reserved', ctypes.c_int32 * 3)]
 
 
 GBF_RUN_GRAPH = 1

@@ -28,8 +28,11 @@ struct gbf_ctx {
   long long ncomp = 0;
   float* fields = nullptr;     // 6 * ncomp
   uint32_t* ID = nullptr;      // 6 * ncomp
-  float* cE = nullptr;
-  float* cH = nullptr;
+  float4* cE4 = nullptr;       // [nmat] CA, CBx, CBy, CBz
+  float* cEs = nullptr;        // [nmat] srce
+  float4* cH4 = nullptr;
+  float* cHs = nullptr;
+  size_t smem_e = 0, smem_h = 0;
   float2* cD = nullptr;
   float2* T = nullptr;
   float* pml_mem = nullptr;    // all Phi arrays
@@ -111,7 +114,7 @@ void gbf_destroy(gbf_ctx* ctx) {
   if (!ctx) return;
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  void* ptrs[] = {ctx->fields, ctx->ID, ctx->cE, ctx->cH, ctx->cD, ctx->T, ctx->pml_mem,
+  void* ptrs[] = {ctx->fields, ctx->ID, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
                   ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -133,6 +136,8 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
+  if ((d.options & ~1) || d.reserved[0] || d.reserved[1] || d.reserved[2])
+    return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
     return fail(nullptr, GBF_EINVAL, "gbf_create: more than 2^31 nodes per component");
@@ -156,8 +161,10 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   auto A = [&](void** p, size_t n) { if (rc == GBF_OK) rc = dev_alloc(ctx, p, n); };
   A((void**)&ctx->fields, sizeof(float) * 6 * npts);
   A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
-  A((void**)&ctx->cE, sizeof(float) * 5 * d.nmat);
-  A((void**)&ctx->cH, sizeof(float) * 5 * d.nmat);
+  A((void**)&ctx->cE4, sizeof(float4) * d.nmat);
+  A((void**)&ctx->cEs, sizeof(float) * d.nmat);
+  A((void**)&ctx->cH4, sizeof(float4) * d.nmat);
+  A((void**)&ctx->cHs, sizeof(float) * d.nmat);
   if (d.maxpoles > 0) {
     A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
     A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * npts);
@@ -192,29 +199,33 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     p.E[c] = ctx->fields + c * npts;
     p.H[c] = ctx->fields + (3 + c) * npts;
   }
-  p.ID = ctx->ID;
-  p.ncomp = npts;
+  for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID + c * npts;
+  p.ncomp = (int)npts;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.sy = d.nz + 1;
   p.sx = (d.ny + 1) * (d.nz + 1);
-  p.cE = ctx->cE; p.cH = ctx->cH; p.cD = ctx->cD; p.T = ctx->T; p.P = d.maxpoles;
+  p.cE4 = ctx->cE4; p.cEs = ctx->cEs; p.cH4 = ctx->cH4; p.cHs = ctx->cHs;
+  p.cD = ctx->cD; p.T = ctx->T; p.P = d.maxpoles;
+  p.nmat = d.nmat;
+  // shared-memory coefficient tables when they are small
+  ctx->smem_h = (size_t)d.nmat * (sizeof(float4) + sizeof(float));
+  ctx->smem_e = (size_t)d.nmat * sizeof(float4) + (size_t)((d.nmat + 1) & ~1) * sizeof(float) +
+                (size_t)d.nmat * 3 * d.maxpoles * sizeof(float2);
+  p.smem = (d.nmat <= kSmemCoefMax && ctx->smem_e <= 32768 && !(d.options & 1)) ? 1 : 0;
+  if (!p.smem) ctx->smem_e = ctx->smem_h = 0;
   p.d_it = ctx->d_it;
   p.chunk = 16;
-  p.nslab = 0;
   float* phi = ctx->pml_mem;
   const float dd[3] = {d.dx, d.dy, d.dz};
   for (int s = 0; s < 6; ++s) {
+    Slab& sl = p.slab[s];
     const int t = d.pml_thickness[s];
-    if (!t) continue;
-    Slab& sl = p.slab[p.nslab++];
-    sl.axis = s % 3;
-    sl.minus = s < 3;
     sl.T = t;
-    sl.n_axis = n3[sl.axis];
-    sl.nu = sl.axis == 0 ? d.ny : d.nx;
-    sl.nv = sl.axis == 2 ? d.ny : d.nz;
-    sl.d = dd[sl.axis];
-    sl.ocount = (long long)t * sl.nu * sl.nv;
+    sl.d = dd[s % 3];
+    if (!t) continue;
+    const int ax = s % 3;
+    const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
+    sl.ocount = (long long)t * nu * nv;
     const long long per = (long long)d.pml_order * sl.ocount;
     sl.phiE1 = phi; phi += per;
     sl.phiE2 = phi; phi += per;
@@ -255,8 +266,20 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
     if (ID[q] >= (uint32_t)nmat)
       return fail(ctx, GBF_EINVAL, "gbf_upload_materials: ID[%zu] = %u >= nmat %d", q, ID[q], nmat);
   CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->cE, coeffE, sizeof(float) * 5 * nmat, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->cH, coeffH, sizeof(float) * 5 * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  std::vector<float4> e4(nmat), h4(nmat);
+  std::vector<float> es(nmat), hs(nmat);
+  for (int m = 0; m < nmat; ++m) {
+    const float* a = coeffE + 5 * m;
+    const float* b = coeffH + 5 * m;
+    e4[m] = make_float4(a[0], a[1], a[2], a[3]);
+    es[m] = a[4];
+    h4[m] = make_float4(b[0], b[1], b[2], b[3]);
+    hs[m] = b[4];
+  }
+  CK(cudaMemcpyAsync(ctx->cE4, e4.data(), sizeof(float4) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cEs, es.data(), sizeof(float) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cH4, h4.data(), sizeof(float4) * nmat, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->cHs, hs.data(), sizeof(float) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->d.maxpoles > 0)
     CK(cudaMemcpyAsync(ctx->cD, coeffD, sizeof(float2) * 3 * ctx->d.maxpoles * nmat,
                        cudaMemcpyHostToDevice, ctx->stream));
@@ -371,7 +394,8 @@ int gbf_reset(gbf_ctx* ctx) {
   CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * 6 * ctx->ncomp, ctx->stream));
   if (ctx->T) CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)d.maxpoles * ctx->ncomp, ctx->stream));
   long long phi_total = 0;
-  for (int s = 0; s < ctx->sp.nslab; ++s) phi_total += 4LL * d.pml_order * ctx->sp.slab[s].ocount;
+  for (int s = 0; s < 6; ++s)
+    if (ctx->sp.slab[s].T) phi_total += 4LL * d.pml_order * ctx->sp.slab[s].ocount;
   if (phi_total) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * phi_total, ctx->stream));
   CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
@@ -421,14 +445,14 @@ static void launch_h(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
   dim3 block(kBX, kBY);
   dim3 grid((p.nz + 1 + kBX - 1) / kBX, (p.ny + 1 + kBY - 1) / kBY, (p.nx + 1 + p.chunk - 1) / p.chunk);
-  pick_h(pml_kind(ctx->d))<<<grid, block, 0, ctx->stream>>>(p);
+  pick_h(pml_kind(ctx->d))<<<grid, block, ctx->smem_h, ctx->stream>>>(p);
 }
 
 static void launch_e(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
   dim3 block(kBX, kBY);
   dim3 grid((p.nz + kBX - 1) / kBX, (p.ny + kBY - 1) / kBY, (p.nx + p.chunk - 1) / p.chunk);
-  pick_e(pml_kind(ctx->d), ctx->d.maxpoles)<<<grid, block, 0, ctx->stream>>>(p);
+  pick_e(pml_kind(ctx->d), ctx->d.maxpoles)<<<grid, block, ctx->smem_e, ctx->stream>>>(p);
 }
 
 static void launch_end(gbf_ctx* ctx) {

@@ -1,0 +1,64 @@
+"""The ``.out`` receiver file (``gprMax/fields_outputs.py:111-161``), written with the
+package's own HDF5 writer. Layout: root attributes gprMax, Title, Iterations, nx_ny_nz,
+dx_dy_dz, dt, nsrc, nrx, srcsteps, rxsteps; ``/srcs/srcN`` groups with Type and Position;
+``/rxs/rxN`` groups with Name and Position and one fp32 [iterations] dataset per output.
+"""
+import numpy as np
+
+from . import hdf5
+
+VERSION = '3.1.7'
+
+
+def write_hdf5_outputfile(outputfile, G):
+    f = hdf5.File(outputfile, 'w')
+    f.attrs['gprMax'] = VERSION
+    f.attrs['Title'] = G.title
+    f.attrs['Iterations'] = np.int64(G.iterations)
+    f.attrs['nx_ny_nz'] = np.array((G.nx, G.ny, G.nz), dtype=np.int64)
+    f.attrs['dx_dy_dz'] = np.array((G.dx, G.dy, G.dz), dtype=np.float64)
+    f.attrs['dt'] = np.float64(G.dt)
+    nsrc = len(G.voltagesources + G.hertziandipoles + G.magneticdipoles + G.transmissionlines)
+    f.attrs['nsrc'] = np.int64(nsrc)
+    f.attrs['nrx'] = np.int64(len(G.rxs))
+    f.attrs['srcsteps'] = np.array(G.srcsteps, dtype=np.int64)
+    f.attrs['rxsteps'] = np.array(G.rxsteps, dtype=np.int64)
+    for n, src in enumerate(G.voltagesources + G.hertziandipoles + G.magneticdipoles):
+        grp = f.create_group('/srcs/src' + str(n + 1))
+        grp.attrs['Type'] = type(src).__name__
+        grp.attrs['Position'] = np.array((src.xcoord * G.dx, src.ycoord * G.dy, src.zcoord * G.dz))
+    for n, rx in enumerate(G.rxs):
+        grp = f.create_group('/rxs/rx' + str(n + 1))
+        if rx.ID:
+            grp.attrs['Name'] = rx.ID
+        grp.attrs['Position'] = np.array((rx.xcoord * G.dx, rx.ycoord * G.dy, rx.zcoord * G.dz))
+        for output, values in rx.outputs.items():
+            grp[output] = np.asarray(values, dtype=np.float32)
+    f.close()
+
+
+def read_outputfile(path):
+    """Receiver traces of an ``.out`` file: ({'rx1': {'Ex': array, ...}, ...}, root attrs)."""
+    root = hdf5.read(path)
+    rxs = {}
+    if 'rxs' in root:
+        for name in root['rxs'].keys():
+            node = root['rxs'][name]
+            rxs[name] = {k: node[k].data for k in node.keys()}
+    return rxs, root.attrs
+
+
+def merge_files(paths, outputfile):
+    """Merge the ``.out`` files of a B-scan into one file whose datasets are
+    [iterations][nmodels] (the layout of the reference's ``tools/outputfiles_merge.py``)."""
+    first = hdf5.read(paths[0])
+    f = hdf5.File(outputfile, 'w')
+    for k, v in first.attrs.items():
+        if v is not None:
+            f.attrs[k] = v
+    f.attrs['Iterations'] = first.attrs['Iterations']
+    traces = [read_outputfile(p)[0] for p in paths]
+    for rx in traces[0]:
+        for comp in traces[0][rx]:
+            f['/rxs/{}/{}'.format(rx, comp)] = np.stack([t[rx][comp] for t in traces], axis=1)
+    f.close()

@@ -46,7 +46,7 @@ def source_tables(G):
 class DeviceModel:
     """One model resident on the GPU (fields, IDs, coefficients, PML and dispersive state)."""
 
-    def __init__(self, G):
+    def __init__(self, G, options=0):
         self.G = G
         self.lib = _native.lib()
         self.ctx = ctypes.c_void_p(0)
@@ -64,6 +64,7 @@ class DeviceModel:
         d.nsrc = len(source_list(G))
         d.nrx = len(G.rxs)
         d.nsnap = len(G.snapshots)
+        d.options = options
         self.desc = d
         self._check(self.lib.gbf_create(ctypes.byref(d), ctypes.byref(self.ctx)), create=True)
         try:

@@ -63,7 +63,9 @@ typedef struct gbf_grid_desc {
     int32_t nsrc;                /* sources (voltage sources, then Hertzian, then magnetic) */
     int32_t nrx;                 /* receivers */
     int32_t nsnap;               /* snapshots */
-    int32_t reserved[4];         /* must be zero */
+    int32_t options;             /* bit 0: read coefficient tables from global memory instead
+                                    of staging them in shared memory (tuning); other bits 0 */
+    int32_t reserved[3];         /* must be zero */
 } gbf_grid_desc;
 
 typedef struct gbf_ctx gbf_ctx;

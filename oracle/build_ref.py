@@ -21,7 +21,12 @@ copy), so the reference kernels can be timed as the CPU baseline on any host.
 directory when it exists, so ``import gprMax.grid`` etc. resolve to the reference's own
 Python modules there while the compiled kernels come from ``oracle/_ref``.
 
-Usage: python oracle/build_ref.py [--src PATH_TO_GPRMAX_CHECKOUT] [--jobs N]
+A second variant, ``--variant nofma`` (output ``oracle/_ref/nofma/gprMax``), compiles the same
+C with ``-ffp-contract=off`` added: every product and sum rounded as written. With it the
+reference's results are reproducible bit for bit on any host, and they are what the golden
+fixtures under ``tests/golden`` record.
+
+Usage: python oracle/build_ref.py [--src PATH_TO_GPRMAX_CHECKOUT] [--jobs N] [--variant nofma]
 """
 import argparse
 import os
@@ -82,11 +87,11 @@ def _march_ok(cc):
         return False
 
 
-def _compile(mod, cc, march):
+def _compile(mod, cc, march, variant=''):
     import numpy as np
     c_file = os.path.join(CSRC, mod + '.c')
     parts = mod.split('.')
-    dest_dir = os.path.join(OUT, *parts[:-1])
+    dest_dir = os.path.join(OUT, variant, *parts[:-1]) if variant else os.path.join(OUT, *parts[:-1])
     os.makedirs(dest_dir, exist_ok=True)
     so = os.path.join(dest_dir, parts[-1] + sysconfig.get_config_var('EXT_SUFFIX'))
     if os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(c_file):
@@ -94,6 +99,8 @@ def _compile(mod, cc, march):
     flags = ['-O3', '-w', '-fopenmp', '-fPIC', '-shared']
     if march:
         flags.append('-march=native')
+    if variant == 'nofma':
+        flags.append('-ffp-contract=off')
     cmd = [cc] + flags + ['-I', sysconfig.get_paths()['include'], '-I', np.get_include(),
                           c_file, '-o', so + '.tmp', '-fopenmp']
     subprocess.run(cmd, check=True)
@@ -101,8 +108,9 @@ def _compile(mod, cc, march):
     return so
 
 
-def build(src=None, jobs=8, modules=None, quiet=False):
-    """Cythonize (when ``src`` exists and Cython is importable) then compile into oracle/_ref."""
+def build(src=None, jobs=8, modules=None, quiet=False, variant=''):
+    """Cythonize (when ``src`` exists and Cython is importable) then compile into oracle/_ref
+    (``oracle/_ref/nofma`` for the no-contraction variant)."""
     modules = modules or ALL_MODULES
     os.makedirs(CSRC, exist_ok=True)
     os.makedirs(os.path.join(PKG, 'pml_updates'), exist_ok=True)
@@ -127,10 +135,12 @@ def build(src=None, jobs=8, modules=None, quiet=False):
     cc = os.environ.get('CC', 'gcc')
     march = _march_ok(cc)
     with ThreadPoolExecutor(jobs) as ex:
-        sos = list(ex.map(lambda m: _compile(m, cc, march), available))
-    with open(os.path.join(PKG, '__init__.py'), 'w') as f:
+        sos = list(ex.map(lambda m: _compile(m, cc, march, variant), available))
+    pkg = os.path.join(OUT, variant, 'gprMax') if variant else PKG
+    os.makedirs(os.path.join(pkg, 'pml_updates'), exist_ok=True)
+    with open(os.path.join(pkg, '__init__.py'), 'w') as f:
         f.write(INIT_TEMPLATE.format(src=os.path.join(src, 'gprMax') if have_src else ''))
-    with open(os.path.join(PKG, 'pml_updates', '__init__.py'), 'w') as f:
+    with open(os.path.join(pkg, 'pml_updates', '__init__.py'), 'w') as f:
         f.write(INIT_TEMPLATE.format(
             src=os.path.join(src, 'gprMax', 'pml_updates') if have_src else ''))
     if not quiet:
@@ -143,5 +153,6 @@ if __name__ == '__main__':
     ap.add_argument('--src', default='/root/reference')
     ap.add_argument('--jobs', type=int, default=os.cpu_count() or 4)
     ap.add_argument('--kernels-only', action='store_true')
+    ap.add_argument('--variant', choices=['', 'nofma'], default='')
     a = ap.parse_args()
-    build(a.src, a.jobs, KERNEL_MODULES if a.kernels_only else ALL_MODULES)
+    build(a.src, a.jobs, KERNEL_MODULES if a.kernels_only else ALL_MODULES, variant=a.variant)

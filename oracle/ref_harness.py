@@ -52,8 +52,12 @@ def _install_shims():
         sys.modules['h5py'] = types.ModuleType('h5py')
 
 
-def load(src='/root/reference'):
-    """Import the reference's model driver; returns the ``gprMax.model_build_run`` module."""
+def load(src='/root/reference', variant=''):
+    """Import the reference's model driver; returns the ``gprMax.model_build_run`` module.
+    ``variant='nofma'`` selects the kernels compiled without floating-point contraction."""
+    global REF_BUILD
+    if variant:
+        REF_BUILD = os.path.join(HERE, '_ref', variant)
     if not os.path.isdir(os.path.join(REF_BUILD, 'gprMax')):
         raise RuntimeError('reference kernels not built: run python oracle/build_ref.py')
     if not os.path.isdir(os.path.join(src, 'gprMax')):
@@ -83,9 +87,9 @@ class _Args:
 
 
 def run_reference(inputfile, src='/root/reference', currentmodelrun=1, modelend=1,
-                  nthreads=None, quiet=True):
+                  nthreads=None, quiet=True, variant=''):
     """Run one model through the reference and return its grid object after the solve."""
-    mbr = load(src)
+    mbr = load(src, variant)
     from gprMax.constants import c, e0, m0, z0
     from gprMax.materials import Material
     Material.maxpoles = 0   # class attribute; reset so models do not leak into each other

@@ -1,0 +1,124 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Needs a gprMax v3.1.7 checkout (``--src``, default ``/root/reference``) and its kernels built
+by ``oracle/build_ref.py`` (both the default build and ``--variant nofma``). Each model runs
+through the reference's own driver (``oracle/ref_harness.py``: input parsing, grid build,
+``solve_cpu``), once per build, in a child process. Writes, per model, ``<name>.npz`` with:
+
+* ``input``: the input-file text;
+* ``iterations``, ``dt``, ``nmat``, ``ID_sha256``, ``coeffE``, ``coeffH`` (and ``coeffD``):
+  the reference's model build;
+* ``rx<n>_<output>``: receiver traces of the no-contraction build (bit-for-bit reproducible);
+* ``field_<C>_sha256`` and ``field_stats`` (sum, sum of |.|, max |.| in float64) of the final
+  fields Ex..Hz of that build;
+* ``fma_rx<n>_<output>``: the same traces from the default (-march=native) build;
+* ``refout_rx<n>_<output>``: for the reference's own test models, the traces stored in their
+  ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote.
+
+It also copies one of those ``_ref.out`` files here as a fixture for the HDF5 reader.
+
+Usage: python tests/golden/make_golden.py [--src /root/reference] [--only NAME ...]
+"""
+import argparse
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, 'tests'))
+sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+
+REFERENCE_MODELS = ['hertzian_dipole_fs', 'hertzian_dipole_dispersive', 'hertzian_dipole_hs',
+                    'magnetic_dipole_fs']
+HDF5_FIXTURE = 'hertzian_dipole_dispersive_ref.out'
+
+CHILD = r'''
+import sys, hashlib, numpy as np
+sys.path.insert(0, {oracle!r})
+import ref_harness as rh
+G = rh.run_reference({inputfile!r}, src={src!r}, nthreads=8, variant={variant!r})
+out = {{'iterations': G.iterations, 'dt': G.dt, 'nmat': len(G.materials),
+        'ID_sha256': hashlib.sha256(np.ascontiguousarray(G.ID).tobytes()).hexdigest(),
+        'coeffE': G.updatecoeffsE, 'coeffH': G.updatecoeffsH}}
+if G.maxpoles:
+    out['coeffD'] = G.updatecoeffsdispersive
+for n, r in enumerate(G.rxs):
+    for k, v in r.outputs.items():
+        out['rx{{}}_{{}}'.format(n + 1, k)] = np.asarray(v, dtype=np.float32)
+stats = []
+for c in ('Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz'):
+    a = np.ascontiguousarray(getattr(G, c))
+    out['field_{{}}_sha256'.format(c)] = hashlib.sha256(a.tobytes()).hexdigest()
+    stats.append([float(a.astype(np.float64).sum()), float(np.abs(a.astype(np.float64)).sum()),
+                  float(np.abs(a).max())])
+out['field_stats'] = np.array(stats)
+for s, snap in enumerate(G.snapshots):
+    out['snap{{}}_electric'.format(s)] = snap.electric
+    out['snap{{}}_magnetic'.format(s)] = snap.magnetic
+np.savez({dest!r}, **out)
+'''
+
+
+def run_child(inputfile, src, variant, dest):
+    code = CHILD.format(oracle=os.path.join(ROOT, 'oracle'), inputfile=inputfile, src=src,
+                        variant=variant, dest=dest)
+    subprocess.run([sys.executable, '-c', code], check=True, cwd=ROOT)
+    return dict(np.load(dest, allow_pickle=False))
+
+
+def make(name, text, src, refout=None):
+    with tempfile.TemporaryDirectory() as tmp:
+        inputfile = os.path.join(tmp, name + '.in')
+        with open(inputfile, 'w') as f:
+            f.write(text)
+        exact = run_child(inputfile, src, 'nofma', os.path.join(tmp, 'exact.npz'))
+        fma = run_child(inputfile, src, '', os.path.join(tmp, 'fma.npz'))
+    out = dict(exact)
+    out['input'] = np.array(text)
+    for k, v in fma.items():
+        if k.startswith('rx'):
+            out['fma_' + k] = v
+    if refout:
+        from gprmax_gb300.outputs import read_outputfile
+        rxs, _ = read_outputfile(refout)
+        for rx, comps in rxs.items():
+            for comp, v in comps.items():
+                out['refout_{}_{}'.format(rx, comp)] = v.astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **out)
+    print('wrote', name, sorted(k for k in out if not k.startswith(('rx', 'fma', 'refout')))[:6])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--src', default='/root/reference')
+    ap.add_argument('--only', nargs='*')
+    a = ap.parse_args()
+    from models import MODELS
+    todo = {n: (t, None) for n, t in MODELS.items()}
+    for n in REFERENCE_MODELS:
+        d = os.path.join(a.src, 'tests', 'models_basic', n)
+        with open(os.path.join(d, n + '.in')) as f:
+            text = f.read()
+        ref = os.path.join(d, n + '_ref.out')
+        todo['ref_' + n] = (text, ref if os.path.exists(ref) else None)
+    for name, (text, ref) in sorted(todo.items()):
+        if a.only and name not in a.only:
+            continue
+        make(name, text, a.src, ref)
+    shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
+                             HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
+    with open(os.path.join(HERE, 'README.txt'), 'w') as f:
+        f.write('Golden fixtures generated by make_golden.py from gprMax v3.1.7 itself; see its '
+                'docstring for the content of each file.\n')
+
+
+if __name__ == '__main__':
+    main()

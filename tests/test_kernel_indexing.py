@@ -1,0 +1,115 @@
+"""CPU check of the GPU kernels' PML index arithmetic (no GPU needed).
+
+Mirrors, in numpy, how ``h_half_step``/``e_half_step`` (gprmax_gb300/csrc/fdtd_kernels.cuh)
+decide which nodes take which slab correction and which Phi element they use: the kernel
+domains, ``slab_p`` and ``phi_index``. For every slab and component it checks that the set of
+(node, profile index) pairs equals the reference's slab loops
+(``gprMax/pml_updates/pml_updates_{electric,magnetic}_*_ext.pyx``, ``ii = xf - i`` etc.), that
+every Phi index lies inside that slab's array, and that no two nodes share a Phi element.
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+# slab positions in kernel order: x0, y0, z0, xmax, ymax, zmax
+# tangential components (component index, Phi array 1 or 2) per slab axis, E and H
+E_COMPS = {0: ((1, 1), (2, 2)), 1: ((0, 1), (2, 2)), 2: ((0, 1), (1, 2))}
+H_COMPS = {0: ((4, 1), (5, 2)), 1: ((3, 1), (5, 2)), 2: ((3, 1), (4, 2))}
+
+
+def slab_p(c, T, n, minus, electric):
+    """Vectorised ``slab_p``: profile index or -1."""
+    c = np.asarray(c)
+    if T == 0:
+        return np.full(c.shape, -1)
+    if minus:
+        if electric:
+            return np.where((c >= 1) & (c <= T), T - c, -1)
+        return np.where(c < T, T - 1 - c, -1)
+    return np.where((c >= n - T) & (c < n), c - (n - T), -1)
+
+
+def phi_index(axis, i, j, k, p, T, ny, nz):
+    if axis == 0:
+        return (p * ny + j) * nz + k
+    if axis == 1:
+        return (i * T + p) * nz + k
+    return (i * ny + j) * T + p
+
+
+def kernel_pairs(n3, thick, electric):
+    """{(slab, comp): set of (i, j, k, p, phi_index)} as the kernels compute them."""
+    nx, ny, nz = n3
+    if electric:
+        dom = [np.arange(nx), np.arange(ny), np.arange(nz)]
+    else:
+        dom = [np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1)]
+    I, J, K = np.meshgrid(*dom, indexing='ij')
+    inside = np.ones(I.shape, bool) if electric else (I < nx) & (J < ny) & (K < nz)
+    out = {}
+    for s in range(6):
+        T = thick[s]
+        if not T:
+            continue
+        axis, minus = s % 3, s < 3
+        coord = (I, J, K)[axis]
+        p = slab_p(coord, T, n3[axis], minus, electric)
+        mem = (p >= 0) & inside
+        comps = (E_COMPS if electric else H_COMPS)[axis]
+        for comp, arr in comps:
+            ii, jj, kk, pp = I[mem], J[mem], K[mem], p[mem]
+            idx = phi_index(axis, ii, jj, kk, pp, T, ny, nz)
+            out[(s, comp)] = set(zip(ii.tolist(), jj.tolist(), kk.tolist(), pp.tolist(), idx.tolist()))
+    return out
+
+
+def reference_pairs(n3, thick, electric):
+    """{(slab, comp): set of (ii, jj, kk, p)} from the reference's slab loops."""
+    nx, ny, nz = n3
+    out = {}
+    for s in range(6):
+        T = thick[s]
+        if not T:
+            continue
+        axis, minus = s % 3, s < 3
+        # slab extents as build_pmls makes them (pml.py:367-429)
+        ext = [[0, nx], [0, ny], [0, nz]]
+        ext[axis] = [0, T] if minus else [n3[axis] - T, n3[axis]]
+        (xs, xf), (ys, yf), (zs, zf) = ext
+        pairs = set()
+        for i, j, k in itertools.product(range(xf - xs), range(yf - ys), range(zf - zs)):
+            loc = [i, j, k]
+            node = [i + xs, j + ys, k + zs]
+            f = (xf, yf, zf)[axis]
+            if minus:
+                node[axis] = f - loc[axis] if electric else f - (loc[axis] + 1)
+            pairs.add((node[0], node[1], node[2], loc[axis]))
+        for comp, arr in (E_COMPS if electric else H_COMPS)[axis]:
+            out[(s, comp)] = pairs
+    return out
+
+
+CASES = [((12, 10, 9), (3, 2, 2, 3, 2, 2)), ((13, 11, 14), (4, 0, 3, 2, 3, 0)),
+         ((9, 12, 10), (0, 5, 0, 0, 4, 3)), ((30, 28, 26), (6, 6, 6, 6, 6, 6))]
+
+
+@pytest.mark.parametrize('n3,thick', CASES)
+@pytest.mark.parametrize('electric', [True, False])
+def test_slab_nodes_and_phi_indices(n3, thick, electric):
+    nx, ny, nz = n3
+    k = kernel_pairs(n3, thick, electric)
+    r = reference_pairs(n3, thick, electric)
+    assert set(k) == set(r)
+    for key in r:
+        s = key[0]
+        T = thick[s]
+        axis = s % 3
+        nu = ny if axis == 0 else nx
+        nv = ny if axis == 2 else nz
+        ocount = T * nu * nv
+        got = k[key]
+        assert {q[:4] for q in got} == r[key], 'slab {} comp {}: node sets differ'.format(*key)
+        idx = [q[4] for q in got]
+        assert min(idx) >= 0 and max(idx) < ocount, 'slab {} comp {}: Phi index out of range'.format(*key)
+        assert len(set(idx)) == len(idx), 'slab {} comp {}: Phi element shared'.format(*key)
