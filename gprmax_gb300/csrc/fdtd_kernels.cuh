@@ -17,19 +17,17 @@
 // floating-point contraction, the results are bit-identical to the reference's CPU kernels
 // compiled the same way.
 //
-// Thread mapping: a block covers 32 consecutive k (one warp per row) by kBY rows j and walks a
-// chunk of x planes, carrying the neighbouring plane of the other field in registers. Slab
-// membership along y and z is fixed per thread and along x per plane, so nodes outside the
-// PML take a path without any PML work. The coefficient tables are staged in shared memory
-// when they fit (the reference keeps them in __constant__ memory, model_build_run.py:512-519).
+// Thread mapping: a persistent grid sweeps the flattened node index in order (consecutive
+// threads on consecutive nodes), one node per thread per pass. Nodes outside the PML box skip
+// all PML work. The coefficient tables are staged in shared memory when they fit (the reference
+// keeps them in __constant__ memory, model_build_run.py:512-519).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace gbf {
 
-constexpr int kBX = 32;   // k extent of a block (one warp)
-constexpr int kBY = 8;    // j extent of a block
+constexpr int kThreads = 256;   // threads per block of the half-step kernels
 constexpr int kMaxPoles = 4;
 constexpr int kSmemCoefMax = 2048;   // materials staged in shared memory
 
@@ -172,9 +170,143 @@ __device__ __forceinline__ void stage_tables(const StepParams& p, bool electric,
 }
 
 // ---------------------------------------------------------------------------------------
-// H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz].
+// Flat persistent sweep: threads take consecutive nodes of the flattened (i, j, k) index, and a
+// grid of a few blocks per SM strides through the whole array in order, so every array is
+// streamed front to back by the whole GPU at once (DRAM-page friendly for the ~20 concurrent
+// streams of a half-step). Neighbours along j, k (and x) are re-read from L1/L2.
+// The node index is advanced incrementally: the stride splits into whole planes, rows and nodes.
+struct FlatWalk {
+  int i, j, k, si, sj, sk, rows;
+  __device__ __forceinline__ FlatWalk(long long q, long long stride, int sx, int sy, int nrows) {
+    rows = nrows;
+    i = (int)(q / sx);
+    int r = (int)(q - (long long)i * sx);
+    j = r / sy;
+    k = r - j * sy;
+    si = (int)(stride / sx);
+    r = (int)(stride - (long long)si * sx);
+    sj = r / sy;
+    sk = r - sj * sy;
+  }
+  __device__ __forceinline__ void advance(int sy) {
+    k += sk;
+    if (k >= sy) { k -= sy; ++j; }
+    j += sj;
+    if (j >= rows) { j -= rows; ++i; }
+    i += si;
+  }
+};
+
+// One slab's correction of one H component (compile-time slab position S, component C).
+// Table per slab axis: x-slab Hy (Phi1, dEz/dx, +), Hz (Phi2, dEy/dx, -); y-slab Hx (Phi1,
+// dEz/dy, -), Hz (Phi2, dEx/dy, +); z-slab Hx (Phi1, dEy/dz, +), Hy (Phi2, dEx/dz, -).
+template <int PK, int S, int C>
+__device__ __forceinline__ float h_slab(float F, float c4, int pp, int i, int j, int k,
+                                        float dA, float dB, const StepParams& p) {
+  constexpr int AX = S % 3;
+  const Slab& sl = p.slab[S];
+  constexpr bool first = (AX == 0) ? (C == 1) : (C == 0);
+  constexpr float sgn = (AX == 0) ? (C == 1 ? 1.f : -1.f) : (AX == 1) ? (C == 0 ? -1.f : 1.f)
+                                                                      : (C == 0 ? 1.f : -1.f);
+  const float dF = first ? dA : dB;
+  const float X = pml_term<PK>(dF / sl.d, first ? sl.phiH1 : sl.phiH2,
+                               phi_index<AX>(i, j, k, pp, sl.T, p.ny, p.nz), sl.ocount, sl.hR,
+                               sl.T, pp);
+  return sgn > 0.f ? F + c4 * X : F - c4 * X;
+}
+
+// Magnetic sources at one node/component (sources.py:202-232, numpy-2 fp32 order).
+__device__ __forceinline__ float apply_h_sources(float F, int comp, int i, int j, int k, int it,
+                                                 float c4, const StepParams& p) {
+  for (int s = 0; s < p.nsrcH; ++s) {
+    const Src& q = p.srcH[s];
+    if (q.comp == comp && q.i == i && q.j == j && q.k == k && it >= q.first && it <= q.last)
+      F = __fsub_rn(F, __fmul_rn(__fmul_rn(c4, __ldg(q.w + it)), q.s0));
+  }
+  return F;
+}
+
+// H update of one node: main update (update_magnetic), slab corrections in slab order, sources.
+// px0/pxmax/py0/pymax are the node's x and y slab profile indices (-1 outside).
 template <int PK>
-__global__ void __launch_bounds__(kBX * kBY, 3)
+__device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, const float* Cs,
+                                       int i, int j, int k, bool src, int it, int px0, int pxmax,
+                                       int py0, int pymax, int pz0, int pzmax, float dEz_y,
+                                       float dEy_z, float dEx_z,
+                                       float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
+                                       uint32_t my, uint32_t mz, float& hx, float& hy, float& hz) {
+  const int nx = p.nx, ny = p.ny, nz = p.nz;
+  const bool iin = i < nx, jin = j < ny, kin = k < nz;
+  // every H slab range needs i < nx, j < ny and k < nz
+  const bool inpml = PK != PML_NONE && iin && jin && kin;
+  // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs y0, z0, ymax, zmax
+  {
+    const bool mainu = (i >= 1) && jin && kin;
+    const bool pml = inpml && (py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0);
+    if (mainu || pml || src) {
+      float F = hx;
+      if (mainu) {
+        const float4 c = C4[mx];
+        F = c.x * F - c.z * dEz_y + c.w * dEy_z;
+      }
+      if (PK != PML_NONE && pml) {
+        const float c4 = Cs[mx];
+        if (py0 >= 0) F = h_slab<PK, 1, 0>(F, c4, py0, i, j, k, dEz_y, dEx_y, p);
+        if (pz0 >= 0) F = h_slab<PK, 2, 0>(F, c4, pz0, i, j, k, dEy_z, dEx_z, p);
+        if (pymax >= 0) F = h_slab<PK, 4, 0>(F, c4, pymax, i, j, k, dEz_y, dEx_y, p);
+        if (pzmax >= 0) F = h_slab<PK, 5, 0>(F, c4, pzmax, i, j, k, dEy_z, dEx_z, p);
+      }
+      if (src) F = apply_h_sources(F, 3, i, j, k, it, Cs[mx], p);
+      hx = F;
+    }
+  }
+  // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs x0, z0, xmax, zmax
+  {
+    const bool mainu = iin && (j >= 1) && kin;
+    const bool pml = inpml && (px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0);
+    if (mainu || pml || src) {
+      float F = hy;
+      if (mainu) {
+        const float4 c = C4[my];
+        F = c.x * F - c.w * dEx_z + c.y * dEz_x;
+      }
+      if (PK != PML_NONE && pml) {
+        const float c4 = Cs[my];
+        if (px0 >= 0) F = h_slab<PK, 0, 1>(F, c4, px0, i, j, k, dEz_x, dEy_x, p);
+        if (pz0 >= 0) F = h_slab<PK, 2, 1>(F, c4, pz0, i, j, k, dEy_z, dEx_z, p);
+        if (pxmax >= 0) F = h_slab<PK, 3, 1>(F, c4, pxmax, i, j, k, dEz_x, dEy_x, p);
+        if (pzmax >= 0) F = h_slab<PK, 5, 1>(F, c4, pzmax, i, j, k, dEy_z, dEx_z, p);
+      }
+      if (src) F = apply_h_sources(F, 4, i, j, k, it, Cs[my], p);
+      hy = F;
+    }
+  }
+  // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs x0, y0, xmax, ymax
+  {
+    const bool mainu = iin && jin && (k >= 1);
+    const bool pml = inpml && (px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0);
+    if (mainu || pml || src) {
+      float F = hz;
+      if (mainu) {
+        const float4 c = C4[mz];
+        F = c.x * F - c.y * dEy_x + c.z * dEx_y;
+      }
+      if (PK != PML_NONE && pml) {
+        const float c4 = Cs[mz];
+        if (px0 >= 0) F = h_slab<PK, 0, 2>(F, c4, px0, i, j, k, dEz_x, dEy_x, p);
+        if (py0 >= 0) F = h_slab<PK, 1, 2>(F, c4, py0, i, j, k, dEz_y, dEx_y, p);
+        if (pxmax >= 0) F = h_slab<PK, 3, 2>(F, c4, pxmax, i, j, k, dEz_x, dEy_x, p);
+        if (pymax >= 0) F = h_slab<PK, 4, 2>(F, c4, pymax, i, j, k, dEz_y, dEx_y, p);
+      }
+      if (src) F = apply_h_sources(F, 5, i, j, k, it, Cs[mz], p);
+      hz = F;
+    }
+  }
+}
+
+// H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz] (every node of the arrays).
+template <int PK>
+__global__ void __launch_bounds__(kThreads, 3)
 h_half_step(const __grid_constant__ StepParams p) {
   extern __shared__ float4 smem_h[];
   float4* s4 = smem_h;
@@ -185,205 +317,56 @@ h_half_step(const __grid_constant__ StepParams p) {
   }
   const float4* C4 = p.smem ? s4 : p.cH4;
   const float* Cs = p.smem ? ss : p.cHs;
-  const int k = blockIdx.x * kBX + threadIdx.x;
-  const int j = blockIdx.y * kBY + threadIdx.y;
-  if (k > p.nz || j > p.ny) return;
-  const int nx = p.nx, ny = p.ny, nz = p.nz;
-  const int i0 = blockIdx.z * p.chunk;
-  const int i1 = min(i0 + p.chunk, nx + 1);
+  const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
   const float* __restrict__ Ex = p.E[0];
   const float* __restrict__ Ey = p.E[1];
   const float* __restrict__ Ez = p.E[2];
   float* __restrict__ Hx = p.H[0];
   float* __restrict__ Hy = p.H[1];
   float* __restrict__ Hz = p.H[2];
-  const bool jin = j < ny, kin = k < nz;
-
-  // PML membership fixed for this thread (y and z); every H slab range needs i < nx, j < ny
-  // and k < nz, so these also apply only on planes i < nx (checked per plane below)
-  int py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
-  if (PK != PML_NONE && jin && kin) {
-    py0 = slab_p<false>(j, p.slab[1].T, ny, true);
-    pymax = slab_p<false>(j, p.slab[4].T, ny, false);
-    pz0 = slab_p<false>(k, p.slab[2].T, nz, true);
-    pzmax = slab_p<false>(k, p.slab[5].T, nz, false);
-  }
-  // magnetic sources owned by this thread's (j, k) column
-  bool colsrc = false;
-  for (int s = 0; s < p.nsrcH; ++s) {
-    const Src& q = p.srcH[s];
-    if (q.j == j && q.k == k && q.i >= i0 && q.i < i1) colsrc = true;
-  }
-  const int it = colsrc ? *p.d_it : 0;
-
-  int idx = i0 * p.sx + j * p.sy + k;
-  float ey_c = __ldg(Ey + idx), ez_c = __ldg(Ez + idx);
-  for (int i = i0; i < i1; ++i, idx += p.sx) {
-    const float ex_c = __ldg(Ex + idx);
-    const float ex_j = jin ? __ldg(Ex + idx + p.sy) : 0.f;
-    const float ez_j = jin ? __ldg(Ez + idx + p.sy) : 0.f;
+  const long long total = (long long)(nx + 1) * sx;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  FlatWalk w(q, stride, sx, sy, ny + 1);
+  // interior box: nodes outside every H slab range (minus [0,T-1], plus [n-T, n-1])
+  const int xlo = p.slab[0].T, xhi = nx - p.slab[3].T;
+  const int ylo = p.slab[1].T, yhi = ny - p.slab[4].T;
+  const int zlo = p.slab[2].T, zhi = nz - p.slab[5].T;
+  int it = 0;
+  if (p.nsrcH) it = *p.d_it;
+  for (; q < total; q += stride, w.advance(sy)) {
+    const int idx = (int)q;
+    const int i = w.i, j = w.j, k = w.k;
+    const bool iin = i < nx, jin = j < ny, kin = k < nz;
+    // issue every load of the node before any store
+    const float ex_c = __ldg(Ex + idx), ey_c = __ldg(Ey + idx), ez_c = __ldg(Ez + idx);
+    const float ex_j = jin ? __ldg(Ex + idx + sy) : 0.f;
+    const float ez_j = jin ? __ldg(Ez + idx + sy) : 0.f;
     const float ex_k = kin ? __ldg(Ex + idx + 1) : 0.f;
     const float ey_k = kin ? __ldg(Ey + idx + 1) : 0.f;
-    float ey_n = 0.f, ez_n = 0.f;
-    if (i < nx) {
-      ey_n = __ldg(Ey + idx + p.sx);
-      ez_n = __ldg(Ez + idx + p.sx);
-    }
-    // every load of the plane is issued before any store, so they are all in flight together
-    const uint32_t mx = __ldg(p.ID[3] + idx);
-    const uint32_t my = __ldg(p.ID[4] + idx);
-    const uint32_t mz = __ldg(p.ID[5] + idx);
-    const float hx0 = Hx[idx], hy0 = Hy[idx], hz0 = Hz[idx];
-    const float dEz_y = ez_j - ez_c;   // Hx main and y-slab
-    const float dEy_z = ey_k - ey_c;   // Hx main and z-slab
-    const float dEx_z = ex_k - ex_c;   // Hy main and z-slab
-    const float dEz_x = ez_n - ez_c;   // Hy main and x-slab
-    const float dEy_x = ey_n - ey_c;   // Hz main and x-slab
-    const float dEx_y = ex_j - ex_c;   // Hz main and y-slab
-    int px0 = -1, pxmax = -1;
-    const bool iin = i < nx;
-    if (PK != PML_NONE && iin && jin && kin) {
+    const float ey_n = iin ? __ldg(Ey + idx + sx) : 0.f;
+    const float ez_n = iin ? __ldg(Ez + idx + sx) : 0.f;
+    const uint32_t mx = __ldg(p.ID[3] + idx), my = __ldg(p.ID[4] + idx), mz = __ldg(p.ID[5] + idx);
+    float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
+    int px0 = -1, pxmax = -1, py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
+    if (PK != PML_NONE && !(i >= xlo && i < xhi && j >= ylo && j < yhi && k >= zlo && k < zhi)) {
       px0 = slab_p<false>(i, p.slab[0].T, nx, true);
       pxmax = slab_p<false>(i, p.slab[3].T, nx, false);
+      py0 = slab_p<false>(j, p.slab[1].T, ny, true);
+      pymax = slab_p<false>(j, p.slab[4].T, ny, false);
+      pz0 = slab_p<false>(k, p.slab[2].T, nz, true);
+      pzmax = slab_p<false>(k, p.slab[5].T, nz, false);
     }
-    const bool src = colsrc;
-
-    // ---- Hx: main i in [1,nx], j in [0,ny), k in [0,nz); PML y-slabs (-, Phi1), z-slabs (+, Phi1)
-    {
-      const bool mainu = (i >= 1) && jin && kin;
-      // slab corrections cover i < nx only (the main update also covers i = nx)
-      const bool pml = PK != PML_NONE && iin &&
-                       (py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0);
-      if (mainu || pml || src) {
-        const uint32_t m = mx;
-        float F = hx0;
-        if (mainu) {
-          const float4 c = C4[m];
-          F = c.x * F - c.z * dEz_y + c.w * dEy_z;
-        }
-        if (PK != PML_NONE && pml) {
-          const float c4 = Cs[m];
-          if (py0 >= 0) {
-            const Slab& sl = p.slab[1];
-            const float X = pml_term<PK>(dEz_y / sl.d, sl.phiH1, phi_index<1>(i, j, k, py0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, py0);
-            F = F - c4 * X;
-          }
-          if (pz0 >= 0) {
-            const Slab& sl = p.slab[2];
-            const float X = pml_term<PK>(dEy_z / sl.d, sl.phiH1, phi_index<2>(i, j, k, pz0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pz0);
-            F = F + c4 * X;
-          }
-          if (pymax >= 0) {
-            const Slab& sl = p.slab[4];
-            const float X = pml_term<PK>(dEz_y / sl.d, sl.phiH1, phi_index<1>(i, j, k, pymax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pymax);
-            F = F - c4 * X;
-          }
-          if (pzmax >= 0) {
-            const Slab& sl = p.slab[5];
-            const float X = pml_term<PK>(dEy_z / sl.d, sl.phiH1, phi_index<2>(i, j, k, pzmax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pzmax);
-            F = F + c4 * X;
-          }
-        }
-        if (src) {
-          for (int s = 0; s < p.nsrcH; ++s) {
-            const Src& q = p.srcH[s];
-            if (q.comp == 3 && q.i == i && q.j == j && q.k == k && it >= q.first && it <= q.last)
-              F = __fsub_rn(F, __fmul_rn(__fmul_rn(Cs[m], __ldg(q.w + it)), q.s0));
-          }
-        }
-        Hx[idx] = F;
-      }
+    bool src = false;
+    for (int s = 0; s < p.nsrcH; ++s) {
+      const Src& qs = p.srcH[s];
+      if (qs.i == i && qs.j == j && qs.k == k) src = true;
     }
-    // ---- Hy: main i in [0,nx), j in [1,ny], k in [0,nz); PML x-slabs (+, Phi1), z-slabs (-, Phi2)
-    {
-      const bool mainu = iin && (j >= 1) && kin;
-      const bool pml = PK != PML_NONE && iin && (px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0);
-      if (mainu || pml || src) {
-        const uint32_t m = my;
-        float F = hy0;
-        if (mainu) {
-          const float4 c = C4[m];
-          F = c.x * F - c.w * dEx_z + c.y * dEz_x;
-        }
-        if (PK != PML_NONE && pml) {
-          const float c4 = Cs[m];
-          if (px0 >= 0) {
-            const Slab& sl = p.slab[0];
-            const float X = pml_term<PK>(dEz_x / sl.d, sl.phiH1, phi_index<0>(i, j, k, px0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, px0);
-            F = F + c4 * X;
-          }
-          if (pz0 >= 0) {
-            const Slab& sl = p.slab[2];
-            const float X = pml_term<PK>(dEx_z / sl.d, sl.phiH2, phi_index<2>(i, j, k, pz0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pz0);
-            F = F - c4 * X;
-          }
-          if (pxmax >= 0) {
-            const Slab& sl = p.slab[3];
-            const float X = pml_term<PK>(dEz_x / sl.d, sl.phiH1, phi_index<0>(i, j, k, pxmax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pxmax);
-            F = F + c4 * X;
-          }
-          if (pzmax >= 0) {
-            const Slab& sl = p.slab[5];
-            const float X = pml_term<PK>(dEx_z / sl.d, sl.phiH2, phi_index<2>(i, j, k, pzmax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pzmax);
-            F = F - c4 * X;
-          }
-        }
-        if (src) {
-          for (int s = 0; s < p.nsrcH; ++s) {
-            const Src& q = p.srcH[s];
-            if (q.comp == 4 && q.i == i && q.j == j && q.k == k && it >= q.first && it <= q.last)
-              F = __fsub_rn(F, __fmul_rn(__fmul_rn(Cs[m], __ldg(q.w + it)), q.s0));
-          }
-        }
-        Hy[idx] = F;
-      }
-    }
-    // ---- Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; PML x-slabs (-, Phi2), y-slabs (+, Phi2)
-    {
-      const bool mainu = iin && jin && (k >= 1);
-      const bool pml = PK != PML_NONE && iin && (px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0);
-      if (mainu || pml || src) {
-        const uint32_t m = mz;
-        float F = hz0;
-        if (mainu) {
-          const float4 c = C4[m];
-          F = c.x * F - c.y * dEy_x + c.z * dEx_y;
-        }
-        if (PK != PML_NONE && pml) {
-          const float c4 = Cs[m];
-          if (px0 >= 0) {
-            const Slab& sl = p.slab[0];
-            const float X = pml_term<PK>(dEy_x / sl.d, sl.phiH2, phi_index<0>(i, j, k, px0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, px0);
-            F = F - c4 * X;
-          }
-          if (py0 >= 0) {
-            const Slab& sl = p.slab[1];
-            const float X = pml_term<PK>(dEx_y / sl.d, sl.phiH2, phi_index<1>(i, j, k, py0, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, py0);
-            F = F + c4 * X;
-          }
-          if (pxmax >= 0) {
-            const Slab& sl = p.slab[3];
-            const float X = pml_term<PK>(dEy_x / sl.d, sl.phiH2, phi_index<0>(i, j, k, pxmax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pxmax);
-            F = F - c4 * X;
-          }
-          if (pymax >= 0) {
-            const Slab& sl = p.slab[4];
-            const float X = pml_term<PK>(dEx_y / sl.d, sl.phiH2, phi_index<1>(i, j, k, pymax, sl.T, ny, nz), sl.ocount, sl.hR, sl.T, pymax);
-            F = F + c4 * X;
-          }
-        }
-        if (src) {
-          for (int s = 0; s < p.nsrcH; ++s) {
-            const Src& q = p.srcH[s];
-            if (q.comp == 5 && q.i == i && q.j == j && q.k == k && it >= q.first && it <= q.last)
-              F = __fsub_rn(F, __fmul_rn(__fmul_rn(Cs[m], __ldg(q.w + it)), q.s0));
-          }
-        }
-        Hz[idx] = F;
-      }
-    }
-    ey_c = ey_n;
-    ez_c = ez_n;
+    h_node<PK>(p, C4, Cs, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, ez_j - ez_c, ey_k - ey_c,
+               ex_k - ex_c, ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
+    Hx[idx] = hx;
+    Hy[idx] = hy;
+    Hz[idx] = hz;
   }
 }
 
@@ -426,9 +409,96 @@ __device__ __forceinline__ float e_slab(float F, float c4, int pp, int i, int j,
   return sgn > 0.f ? F + c4 * X : F - c4 * X;
 }
 
+// E update of one node for all three components: main update (update_electric, or part A of
+// the dispersive update), slab corrections in slab order, sources, dispersive part B.
+template <int PK, int NP>
+__device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
+                                       const float2* CD, int i, int j, int k, bool src, int it,
+                                       int px0, int pxmax, int py0, int pymax, int pz0,
+                                       int pzmax, float dHz_y,
+                                       float dHy_z, float dHx_z, float dHz_x, float dHy_x,
+                                       float dHx_y, const uint32_t* m, float* e, float2 (*t)[NP > 0 ? NP : 1]) {
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    bool mainu, pml;
+    if (comp == 0) {
+      mainu = (j >= 1) && (k >= 1);
+      pml = py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0;
+    } else if (comp == 1) {
+      mainu = (i >= 1) && (k >= 1);
+      pml = px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0;
+    } else {
+      mainu = (i >= 1) && (j >= 1);
+      pml = px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0;
+    }
+    if (PK == PML_NONE) pml = false;
+    if (!(mainu || pml || src)) continue;
+    const uint32_t mm = m[comp];
+    const float Eold = e[comp];
+    float F = Eold;
+    float2 TA[NP > 0 ? NP : 1];
+    if (mainu) {
+      // curl terms in the reference's order: CA*E + CB1*d1 - CB2*d2
+      const float4 c = C4[mm];
+      float t1, t2;
+      if (comp == 0) { t1 = c.z * dHz_y; t2 = c.w * dHy_z; }
+      else if (comp == 1) { t1 = c.w * dHx_z; t2 = c.y * dHz_x; }
+      else { t1 = c.y * dHy_x; t2 = c.z * dHx_y; }
+      if (NP == 0) {
+        F = c.x * Eold + t1 - t2;
+      } else {
+        float phi = 0.f;
+        const float2* cd = CD + mm * 3 * NP;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          const float2 Tq = t[comp][q];
+          const float2 a = cd[3 * q + 0];
+          const float2 b = cd[3 * q + 1];
+          const float2 z = cd[3 * q + 2];
+          phi = phi + a.x * Tq.x;
+          TA[q].x = (b.x * Tq.x - b.y * Tq.y) + z.x * Eold;
+          TA[q].y = (b.x * Tq.y + b.y * Tq.x) + z.y * Eold;
+        }
+        F = c.x * Eold + t1 - t2 - Cs[mm] * phi;
+      }
+    }
+    if (PK != PML_NONE && pml) {
+      const float c4 = Cs[mm];
+      // slab order x0, y0, z0, xmax, ymax, zmax; a component is tangential to two axes
+      if (comp == 0) {
+        if (py0 >= 0) F = e_slab<PK, 1, 0>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
+        if (pz0 >= 0) F = e_slab<PK, 2, 0>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
+        if (pymax >= 0) F = e_slab<PK, 4, 0>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
+        if (pzmax >= 0) F = e_slab<PK, 5, 0>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
+      } else if (comp == 1) {
+        if (px0 >= 0) F = e_slab<PK, 0, 1>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
+        if (pz0 >= 0) F = e_slab<PK, 2, 1>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
+        if (pxmax >= 0) F = e_slab<PK, 3, 1>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
+        if (pzmax >= 0) F = e_slab<PK, 5, 1>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
+      } else {
+        if (px0 >= 0) F = e_slab<PK, 0, 2>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
+        if (py0 >= 0) F = e_slab<PK, 1, 2>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
+        if (pxmax >= 0) F = e_slab<PK, 3, 2>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
+        if (pymax >= 0) F = e_slab<PK, 4, 2>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
+      }
+    }
+    if (src) F = apply_e_sources(F, comp, i, j, k, it, Cs[mm], p);
+    e[comp] = F;
+    if (NP > 0 && mainu) {
+      const float2* cd = CD + mm * 3 * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float2 z = cd[3 * q + 2];
+        t[comp][q].x = TA[q].x - z.x * F;
+        t[comp][q].y = TA[q].y - z.y * F;
+      }
+    }
+  }
+}
+
 // E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz). NP = dispersive poles.
 template <int PK, int NP>
-__global__ void __launch_bounds__(kBX * kBY, 3)
+__global__ void __launch_bounds__(kThreads, 3)
 e_half_step(const __grid_constant__ StepParams p) {
   extern __shared__ float4 smem_e[];
   float4* s4 = smem_e;
@@ -441,148 +511,65 @@ e_half_step(const __grid_constant__ StepParams p) {
   const float4* C4 = p.smem ? s4 : p.cE4;
   const float* Cs = p.smem ? ss : p.cEs;
   const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
-  const int k = blockIdx.x * kBX + threadIdx.x;
-  const int j = blockIdx.y * kBY + threadIdx.y;
-  if (k >= p.nz || j >= p.ny) return;
-  const int nx = p.nx, ny = p.ny, nz = p.nz;
-  const int i0 = blockIdx.z * p.chunk;
-  const int i1 = min(i0 + p.chunk, nx);
+  const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
   const float* __restrict__ Hx = p.H[0];
   const float* __restrict__ Hy = p.H[1];
   const float* __restrict__ Hz = p.H[2];
-
-  int py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
-  if (PK != PML_NONE) {
-    py0 = slab_p<true>(j, p.slab[1].T, ny, true);
-    pymax = slab_p<true>(j, p.slab[4].T, ny, false);
-    pz0 = slab_p<true>(k, p.slab[2].T, nz, true);
-    pzmax = slab_p<true>(k, p.slab[5].T, nz, false);
-  }
-  bool colsrc = false;
-  for (int s = 0; s < p.nsrcE; ++s) {
-    const Src& q = p.srcE[s];
-    if (q.j == j && q.k == k && q.i >= i0 && q.i < i1) colsrc = true;
-  }
-  const int it = colsrc ? *p.d_it : 0;
-
-  int idx = i0 * p.sx + j * p.sy + k;
-  float hy_p = 0.f, hz_p = 0.f;   // H of plane i-1
-  if (i0 >= 1) {
-    hy_p = __ldg(Hy + idx - p.sx);
-    hz_p = __ldg(Hz + idx - p.sx);
-  }
-  for (int i = i0; i < i1; ++i, idx += p.sx) {
+  constexpr int NPV = NP > 0 ? NP : 1;
+  const long long total = (long long)nx * sx;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  FlatWalk w(q, stride, sx, sy, ny + 1);
+  // interior box: nodes outside every E slab range (minus [1,T], plus [n-T, n-1])
+  const int xlo = p.slab[0].T, xhi = nx - p.slab[3].T;
+  const int ylo = p.slab[1].T, yhi = ny - p.slab[4].T;
+  const int zlo = p.slab[2].T, zhi = nz - p.slab[5].T;
+  int it = 0;
+  if (p.nsrcE) it = *p.d_it;
+  for (; q < total; q += stride, w.advance(sy)) {
+    const int idx = (int)q;
+    const int i = w.i, j = w.j, k = w.k;
+    if (j >= ny || k >= nz) continue;
+    // issue every load of the node before any store
     const float hx_c = __ldg(Hx + idx), hy_c = __ldg(Hy + idx), hz_c = __ldg(Hz + idx);
-    float hx_j = 0.f, hz_j = 0.f, hx_k = 0.f, hy_k = 0.f;
-    if (j >= 1) { hx_j = __ldg(Hx + idx - p.sy); hz_j = __ldg(Hz + idx - p.sy); }
-    if (k >= 1) { hx_k = __ldg(Hx + idx - 1); hy_k = __ldg(Hy + idx - 1); }
-    const float dHz_y = hz_c - hz_j;   // Ex main and y-slab
-    const float dHy_z = hy_c - hy_k;   // Ex main and z-slab
-    const float dHx_z = hx_c - hx_k;   // Ey main and z-slab
-    const float dHz_x = hz_c - hz_p;   // Ey main and x-slab
-    const float dHy_x = hy_c - hy_p;   // Ez main and x-slab
-    const float dHx_y = hx_c - hx_j;   // Ez main and y-slab
-    int px0 = -1, pxmax = -1;
-    if (PK != PML_NONE) {
+    const float hx_j = j >= 1 ? __ldg(Hx + idx - sy) : 0.f;
+    const float hz_j = j >= 1 ? __ldg(Hz + idx - sy) : 0.f;
+    const float hx_k = k >= 1 ? __ldg(Hx + idx - 1) : 0.f;
+    const float hy_k = k >= 1 ? __ldg(Hy + idx - 1) : 0.f;
+    const float hy_p = i >= 1 ? __ldg(Hy + idx - sx) : 0.f;
+    const float hz_p = i >= 1 ? __ldg(Hz + idx - sx) : 0.f;
+    uint32_t m[3];
+    float e[3];
+    float2 t[3][NPV];
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+      m[comp] = __ldg(p.ID[comp] + idx);
+      e[comp] = p.E[comp][idx];
+#pragma unroll
+      for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
+    }
+    int px0 = -1, pxmax = -1, py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
+    if (PK != PML_NONE && !(i > xlo && i < xhi && j > ylo && j < yhi && k > zlo && k < zhi)) {
       px0 = slab_p<true>(i, p.slab[0].T, nx, true);
       pxmax = slab_p<true>(i, p.slab[3].T, nx, false);
+      py0 = slab_p<true>(j, p.slab[1].T, ny, true);
+      pymax = slab_p<true>(j, p.slab[4].T, ny, false);
+      pz0 = slab_p<true>(k, p.slab[2].T, nz, true);
+      pzmax = slab_p<true>(k, p.slab[5].T, nz, false);
     }
-    const bool src = colsrc;
-    // every load of the plane is issued before any store, so they are all in flight together
-    uint32_t mm[3];
-    float eold[3];
-    float2 tt[3][NP > 0 ? NP : 1];
+    bool src = false;
+    for (int s = 0; s < p.nsrcE; ++s) {
+      const Src& qs = p.srcE[s];
+      if (qs.i == i && qs.j == j && qs.k == k) src = true;
+    }
+    e_node<PK, NP>(p, C4, Cs, CD, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, hz_c - hz_j,
+                   hy_c - hy_k, hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-      mm[comp] = __ldg(p.ID[comp] + idx);
-      eold[comp] = p.E[comp][idx];
+      p.E[comp][idx] = e[comp];
 #pragma unroll
-      for (int q = 0; q < NP; ++q)
-        tt[comp][q] = p.T[(comp * NP + q) * (long long)p.ncomp + idx];
+      for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
     }
-
-#pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-      bool mainu, pml;
-      if (comp == 0) {
-        mainu = (j >= 1) && (k >= 1);
-        pml = py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0;
-      } else if (comp == 1) {
-        mainu = (i >= 1) && (k >= 1);
-        pml = px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0;
-      } else {
-        mainu = (i >= 1) && (j >= 1);
-        pml = px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0;
-      }
-      if (PK == PML_NONE) pml = false;
-      if (!(mainu || pml || src)) continue;
-      float* __restrict__ E = p.E[comp];
-      const uint32_t m = mm[comp];
-      const float Eold = eold[comp];
-      float F = Eold;
-      float2 TA[NP > 0 ? NP : 1];
-      if (mainu) {
-        // curl terms in the reference's order: CA*E + CB1*d1 - CB2*d2
-        const float4 c = C4[m];
-        float t1, t2;
-        if (comp == 0) { t1 = c.z * dHz_y; t2 = c.w * dHy_z; }
-        else if (comp == 1) { t1 = c.w * dHx_z; t2 = c.y * dHz_x; }
-        else { t1 = c.y * dHy_x; t2 = c.z * dHx_y; }
-        if (NP == 0) {
-          F = c.x * Eold + t1 - t2;
-        } else {
-          float phi = 0.f;
-          const float2* cd = CD + m * 3 * NP;
-#pragma unroll
-          for (int q = 0; q < NP; ++q) {
-            const float2 Tq = tt[comp][q];
-            const float2 a = cd[3 * q + 0];
-            const float2 b = cd[3 * q + 1];
-            const float2 z = cd[3 * q + 2];
-            phi = phi + a.x * Tq.x;
-            TA[q].x = (b.x * Tq.x - b.y * Tq.y) + z.x * Eold;
-            TA[q].y = (b.x * Tq.y + b.y * Tq.x) + z.y * Eold;
-          }
-          F = c.x * Eold + t1 - t2 - Cs[m] * phi;
-        }
-      }
-      if (PK != PML_NONE && pml) {
-        const float c4 = Cs[m];
-        // slab order x0, y0, z0, xmax, ymax, zmax; a component is tangential to two axes
-        if (comp == 0) {
-          if (py0 >= 0) F = e_slab<PK, 1, 0>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
-          if (pz0 >= 0) F = e_slab<PK, 2, 0>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
-          if (pymax >= 0) F = e_slab<PK, 4, 0>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
-          if (pzmax >= 0) F = e_slab<PK, 5, 0>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
-        } else if (comp == 1) {
-          if (px0 >= 0) F = e_slab<PK, 0, 1>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
-          if (pz0 >= 0) F = e_slab<PK, 2, 1>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
-          if (pxmax >= 0) F = e_slab<PK, 3, 1>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
-          if (pzmax >= 0) F = e_slab<PK, 5, 1>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
-        } else {
-          if (px0 >= 0) F = e_slab<PK, 0, 2>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
-          if (py0 >= 0) F = e_slab<PK, 1, 2>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
-          if (pxmax >= 0) F = e_slab<PK, 3, 2>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
-          if (pymax >= 0) F = e_slab<PK, 4, 2>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
-        }
-      }
-      if (src) F = apply_e_sources(F, comp, i, j, k, it, Cs[m], p);
-      E[idx] = F;
-      if (NP > 0 && mainu) {
-        const float2* cd = CD + m * 3 * NP;
-        float2* Tc = p.T + (comp * NP) * (long long)p.ncomp + idx;
-#pragma unroll
-        for (int q = 0; q < NP; ++q) {
-          const float2 z = cd[3 * q + 2];
-          float2 o;
-          o.x = TA[q].x - z.x * F;
-          o.y = TA[q].y - z.y * F;
-          Tc[q * (long long)p.ncomp] = o;
-        }
-      }
-    }
-    hy_p = hy_c;
-    hz_p = hz_c;
   }
 }
 

@@ -52,6 +52,7 @@ struct gbf_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
+  int grid_h = 0, grid_e = 0;  // persistent grid sizes
 };
 
 static std::string g_create_err;
@@ -441,18 +442,31 @@ static EKern pick_e(int pk, int np) {
   }
 }
 
+// Persistent grid: as many blocks as fit on the device at once (at least one per SM).
+static int persistent_blocks(const void* kern, size_t smem) {
+  int dev = 0, sms = 1, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem);
+  return sms * (per > 0 ? per : 1);
+}
+
 static void launch_h(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
-  dim3 block(kBX, kBY);
-  dim3 grid((p.nz + 1 + kBX - 1) / kBX, (p.ny + 1 + kBY - 1) / kBY, (p.nx + 1 + p.chunk - 1) / p.chunk);
-  pick_h(pml_kind(ctx->d))<<<grid, block, ctx->smem_h, ctx->stream>>>(p);
+  HKern kern = pick_h(pml_kind(ctx->d));
+  if (!ctx->grid_h) ctx->grid_h = persistent_blocks((const void*)kern, ctx->smem_h);
+  dim3 block(kThreads);
+  dim3 grid(ctx->grid_h);
+  kern<<<grid, block, ctx->smem_h, ctx->stream>>>(p);
 }
 
 static void launch_e(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
-  dim3 block(kBX, kBY);
-  dim3 grid((p.nz + kBX - 1) / kBX, (p.ny + kBY - 1) / kBY, (p.nx + p.chunk - 1) / p.chunk);
-  pick_e(pml_kind(ctx->d), ctx->d.maxpoles)<<<grid, block, ctx->smem_e, ctx->stream>>>(p);
+  EKern kern = pick_e(pml_kind(ctx->d), ctx->d.maxpoles);
+  if (!ctx->grid_e) ctx->grid_e = persistent_blocks((const void*)kern, ctx->smem_e);
+  dim3 block(kThreads);
+  dim3 grid(ctx->grid_e);
+  kern<<<grid, block, ctx->smem_e, ctx->stream>>>(p);
 }
 
 static void launch_end(gbf_ctx* ctx) {
