@@ -11,7 +11,8 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
-SOURCES = ['gbfdtd.cu', 'fdtd_kernels.cuh']
+SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fdtd_kernels.cuh']
+PML_KINDS = 5   # kernels_inst.cu is compiled once per PML kind
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # --fmad=false: every product and sum is rounded as written, which makes the GPU results
@@ -38,10 +39,31 @@ def _stale():
 
 
 def build(force=False, verbose=False):
-    """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources."""
+    """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources.
+
+    The main translation unit and one kernel-instantiation unit per PML kind are compiled in
+    parallel, then linked."""
     if not force and not _stale():
         return LIBPATH
-    cmd = [_nvcc()] + ARCH + NVCC_FLAGS + [os.path.join(CSRC, 'gbfdtd.cu'), '-o', LIBPATH + '.tmp']
+    from concurrent.futures import ThreadPoolExecutor
+    objdir = os.path.join(CSRC, '_build')
+    os.makedirs(objdir, exist_ok=True)
+    compile_flags = [f for f in NVCC_FLAGS if f != '-shared']
+    jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), [])]
+    for pk in range(PML_KINDS):
+        jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
+                     os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
+
+    def compile_one(job):
+        src, obj, extra = job
+        cmd = [_nvcc()] + ARCH + compile_flags + extra + ['-c', src, '-o', obj]
+        if verbose:
+            print(' '.join(cmd))
+        subprocess.run(cmd, check=True, cwd=CSRC)
+        return obj
+    with ThreadPoolExecutor(len(jobs)) as ex:
+        objs = list(ex.map(compile_one, jobs))
+    cmd = [_nvcc()] + ARCH + ['-shared'] + objs + ['-o', LIBPATH + '.tmp']
     if verbose:
         print(' '.join(cmd))
     subprocess.run(cmd, check=True, cwd=CSRC)

@@ -28,6 +28,10 @@
 namespace gbf {
 
 constexpr int kThreads = 256;   // threads per block of the half-step kernels
+constexpr int kSrcInline = 8;   // sources whose node index travels in the kernel parameters
+constexpr int kPackBits = 10;   // bits per material ID in a packed word (IDs < 1024)
+constexpr uint32_t kPackMask = (1u << kPackBits) - 1u;
+constexpr uint32_t kDispersiveBit = 1u << 30;
 constexpr int kMaxPoles = 4;
 constexpr int kSmemCoefMax = 2048;   // materials staged in shared memory
 
@@ -47,6 +51,16 @@ struct Slab {
   const float* hR;  // same for H
 };
 
+struct StepParams;
+typedef void (*HKernFn)(StepParams);
+typedef void (*EKernFn)(StepParams);
+// per-kind kernel tables (kernels_inst.cu, one object per PML kind)
+void kernels_pk0(int np, int idp, HKernFn* h, EKernFn* e);
+void kernels_pk1(int np, int idp, HKernFn* h, EKernFn* e);
+void kernels_pk2(int np, int idp, HKernFn* h, EKernFn* e);
+void kernels_pk3(int np, int idp, HKernFn* h, EKernFn* e);
+void kernels_pk4(int np, int idp, HKernFn* h, EKernFn* e);
+
 struct Src {
   int kind, comp, i, j, k, first, last, pad;
   float s0, s1;
@@ -57,6 +71,8 @@ struct StepParams {
   float* E[3];
   float* H[3];
   const uint32_t* ID[6];  // per component [ncomp]
+  const uint32_t* PE;     // packed E IDs per node: x | y << 10 | z << 20 | dispersive << 30
+  const uint32_t* PH;     // packed H IDs per node: x | y << 10 | z << 20
   int ncomp;              // nodes per component (< 2^31)
   int nx, ny, nz;
   int sy, sx;             // strides: j -> nz+1, i -> (ny+1)(nz+1)
@@ -73,6 +89,8 @@ struct StepParams {
   int nsrcE, nsrcH;
   const Src* srcE;
   const Src* srcH;
+  int srcqE[kSrcInline];  // flat node index of the first sources (lets a node test itself cheaply)
+  int srcqH[kSrcInline];
   const int* d_it;
   int chunk;              // x planes per block
 };
@@ -226,6 +244,20 @@ __device__ __forceinline__ float apply_h_sources(float F, int comp, int i, int j
   return F;
 }
 
+// Does any source sit on flat node `idx`? The first kSrcInline sources are tested from the
+// kernel parameters; further ones from their list.
+__device__ __forceinline__ bool node_has_source(int idx, int n, const int* inl, const Src* list,
+                                                int sx, int sy) {
+  bool hit = false;
+  const int m = n < kSrcInline ? n : kSrcInline;
+  for (int s = 0; s < m; ++s) hit |= (inl[s] == idx);
+  for (int s = kSrcInline; s < n; ++s) {
+    const Src& q = list[s];
+    hit |= (q.i * sx + q.j * sy + q.k == idx);
+  }
+  return hit;
+}
+
 // H update of one node: main update (update_magnetic), slab corrections in slab order, sources.
 // px0/pxmax/py0/pymax are the node's x and y slab profile indices (-1 outside).
 template <int PK>
@@ -305,8 +337,8 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
 }
 
 // H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz] (every node of the arrays).
-template <int PK>
-__global__ void __launch_bounds__(kThreads, 3)
+template <int PK, int IDP>
+__global__ void __launch_bounds__(kThreads, 5)
 h_half_step(const __grid_constant__ StepParams p) {
   extern __shared__ float4 smem_h[];
   float4* s4 = smem_h;
@@ -346,7 +378,17 @@ h_half_step(const __grid_constant__ StepParams p) {
     const float ey_k = kin ? __ldg(Ey + idx + 1) : 0.f;
     const float ey_n = iin ? __ldg(Ey + idx + sx) : 0.f;
     const float ez_n = iin ? __ldg(Ez + idx + sx) : 0.f;
-    const uint32_t mx = __ldg(p.ID[3] + idx), my = __ldg(p.ID[4] + idx), mz = __ldg(p.ID[5] + idx);
+    uint32_t mx, my, mz;
+    if (IDP == 1) {
+      const uint32_t w = __ldg(p.PH + idx);
+      mx = w & kPackMask;
+      my = (w >> kPackBits) & kPackMask;
+      mz = (w >> (2 * kPackBits)) & kPackMask;
+    } else {
+      mx = __ldg(p.ID[3] + idx);
+      my = __ldg(p.ID[4] + idx);
+      mz = __ldg(p.ID[5] + idx);
+    }
     float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
     int px0 = -1, pxmax = -1, py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
     if (PK != PML_NONE && !(i >= xlo && i < xhi && j >= ylo && j < yhi && k >= zlo && k < zhi)) {
@@ -357,11 +399,7 @@ h_half_step(const __grid_constant__ StepParams p) {
       pz0 = slab_p<false>(k, p.slab[2].T, nz, true);
       pzmax = slab_p<false>(k, p.slab[5].T, nz, false);
     }
-    bool src = false;
-    for (int s = 0; s < p.nsrcH; ++s) {
-      const Src& qs = p.srcH[s];
-      if (qs.i == i && qs.j == j && qs.k == k) src = true;
-    }
+    const bool src = p.nsrcH && node_has_source(idx, p.nsrcH, p.srcqH, p.srcH, sx, sy);
     h_node<PK>(p, C4, Cs, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, ez_j - ez_c, ey_k - ey_c,
                ex_k - ex_c, ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
     Hx[idx] = hx;
@@ -497,8 +535,8 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
 }
 
 // E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz). NP = dispersive poles.
-template <int PK, int NP>
-__global__ void __launch_bounds__(kThreads, 3)
+template <int PK, int NP, int IDP>
+__global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
 e_half_step(const __grid_constant__ StepParams p) {
   extern __shared__ float4 smem_e[];
   float4* s4 = smem_e;
@@ -541,9 +579,22 @@ e_half_step(const __grid_constant__ StepParams p) {
     uint32_t m[3];
     float e[3];
     float2 t[3][NPV];
+    // dispersive state is identically zero on nodes whose materials have no poles (their
+    // coefficients are all zero), so it is not written there; it is still read with the
+    // node's other loads, which keeps those loads independent of the ID load
+    bool disp = NP > 0;
+    if (IDP == 1) {
+      const uint32_t w = __ldg(p.PE + idx);
+      m[0] = w & kPackMask;
+      m[1] = (w >> kPackBits) & kPackMask;
+      m[2] = (w >> (2 * kPackBits)) & kPackMask;
+      disp = NP > 0 && (w & kDispersiveBit);
+    } else {
+#pragma unroll
+      for (int comp = 0; comp < 3; ++comp) m[comp] = __ldg(p.ID[comp] + idx);
+    }
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-      m[comp] = __ldg(p.ID[comp] + idx);
       e[comp] = p.E[comp][idx];
 #pragma unroll
       for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
@@ -557,22 +608,21 @@ e_half_step(const __grid_constant__ StepParams p) {
       pz0 = slab_p<true>(k, p.slab[2].T, nz, true);
       pzmax = slab_p<true>(k, p.slab[5].T, nz, false);
     }
-    bool src = false;
-    for (int s = 0; s < p.nsrcE; ++s) {
-      const Src& qs = p.srcE[s];
-      if (qs.i == i && qs.j == j && qs.k == k) src = true;
-    }
+    const bool src = p.nsrcE && node_has_source(idx, p.nsrcE, p.srcqE, p.srcE, sx, sy);
     e_node<PK, NP>(p, C4, Cs, CD, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, hz_c - hz_j,
                    hy_c - hy_k, hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
       p.E[comp][idx] = e[comp];
+      if (disp) {
 #pragma unroll
-      for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
+        for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
+      }
     }
   }
 }
 
+#ifndef GBF_KERNELS_ONLY
 // ---------------------------------------------------------------------------------------
 // End of an iteration: electric sources on nodes outside the E kernel's domain, then the
 // receiver samples that the next iteration starts from (fields_outputs.py:40-67, grid.py:
@@ -665,4 +715,18 @@ __global__ void snapshot_store(const __grid_constant__ StepParams p, const SnapP
   }
 }
 
+// Packed per-node material words for the half-step kernels (IDs < 1024): E word holds the Ex,
+// Ey, Ez IDs and a flag that one of them has dispersive poles; H word the Hx, Hy, Hz IDs.
+__global__ void pack_ids(const __grid_constant__ StepParams p, const unsigned char* dispersive,
+                         uint32_t* pe, uint32_t* ph) {
+  const int n = p.ncomp;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const uint32_t ex = p.ID[0][q], ey = p.ID[1][q], ez = p.ID[2][q];
+    uint32_t w = ex | (ey << kPackBits) | (ez << (2 * kPackBits));
+    if (dispersive && (dispersive[ex] | dispersive[ey] | dispersive[ez])) w |= kDispersiveBit;
+    pe[q] = w;
+    ph[q] = p.ID[3][q] | (p.ID[4][q] << kPackBits) | (p.ID[5][q] << (2 * kPackBits));
+  }
+}
+#endif  // GBF_KERNELS_ONLY
 }  // namespace gbf

@@ -28,6 +28,10 @@ struct gbf_ctx {
   long long ncomp = 0;
   float* fields = nullptr;     // 6 * ncomp
   uint32_t* ID = nullptr;      // 6 * ncomp
+  uint32_t* PE = nullptr;      // packed E IDs (ncomp), when nmat <= 1024
+  uint32_t* PH = nullptr;      // packed H IDs
+  unsigned char* disp = nullptr;   // per material: has dispersive poles
+  int idp = 3;                 // 1: packed IDs, 3: three ID arrays per half-step
   float4* cE4 = nullptr;       // [nmat] CA, CBx, CBy, CBz
   float* cEs = nullptr;        // [nmat] srce
   float4* cH4 = nullptr;
@@ -115,7 +119,7 @@ void gbf_destroy(gbf_ctx* ctx) {
   if (!ctx) return;
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  void* ptrs[] = {ctx->fields, ctx->ID, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
+  void* ptrs[] = {ctx->fields, ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
                   ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -162,6 +166,12 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   auto A = [&](void** p, size_t n) { if (rc == GBF_OK) rc = dev_alloc(ctx, p, n); };
   A((void**)&ctx->fields, sizeof(float) * 6 * npts);
   A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
+  if (d.nmat <= 1024) {
+    ctx->idp = 1;
+    A((void**)&ctx->PE, sizeof(uint32_t) * npts);
+    A((void**)&ctx->PH, sizeof(uint32_t) * npts);
+  }
+  A((void**)&ctx->disp, (size_t)d.nmat);
   A((void**)&ctx->cE4, sizeof(float4) * d.nmat);
   A((void**)&ctx->cEs, sizeof(float) * d.nmat);
   A((void**)&ctx->cH4, sizeof(float4) * d.nmat);
@@ -201,6 +211,9 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     p.H[c] = ctx->fields + (3 + c) * npts;
   }
   for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID + c * npts;
+  p.PE = ctx->PE;
+  p.PH = ctx->PH;
+  for (int q = 0; q < kSrcInline; ++q) p.srcqE[q] = p.srcqH[q] = -1;
   p.ncomp = (int)npts;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.sy = d.nz + 1;
@@ -281,9 +294,20 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   CK(cudaMemcpyAsync(ctx->cEs, es.data(), sizeof(float) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->cH4, h4.data(), sizeof(float4) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->cHs, hs.data(), sizeof(float) * nmat, cudaMemcpyHostToDevice, ctx->stream));
-  if (ctx->d.maxpoles > 0)
+  std::vector<unsigned char> disp(nmat, 0);
+  if (ctx->d.maxpoles > 0) {
     CK(cudaMemcpyAsync(ctx->cD, coeffD, sizeof(float2) * 3 * ctx->d.maxpoles * nmat,
                        cudaMemcpyHostToDevice, ctx->stream));
+    for (int m = 0; m < nmat; ++m)
+      for (int q = 0; q < 6 * ctx->d.maxpoles; ++q)
+        if (coeffD[(size_t)m * 6 * ctx->d.maxpoles + q] != 0.f) disp[m] = 1;
+  }
+  CK(cudaMemcpyAsync(ctx->disp, disp.data(), nmat, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->idp == 1) {
+    pack_ids<<<1024, 256, 0, ctx->stream>>>(ctx->sp, ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
+                                           ctx->PE, ctx->PH);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->materials = true;
   return GBF_OK;
@@ -342,6 +366,11 @@ int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, co
                      cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   invalidate_graph(ctx);
+  for (int q = 0; q < kSrcInline; ++q) ctx->sp.srcqE[q] = ctx->sp.srcqH[q] = -1;
+  for (size_t q = 0; q < inE.size() && q < (size_t)kSrcInline; ++q)
+    ctx->sp.srcqE[q] = inE[q].i * ctx->sp.sx + inE[q].j * ctx->sp.sy + inE[q].k;
+  for (size_t q = 0; q < inH.size() && q < (size_t)kSrcInline; ++q)
+    ctx->sp.srcqH[q] = inH[q].i * ctx->sp.sx + inH[q].j * ctx->sp.sy + inH[q].k;
   ctx->sp.nsrcE = (int)inE.size();
   ctx->sp.srcE = ctx->srcs;
   ctx->sp.nsrcH = (int)inH.size();
@@ -408,37 +437,17 @@ int gbf_reset(gbf_ctx* ctx) {
 }  // extern "C"
 
 // ---- launch helpers ------------------------------------------------------------------
-typedef void (*HKern)(StepParams);
-typedef void (*EKern)(StepParams);
+typedef HKernFn HKern;
+typedef EKernFn EKern;
 
-static HKern pick_h(int pk) {
-  switch (pk) {
-    case PML_HORI1: return h_half_step<PML_HORI1>;
-    case PML_HORI2: return h_half_step<PML_HORI2>;
-    case PML_MRI1: return h_half_step<PML_MRI1>;
-    case PML_MRI2: return h_half_step<PML_MRI2>;
-    default: return h_half_step<PML_NONE>;
-  }
-}
-
-template <int PK>
-static EKern pick_e_np(int np) {
-  switch (np) {
-    case 1: return e_half_step<PK, 1>;
-    case 2: return e_half_step<PK, 2>;
-    case 3: return e_half_step<PK, 3>;
-    case 4: return e_half_step<PK, 4>;
-    default: return e_half_step<PK, 0>;
-  }
-}
-
-static EKern pick_e(int pk, int np) {
-  switch (pk) {
-    case PML_HORI1: return pick_e_np<PML_HORI1>(np);
-    case PML_HORI2: return pick_e_np<PML_HORI2>(np);
-    case PML_MRI1: return pick_e_np<PML_MRI1>(np);
-    case PML_MRI2: return pick_e_np<PML_MRI2>(np);
-    default: return pick_e_np<PML_NONE>(np);
+static void pick_kernels(gbf_ctx* ctx, HKern* h, EKern* e) {
+  const int np = ctx->d.maxpoles, idp = ctx->idp;
+  switch (pml_kind(ctx->d)) {
+    case PML_HORI1: kernels_pk1(np, idp, h, e); break;
+    case PML_HORI2: kernels_pk2(np, idp, h, e); break;
+    case PML_MRI1: kernels_pk3(np, idp, h, e); break;
+    case PML_MRI2: kernels_pk4(np, idp, h, e); break;
+    default: kernels_pk0(np, idp, h, e); break;
   }
 }
 
@@ -453,7 +462,9 @@ static int persistent_blocks(const void* kern, size_t smem) {
 
 static void launch_h(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
-  HKern kern = pick_h(pml_kind(ctx->d));
+  HKern kern;
+  EKern ek;
+  pick_kernels(ctx, &kern, &ek);
   if (!ctx->grid_h) ctx->grid_h = persistent_blocks((const void*)kern, ctx->smem_h);
   dim3 block(kThreads);
   dim3 grid(ctx->grid_h);
@@ -462,7 +473,9 @@ static void launch_h(gbf_ctx* ctx) {
 
 static void launch_e(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
-  EKern kern = pick_e(pml_kind(ctx->d), ctx->d.maxpoles);
+  HKern hk;
+  EKern kern;
+  pick_kernels(ctx, &hk, &kern);
   if (!ctx->grid_e) ctx->grid_e = persistent_blocks((const void*)kern, ctx->smem_e);
   dim3 block(kThreads);
   dim3 grid(ctx->grid_e);

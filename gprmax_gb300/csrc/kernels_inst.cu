@@ -1,0 +1,37 @@
+// kernels_inst.cu — instantiations of the half-step kernels for one PML kind (GBF_PK), compiled
+// once per kind so the library builds in parallel.
+#define GBF_KERNELS_ONLY
+#include "fdtd_kernels.cuh"
+
+#ifndef GBF_PK
+#error "GBF_PK must be defined (0..4)"
+#endif
+
+namespace gbf {
+
+#define GBF_CAT2(a, b) a##b
+#define GBF_CAT(a, b) GBF_CAT2(a, b)
+
+template <int IDP>
+static EKernFn e_for(int np) {
+  switch (np) {
+    case 1: return e_half_step<GBF_PK, 1, IDP>;
+    case 2: return e_half_step<GBF_PK, 2, IDP>;
+    case 3: return e_half_step<GBF_PK, 3, IDP>;
+    case 4: return e_half_step<GBF_PK, 4, IDP>;
+    default: return e_half_step<GBF_PK, 0, IDP>;
+  }
+}
+
+// Kernels for PML kind GBF_PK, `np` dispersive poles and ID layout `idp` (1 packed, 3 plain).
+void GBF_CAT(kernels_pk, GBF_PK)(int np, int idp, HKernFn* h, EKernFn* e) {
+  if (idp == 1) {
+    *h = h_half_step<GBF_PK, 1>;
+    *e = e_for<1>(np);
+  } else {
+    *h = h_half_step<GBF_PK, 3>;
+    *e = e_for<3>(np);
+  }
+}
+
+}  // namespace gbf
