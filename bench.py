@@ -36,6 +36,21 @@ sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 
 METRIC = 'Mcells/s'
 WORKLOAD = 'dispersive_soil_400x400x200_debye50_pml10'
+# ncu summary of the E half-step on the soil workload; its `dram_bytes_per_cell:` line gives the
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch per cell
+TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'e_half_step_dispersive_soil_256x256x128.md')
+
+
+def measured_traffic(cells):
+    """DRAM bytes of one E half-step launch over `cells` cells, scaled from the ncu capture."""
+    try:
+        with open(TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.startswith('dram_bytes_per_cell:'):
+                    return int(round(float(line.split(':')[1]) * cells))
+    except OSError:
+        pass
+    return None
 
 
 def load_peaks():
@@ -56,15 +71,26 @@ def slab_cells(G):
 
 
 def algorithmic_bytes(G):
-    """Bytes per launch that each half-step must move at minimum (fp32 fields, uint32 IDs,
-    complex64 dispersive state), per cell: H half-step reads E, H, 3 IDs and writes H
-    (48 B); E half-step the same plus 48 B per pole (T read and written); PML adds, per
-    slab cell and CFS order, two Phi values read and written (16 B) in each half-step."""
+    """Bytes per launch each half-step must move, in the device representation: fp32 fields,
+    the node's three material IDs packed in one 32-bit word (nmat <= 1024; otherwise three
+    uint32 IDs), complex64 dispersive state. Per node: H half-step reads E and H and the ID word
+    and writes H (12 + 12 + 4 + 12 = 40 B); E half-step the same (40 B) plus, on nodes whose
+    materials have poles, 8 B per pole and component read and written (48 B per pole). PML adds
+    per slab node and CFS order two Phi values read and written (16 B) in each half-step.
+    Neighbour values along j, k and x are re-reads of the same arrays (cache hits)."""
     cells = G.nx * G.ny * G.nz
+    idb = 4 if len(G.materials) <= 1024 else 12
     order = max(len(G.cfs), 1)
     pml = slab_cells(G) * 16 * order
-    h = cells * 48 + pml
-    e = cells * (48 + 48 * G.maxpoles) + pml
+    h = cells * (36 + idb) + pml
+    e = cells * (36 + idb) + pml
+    if G.maxpoles:
+        disp = np.zeros(len(G.materials), dtype=bool)
+        d = np.asarray(G.updatecoeffsdispersive)
+        disp[:] = np.any(d != 0, axis=1)
+        ids = G.ID[:3, :G.nx, :G.ny, :G.nz]
+        dcells = int(np.count_nonzero(disp[ids[0]] | disp[ids[1]] | disp[ids[2]]))
+        e += dcells * 48 * G.maxpoles
     return h, e
 
 
@@ -234,14 +260,7 @@ def run_gb300(args):
     t_e = ms_e / npf / 1e3
     t_h = ms_h / npf / 1e3
     achieved = bytes_e / t_e / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, 'profiles', 'e_half_step_soil_traffic.json')
-    if os.path.exists(tf):
-        try:
-            with open(tf) as f:
-                traffic = json.load(f).get('dram_bytes_per_launch')
-        except Exception:
-            traffic = None
+    traffic = measured_traffic(cells)
     if rank != 0:
         return
     out = {
