@@ -52,7 +52,7 @@ def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
 
 
 def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
-                    timewindow='12e-9', cylinder=True, messages=False):
+                    timewindow='12e-9', cylinder=True, pml=10, messages=False):
     """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
 
     Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
@@ -69,7 +69,7 @@ def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed
     yc = ny * dx / 2
     lines = ['#domain: {:g} {:g} {:g}'.format(nx * dx, ny * dx, nz * dx),
              '#dx_dy_dz: {0:g} {0:g} {0:g}'.format(dx), '#time_window: {}'.format(timewindow),
-             '#pml_cells: 10', '#waveform: ricker 1 1.5e9 w',
+             '#pml_cells: {}'.format(pml), '#waveform: ricker 1 1.5e9 w',
              '#hertzian_dipole: x {:g} {:g} {:g} w'.format(xc - 0.02, yc, zsurf + 0.01),
              '#rx: {:g} {:g} {:g}'.format(xc + 0.02, yc, zsurf + 0.01)]
     for m in range(nmat):
