@@ -17,7 +17,8 @@ HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # --fmad=false: every product and sum is rounded as written, which makes the GPU results
 # bit-identical to the reference's CPU kernels compiled without floating-point contraction
-NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '--fmad=false', '-Xcompiler', '-fPIC', '-shared']
+NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '--fmad=false', '-Xcompiler', '-fPIC',
+              '-Xcompiler', '-ffp-contract=off', '-shared']
 
 _lock = threading.Lock()
 _lib = None
@@ -108,6 +109,7 @@ _SIGS = {
     'gbf_device_bytes': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
+    'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
 }
 
 

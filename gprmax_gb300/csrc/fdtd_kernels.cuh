@@ -42,7 +42,9 @@ enum PmlKind : int { PML_NONE = 0, PML_HORI1 = 1, PML_HORI2 = 2, PML_MRI1 = 3, P
 struct Slab {
   int T;            // thickness in cells, 0 = absent
   float d;          // cell size along the axis (fp32, the reference kernels' `float d`)
-  long long ocount; // Phi elements per CFS order
+  float rcp;        // 1/d rounded to nearest (fp32)
+  int fastdiv;      // 1: x/d may be formed from rcp (verified on the host for this d)
+  int ocount;       // Phi elements per CFS order (< 2^30: a slab holds under half the nodes)
   float* phiE1;     // Phi arrays [order][...] of the first/second tangential E component
   float* phiE2;
   float* phiH1;
@@ -96,78 +98,156 @@ struct StepParams {
 };
 
 // ---------------------------------------------------------------------------------------
-// CFS-PML correction of one field value (pml_updates_{electric,magnetic}_{HORIPML,MRIPML}).
-// Returns X such that the field changes by (+/-) c4 * X, and advances the Phi recursion.
-// RA01, IRA, RC0 ... are recomputed from the stored rows exactly as the reference does.
+// CFS-PML correction (pml_updates_{electric,magnetic}_{HORIPML,MRIPML}_ext.pyx).
+// A node lies in at most one slab per axis (each slab is thinner than half the domain). For an
+// axis, both tangential field components use the same profile row and Phi index; PmlRow holds
+// that row, pml_update returns X such that the component changes by (+/-) c4 * X and advances
+// the Phi recursion. RA01, IRA, RC0 ... are recomputed from the stored rows as the reference does.
+struct PmlRow {
+  float RA0, RB0, RE0, RF0, RA1, RB1, RE1, RF1;
+};
+
 template <int PK>
-__device__ __forceinline__ float pml_term(float dF, float* phi, long long pidx, long long ocount,
-                                          const float* __restrict__ R, int T, int p) {
+__device__ __forceinline__ PmlRow load_row(const float* __restrict__ R, int T, int pr) {
   constexpr int order = (PK == PML_HORI2 || PK == PML_MRI2) ? 2 : 1;
-  const float RA0 = __ldg(R + (0 * order + 0) * T + p);
-  const float RB0 = __ldg(R + (1 * order + 0) * T + p);
-  const float RE0 = __ldg(R + (2 * order + 0) * T + p);
-  const float RF0 = __ldg(R + (3 * order + 0) * T + p);
+  PmlRow c;
+  c.RA0 = __ldg(R + (0 * order + 0) * T + pr);
+  c.RB0 = __ldg(R + (1 * order + 0) * T + pr);
+  c.RE0 = __ldg(R + (2 * order + 0) * T + pr);
+  c.RF0 = __ldg(R + (3 * order + 0) * T + pr);
+  if (order == 2) {
+    c.RA1 = __ldg(R + (0 * order + 1) * T + pr);
+    c.RB1 = __ldg(R + (1 * order + 1) * T + pr);
+    c.RE1 = __ldg(R + (2 * order + 1) * T + pr);
+    c.RF1 = __ldg(R + (3 * order + 1) * T + pr);
+  } else {
+    c.RA1 = c.RB1 = c.RE1 = c.RF1 = 0.f;
+  }
+  return c;
+}
+
+template <int PK>
+__device__ __forceinline__ float pml_update(float dF, float* phi, int pidx, int ocount,
+                                            const PmlRow& c) {
   const float ph0 = phi[pidx];
   if (PK == PML_HORI1) {
-    const float RA01 = RA0 - 1.0f;
-    const float X = RA01 * dF + RB0 * ph0;
-    phi[pidx] = RE0 * ph0 - RF0 * dF;
+    const float RA01 = c.RA0 - 1.0f;
+    const float X = RA01 * dF + c.RB0 * ph0;
+    phi[pidx] = c.RE0 * ph0 - c.RF0 * dF;
     return X;
   } else if (PK == PML_HORI2) {
-    const float RA1 = __ldg(R + (0 * order + 1) * T + p);
-    const float RB1 = __ldg(R + (1 * order + 1) * T + p);
-    const float RE1 = __ldg(R + (2 * order + 1) * T + p);
-    const float RF1 = __ldg(R + (3 * order + 1) * T + p);
-    const float RA01 = RA0 * RA1 - 1.0f;
+    const float RA01 = c.RA0 * c.RA1 - 1.0f;
     const float ph1 = phi[pidx + ocount];
-    const float X = RA01 * dF + RA1 * RB0 * ph0 + RB1 * ph1;
-    phi[pidx + ocount] = RE1 * ph1 - RF1 * (RA0 * dF + RB0 * ph0);
-    phi[pidx] = RE0 * ph0 - RF0 * dF;
+    const float X = RA01 * dF + c.RA1 * c.RB0 * ph0 + c.RB1 * ph1;
+    phi[pidx + ocount] = c.RE1 * ph1 - c.RF1 * (c.RA0 * dF + c.RB0 * ph0);
+    phi[pidx] = c.RE0 * ph0 - c.RF0 * dF;
     return X;
   } else if (PK == PML_MRI1) {
-    const float IRA = 1.0f / RA0;
+    const float IRA = 1.0f / c.RA0;
     const float IRA1 = IRA - 1.0f;
-    const float RC0 = IRA * RB0 * RF0;
+    const float RC0 = IRA * c.RB0 * c.RF0;
     const float X = IRA1 * dF - IRA * ph0;
-    phi[pidx] = RE0 * ph0 + RC0 * dF - RC0 * ph0;
+    phi[pidx] = c.RE0 * ph0 + RC0 * dF - RC0 * ph0;
     return X;
   } else {  // PML_MRI2
-    const float RA1 = __ldg(R + (0 * order + 1) * T + p);
-    const float RB1 = __ldg(R + (1 * order + 1) * T + p);
-    const float RE1 = __ldg(R + (2 * order + 1) * T + p);
-    const float RF1 = __ldg(R + (3 * order + 1) * T + p);
-    const float IRA = 1.0f / (RA0 + RA1);
+    const float IRA = 1.0f / (c.RA0 + c.RA1);
     const float IRA1 = IRA - 1.0f;
-    const float RC0 = IRA * RF0;
-    const float RC1 = IRA * RF1;
+    const float RC0 = IRA * c.RF0;
+    const float RC1 = IRA * c.RF1;
     const float ph1 = phi[pidx + ocount];
-    const float Psi = RB0 * ph0 + RB1 * ph1;
+    const float Psi = c.RB0 * ph0 + c.RB1 * ph1;
     const float X = IRA1 * dF - IRA * Psi;
-    phi[pidx + ocount] = RE1 * ph1 + RC1 * (dF - Psi);
-    phi[pidx] = RE0 * ph0 + RC0 * (dF - Psi);
+    phi[pidx + ocount] = c.RE1 * ph1 + RC1 * (dF - Psi);
+    phi[pidx] = c.RE0 * ph0 + RC0 * (dF - Psi);
     return X;
   }
 }
 
-// Phi index of node (i, j, k) at profile index p (layouts: x [p][j][k], y [i][p][k], z [i][j][p]).
-template <int AXIS>
-__device__ __forceinline__ long long phi_index(int i, int j, int k, int p, int T, int ny, int nz) {
-  if (AXIS == 0) return ((long long)p * ny + j) * nz + k;
-  if (AXIS == 1) return ((long long)i * T + p) * nz + k;
-  return ((long long)i * ny + j) * T + p;
+// x / d rounded to nearest, as IEEE division gives it. When the host has verified d
+// (Slab::fastdiv), the quotient comes from the correctly rounded reciprocal r with one
+// residual correction (Markstein, IBM J. Res. Develop. 34(1), 1990): q = x*r, e = x - q*d
+// (exact, one fused multiply-add), result q + e*r. The correction is used while |x| lies in
+// [2^-60, 2^80), where q, e and e*r stay normal for cell sizes in [2^-20, 2^20]; zeros keep q
+// (which carries their sign) and every other x takes the division.
+constexpr uint32_t kDivLo = 67u << 23;    // bits of 2^-60
+constexpr uint32_t kDivHi = 207u << 23;   // bits of 2^80
+__device__ __forceinline__ float div_cell(float x, float d, float r, int fast) {
+  if (fast) {
+    const float q = __fmul_rn(x, r);
+    const uint32_t ax = __float_as_uint(x) & 0x7fffffffu;
+    if (ax - kDivLo < kDivHi - kDivLo) return __fmaf_rn(__fmaf_rn(-q, d, x), r, q);
+    if (ax == 0u) return q;
+  }
+  return __fdiv_rn(x, d);
 }
 
-// Slab membership and profile index of coordinate c along a slab's axis.
-// E ranges: minus c in [1, T] (p = T - c), plus c in [n - T, n - 1] (p = c - (n - T)).
-// H ranges: minus c in [0, T - 1] (p = T - 1 - c), plus as E.
+// Phi index of node (i, j, k) at profile index pr (layouts: x [pr][j][k], y [i][pr][k],
+// z [i][j][pr]).
+template <int AXIS>
+__device__ __forceinline__ int phi_index(int i, int j, int k, int pr, int T, int ny, int nz) {
+  if (AXIS == 0) return (pr * ny + j) * nz + k;
+  if (AXIS == 1) return (i * T + pr) * nz + k;
+  return (i * ny + j) * T + pr;
+}
+
+// Slab membership of coordinate c along one axis (n cells, minus/plus thickness Tm/Tp).
+// E ranges: minus c in [1, Tm] (pr = Tm - c), plus c in [n - Tp, n - 1] (pr = c - (n - Tp)).
+// H ranges: minus c in [0, Tm - 1] (pr = Tm - 1 - c), plus as E.
+// Returns 0 outside, 1 in the minus slab, 2 in the plus slab.
 template <bool ELECTRIC>
-__device__ __forceinline__ int slab_p(int c, int T, int n, bool minus) {
-  if (T == 0) return -1;
-  if (minus) {
-    if (ELECTRIC) return (c >= 1 && c <= T) ? T - c : -1;
-    return (c < T) ? T - 1 - c : -1;
+__device__ __forceinline__ int axis_member(int c, int n, int Tm, int Tp, int& pr) {
+  const int pm = ELECTRIC ? Tm - c : Tm - 1 - c;
+  const int pp = c - (n - Tp);
+  const bool inm = (unsigned)pm < (unsigned)Tm;
+  const bool inp = (unsigned)pp < (unsigned)Tp;
+  pr = inp ? pp : pm;
+  return inp ? 2 : (inm ? 1 : 0);
+}
+
+// The two X values of one axis for the node: first/second tangential component (x: y, z;
+// y: x, z; z: x, y) with their Phi arrays 1 and 2. `where` is axis_member's result (1 or 2).
+template <int PK, bool ELECTRIC, int AX>
+__device__ __forceinline__ void pml_axis(const StepParams& p, int where, int pr, int i, int j,
+                                         int k, float dA, float dB, float& XA, float& XB) {
+  const Slab& sl = p.slab[AX + (where == 2 ? 3 : 0)];
+  const int T = sl.T;
+  const int pidx = phi_index<AX>(i, j, k, pr, T, p.ny, p.nz);
+  const PmlRow c = load_row<PK>(ELECTRIC ? sl.eR : sl.hR, T, pr);
+  const float d = sl.d, r = sl.rcp;
+  const int fast = sl.fastdiv;
+  XA = pml_update<PK>(div_cell(dA, d, r, fast), ELECTRIC ? sl.phiE1 : sl.phiH1, pidx, sl.ocount, c);
+  XB = pml_update<PK>(div_cell(dB, d, r, fast), ELECTRIC ? sl.phiE2 : sl.phiH2, pidx, sl.ocount, c);
+}
+
+// Sign with which axis AX's X enters component C: H x-axis Hy +, Hz -; y-axis Hx -, Hz +;
+// z-axis Hx +, Hy -. E has the opposite signs.
+template <bool ELECTRIC, int AX, int C>
+__host__ __device__ static constexpr bool pml_plus() {
+  return ELECTRIC != ((AX == 0) ? (C == 1) : (AX == 1) ? (C == 2) : (C == 0));
+}
+
+// Apply the slab corrections of component C (tangential axes a < b) in the reference's slab
+// order x0, y0, z0, xmax, ymax, zmax: b comes first only when the node is in a's plus slab and
+// in b's minus slab. Each correction is F +/- c4 * X.
+template <bool ELECTRIC, int C>
+__device__ __forceinline__ float apply_pml(float F, float c4, const int* where, const float* XA,
+                                           const float* XB) {
+  constexpr int a = C == 0 ? 1 : 0;
+  constexpr int b = C == 2 ? 1 : 2;
+  // C is the first tangential component of axis a when a == 0 ? C == 1 : C == 0
+  const float ta = c4 * ((a == 0 ? C == 1 : C == 0) ? XA[a] : XB[a]);
+  const float tb = c4 * ((b == 0 ? C == 1 : C == 0) ? XA[b] : XB[b]);
+  constexpr bool pa = pml_plus<ELECTRIC, a, C>();
+  constexpr bool pb = pml_plus<ELECTRIC, b, C>();
+  const bool ina = where[a] != 0, inb = where[b] != 0;
+  if (ina && inb && where[a] == 2 && where[b] == 1) {
+    F = pb ? F + tb : F - tb;
+    F = pa ? F + ta : F - ta;
+  } else {
+    if (ina) F = pa ? F + ta : F - ta;
+    if (inb) F = pb ? F + tb : F - tb;
   }
-  return (c >= n - T && c < n) ? c - (n - T) : -1;
+  return F;
 }
 
 // Stage the coefficient tables in shared memory (when they fit).
@@ -215,24 +295,6 @@ struct FlatWalk {
   }
 };
 
-// One slab's correction of one H component (compile-time slab position S, component C).
-// Table per slab axis: x-slab Hy (Phi1, dEz/dx, +), Hz (Phi2, dEy/dx, -); y-slab Hx (Phi1,
-// dEz/dy, -), Hz (Phi2, dEx/dy, +); z-slab Hx (Phi1, dEy/dz, +), Hy (Phi2, dEx/dz, -).
-template <int PK, int S, int C>
-__device__ __forceinline__ float h_slab(float F, float c4, int pp, int i, int j, int k,
-                                        float dA, float dB, const StepParams& p) {
-  constexpr int AX = S % 3;
-  const Slab& sl = p.slab[S];
-  constexpr bool first = (AX == 0) ? (C == 1) : (C == 0);
-  constexpr float sgn = (AX == 0) ? (C == 1 ? 1.f : -1.f) : (AX == 1) ? (C == 0 ? -1.f : 1.f)
-                                                                      : (C == 0 ? 1.f : -1.f);
-  const float dF = first ? dA : dB;
-  const float X = pml_term<PK>(dF / sl.d, first ? sl.phiH1 : sl.phiH2,
-                               phi_index<AX>(i, j, k, pp, sl.T, p.ny, p.nz), sl.ocount, sl.hR,
-                               sl.T, pp);
-  return sgn > 0.f ? F + c4 * X : F - c4 * X;
-}
-
 // Magnetic sources at one node/component (sources.py:202-232, numpy-2 fp32 order).
 __device__ __forceinline__ float apply_h_sources(float F, int comp, int i, int j, int k, int it,
                                                  float c4, const StepParams& p) {
@@ -259,77 +321,65 @@ __device__ __forceinline__ bool node_has_source(int idx, int n, const int* inl, 
 }
 
 // H update of one node: main update (update_magnetic), slab corrections in slab order, sources.
-// px0/pxmax/py0/pymax are the node's x and y slab profile indices (-1 outside).
+// where[a] / pr[a]: slab membership and profile index along each axis (axis_member; 0 outside
+// the PML). The X values of the node's slabs are formed first (they depend only on the E
+// differences and the Phi state), then each component takes its main update and its
+// corrections in the reference's order.
 template <int PK>
 __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, const float* Cs,
-                                       int i, int j, int k, bool src, int it, int px0, int pxmax,
-                                       int py0, int pymax, int pz0, int pzmax, float dEz_y,
-                                       float dEy_z, float dEx_z,
+                                       int i, int j, int k, bool src, int it, const int* where,
+                                       const int* pr, float dEz_y, float dEy_z, float dEx_z,
                                        float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
                                        uint32_t my, uint32_t mz, float& hx, float& hy, float& hz) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const bool iin = i < nx, jin = j < ny, kin = k < nz;
-  // every H slab range needs i < nx, j < ny and k < nz
-  const bool inpml = PK != PML_NONE && iin && jin && kin;
-  // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs y0, z0, ymax, zmax
+  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
+  if (PK != PML_NONE) {
+    if (where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0]);
+    if (where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1]);
+    if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2]);
+  }
+  // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
     const bool mainu = (i >= 1) && jin && kin;
-    const bool pml = inpml && (py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0);
+    const bool pml = PK != PML_NONE && (where[1] || where[2]);
     if (mainu || pml || src) {
       float F = hx;
       if (mainu) {
         const float4 c = C4[mx];
         F = c.x * F - c.z * dEz_y + c.w * dEy_z;
       }
-      if (PK != PML_NONE && pml) {
-        const float c4 = Cs[mx];
-        if (py0 >= 0) F = h_slab<PK, 1, 0>(F, c4, py0, i, j, k, dEz_y, dEx_y, p);
-        if (pz0 >= 0) F = h_slab<PK, 2, 0>(F, c4, pz0, i, j, k, dEy_z, dEx_z, p);
-        if (pymax >= 0) F = h_slab<PK, 4, 0>(F, c4, pymax, i, j, k, dEz_y, dEx_y, p);
-        if (pzmax >= 0) F = h_slab<PK, 5, 0>(F, c4, pzmax, i, j, k, dEy_z, dEx_z, p);
-      }
+      if (pml) F = apply_pml<false, 0>(F, Cs[mx], where, XA, XB);
       if (src) F = apply_h_sources(F, 3, i, j, k, it, Cs[mx], p);
       hx = F;
     }
   }
-  // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs x0, z0, xmax, zmax
+  // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
   {
     const bool mainu = iin && (j >= 1) && kin;
-    const bool pml = inpml && (px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0);
+    const bool pml = PK != PML_NONE && (where[0] || where[2]);
     if (mainu || pml || src) {
       float F = hy;
       if (mainu) {
         const float4 c = C4[my];
         F = c.x * F - c.w * dEx_z + c.y * dEz_x;
       }
-      if (PK != PML_NONE && pml) {
-        const float c4 = Cs[my];
-        if (px0 >= 0) F = h_slab<PK, 0, 1>(F, c4, px0, i, j, k, dEz_x, dEy_x, p);
-        if (pz0 >= 0) F = h_slab<PK, 2, 1>(F, c4, pz0, i, j, k, dEy_z, dEx_z, p);
-        if (pxmax >= 0) F = h_slab<PK, 3, 1>(F, c4, pxmax, i, j, k, dEz_x, dEy_x, p);
-        if (pzmax >= 0) F = h_slab<PK, 5, 1>(F, c4, pzmax, i, j, k, dEy_z, dEx_z, p);
-      }
+      if (pml) F = apply_pml<false, 1>(F, Cs[my], where, XA, XB);
       if (src) F = apply_h_sources(F, 4, i, j, k, it, Cs[my], p);
       hy = F;
     }
   }
-  // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs x0, y0, xmax, ymax
+  // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs along x and y
   {
     const bool mainu = iin && jin && (k >= 1);
-    const bool pml = inpml && (px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0);
+    const bool pml = PK != PML_NONE && (where[0] || where[1]);
     if (mainu || pml || src) {
       float F = hz;
       if (mainu) {
         const float4 c = C4[mz];
         F = c.x * F - c.y * dEy_x + c.z * dEx_y;
       }
-      if (PK != PML_NONE && pml) {
-        const float c4 = Cs[mz];
-        if (px0 >= 0) F = h_slab<PK, 0, 2>(F, c4, px0, i, j, k, dEz_x, dEy_x, p);
-        if (py0 >= 0) F = h_slab<PK, 1, 2>(F, c4, py0, i, j, k, dEz_y, dEx_y, p);
-        if (pxmax >= 0) F = h_slab<PK, 3, 2>(F, c4, pxmax, i, j, k, dEz_x, dEy_x, p);
-        if (pymax >= 0) F = h_slab<PK, 4, 2>(F, c4, pymax, i, j, k, dEz_y, dEx_y, p);
-      }
+      if (pml) F = apply_pml<false, 2>(F, Cs[mz], where, XA, XB);
       if (src) F = apply_h_sources(F, 5, i, j, k, it, Cs[mz], p);
       hz = F;
     }
@@ -390,18 +440,16 @@ h_half_step(const __grid_constant__ StepParams p) {
       mz = __ldg(p.ID[5] + idx);
     }
     float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
-    int px0 = -1, pxmax = -1, py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
-    if (PK != PML_NONE && !(i >= xlo && i < xhi && j >= ylo && j < yhi && k >= zlo && k < zhi)) {
-      px0 = slab_p<false>(i, p.slab[0].T, nx, true);
-      pxmax = slab_p<false>(i, p.slab[3].T, nx, false);
-      py0 = slab_p<false>(j, p.slab[1].T, ny, true);
-      pymax = slab_p<false>(j, p.slab[4].T, ny, false);
-      pz0 = slab_p<false>(k, p.slab[2].T, nz, true);
-      pzmax = slab_p<false>(k, p.slab[5].T, nz, false);
+    int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
+    if (PK != PML_NONE && iin && jin && kin &&
+        !(i >= xlo && i < xhi && j >= ylo && j < yhi && k >= zlo && k < zhi)) {
+      where[0] = axis_member<false>(i, nx, p.slab[0].T, p.slab[3].T, pr[0]);
+      where[1] = axis_member<false>(j, ny, p.slab[1].T, p.slab[4].T, pr[1]);
+      where[2] = axis_member<false>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
     }
     const bool src = p.nsrcH && node_has_source(idx, p.nsrcH, p.srcqH, p.srcH, sx, sy);
-    h_node<PK>(p, C4, Cs, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, ez_j - ez_c, ey_k - ey_c,
-               ex_k - ex_c, ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
+    h_node<PK>(p, C4, Cs, i, j, k, src, it, where, pr, ez_j - ez_c, ey_k - ey_c, ex_k - ex_c,
+               ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
     Hx[idx] = hx;
     Hy[idx] = hy;
     Hz[idx] = hz;
@@ -429,45 +477,33 @@ __device__ __forceinline__ float apply_e_sources(float F, int comp, int i, int j
   return F;
 }
 
-// One slab's correction of one E component (compile-time slab position S and component C).
-// Table per slab axis: x-slab Ey (Phi1, dHz/dx, -), Ez (Phi2, dHy/dx, +); y-slab Ex (Phi1,
-// dHz/dy, +), Ez (Phi2, dHx/dy, -); z-slab Ex (Phi1, dHy/dz, -), Ey (Phi2, dHx/dz, +).
-template <int PK, int S, int C>
-__device__ __forceinline__ float e_slab(float F, float c4, int pp, int i, int j, int k,
-                                        float dA, float dB, const StepParams& p) {
-  constexpr int AX = S % 3;
-  const Slab& sl = p.slab[S];
-  constexpr bool first = (AX == 0) ? (C == 1) : (C == 0);
-  constexpr float sgn = (AX == 0) ? (C == 1 ? -1.f : 1.f) : (AX == 1) ? (C == 0 ? 1.f : -1.f)
-                                                                      : (C == 0 ? -1.f : 1.f);
-  const float dF = first ? dA : dB;
-  const float X = pml_term<PK>(dF / sl.d, first ? sl.phiE1 : sl.phiE2,
-                               phi_index<AX>(i, j, k, pp, sl.T, p.ny, p.nz), sl.ocount, sl.eR,
-                               sl.T, pp);
-  return sgn > 0.f ? F + c4 * X : F - c4 * X;
-}
-
 // E update of one node for all three components: main update (update_electric, or part A of
 // the dispersive update), slab corrections in slab order, sources, dispersive part B.
+// where[a] / pr[a]: slab membership and profile index along each axis (0 outside the PML).
 template <int PK, int NP>
 __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
                                        const float2* CD, int i, int j, int k, bool src, int it,
-                                       int px0, int pxmax, int py0, int pymax, int pz0,
-                                       int pzmax, float dHz_y,
+                                       const int* where, const int* pr, float dHz_y,
                                        float dHy_z, float dHx_z, float dHz_x, float dHy_x,
                                        float dHx_y, const uint32_t* m, float* e, float2 (*t)[NP > 0 ? NP : 1]) {
+  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
+  if (PK != PML_NONE) {
+    if (where[0]) pml_axis<PK, true, 0>(p, where[0], pr[0], i, j, k, dHz_x, dHy_x, XA[0], XB[0]);
+    if (where[1]) pml_axis<PK, true, 1>(p, where[1], pr[1], i, j, k, dHz_y, dHx_y, XA[1], XB[1]);
+    if (where[2]) pml_axis<PK, true, 2>(p, where[2], pr[2], i, j, k, dHy_z, dHx_z, XA[2], XB[2]);
+  }
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
     bool mainu, pml;
     if (comp == 0) {
       mainu = (j >= 1) && (k >= 1);
-      pml = py0 >= 0 || pymax >= 0 || pz0 >= 0 || pzmax >= 0;
+      pml = where[1] || where[2];
     } else if (comp == 1) {
       mainu = (i >= 1) && (k >= 1);
-      pml = px0 >= 0 || pxmax >= 0 || pz0 >= 0 || pzmax >= 0;
+      pml = where[0] || where[2];
     } else {
       mainu = (i >= 1) && (j >= 1);
-      pml = px0 >= 0 || pxmax >= 0 || py0 >= 0 || pymax >= 0;
+      pml = where[0] || where[1];
     }
     if (PK == PML_NONE) pml = false;
     if (!(mainu || pml || src)) continue;
@@ -502,23 +538,9 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
     }
     if (PK != PML_NONE && pml) {
       const float c4 = Cs[mm];
-      // slab order x0, y0, z0, xmax, ymax, zmax; a component is tangential to two axes
-      if (comp == 0) {
-        if (py0 >= 0) F = e_slab<PK, 1, 0>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
-        if (pz0 >= 0) F = e_slab<PK, 2, 0>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
-        if (pymax >= 0) F = e_slab<PK, 4, 0>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
-        if (pzmax >= 0) F = e_slab<PK, 5, 0>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
-      } else if (comp == 1) {
-        if (px0 >= 0) F = e_slab<PK, 0, 1>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
-        if (pz0 >= 0) F = e_slab<PK, 2, 1>(F, c4, pz0, i, j, k, dHy_z, dHx_z, p);
-        if (pxmax >= 0) F = e_slab<PK, 3, 1>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
-        if (pzmax >= 0) F = e_slab<PK, 5, 1>(F, c4, pzmax, i, j, k, dHy_z, dHx_z, p);
-      } else {
-        if (px0 >= 0) F = e_slab<PK, 0, 2>(F, c4, px0, i, j, k, dHz_x, dHy_x, p);
-        if (py0 >= 0) F = e_slab<PK, 1, 2>(F, c4, py0, i, j, k, dHz_y, dHx_y, p);
-        if (pxmax >= 0) F = e_slab<PK, 3, 2>(F, c4, pxmax, i, j, k, dHz_x, dHy_x, p);
-        if (pymax >= 0) F = e_slab<PK, 4, 2>(F, c4, pymax, i, j, k, dHz_y, dHx_y, p);
-      }
+      if (comp == 0) F = apply_pml<true, 0>(F, c4, where, XA, XB);
+      else if (comp == 1) F = apply_pml<true, 1>(F, c4, where, XA, XB);
+      else F = apply_pml<true, 2>(F, c4, where, XA, XB);
     }
     if (src) F = apply_e_sources(F, comp, i, j, k, it, Cs[mm], p);
     e[comp] = F;
@@ -599,18 +621,15 @@ e_half_step(const __grid_constant__ StepParams p) {
 #pragma unroll
       for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
     }
-    int px0 = -1, pxmax = -1, py0 = -1, pymax = -1, pz0 = -1, pzmax = -1;
+    int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
     if (PK != PML_NONE && !(i > xlo && i < xhi && j > ylo && j < yhi && k > zlo && k < zhi)) {
-      px0 = slab_p<true>(i, p.slab[0].T, nx, true);
-      pxmax = slab_p<true>(i, p.slab[3].T, nx, false);
-      py0 = slab_p<true>(j, p.slab[1].T, ny, true);
-      pymax = slab_p<true>(j, p.slab[4].T, ny, false);
-      pz0 = slab_p<true>(k, p.slab[2].T, nz, true);
-      pzmax = slab_p<true>(k, p.slab[5].T, nz, false);
+      where[0] = axis_member<true>(i, nx, p.slab[0].T, p.slab[3].T, pr[0]);
+      where[1] = axis_member<true>(j, ny, p.slab[1].T, p.slab[4].T, pr[1]);
+      where[2] = axis_member<true>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
     }
     const bool src = p.nsrcE && node_has_source(idx, p.nsrcE, p.srcqE, p.srcE, sx, sy);
-    e_node<PK, NP>(p, C4, Cs, CD, i, j, k, src, it, px0, pxmax, py0, pymax, pz0, pzmax, hz_c - hz_j,
-                   hy_c - hy_k, hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
+    e_node<PK, NP>(p, C4, Cs, CD, i, j, k, src, it, where, pr, hz_c - hz_j, hy_c - hy_k,
+                   hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
       p.E[comp][idx] = e[comp];

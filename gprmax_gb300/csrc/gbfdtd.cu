@@ -11,7 +11,9 @@
 // step, so a step is a fixed launch sequence that a CUDA graph can replay.
 #include <cstdarg>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -96,6 +98,37 @@ static int dev_alloc(gbf_ctx* ctx, void** p, size_t n) {
   return GBF_OK;
 }
 
+// Does x/d computed as the corrected product with r = 1/d (div_cell in fdtd_kernels.cuh)
+// equal the IEEE quotient for every x? The quotient's significand depends only on the
+// significands of x and d while nothing leaves the normal range, and the kernel uses the
+// product only for |x| in [2^-60, 2^80) with d in [2^-20, 2^20]; so one binade of x (all 2^23
+// significands, positive; round-to-nearest is symmetric) decides it. Results are cached per d.
+static bool reciprocal_division_exact(float d) {
+  if (!(d >= 0x1p-20f && d <= 0x1p20f)) return false;
+  static std::mutex mu;
+  static std::vector<std::pair<uint32_t, bool>> cache;
+  uint32_t bits;
+  memcpy(&bits, &d, 4);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto& c : cache)
+      if (c.first == bits) return c.second;
+  }
+  const float r = 1.0f / d;
+  bool ok = true;
+  for (uint32_t m = 0; m < (1u << 23) && ok; ++m) {
+    const uint32_t xb = (127u << 23) | m;
+    float x;
+    memcpy(&x, &xb, 4);
+    const float q = x * r;
+    const float q1 = fmaf(fmaf(-q, d, x), r, q);
+    ok = (q1 == x / d);
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  cache.emplace_back(bits, ok);
+  return ok;
+}
+
 static int pml_kind(const gbf_grid_desc& d) {
   bool any = false;
   for (int s = 0; s < 6; ++s) any |= d.pml_thickness[s] > 0;
@@ -107,6 +140,8 @@ static int pml_kind(const gbf_grid_desc& d) {
 extern "C" {
 
 const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
+
+int gbf_check_cell_division(float d) { return reciprocal_division_exact(d) ? 1 : 0; }
 
 int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n) {
   if (!buf || n == 0) return GBF_EINVAL;
@@ -141,7 +176,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~1) || d.reserved[0] || d.reserved[1] || d.reserved[2])
+  if ((d.options & ~3) || d.reserved[0] || d.reserved[1] || d.reserved[2])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
@@ -236,10 +271,12 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     const int t = d.pml_thickness[s];
     sl.T = t;
     sl.d = dd[s % 3];
+    sl.rcp = 1.0f / sl.d;
+    sl.fastdiv = (t && !(d.options & 2) && reciprocal_division_exact(sl.d)) ? 1 : 0;
     if (!t) continue;
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
-    sl.ocount = (long long)t * nu * nv;
+    sl.ocount = (int)(t * nu * nv);
     const long long per = (long long)d.pml_order * sl.ocount;
     sl.phiE1 = phi; phi += per;
     sl.phiE2 = phi; phi += per;

@@ -64,7 +64,9 @@ typedef struct gbf_grid_desc {
     int32_t nrx;                 /* receivers */
     int32_t nsnap;               /* snapshots */
     int32_t options;             /* bit 0: read coefficient tables from global memory instead
-                                    of staging them in shared memory (tuning); other bits 0 */
+                                    of staging them in shared memory (tuning); bit 1: form the
+                                    PML differences dF/d by division even where the reciprocal
+                                    product is exact (gbf_check_cell_division); other bits 0 */
     int32_t reserved[3];         /* must be zero */
 } gbf_grid_desc;
 
@@ -159,6 +161,13 @@ int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n);
 
 /* Library version string. */
 const char* gbf_version(void);
+
+/* 1 if, for this cell size, the PML kernels may form dF/d as the product with the rounded
+ * reciprocal corrected once by the exact residual, because that equals the IEEE quotient for
+ * every dF; 0 otherwise (the kernels then divide). Host only, no device needed; gbf_create
+ * checks each slab's cell size this way. No counterpart in the reference, whose PML kernels
+ * divide (pml_updates_electric_HORIPML_ext.pyx:80 `dHz = (...) / dx`). */
+int gbf_check_cell_division(float d);
 
 #ifdef __cplusplus
 }

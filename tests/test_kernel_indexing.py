@@ -2,7 +2,8 @@
 
 Mirrors, in numpy, how ``h_half_step``/``e_half_step`` (gprmax_gb300/csrc/fdtd_kernels.cuh)
 decide which nodes take which slab correction and which Phi element they use: the kernel
-domains, ``slab_p`` and ``phi_index``. For every slab and component it checks that the set of
+domains, ``axis_member`` (one slab per axis: minus, plus or none) and ``phi_index``. For every
+slab and component it checks that the set of
 (node, profile index) pairs equals the reference's slab loops
 (``gprMax/pml_updates/pml_updates_{electric,magnetic}_*_ext.pyx``, ``ii = xf - i`` etc.), that
 every Phi index lies inside that slab's array, and that no two nodes share a Phi element.
@@ -18,16 +19,16 @@ E_COMPS = {0: ((1, 1), (2, 2)), 1: ((0, 1), (2, 2)), 2: ((0, 1), (1, 2))}
 H_COMPS = {0: ((4, 1), (5, 2)), 1: ((3, 1), (5, 2)), 2: ((3, 1), (4, 2))}
 
 
-def slab_p(c, T, n, minus, electric):
-    """Vectorised ``slab_p``: profile index or -1."""
+def axis_member(c, n, Tm, Tp, electric):
+    """Vectorised ``axis_member``: (where, pr) with where 0 outside, 1 minus, 2 plus."""
     c = np.asarray(c)
-    if T == 0:
-        return np.full(c.shape, -1)
-    if minus:
-        if electric:
-            return np.where((c >= 1) & (c <= T), T - c, -1)
-        return np.where(c < T, T - 1 - c, -1)
-    return np.where((c >= n - T) & (c < n), c - (n - T), -1)
+    pm = (Tm - c) if electric else (Tm - 1 - c)
+    pp = c - (n - Tp)
+    inm = (pm >= 0) & (pm < Tm)
+    inp = (pp >= 0) & (pp < Tp)
+    where = np.where(inp, 2, np.where(inm, 1, 0))
+    pr = np.where(inp, pp, pm)
+    return where, pr
 
 
 def phi_index(axis, i, j, k, p, T, ny, nz):
@@ -48,19 +49,20 @@ def kernel_pairs(n3, thick, electric):
     I, J, K = np.meshgrid(*dom, indexing='ij')
     inside = np.ones(I.shape, bool) if electric else (I < nx) & (J < ny) & (K < nz)
     out = {}
-    for s in range(6):
-        T = thick[s]
-        if not T:
-            continue
-        axis, minus = s % 3, s < 3
-        coord = (I, J, K)[axis]
-        p = slab_p(coord, T, n3[axis], minus, electric)
-        mem = (p >= 0) & inside
-        comps = (E_COMPS if electric else H_COMPS)[axis]
-        for comp, arr in comps:
-            ii, jj, kk, pp = I[mem], J[mem], K[mem], p[mem]
-            idx = phi_index(axis, ii, jj, kk, pp, T, ny, nz)
-            out[(s, comp)] = set(zip(ii.tolist(), jj.tolist(), kk.tolist(), pp.tolist(), idx.tolist()))
+    for axis in range(3):
+        Tm, Tp = thick[axis], thick[axis + 3]
+        where, pr = axis_member((I, J, K)[axis], n3[axis], Tm, Tp, electric)
+        for side, s in ((1, axis), (2, axis + 3)):
+            T = thick[s]
+            if not T:
+                continue
+            mem = (where == side) & inside
+            comps = (E_COMPS if electric else H_COMPS)[axis]
+            for comp, arr in comps:
+                ii, jj, kk, pp = I[mem], J[mem], K[mem], pr[mem]
+                idx = phi_index(axis, ii, jj, kk, pp, T, ny, nz)
+                out[(s, comp)] = set(zip(ii.tolist(), jj.tolist(), kk.tolist(), pp.tolist(),
+                                         idx.tolist()))
     return out
 
 
