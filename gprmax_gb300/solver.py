@@ -13,12 +13,23 @@ import numpy as np
 from . import _native
 from .exceptions import SolverError
 from .receivers import OUTPUT_INDEX
+from .sources import active_range, kernel_record
 
 PML_SLABS = ['x0', 'y0', 'z0', 'xmax', 'ymax', 'zmax']
 
 
 def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p(0)
+
+
+def pole_count(G):
+    """Dispersive poles per material: ``G.maxpoles`` on grids built by this package; the
+    reference keeps the count on its ``Material`` class (``materials.py:30``), equal to the
+    largest ``poles`` of the grid's materials."""
+    mp = getattr(G, 'maxpoles', None)
+    if mp is None:
+        mp = max((int(getattr(m, 'poles', 0)) for m in G.materials), default=0)
+    return int(mp)
 
 
 def source_list(G):
@@ -35,12 +46,54 @@ def source_tables(G):
     scale = np.zeros((max(n, 1), 2), dtype=np.float32)
     waves = np.zeros((max(n, 1), G.iterations), dtype=np.float32)
     for s, src in enumerate(srcs):
-        kind, comp, sc, table = src.kernel_record(G)
-        first, last = src.active_range()
+        kind, comp, sc, table = kernel_record(src, G)
+        first, last = active_range(src, G)
         info[s] = (kind, comp, src.xcoord, src.ycoord, src.zcoord, first, last, 0)
         scale[s] = sc
         waves[s] = table
     return info, scale, waves
+
+
+def model_inputs(G, options=0):
+    """Everything the C ABI receives for grid ``G``: the descriptor and the host arrays, in
+    the reference's layouts. Reads only attributes that the reference's own grid object also
+    carries, so a grid built by the reference's ``run_model`` can be handed over unchanged."""
+    if getattr(G, 'transmissionlines', None):
+        raise SolverError('transmission lines are not supported by the GB300 solver core')
+    d = _native.GridDesc()
+    d.nx, d.ny, d.nz = G.nx, G.ny, G.nz
+    d.iterations = G.iterations
+    d.nmat = len(G.materials)
+    d.maxpoles = pole_count(G)
+    d.pml_formulation = 0 if G.pmlformulation == 'HORIPML' else 1
+    d.pml_order = max(len(G.cfs), 1)
+    thick = {pml.ID: pml.thickness for pml in G.pmls}
+    for s, key in enumerate(PML_SLABS):
+        d.pml_thickness[s] = thick.get(key, 0)
+    d.dx, d.dy, d.dz = np.float32(G.dx), np.float32(G.dy), np.float32(G.dz)
+    d.nsrc = len(source_list(G))
+    d.nrx = len(G.rxs)
+    d.nsnap = len(G.snapshots)
+    d.options = options
+    inp = {'desc': d,
+           'ID': np.ascontiguousarray(G.ID, dtype=np.uint32),
+           'coeffE': np.ascontiguousarray(G.updatecoeffsE, dtype=np.float32),
+           'coeffH': np.ascontiguousarray(G.updatecoeffsH, dtype=np.float32),
+           'coeffD': None, 'pml': [], 'sources': None, 'rx': None, 'snapshots': None}
+    if d.maxpoles > 0:
+        inp['coeffD'] = np.ascontiguousarray(G.updatecoeffsdispersive, dtype=np.complex64)
+    for pml in G.pmls:
+        rows = [np.ascontiguousarray(getattr(pml, n), dtype=np.float32)
+                for n in ('ERA', 'ERB', 'ERE', 'ERF', 'HRA', 'HRB', 'HRE', 'HRF')]
+        inp['pml'].append((PML_SLABS.index(pml.ID), rows))
+    if d.nsrc:
+        inp['sources'] = source_tables(G)
+    if G.rxs:
+        inp['rx'] = np.array([[r.xcoord, r.ycoord, r.zcoord] for r in G.rxs], dtype=np.int32)
+    if G.snapshots:
+        inp['snapshots'] = np.array([[s.xs, s.ys, s.zs, s.dx, s.dy, s.dz, s.nx, s.ny, s.nz, s.time]
+                                     for s in G.snapshots], dtype=np.int32)
+    return inp
 
 
 class DeviceModel:
@@ -50,22 +103,9 @@ class DeviceModel:
         self.G = G
         self.lib = _native.lib()
         self.ctx = ctypes.c_void_p(0)
-        d = _native.GridDesc()
-        d.nx, d.ny, d.nz = G.nx, G.ny, G.nz
-        d.iterations = G.iterations
-        d.nmat = len(G.materials)
-        d.maxpoles = G.maxpoles
-        d.pml_formulation = 0 if G.pmlformulation == 'HORIPML' else 1
-        d.pml_order = max(len(G.cfs), 1)
-        thick = {pml.ID: pml.thickness for pml in G.pmls}
-        for s, key in enumerate(PML_SLABS):
-            d.pml_thickness[s] = thick.get(key, 0)
-        d.dx, d.dy, d.dz = np.float32(G.dx), np.float32(G.dy), np.float32(G.dz)
-        d.nsrc = len(source_list(G))
-        d.nrx = len(G.rxs)
-        d.nsnap = len(G.snapshots)
-        d.options = options
-        self.desc = d
+        self.inputs = model_inputs(G, options)
+        d = self.desc = self.inputs['desc']
+        self.maxpoles = d.maxpoles
         self._check(self.lib.gbf_create(ctypes.byref(d), ctypes.byref(self.ctx)), create=True)
         try:
             self._upload()
@@ -80,31 +120,22 @@ class DeviceModel:
             raise SolverError('libgbfdtd error {}: {}'.format(rc, buf.value.decode()))
 
     def _upload(self):
-        G = self.G
-        ID = np.ascontiguousarray(G.ID, dtype=np.uint32)
-        cE = np.ascontiguousarray(G.updatecoeffsE, dtype=np.float32)
-        cH = np.ascontiguousarray(G.updatecoeffsH, dtype=np.float32)
-        cD = None
-        if G.maxpoles > 0:
-            cD = np.ascontiguousarray(G.updatecoeffsdispersive, dtype=np.complex64)
-        self._check(self.lib.gbf_upload_materials(self.ctx, _ptr(ID), _ptr(cE), _ptr(cH), _ptr(cD)))
-        for pml in G.pmls:
-            rows = [np.ascontiguousarray(getattr(pml, n), dtype=np.float32)
-                    for n in ('ERA', 'ERB', 'ERE', 'ERF', 'HRA', 'HRB', 'HRE', 'HRF')]
+        inp = self.inputs
+        self._check(self.lib.gbf_upload_materials(self.ctx, _ptr(inp['ID']), _ptr(inp['coeffE']),
+                                                  _ptr(inp['coeffH']), _ptr(inp['coeffD'])))
+        for slab, rows in inp['pml']:
             arr = (ctypes.c_void_p * 8)(*[r.ctypes.data for r in rows])
-            self._check(self.lib.gbf_upload_pml(self.ctx, PML_SLABS.index(pml.ID), arr))
-            self._keep = rows
-        if self.desc.nsrc:
-            info, scale, waves = source_tables(G)
+            self._check(self.lib.gbf_upload_pml(self.ctx, slab, arr))
+        if inp['sources'] is not None:
+            info, scale, waves = inp['sources']
             self._check(self.lib.gbf_upload_sources(self.ctx, _ptr(info), _ptr(scale), _ptr(waves)))
-        if G.rxs:
-            coords = np.array([[r.xcoord, r.ycoord, r.zcoord] for r in G.rxs], dtype=np.int32)
-            self._check(self.lib.gbf_set_receivers(self.ctx, _ptr(coords)))
-        if G.snapshots:
-            defs = np.array([[s.xs, s.ys, s.zs, s.dx, s.dy, s.dz, s.nx, s.ny, s.nz, s.time]
-                             for s in G.snapshots], dtype=np.int32)
-            self._check(self.lib.gbf_set_snapshots(self.ctx, _ptr(defs)))
+        if inp['rx'] is not None:
+            self._check(self.lib.gbf_set_receivers(self.ctx, _ptr(inp['rx'])))
+        if inp['snapshots'] is not None:
+            self._check(self.lib.gbf_set_snapshots(self.ctx, _ptr(inp['snapshots'])))
         self.reset()
+        self.synchronize()
+        self.inputs = None   # every host array has been copied to the device
 
     def reset(self):
         self._check(self.lib.gbf_reset(self.ctx))
@@ -152,7 +183,7 @@ class DeviceModel:
     def dispersive(self):
         """complex64 [3][maxpoles][nx+1][ny+1][nz+1] (Tx, Ty, Tz)."""
         G = self.G
-        out = np.zeros((3, G.maxpoles, G.nx + 1, G.ny + 1, G.nz + 1), dtype=np.complex64)
+        out = np.zeros((3, self.maxpoles, G.nx + 1, G.ny + 1, G.nz + 1), dtype=np.complex64)
         self._check(self.lib.gbf_download_dispersive(self.ctx, _ptr(out)))
         return out
 
@@ -194,11 +225,13 @@ class DeviceModel:
                 r.outputs[name] = rx[OUTPUT_INDEX[name], :, n].copy()
         for s, snap in enumerate(G.snapshots):
             f = self.snapshot(s)
-            snap.set_fields(*f)
+            # the VTK point layout the reference's Snapshot.store leaves (snapshots.py:129-130)
+            snap.electric = np.stack(f[:3]).reshape(-1, order='F')
+            snap.magnetic = np.stack(f[3:]).reshape(-1, order='F')
         if fields:
             f = self.fields()
             G.Ex, G.Ey, G.Ez, G.Hx, G.Hy, G.Hz = (f[c] for c in range(6))
-            if G.maxpoles > 0:
+            if self.maxpoles > 0:
                 T = self.dispersive()
                 G.Tx, G.Ty, G.Tz = T[0], T[1], T[2]
 

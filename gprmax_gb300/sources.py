@@ -46,14 +46,6 @@ class Source:
         if t.size:
             self.waveformvalues_wholestep[active] = waveform.values(t, G.dt)
             self.waveformvalues_halfstep[active] = waveform.values(t + 0.5 * G.dt, G.dt)
-        self.active = active
-
-    def active_range(self):
-        """First and last active iteration (inclusive); (0, -1) when never active."""
-        idx = np.nonzero(self.active)[0]
-        if idx.size == 0:
-            return 0, -1
-        return int(idx[0]), int(idx[-1])
 
 
 class VoltageSource(Source):
@@ -85,16 +77,6 @@ class VoltageSource(Source):
         G.ID[comp, i, j, k] = newmaterial.numID
         G.materials.append(newmaterial)
 
-    def kernel_record(self, G):
-        comp = 'xyz'.index(self.polarisation)
-        if self.resistance != 0:
-            other = {'x': G.dy * G.dz, 'y': G.dx * G.dz, 'z': G.dx * G.dy}[self.polarisation]
-            scale = (np.float32(1 / (self.resistance * other)), np.float32(1))
-            return KIND_VOLTAGE_RESISTIVE, comp, scale, self.waveformvalues_wholestep
-        d = {'x': G.dx, 'y': G.dy, 'z': G.dz}[self.polarisation]
-        return KIND_VOLTAGE_HARD, comp, (np.float32(d), np.float32(1)), self.waveformvalues_halfstep
-
-
 class HertzianDipole(Source):
     """Additive electric current element of length ``dl`` on one E edge."""
 
@@ -102,16 +84,41 @@ class HertzianDipole(Source):
         super().__init__()
         self.dl = None
 
-    def kernel_record(self, G):
-        comp = 'xyz'.index(self.polarisation)
-        scale = (np.float32(self.dl), np.float32(1 / (G.dx * G.dy * G.dz)))
-        return KIND_HERTZIAN, comp, scale, self.waveformvalues_wholestep
-
-
 class MagneticDipole(Source):
     """Additive magnetic current element on one H edge."""
 
-    def kernel_record(self, G):
-        comp = 3 + 'xyz'.index(self.polarisation)
+
+def active_range(src, G):
+    """First and last iteration (inclusive) at which the source is active: those whose time
+    ``G.dt * iteration`` lies in [start, stop] (``sources.py:61-64``); (0, -1) when none."""
+    t = G.dt * np.arange(G.iterations, dtype=np.float64)
+    idx = np.nonzero((t >= src.start) & (t <= src.stop))[0]
+    if idx.size == 0:
+        return 0, -1
+    return int(idx[0]), int(idx[-1])
+
+
+def kernel_record(src, G):
+    """(kind, component, (s0, s1), waveform table) of one source for the native solver.
+
+    Reads only attributes the reference's own source objects carry (``polarisation``,
+    ``resistance``, ``dl``, ``waveformvalues_wholestep``/``_halfstep``), so it serves sources
+    built by this package's parser and by the reference's alike."""
+    name = type(src).__name__
+    if name == 'VoltageSource':
+        comp = 'xyz'.index(src.polarisation)
+        if src.resistance != 0:
+            other = {'x': G.dy * G.dz, 'y': G.dx * G.dz, 'z': G.dx * G.dy}[src.polarisation]
+            scale = (np.float32(1 / (src.resistance * other)), np.float32(1))
+            return KIND_VOLTAGE_RESISTIVE, comp, scale, src.waveformvalues_wholestep
+        d = {'x': G.dx, 'y': G.dy, 'z': G.dz}[src.polarisation]
+        return KIND_VOLTAGE_HARD, comp, (np.float32(d), np.float32(1)), src.waveformvalues_halfstep
+    if name == 'HertzianDipole':
+        comp = 'xyz'.index(src.polarisation)
+        scale = (np.float32(src.dl), np.float32(1 / (G.dx * G.dy * G.dz)))
+        return KIND_HERTZIAN, comp, scale, src.waveformvalues_wholestep
+    if name == 'MagneticDipole':
+        comp = 3 + 'xyz'.index(src.polarisation)
         scale = (np.float32(1 / (G.dx * G.dy * G.dz)), np.float32(1))
-        return KIND_MAGNETIC, comp, scale, self.waveformvalues_halfstep
+        return KIND_MAGNETIC, comp, scale, src.waveformvalues_halfstep
+    raise TypeError('source type {} is not supported by the GB300 solver core'.format(name))
