@@ -110,6 +110,8 @@ _SIGS = {
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
+    'gbf_sweep_boxes': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
+                                       ctypes.c_int32, _P]),
 }
 
 

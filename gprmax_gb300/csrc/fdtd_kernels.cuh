@@ -17,9 +17,10 @@
 // floating-point contraction, the results are bit-identical to the reference's CPU kernels
 // compiled the same way.
 //
-// Thread mapping: a persistent grid sweeps the flattened node index in order (consecutive
-// threads on consecutive nodes), one node per thread per pass. Nodes outside the PML box skip
-// all PML work. The coefficient tables are staged in shared memory when they fit (the reference
+// Thread mapping: a persistent grid sweeps the nodes box by box (consecutive threads on
+// consecutive nodes), one node per thread per pass: first the core box, where no PML slab and no
+// domain face is near and the update has no branches, then the five shell boxes that hold the
+// PML slabs and the faces, so their warps run the PML code densely. The coefficient tables are staged in shared memory when they fit (the reference
 // keeps them in __constant__ memory, model_build_run.py:512-519).
 #pragma once
 #include <cstdint>
@@ -69,6 +70,16 @@ struct Src {
   const float* w;   // this source's waveform table [iterations]
 };
 
+// A sweep box: nodes (i0 + a, j0 + b, k0 + c + (c >= ksplit ? kgap : 0)) for a < bi, b < bj,
+// c < bk, at positions [start, start + count) of the half-step's virtual node index. Box 0 is
+// the core (whole rows away from the x and y slabs and faces); boxes 1-4 are the x-minus and
+// x-plus planes and the y-minus and y-plus rows between them; box 5 is spare (empty).
+constexpr int kBoxes = 6;
+struct Box {
+  int i0, j0, k0, bi, bj, bk, ksplit, kgap;
+  int start, count;
+};
+
 struct StepParams {
   float* E[3];
   float* H[3];
@@ -94,7 +105,8 @@ struct StepParams {
   int srcqE[kSrcInline];  // flat node index of the first sources (lets a node test itself cheaply)
   int srcqH[kSrcInline];
   const int* d_it;
-  int chunk;              // x planes per block
+  Box boxE[kBoxes];       // sweep boxes of the E half-step (domain [0,nx) x [0,ny) x [0,nz))
+  Box boxH[kBoxes];       // and of the H half-step (domain [0,nx] x [0,ny] x [0,nz])
 };
 
 // ---------------------------------------------------------------------------------------
@@ -268,30 +280,32 @@ __device__ __forceinline__ void stage_tables(const StepParams& p, bool electric,
 }
 
 // ---------------------------------------------------------------------------------------
-// Flat persistent sweep: threads take consecutive nodes of the flattened (i, j, k) index, and a
-// grid of a few blocks per SM strides through the whole array in order, so every array is
-// streamed front to back by the whole GPU at once (DRAM-page friendly for the ~20 concurrent
-// streams of a half-step). Neighbours along j, k (and x) are re-read from L1/L2.
-// The node index is advanced incrementally: the stride splits into whole planes, rows and nodes.
-struct FlatWalk {
-  int i, j, k, si, sj, sk, rows;
-  __device__ __forceinline__ FlatWalk(long long q, long long stride, int sx, int sy, int nrows) {
-    rows = nrows;
-    i = (int)(q / sx);
-    int r = (int)(q - (long long)i * sx);
-    j = r / sy;
-    k = r - j * sy;
-    si = (int)(stride / sx);
-    r = (int)(stride - (long long)si * sx);
-    sj = r / sy;
-    sk = r - sj * sy;
+// Persistent sweep: a grid of a few blocks per SM strides through each box's nodes in order
+// (consecutive threads on consecutive nodes), so every array is streamed front to back by the
+// whole GPU at once; neighbours along j, k (and x) are re-reads served by L1/L2. The position in
+// the box advances incrementally: the grid stride splits into whole planes, rows and nodes.
+struct BoxWalk {
+  int a, b, c, sa, sb, sc;
+  __device__ __forceinline__ BoxWalk(int q, int stride, const Box& B) {
+    const int plane = B.bj * B.bk;
+    a = q / plane;
+    int r = q - a * plane;
+    b = r / B.bk;
+    c = r - b * B.bk;
+    sa = stride / plane;
+    r = stride - sa * plane;
+    sb = r / B.bk;
+    sc = r - sb * B.bk;
   }
-  __device__ __forceinline__ void advance(int sy) {
-    k += sk;
-    if (k >= sy) { k -= sy; ++j; }
-    j += sj;
-    if (j >= rows) { j -= rows; ++i; }
-    i += si;
+  __device__ __forceinline__ void advance(const Box& B) {
+    c += sc;
+    if (c >= B.bk) { c -= B.bk; ++b; }
+    b += sb;
+    if (b >= B.bj) { b -= B.bj; ++a; }
+    a += sa;
+  }
+  __device__ __forceinline__ int k(const Box& B) const {
+    return B.k0 + c + (c >= B.ksplit ? B.kgap : 0);
   }
 };
 
@@ -325,23 +339,24 @@ __device__ __forceinline__ bool node_has_source(int idx, int n, const int* inl, 
 // the PML). The X values of the node's slabs are formed first (they depend only on the E
 // differences and the Phi state), then each component takes its main update and its
 // corrections in the reference's order.
-template <int PK>
+template <int PK, bool CORE>
 __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, const float* Cs,
                                        int i, int j, int k, bool src, int it, const int* where,
                                        const int* pr, float dEz_y, float dEy_z, float dEx_z,
                                        float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
                                        uint32_t my, uint32_t mz, float& hx, float& hy, float& hz) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
-  const bool iin = i < nx, jin = j < ny, kin = k < nz;
+  const bool iin = CORE || i < nx, jin = CORE || j < ny, kin = k < nz;
+  const bool ipos = CORE || i >= 1, jpos = CORE || j >= 1;
   float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
   if (PK != PML_NONE) {
-    if (where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0]);
-    if (where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1]);
+    if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0]);
+    if (!CORE && where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1]);
     if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2]);
   }
   // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
-    const bool mainu = (i >= 1) && jin && kin;
+    const bool mainu = ipos && jin && kin;
     const bool pml = PK != PML_NONE && (where[1] || where[2]);
     if (mainu || pml || src) {
       float F = hx;
@@ -356,7 +371,7 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   }
   // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
   {
-    const bool mainu = iin && (j >= 1) && kin;
+    const bool mainu = iin && jpos && kin;
     const bool pml = PK != PML_NONE && (where[0] || where[2]);
     if (mainu || pml || src) {
       float F = hy;
@@ -386,7 +401,58 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   }
 }
 
-// H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz] (every node of the arrays).
+// One H node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j
+// in [1, n-1] and outside the x and y slabs), so only k decides neighbours and PML terms.
+template <int PK, int IDP, bool CORE>
+__device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, const float* Cs,
+                                       int i, int j, int k, int it) {
+  const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
+  const int idx = i * sx + j * sy + k;
+  const float* __restrict__ Ex = p.E[0];
+  const float* __restrict__ Ey = p.E[1];
+  const float* __restrict__ Ez = p.E[2];
+  float* __restrict__ Hx = p.H[0];
+  float* __restrict__ Hy = p.H[1];
+  float* __restrict__ Hz = p.H[2];
+  const bool iin = CORE || i < nx, jin = CORE || j < ny, kin = k < nz;
+  // issue every load of the node before any store
+  const float ex_c = __ldg(Ex + idx), ey_c = __ldg(Ey + idx), ez_c = __ldg(Ez + idx);
+  const float ex_j = jin ? __ldg(Ex + idx + sy) : 0.f;
+  const float ez_j = jin ? __ldg(Ez + idx + sy) : 0.f;
+  const float ex_k = kin ? __ldg(Ex + idx + 1) : 0.f;
+  const float ey_k = kin ? __ldg(Ey + idx + 1) : 0.f;
+  const float ey_n = iin ? __ldg(Ey + idx + sx) : 0.f;
+  const float ez_n = iin ? __ldg(Ez + idx + sx) : 0.f;
+  uint32_t mx, my, mz;
+  if (IDP == 1) {
+    const uint32_t w = __ldg(p.PH + idx);
+    mx = w & kPackMask;
+    my = (w >> kPackBits) & kPackMask;
+    mz = (w >> (2 * kPackBits)) & kPackMask;
+  } else {
+    mx = __ldg(p.ID[3] + idx);
+    my = __ldg(p.ID[4] + idx);
+    mz = __ldg(p.ID[5] + idx);
+  }
+  float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
+  int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
+  if (PK != PML_NONE && iin && jin && kin) {
+    if (!CORE) {
+      where[0] = axis_member<false>(i, nx, p.slab[0].T, p.slab[3].T, pr[0]);
+      where[1] = axis_member<false>(j, ny, p.slab[1].T, p.slab[4].T, pr[1]);
+    }
+    where[2] = axis_member<false>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
+  }
+  const bool src = p.nsrcH && node_has_source(idx, p.nsrcH, p.srcqH, p.srcH, sx, sy);
+  h_node<PK, CORE>(p, C4, Cs, i, j, k, src, it, where, pr, ez_j - ez_c, ey_k - ey_c, ex_k - ex_c,
+                   ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
+  Hx[idx] = hx;
+  Hy[idx] = hy;
+  Hz[idx] = hz;
+}
+
+// H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz] (every node of the arrays),
+// swept box by box (core first) by one persistent grid.
 template <int PK, int IDP>
 __global__ void __launch_bounds__(kThreads, 5)
 h_half_step(const __grid_constant__ StepParams p) {
@@ -399,60 +465,27 @@ h_half_step(const __grid_constant__ StepParams p) {
   }
   const float4* C4 = p.smem ? s4 : p.cH4;
   const float* Cs = p.smem ? ss : p.cHs;
-  const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
-  const float* __restrict__ Ex = p.E[0];
-  const float* __restrict__ Ey = p.E[1];
-  const float* __restrict__ Ez = p.E[2];
-  float* __restrict__ Hx = p.H[0];
-  float* __restrict__ Hy = p.H[1];
-  float* __restrict__ Hz = p.H[2];
-  const long long total = (long long)(nx + 1) * sx;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  FlatWalk w(q, stride, sx, sy, ny + 1);
-  // interior box: nodes outside every H slab range (minus [0,T-1], plus [n-T, n-1])
-  const int xlo = p.slab[0].T, xhi = nx - p.slab[3].T;
-  const int ylo = p.slab[1].T, yhi = ny - p.slab[4].T;
-  const int zlo = p.slab[2].T, zhi = nz - p.slab[5].T;
   int it = 0;
   if (p.nsrcH) it = *p.d_it;
-  for (; q < total; q += stride, w.advance(sy)) {
-    const int idx = (int)q;
-    const int i = w.i, j = w.j, k = w.k;
-    const bool iin = i < nx, jin = j < ny, kin = k < nz;
-    // issue every load of the node before any store
-    const float ex_c = __ldg(Ex + idx), ey_c = __ldg(Ey + idx), ez_c = __ldg(Ez + idx);
-    const float ex_j = jin ? __ldg(Ex + idx + sy) : 0.f;
-    const float ez_j = jin ? __ldg(Ez + idx + sy) : 0.f;
-    const float ex_k = kin ? __ldg(Ex + idx + 1) : 0.f;
-    const float ey_k = kin ? __ldg(Ey + idx + 1) : 0.f;
-    const float ey_n = iin ? __ldg(Ey + idx + sx) : 0.f;
-    const float ez_n = iin ? __ldg(Ez + idx + sx) : 0.f;
-    uint32_t mx, my, mz;
-    if (IDP == 1) {
-      const uint32_t w = __ldg(p.PH + idx);
-      mx = w & kPackMask;
-      my = (w >> kPackBits) & kPackMask;
-      mz = (w >> (2 * kPackBits)) & kPackMask;
-    } else {
-      mx = __ldg(p.ID[3] + idx);
-      my = __ldg(p.ID[4] + idx);
-      mz = __ldg(p.ID[5] + idx);
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  {
+    const Box& B = p.boxH[0];
+    const int end = B.start + B.count;
+    if (q < end) {
+      BoxWalk w(q - B.start, stride, B);
+      for (; q < end; q += stride, w.advance(B))
+        h_site<PK, IDP, true>(p, C4, Cs, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
-    float hx = Hx[idx], hy = Hy[idx], hz = Hz[idx];
-    int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
-    if (PK != PML_NONE && iin && jin && kin &&
-        !(i >= xlo && i < xhi && j >= ylo && j < yhi && k >= zlo && k < zhi)) {
-      where[0] = axis_member<false>(i, nx, p.slab[0].T, p.slab[3].T, pr[0]);
-      where[1] = axis_member<false>(j, ny, p.slab[1].T, p.slab[4].T, pr[1]);
-      where[2] = axis_member<false>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
-    }
-    const bool src = p.nsrcH && node_has_source(idx, p.nsrcH, p.srcqH, p.srcH, sx, sy);
-    h_node<PK>(p, C4, Cs, i, j, k, src, it, where, pr, ez_j - ez_c, ey_k - ey_c, ex_k - ex_c,
-               ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
-    Hx[idx] = hx;
-    Hy[idx] = hy;
-    Hz[idx] = hz;
+  }
+#pragma unroll 1
+  for (int b = 1; b < kBoxes; ++b) {
+    const Box& B = p.boxH[b];
+    const int end = B.start + B.count;
+    if (q >= end) continue;
+    BoxWalk w(q - B.start, stride, B);
+    for (; q < end; q += stride, w.advance(B))
+      h_site<PK, IDP, false>(p, C4, Cs, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
 }
 
@@ -480,7 +513,7 @@ __device__ __forceinline__ float apply_e_sources(float F, int comp, int i, int j
 // E update of one node for all three components: main update (update_electric, or part A of
 // the dispersive update), slab corrections in slab order, sources, dispersive part B.
 // where[a] / pr[a]: slab membership and profile index along each axis (0 outside the PML).
-template <int PK, int NP>
+template <int PK, int NP, bool CORE>
 __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
                                        const float2* CD, int i, int j, int k, bool src, int it,
                                        const int* where, const int* pr, float dHz_y,
@@ -488,21 +521,21 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
                                        float dHx_y, const uint32_t* m, float* e, float2 (*t)[NP > 0 ? NP : 1]) {
   float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
   if (PK != PML_NONE) {
-    if (where[0]) pml_axis<PK, true, 0>(p, where[0], pr[0], i, j, k, dHz_x, dHy_x, XA[0], XB[0]);
-    if (where[1]) pml_axis<PK, true, 1>(p, where[1], pr[1], i, j, k, dHz_y, dHx_y, XA[1], XB[1]);
+    if (!CORE && where[0]) pml_axis<PK, true, 0>(p, where[0], pr[0], i, j, k, dHz_x, dHy_x, XA[0], XB[0]);
+    if (!CORE && where[1]) pml_axis<PK, true, 1>(p, where[1], pr[1], i, j, k, dHz_y, dHx_y, XA[1], XB[1]);
     if (where[2]) pml_axis<PK, true, 2>(p, where[2], pr[2], i, j, k, dHy_z, dHx_z, XA[2], XB[2]);
   }
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
     bool mainu, pml;
     if (comp == 0) {
-      mainu = (j >= 1) && (k >= 1);
+      mainu = (CORE || j >= 1) && (k >= 1);
       pml = where[1] || where[2];
     } else if (comp == 1) {
-      mainu = (i >= 1) && (k >= 1);
+      mainu = (CORE || i >= 1) && (k >= 1);
       pml = where[0] || where[2];
     } else {
-      mainu = (i >= 1) && (j >= 1);
+      mainu = CORE || ((i >= 1) && (j >= 1));
       pml = where[0] || where[1];
     }
     if (PK == PML_NONE) pml = false;
@@ -556,7 +589,71 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
   }
 }
 
-// E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz). NP = dispersive poles.
+// One E node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j
+// >= 1 and outside the x and y slabs), so only k decides neighbours and PML terms.
+template <int PK, int NP, int IDP, bool CORE>
+__device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, const float* Cs,
+                                       const float2* CD, int i, int j, int k, int it) {
+  const int sx = p.sx, sy = p.sy;
+  const int idx = i * sx + j * sy + k;
+  const float* __restrict__ Hx = p.H[0];
+  const float* __restrict__ Hy = p.H[1];
+  const float* __restrict__ Hz = p.H[2];
+  constexpr int NPV = NP > 0 ? NP : 1;
+  // issue every load of the node before any store
+  const float hx_c = __ldg(Hx + idx), hy_c = __ldg(Hy + idx), hz_c = __ldg(Hz + idx);
+  const float hx_j = (CORE || j >= 1) ? __ldg(Hx + idx - sy) : 0.f;
+  const float hz_j = (CORE || j >= 1) ? __ldg(Hz + idx - sy) : 0.f;
+  const float hx_k = k >= 1 ? __ldg(Hx + idx - 1) : 0.f;
+  const float hy_k = k >= 1 ? __ldg(Hy + idx - 1) : 0.f;
+  const float hy_p = (CORE || i >= 1) ? __ldg(Hy + idx - sx) : 0.f;
+  const float hz_p = (CORE || i >= 1) ? __ldg(Hz + idx - sx) : 0.f;
+  uint32_t m[3];
+  float e[3];
+  float2 t[3][NPV];
+  // dispersive state is identically zero on nodes whose materials have no poles (their
+  // coefficients are all zero), so it is not written there; it is still read with the
+  // node's other loads, which keeps those loads independent of the ID load
+  bool disp = NP > 0;
+  if (IDP == 1) {
+    const uint32_t w = __ldg(p.PE + idx);
+    m[0] = w & kPackMask;
+    m[1] = (w >> kPackBits) & kPackMask;
+    m[2] = (w >> (2 * kPackBits)) & kPackMask;
+    disp = NP > 0 && (w & kDispersiveBit);
+  } else {
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) m[comp] = __ldg(p.ID[comp] + idx);
+  }
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    e[comp] = p.E[comp][idx];
+#pragma unroll
+    for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
+  }
+  int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
+  if (PK != PML_NONE) {
+    if (!CORE) {
+      where[0] = axis_member<true>(i, p.nx, p.slab[0].T, p.slab[3].T, pr[0]);
+      where[1] = axis_member<true>(j, p.ny, p.slab[1].T, p.slab[4].T, pr[1]);
+    }
+    where[2] = axis_member<true>(k, p.nz, p.slab[2].T, p.slab[5].T, pr[2]);
+  }
+  const bool src = p.nsrcE && node_has_source(idx, p.nsrcE, p.srcqE, p.srcE, sx, sy);
+  e_node<PK, NP, CORE>(p, C4, Cs, CD, i, j, k, src, it, where, pr, hz_c - hz_j, hy_c - hy_k,
+                       hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp) {
+    p.E[comp][idx] = e[comp];
+    if (disp) {
+#pragma unroll
+      for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
+    }
+  }
+}
+
+// E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz), swept box by box (core
+// first) by one persistent grid. NP = dispersive poles.
 template <int PK, int NP, int IDP>
 __global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
 e_half_step(const __grid_constant__ StepParams p) {
@@ -571,73 +668,27 @@ e_half_step(const __grid_constant__ StepParams p) {
   const float4* C4 = p.smem ? s4 : p.cE4;
   const float* Cs = p.smem ? ss : p.cEs;
   const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
-  const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
-  const float* __restrict__ Hx = p.H[0];
-  const float* __restrict__ Hy = p.H[1];
-  const float* __restrict__ Hz = p.H[2];
-  constexpr int NPV = NP > 0 ? NP : 1;
-  const long long total = (long long)nx * sx;
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  FlatWalk w(q, stride, sx, sy, ny + 1);
-  // interior box: nodes outside every E slab range (minus [1,T], plus [n-T, n-1])
-  const int xlo = p.slab[0].T, xhi = nx - p.slab[3].T;
-  const int ylo = p.slab[1].T, yhi = ny - p.slab[4].T;
-  const int zlo = p.slab[2].T, zhi = nz - p.slab[5].T;
   int it = 0;
   if (p.nsrcE) it = *p.d_it;
-  for (; q < total; q += stride, w.advance(sy)) {
-    const int idx = (int)q;
-    const int i = w.i, j = w.j, k = w.k;
-    if (j >= ny || k >= nz) continue;
-    // issue every load of the node before any store
-    const float hx_c = __ldg(Hx + idx), hy_c = __ldg(Hy + idx), hz_c = __ldg(Hz + idx);
-    const float hx_j = j >= 1 ? __ldg(Hx + idx - sy) : 0.f;
-    const float hz_j = j >= 1 ? __ldg(Hz + idx - sy) : 0.f;
-    const float hx_k = k >= 1 ? __ldg(Hx + idx - 1) : 0.f;
-    const float hy_k = k >= 1 ? __ldg(Hy + idx - 1) : 0.f;
-    const float hy_p = i >= 1 ? __ldg(Hy + idx - sx) : 0.f;
-    const float hz_p = i >= 1 ? __ldg(Hz + idx - sx) : 0.f;
-    uint32_t m[3];
-    float e[3];
-    float2 t[3][NPV];
-    // dispersive state is identically zero on nodes whose materials have no poles (their
-    // coefficients are all zero), so it is not written there; it is still read with the
-    // node's other loads, which keeps those loads independent of the ID load
-    bool disp = NP > 0;
-    if (IDP == 1) {
-      const uint32_t w = __ldg(p.PE + idx);
-      m[0] = w & kPackMask;
-      m[1] = (w >> kPackBits) & kPackMask;
-      m[2] = (w >> (2 * kPackBits)) & kPackMask;
-      disp = NP > 0 && (w & kDispersiveBit);
-    } else {
-#pragma unroll
-      for (int comp = 0; comp < 3; ++comp) m[comp] = __ldg(p.ID[comp] + idx);
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  {
+    const Box& B = p.boxE[0];
+    const int end = B.start + B.count;
+    if (q < end) {
+      BoxWalk w(q - B.start, stride, B);
+      for (; q < end; q += stride, w.advance(B))
+        e_site<PK, NP, IDP, true>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
-#pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-      e[comp] = p.E[comp][idx];
-#pragma unroll
-      for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
-    }
-    int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
-    if (PK != PML_NONE && !(i > xlo && i < xhi && j > ylo && j < yhi && k > zlo && k < zhi)) {
-      where[0] = axis_member<true>(i, nx, p.slab[0].T, p.slab[3].T, pr[0]);
-      where[1] = axis_member<true>(j, ny, p.slab[1].T, p.slab[4].T, pr[1]);
-      where[2] = axis_member<true>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
-    }
-    const bool src = p.nsrcE && node_has_source(idx, p.nsrcE, p.srcqE, p.srcE, sx, sy);
-    e_node<PK, NP>(p, C4, Cs, CD, i, j, k, src, it, where, pr, hz_c - hz_j, hy_c - hy_k,
-                   hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
-#pragma unroll
-    for (int comp = 0; comp < 3; ++comp) {
-      p.E[comp][idx] = e[comp];
-      if (disp) {
-#pragma unroll
-        for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
-      }
-    }
+  }
+#pragma unroll 1
+  for (int b = 1; b < kBoxes; ++b) {
+    const Box& B = p.boxE[b];
+    const int end = B.start + B.count;
+    if (q >= end) continue;
+    BoxWalk w(q - B.start, stride, B);
+    for (; q < end; q += stride, w.advance(B))
+      e_site<PK, NP, IDP, false>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
 }
 

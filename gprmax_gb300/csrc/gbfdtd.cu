@@ -129,6 +129,43 @@ static bool reciprocal_division_exact(float d) {
   return ok;
 }
 
+// Sweep boxes of one half-step (Box in fdtd_kernels.cuh). Along x and y the domain splits into
+// [0, lo), the core range [lo, hi) and [hi, end): E (end = n) has its minus slab at [1, Tm] and
+// needs c >= 1 for every neighbour, so lo = Tm + 1; H (end = n + 1) has its minus slab at
+// [0, Tm - 1] and needs c in [1, n - 1], so lo = max(Tm, 1); both have hi = n - Tp. Rows stay
+// whole along z (the kernels test z-slab membership per node), so every box streams whole rows.
+static void make_boxes(bool electric, const int n[3], const int T[6], Box out[kBoxes]) {
+  int lo[3], hi[3], end[3];
+  for (int a = 0; a < 3; ++a) {
+    end[a] = electric ? n[a] : n[a] + 1;
+    lo[a] = electric ? T[a] + 1 : (T[a] > 1 ? T[a] : 1);
+    hi[a] = n[a] - T[a + 3];
+    if (lo[a] > end[a]) lo[a] = end[a];
+    if (hi[a] < lo[a]) hi[a] = lo[a];
+  }
+  auto box = [](int i0, int bi, int j0, int bj, int k0, int bk, int ksplit, int kgap) {
+    Box b;
+    b.i0 = i0; b.bi = bi; b.j0 = j0; b.bj = bj; b.k0 = k0; b.bk = bk;
+    b.ksplit = ksplit; b.kgap = kgap;
+    b.start = 0;
+    b.count = (bi > 0 && bj > 0 && bk > 0) ? bi * bj * bk : 0;
+    if (!b.count) b.bi = b.bj = b.bk = 1;   // keep the walker's divisors non-zero
+    return b;
+  };
+  const int cx = hi[0] - lo[0], cy = hi[1] - lo[1], ez = end[2];
+  out[0] = box(lo[0], cx, lo[1], cy, 0, ez, ez, 0);                           // core rows
+  out[1] = box(0, lo[0], 0, end[1], 0, ez, ez, 0);                            // x minus planes
+  out[2] = box(hi[0], end[0] - hi[0], 0, end[1], 0, ez, ez, 0);               // x plus planes
+  out[3] = box(lo[0], cx, 0, lo[1], 0, ez, ez, 0);                            // y minus rows
+  out[4] = box(lo[0], cx, hi[1], end[1] - hi[1], 0, ez, ez, 0);               // y plus rows
+  out[5] = box(0, 0, 0, 0, 0, 0, 0, 0);                                       // unused
+  int start = 0;
+  for (int b = 0; b < kBoxes; ++b) {
+    out[b].start = start;
+    start += out[b].count;
+  }
+}
+
 static int pml_kind(const gbf_grid_desc& d) {
   bool any = false;
   for (int s = 0; s < 6; ++s) any |= d.pml_thickness[s] > 0;
@@ -142,6 +179,23 @@ extern "C" {
 const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
 
 int gbf_check_cell_division(float d) { return reciprocal_division_exact(d) ? 1 : 0; }
+
+int gbf_sweep_boxes(int32_t nx, int32_t ny, int32_t nz, const int32_t thickness[6],
+                    int32_t electric, int32_t* boxes) {
+  if (nx < 1 || ny < 1 || nz < 1 || !thickness || !boxes) return GBF_EINVAL;
+  for (int s = 0; s < 6; ++s)
+    if (thickness[s] < 0 || 2 * thickness[s] >= (s % 3 == 0 ? nx : s % 3 == 1 ? ny : nz))
+      return GBF_EINVAL;
+  const int n[3] = {nx, ny, nz};
+  Box b[kBoxes];
+  make_boxes(electric != 0, n, thickness, b);
+  for (int q = 0; q < kBoxes; ++q) {
+    const int v[10] = {b[q].i0, b[q].j0, b[q].k0, b[q].bi, b[q].bj, b[q].bk, b[q].ksplit,
+                       b[q].kgap, b[q].start, b[q].count};
+    memcpy(boxes + 10 * q, v, sizeof(v));
+  }
+  return GBF_OK;
+}
 
 int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n) {
   if (!buf || n == 0) return GBF_EINVAL;
@@ -263,7 +317,11 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   p.smem = (d.nmat <= kSmemCoefMax && ctx->smem_e <= 32768 && !(d.options & 1)) ? 1 : 0;
   if (!p.smem) ctx->smem_e = ctx->smem_h = 0;
   p.d_it = ctx->d_it;
-  p.chunk = 16;
+  {
+    const int n3b[3] = {d.nx, d.ny, d.nz};
+    make_boxes(true, n3b, d.pml_thickness, p.boxE);
+    make_boxes(false, n3b, d.pml_thickness, p.boxH);
+  }
   float* phi = ctx->pml_mem;
   const float dd[3] = {d.dx, d.dy, d.dz};
   for (int s = 0; s < 6; ++s) {

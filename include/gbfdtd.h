@@ -169,6 +169,14 @@ const char* gbf_version(void);
  * divide (pml_updates_electric_HORIPML_ext.pyx:80 `dHz = (...) / dx`). */
 int gbf_check_cell_division(float d);
 
+/* The sweep boxes a half-step kernel walks for a grid (electric != 0: E half-step, domain
+ * [0,nx) x [0,ny) x [0,nz); else H, domain [0,nx] x [0,ny] x [0,nz]): six rows of ten int32
+ * (i0, j0, k0, bi, bj, bk, ksplit, kgap, start, count), box 0 the PML-free core. Host only, no
+ * device needed; for checking the decomposition. No counterpart in the reference, whose kernels
+ * loop over the whole domain and then over each slab (fields_updates_ext.pyx:30-110, pml.py). */
+int gbf_sweep_boxes(int32_t nx, int32_t ny, int32_t nz, const int32_t thickness[6],
+                    int32_t electric, int32_t* boxes);
+
 #ifdef __cplusplus
 }
 #endif

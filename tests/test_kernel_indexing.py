@@ -115,3 +115,55 @@ def test_slab_nodes_and_phi_indices(n3, thick, electric):
         idx = [q[4] for q in got]
         assert min(idx) >= 0 and max(idx) < ocount, 'slab {} comp {}: Phi index out of range'.format(*key)
         assert len(set(idx)) == len(idx), 'slab {} comp {}: Phi element shared'.format(*key)
+
+
+def _boxes(lib, n3, thick, electric):
+    import ctypes
+    out = np.zeros((6, 10), dtype=np.int32)
+    t = np.asarray(thick, dtype=np.int32)
+    rc = lib.gbf_sweep_boxes(n3[0], n3[1], n3[2], t.ctypes.data_as(ctypes.c_void_p),
+                             1 if electric else 0, out.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0
+    return out
+
+
+@pytest.fixture(scope='module')
+def native_lib():
+    from gprmax_gb300 import _native
+    _native.build()
+    return _native.load()
+
+
+@pytest.mark.parametrize('n3,thick', CASES + [((7, 9, 5), (0, 0, 0, 0, 0, 0)),
+                                              ((400, 400, 200), (10,) * 6)])
+@pytest.mark.parametrize('electric', [True, False])
+def test_sweep_boxes_cover_the_domain_once(native_lib, n3, thick, electric):
+    """The boxes the half-step kernels walk (host ``make_boxes``): every node of the kernel's
+    domain exactly once, the walk's virtual index contiguous, and the core box (box 0) only on
+    rows whose i and j have both neighbours inside the arrays and lie outside the x and y
+    slabs (the kernels handle z per node)."""
+    nx, ny, nz = n3
+    ext = (nx, ny, nz) if electric else (nx + 1, ny + 1, nz + 1)
+    boxes = _boxes(native_lib, n3, thick, electric)
+    seen = np.zeros(ext, dtype=np.int32)
+    start = 0
+    for b, (i0, j0, k0, bi, bj, bk, ksplit, kgap, st, count) in enumerate(boxes):
+        assert st == start
+        start += count
+        if count == 0:
+            continue
+        assert count == bi * bj * bk
+        c = np.arange(bk)
+        kk = k0 + c + np.where(c >= ksplit, kgap, 0)
+        ii = i0 + np.arange(bi)
+        jj = j0 + np.arange(bj)
+        assert ii.min() >= 0 and jj.min() >= 0 and kk.min() >= 0
+        assert ii.max() < ext[0] and jj.max() < ext[1] and kk.max() < ext[2]
+        seen[np.ix_(ii, jj, kk)] += 1
+        if b == 0:
+            for axis, idx in enumerate((ii, jj)):
+                where, _ = axis_member(idx, n3[axis], thick[axis], thick[axis + 3], electric)
+                assert not where.any(), 'core box reaches an x or y slab'
+                assert idx.min() >= 1 and idx.max() <= n3[axis] - 1
+    assert start == np.prod(ext)
+    assert (seen == 1).all()
