@@ -221,14 +221,22 @@ __device__ __forceinline__ int axis_member(int c, int n, int Tm, int Tp, int& pr
 template <int PK, bool ELECTRIC, int AX>
 __device__ __forceinline__ void pml_axis(const StepParams& p, int where, int pr, int i, int j,
                                          int k, float dA, float dB, float& XA, float& XB) {
-  const Slab& sl = p.slab[AX + (where == 2 ? 3 : 0)];
-  const int T = sl.T;
+  // the two slabs of the axis are selected field by field, which keeps every parameter read a
+  // constant-bank operand (no indexed parameter loads)
+  const Slab& m = p.slab[AX];
+  const Slab& q = p.slab[AX + 3];
+  const bool plus = where == 2;
+  const int T = plus ? q.T : m.T;
   const int pidx = phi_index<AX>(i, j, k, pr, T, p.ny, p.nz);
-  const PmlRow c = load_row<PK>(ELECTRIC ? sl.eR : sl.hR, T, pr);
-  const float d = sl.d, r = sl.rcp;
-  const int fast = sl.fastdiv;
-  XA = pml_update<PK>(div_cell(dA, d, r, fast), ELECTRIC ? sl.phiE1 : sl.phiH1, pidx, sl.ocount, c);
-  XB = pml_update<PK>(div_cell(dB, d, r, fast), ELECTRIC ? sl.phiE2 : sl.phiH2, pidx, sl.ocount, c);
+  const float* R = ELECTRIC ? (plus ? q.eR : m.eR) : (plus ? q.hR : m.hR);
+  const PmlRow c = load_row<PK>(R, T, pr);
+  const float d = m.d, r = m.rcp;   // the same cell size on both sides of an axis
+  const int fast = m.fastdiv;
+  const int ocount = plus ? q.ocount : m.ocount;
+  float* ph1 = ELECTRIC ? (plus ? q.phiE1 : m.phiE1) : (plus ? q.phiH1 : m.phiH1);
+  float* ph2 = ELECTRIC ? (plus ? q.phiE2 : m.phiE2) : (plus ? q.phiH2 : m.phiH2);
+  XA = pml_update<PK>(div_cell(dA, d, r, fast), ph1, pidx, ocount, c);
+  XB = pml_update<PK>(div_cell(dB, d, r, fast), ph2, pidx, ocount, c);
 }
 
 // Sign with which axis AX's X enters component C: H x-axis Hy +, Hz -; y-axis Hx -, Hz +;
@@ -358,46 +366,40 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   {
     const bool mainu = ipos && jin && kin;
     const bool pml = PK != PML_NONE && (where[1] || where[2]);
-    if (mainu || pml || src) {
-      float F = hx;
-      if (mainu) {
-        const float4 c = C4[mx];
-        F = c.x * F - c.z * dEz_y + c.w * dEy_z;
-      }
-      if (pml) F = apply_pml<false, 0>(F, Cs[mx], where, XA, XB);
-      if (src) F = apply_h_sources(F, 3, i, j, k, it, Cs[mx], p);
-      hx = F;
-    }
+    // the main update is formed on every node and kept where it applies (no branch)
+    const float4 c = C4[mx];
+    const float Fo = hx;
+    float F = c.x * Fo - c.z * dEz_y + c.w * dEy_z;
+    F = mainu ? F : Fo;
+    if (pml) F = apply_pml<false, 0>(F, Cs[mx], where, XA, XB);
+    if (src) F = apply_h_sources(F, 3, i, j, k, it, Cs[mx], p);
+    hx = F;
   }
   // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
   {
     const bool mainu = iin && jpos && kin;
     const bool pml = PK != PML_NONE && (where[0] || where[2]);
-    if (mainu || pml || src) {
-      float F = hy;
-      if (mainu) {
-        const float4 c = C4[my];
-        F = c.x * F - c.w * dEx_z + c.y * dEz_x;
-      }
-      if (pml) F = apply_pml<false, 1>(F, Cs[my], where, XA, XB);
-      if (src) F = apply_h_sources(F, 4, i, j, k, it, Cs[my], p);
-      hy = F;
-    }
+    // the main update is formed on every node and kept where it applies (no branch)
+    const float4 c = C4[my];
+    const float Fo = hy;
+    float F = c.x * Fo - c.w * dEx_z + c.y * dEz_x;
+    F = mainu ? F : Fo;
+    if (pml) F = apply_pml<false, 1>(F, Cs[my], where, XA, XB);
+    if (src) F = apply_h_sources(F, 4, i, j, k, it, Cs[my], p);
+    hy = F;
   }
   // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs along x and y
   {
     const bool mainu = iin && jin && (k >= 1);
     const bool pml = PK != PML_NONE && (where[0] || where[1]);
-    if (mainu || pml || src) {
-      float F = hz;
-      if (mainu) {
-        const float4 c = C4[mz];
-        F = c.x * F - c.y * dEy_x + c.z * dEx_y;
-      }
-      if (pml) F = apply_pml<false, 2>(F, Cs[mz], where, XA, XB);
-      if (src) F = apply_h_sources(F, 5, i, j, k, it, Cs[mz], p);
-      hz = F;
-    }
+    // the main update is formed on every node and kept where it applies (no branch)
+    const float4 c = C4[mz];
+    const float Fo = hz;
+    float F = c.x * Fo - c.y * dEy_x + c.z * dEx_y;
+    F = mainu ? F : Fo;
+    if (pml) F = apply_pml<false, 2>(F, Cs[mz], where, XA, XB);
+    if (src) F = apply_h_sources(F, 5, i, j, k, it, Cs[mz], p);
+    hz = F;
   }
 }
 
@@ -539,36 +541,35 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
       pml = where[0] || where[1];
     }
     if (PK == PML_NONE) pml = false;
-    if (!(mainu || pml || src)) continue;
     const uint32_t mm = m[comp];
     const float Eold = e[comp];
-    float F = Eold;
     float2 TA[NP > 0 ? NP : 1];
-    if (mainu) {
-      // curl terms in the reference's order: CA*E + CB1*d1 - CB2*d2
-      const float4 c = C4[mm];
-      float t1, t2;
-      if (comp == 0) { t1 = c.z * dHz_y; t2 = c.w * dHy_z; }
-      else if (comp == 1) { t1 = c.w * dHx_z; t2 = c.y * dHz_x; }
-      else { t1 = c.y * dHy_x; t2 = c.z * dHx_y; }
-      if (NP == 0) {
-        F = c.x * Eold + t1 - t2;
-      } else {
-        float phi = 0.f;
-        const float2* cd = CD + mm * 3 * NP;
+    // the main update is formed on every node and kept where it applies (no branch); curl
+    // terms in the reference's order: CA*E + CB1*d1 - CB2*d2
+    const float4 c = C4[mm];
+    float t1, t2;
+    if (comp == 0) { t1 = c.z * dHz_y; t2 = c.w * dHy_z; }
+    else if (comp == 1) { t1 = c.w * dHx_z; t2 = c.y * dHz_x; }
+    else { t1 = c.y * dHy_x; t2 = c.z * dHx_y; }
+    float F;
+    if (NP == 0) {
+      F = c.x * Eold + t1 - t2;
+    } else {
+      float phi = 0.f;
+      const float2* cd = CD + mm * 3 * NP;
 #pragma unroll
-        for (int q = 0; q < NP; ++q) {
-          const float2 Tq = t[comp][q];
-          const float2 a = cd[3 * q + 0];
-          const float2 b = cd[3 * q + 1];
-          const float2 z = cd[3 * q + 2];
-          phi = phi + a.x * Tq.x;
-          TA[q].x = (b.x * Tq.x - b.y * Tq.y) + z.x * Eold;
-          TA[q].y = (b.x * Tq.y + b.y * Tq.x) + z.y * Eold;
-        }
-        F = c.x * Eold + t1 - t2 - Cs[mm] * phi;
+      for (int q = 0; q < NP; ++q) {
+        const float2 Tq = t[comp][q];
+        const float2 a = cd[3 * q + 0];
+        const float2 b = cd[3 * q + 1];
+        const float2 z = cd[3 * q + 2];
+        phi = phi + a.x * Tq.x;
+        TA[q].x = (b.x * Tq.x - b.y * Tq.y) + z.x * Eold;
+        TA[q].y = (b.x * Tq.y + b.y * Tq.x) + z.y * Eold;
       }
+      F = c.x * Eold + t1 - t2 - Cs[mm] * phi;
     }
+    F = mainu ? F : Eold;
     if (PK != PML_NONE && pml) {
       const float c4 = Cs[mm];
       if (comp == 0) F = apply_pml<true, 0>(F, c4, where, XA, XB);
@@ -577,13 +578,14 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
     }
     if (src) F = apply_e_sources(F, comp, i, j, k, it, Cs[mm], p);
     e[comp] = F;
-    if (NP > 0 && mainu) {
+    if (NP > 0) {
       const float2* cd = CD + mm * 3 * NP;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const float2 z = cd[3 * q + 2];
-        t[comp][q].x = TA[q].x - z.x * F;
-        t[comp][q].y = TA[q].y - z.y * F;
+        const float tx = TA[q].x - z.x * F, ty = TA[q].y - z.y * F;
+        t[comp][q].x = mainu ? tx : t[comp][q].x;
+        t[comp][q].y = mainu ? ty : t[comp][q].y;
       }
     }
   }

@@ -330,7 +330,9 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     sl.T = t;
     sl.d = dd[s % 3];
     sl.rcp = 1.0f / sl.d;
-    sl.fastdiv = (t && !(d.options & 2) && reciprocal_division_exact(sl.d)) ? 1 : 0;
+    // per axis (the kernels read it from the minus slab of either side's axis)
+    const bool axis_pml = d.pml_thickness[s % 3] || d.pml_thickness[s % 3 + 3];
+    sl.fastdiv = (axis_pml && !(d.options & 2) && reciprocal_division_exact(sl.d)) ? 1 : 0;
     if (!t) continue;
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
