@@ -110,6 +110,13 @@ _SIGS = {
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
+    'gbf_batch_create': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
+    'gbf_batch_destroy': (None, [_P]),
+    'gbf_batch_run': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32]),
+    'gbf_batch_run_timed': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32,
+                                           ctypes.POINTER(ctypes.c_float)]),
+    'gbf_batch_synchronize': (ctypes.c_int, [_P]),
+    'gbf_batch_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_sweep_boxes': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
                                        ctypes.c_int32, _P]),
 }

@@ -55,14 +55,22 @@ struct Slab {
 };
 
 struct StepParams;
+struct BatchParams;
 typedef void (*HKernFn)(StepParams);
 typedef void (*EKernFn)(StepParams);
+typedef void (*BKernFn)(BatchParams);
 // per-kind kernel tables (kernels_inst.cu, one object per PML kind)
 void kernels_pk0(int np, int idp, HKernFn* h, EKernFn* e);
 void kernels_pk1(int np, int idp, HKernFn* h, EKernFn* e);
 void kernels_pk2(int np, int idp, HKernFn* h, EKernFn* e);
 void kernels_pk3(int np, int idp, HKernFn* h, EKernFn* e);
 void kernels_pk4(int np, int idp, HKernFn* h, EKernFn* e);
+// batched forms (kernels_inst.cu)
+void batch_kernels_pk0(int np, int idp, BKernFn* h, BKernFn* e);
+void batch_kernels_pk1(int np, int idp, BKernFn* h, BKernFn* e);
+void batch_kernels_pk2(int np, int idp, BKernFn* h, BKernFn* e);
+void batch_kernels_pk3(int np, int idp, BKernFn* h, BKernFn* e);
+void batch_kernels_pk4(int np, int idp, BKernFn* h, BKernFn* e);
 
 struct Src {
   int kind, comp, i, j, k, first, last, pad;
@@ -455,22 +463,13 @@ __device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, co
 
 // H half-step. Domain: i in [0, nx], j in [0, ny], k in [0, nz] (every node of the arrays),
 // swept box by box (core first) by one persistent grid.
+// The H sweep of one model over its boxes. q is the thread's position in the launch's virtual
+// node index and base the position of the model's first node there; returns q after the
+// model's last node.
 template <int PK, int IDP>
-__global__ void __launch_bounds__(kThreads, 5)
-h_half_step(const __grid_constant__ StepParams p) {
-  extern __shared__ float4 smem_h[];
-  float4* s4 = smem_h;
-  float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
-  if (p.smem) {
-    stage_tables(p, false, s4, ss, nullptr);
-    __syncthreads();
-  }
-  const float4* C4 = p.smem ? s4 : p.cH4;
-  const float* Cs = p.smem ? ss : p.cHs;
-  int it = 0;
-  if (p.nsrcH) it = *p.d_it;
-  const int stride = gridDim.x * blockDim.x;
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ int h_sweep(const StepParams& p, const float4* C4, const float* Cs,
+                                       int q, int base, int stride, int it) {
+  q -= base;
   {
     const Box& B = p.boxH[0];
     const int end = B.start + B.count;
@@ -488,6 +487,69 @@ h_half_step(const __grid_constant__ StepParams p) {
     BoxWalk w(q - B.start, stride, B);
     for (; q < end; q += stride, w.advance(B))
       h_site<PK, IDP, false>(p, C4, Cs, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
+  }
+  return q + base;
+}
+
+template <int PK, int IDP>
+__global__ void __launch_bounds__(kThreads, 5)
+h_half_step(const __grid_constant__ StepParams p) {
+  extern __shared__ float4 smem_h[];
+  float4* s4 = smem_h;
+  float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
+  if (p.smem) {
+    stage_tables(p, false, s4, ss, nullptr);
+    __syncthreads();
+  }
+  const float4* C4 = p.smem ? s4 : p.cH4;
+  const float* Cs = p.smem ? ss : p.cHs;
+  int it = 0;
+  if (p.nsrcH) it = *p.d_it;
+  h_sweep<PK, IDP>(p, C4, Cs, blockIdx.x * blockDim.x + threadIdx.x, 0, gridDim.x * blockDim.x, it);
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched half-steps: many models advance in one launch. The launch's virtual node index is
+// the concatenation of the models' sweeps, each padded to whole blocks (range[m] .. range[m+1]),
+// so the threads of a block always work on the same model: on reaching a model a block copies
+// its parameters (and coefficient tables) into shared memory, sweeps it, and moves on.
+struct BatchParams {
+  const StepParams* models;   // [n] device copies of the models' parameters
+  const int* rangeH;          // [n + 1] starts of the models' H sweeps (multiples of kThreads)
+  const int* rangeE;          // [n + 1] same for the E sweeps
+  int n;
+};
+
+__device__ __forceinline__ void load_params(StepParams& dst, const StepParams* src) {
+  static_assert(sizeof(StepParams) % 8 == 0, "StepParams size");
+  const unsigned long long* a = reinterpret_cast<const unsigned long long*>(src);
+  unsigned long long* b = reinterpret_cast<unsigned long long*>(&dst);
+  for (int w = threadIdx.x; w < (int)(sizeof(StepParams) / 8); w += blockDim.x) b[w] = a[w];
+}
+
+template <int PK, int IDP>
+__global__ void __launch_bounds__(kThreads, 4)
+h_half_step_batch(const __grid_constant__ BatchParams bp) {
+  __shared__ StepParams p;
+  extern __shared__ float4 smem_hb[];
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll 1
+  for (int m = 0; m < bp.n; ++m) {
+    const int end = __ldg(bp.rangeH + m + 1);
+    if (q >= end) continue;   // the same for every thread of the block
+    __syncthreads();
+    load_params(p, bp.models + m);
+    __syncthreads();
+    float4* s4 = smem_hb;
+    float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
+    if (p.smem) stage_tables(p, false, s4, ss, nullptr);
+    __syncthreads();
+    const float4* C4 = p.smem ? s4 : p.cH4;
+    const float* Cs = p.smem ? ss : p.cHs;
+    const int it = p.nsrcH ? *p.d_it : 0;
+    q = h_sweep<PK, IDP>(p, C4, Cs, q, __ldg(bp.rangeH + m), stride, it);
+    if (q < end) q += stride;   // past the model's last node, inside its padding
   }
 }
 
@@ -656,24 +718,11 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
 
 // E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz), swept box by box (core
 // first) by one persistent grid. NP = dispersive poles.
+// The E sweep of one model over its boxes (see h_sweep).
 template <int PK, int NP, int IDP>
-__global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
-e_half_step(const __grid_constant__ StepParams p) {
-  extern __shared__ float4 smem_e[];
-  float4* s4 = smem_e;
-  float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
-  float2* sd = reinterpret_cast<float2*>(ss + (p.smem ? ((p.nmat + 1) & ~1) : 0));
-  if (p.smem) {
-    stage_tables(p, true, s4, ss, NP > 0 ? sd : nullptr);
-    __syncthreads();
-  }
-  const float4* C4 = p.smem ? s4 : p.cE4;
-  const float* Cs = p.smem ? ss : p.cEs;
-  const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
-  int it = 0;
-  if (p.nsrcE) it = *p.d_it;
-  const int stride = gridDim.x * blockDim.x;
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, const float* Cs,
+                                       const float2* CD, int q, int base, int stride, int it) {
+  q -= base;
   {
     const Box& B = p.boxE[0];
     const int end = B.start + B.count;
@@ -692,6 +741,66 @@ e_half_step(const __grid_constant__ StepParams p) {
     for (; q < end; q += stride, w.advance(B))
       e_site<PK, NP, IDP, false>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
+  return q + base;
+}
+
+// Shared-memory layout of the E tables: float4 rows, srce column (padded to 8 bytes), then the
+// dispersive coefficients.
+__device__ __forceinline__ void e_tables(const StepParams& p, float4* smem, float4*& s4,
+                                         float*& ss, float2*& sd) {
+  s4 = smem;
+  ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
+  sd = reinterpret_cast<float2*>(ss + (p.smem ? ((p.nmat + 1) & ~1) : 0));
+}
+
+template <int PK, int NP, int IDP>
+__global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
+e_half_step(const __grid_constant__ StepParams p) {
+  extern __shared__ float4 smem_e[];
+  float4* s4;
+  float* ss;
+  float2* sd;
+  e_tables(p, smem_e, s4, ss, sd);
+  if (p.smem) {
+    stage_tables(p, true, s4, ss, NP > 0 ? sd : nullptr);
+    __syncthreads();
+  }
+  const float4* C4 = p.smem ? s4 : p.cE4;
+  const float* Cs = p.smem ? ss : p.cEs;
+  const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
+  int it = 0;
+  if (p.nsrcE) it = *p.d_it;
+  e_sweep<PK, NP, IDP>(p, C4, Cs, CD, blockIdx.x * blockDim.x + threadIdx.x, 0,
+                       gridDim.x * blockDim.x, it);
+}
+
+template <int PK, int NP, int IDP>
+__global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
+e_half_step_batch(const __grid_constant__ BatchParams bp) {
+  __shared__ StepParams p;
+  extern __shared__ float4 smem_eb[];
+  const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll 1
+  for (int m = 0; m < bp.n; ++m) {
+    const int end = __ldg(bp.rangeE + m + 1);
+    if (q >= end) continue;   // the same for every thread of the block
+    __syncthreads();
+    load_params(p, bp.models + m);
+    __syncthreads();
+    float4* s4;
+    float* ss;
+    float2* sd;
+    e_tables(p, smem_eb, s4, ss, sd);
+    if (p.smem) stage_tables(p, true, s4, ss, NP > 0 ? sd : nullptr);
+    __syncthreads();
+    const float4* C4 = p.smem ? s4 : p.cE4;
+    const float* Cs = p.smem ? ss : p.cEs;
+    const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
+    const int it = p.nsrcE ? *p.d_it : 0;
+    q = e_sweep<PK, NP, IDP>(p, C4, Cs, CD, q, __ldg(bp.rangeE + m), stride, it);
+    if (q < end) q += stride;   // past the model's last node, inside its padding
+  }
 }
 
 #ifndef GBF_KERNELS_ONLY
@@ -709,7 +818,7 @@ struct RxParams {
   const Src* srcOut;
 };
 
-__global__ void end_of_step(const __grid_constant__ StepParams p, const __grid_constant__ RxParams r, int* d_it) {
+__device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxParams& r, int* d_it) {
   const int it = *d_it;
   if (threadIdx.x == 0) {
     for (int s = 0; s < r.nsrcOut; ++s) {
@@ -754,6 +863,20 @@ __global__ void end_of_step(const __grid_constant__ StepParams p, const __grid_c
   }
   __syncthreads();
   if (threadIdx.x == 0) *d_it = it + 1;
+}
+
+__global__ void end_of_step(const __grid_constant__ StepParams p, const __grid_constant__ RxParams r, int* d_it) {
+  end_of_step_body(p, r, d_it);
+}
+
+// The end of an iteration for every model of a batch: one block per model.
+__global__ void end_of_step_batch(const StepParams* models, const RxParams* rxs) {
+  __shared__ StepParams p;
+  __shared__ RxParams r;
+  load_params(p, models + blockIdx.x);
+  if (threadIdx.x == 0) r = rxs[blockIdx.x];
+  __syncthreads();
+  end_of_step_body(p, r, const_cast<int*>(p.d_it));
 }
 
 // Snapshot: cell averages over a strided sub-volume (snapshots_ext.pyx:24-71).

@@ -768,3 +768,217 @@ int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes) {
 }
 
 }  // extern "C"
+
+// ---- batches: many models advanced by one launch per half-step ------------------------
+struct gbf_batch {
+  std::vector<gbf_ctx*> models;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  StepParams* d_models = nullptr;
+  RxParams* d_rx = nullptr;
+  int* d_rangeH = nullptr;     // [n + 1]
+  int* d_rangeE = nullptr;
+  BKernFn hk = nullptr, ek = nullptr;
+  size_t smem_h = 0, smem_e = 0;
+  int grid_h = 0, grid_e = 0;
+  int it = 0;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_steps = 0;
+};
+
+static int bfail(gbf_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  else g_create_err = buf;
+  return code;
+}
+
+#define BK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return bfail(b, e_ == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA,           \
+                   "%s failed: %s", #call, cudaGetErrorString(e_));                       \
+  } while (0)
+
+static void batch_kernels(int pk, int np, int idp, BKernFn* h, BKernFn* e) {
+  switch (pk) {
+    case PML_HORI1: batch_kernels_pk1(np, idp, h, e); break;
+    case PML_HORI2: batch_kernels_pk2(np, idp, h, e); break;
+    case PML_MRI1: batch_kernels_pk3(np, idp, h, e); break;
+    case PML_MRI2: batch_kernels_pk4(np, idp, h, e); break;
+    default: batch_kernels_pk0(np, idp, h, e); break;
+  }
+}
+
+static void batch_step(gbf_batch* b) {
+  BatchParams bp;
+  bp.models = b->d_models;
+  bp.rangeH = b->d_rangeH;
+  bp.rangeE = b->d_rangeE;
+  bp.n = (int)b->models.size();
+  b->hk<<<b->grid_h, kThreads, b->smem_h, b->stream>>>(bp);
+  b->ek<<<b->grid_e, kThreads, b->smem_e, b->stream>>>(bp);
+  end_of_step_batch<<<bp.n, 256, 0, b->stream>>>(b->d_models, b->d_rx);
+}
+
+// The whole requested time loop as one CUDA graph (re-captured when the length changes).
+static int ensure_batch_graph(gbf_batch* b, int nsteps) {
+  if (b->gexec && b->graph_steps == nsteps) return GBF_OK;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < nsteps; ++s) batch_step(b);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (e != cudaSuccess) return bfail(b, GBF_ECUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&b->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return bfail(b, GBF_ECUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e));
+  b->graph_steps = nsteps;
+  return GBF_OK;
+}
+
+static int check_batch_steps(gbf_batch* b, int nsteps) {
+  for (gbf_ctx* c : b->models)
+    if (nsteps < 0 || b->it + nsteps > c->d.iterations)
+      return bfail(b, GBF_EINVAL, "gbf_batch_run: %d steps from iteration %d exceed a model's %d iterations", nsteps, b->it, c->d.iterations);
+  return GBF_OK;
+}
+
+extern "C" {
+
+int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
+  if (!models || nmodels < 1 || !out) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: no models");
+  *out = nullptr;
+  const gbf_ctx* m0 = models[0];
+  if (!m0) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: null model 0");
+  const int pk = pml_kind(m0->d);
+  for (int m = 0; m < nmodels; ++m) {
+    const gbf_ctx* c = models[m];
+    if (!c) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: null model %d", m);
+    if (!c->materials) return bfail(nullptr, GBF_ESTATE, "gbf_batch_create: model %d has no materials", m);
+    if (c->device != m0->device) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models on different devices");
+    if (pml_kind(c->d) != pk || c->d.maxpoles != m0->d.maxpoles || c->idp != m0->idp)
+      return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d differs in PML kind, poles or ID layout from model 0", m);
+    if (c->d.nsnap) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d has snapshots (run it alone)", m);
+    if (c->it != m0->it) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models at different iterations");
+  }
+  gbf_batch* b = new gbf_batch();
+  b->models.assign(models, models + nmodels);
+  b->device = m0->device;
+  b->it = m0->it;
+  auto cleanup = [&](int rc) { gbf_batch_destroy(b); return rc; };
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { bfail(nullptr, GBF_ECUDA, "gbf_batch_create: %s", cudaGetErrorString(e)); return cleanup(GBF_ECUDA); }
+  std::vector<StepParams> sp(nmodels);
+  std::vector<RxParams> rp(nmodels);
+  std::vector<int> rh(nmodels + 1), re(nmodels + 1);
+  long long h = 0, ev = 0;
+  for (int m = 0; m < nmodels; ++m) {
+    gbf_ctx* c = b->models[m];
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) { bfail(nullptr, GBF_ECUDA, "gbf_batch_create: model %d stream failed", m); return cleanup(GBF_ECUDA); }
+    sp[m] = c->sp;
+    rp[m] = c->rp;
+    rh[m] = (int)h;
+    re[m] = (int)ev;
+    const Box& lh = c->sp.boxH[kBoxes - 1];
+    const Box& le = c->sp.boxE[kBoxes - 1];
+    h += ((long long)(lh.start + lh.count) + kThreads - 1) / kThreads * kThreads;
+    ev += ((long long)(le.start + le.count) + kThreads - 1) / kThreads * kThreads;
+    if (h > (1LL << 31) - 1 || ev > (1LL << 31) - 1) { bfail(nullptr, GBF_EINVAL, "gbf_batch_create: more than 2^31 nodes in the batch"); return cleanup(GBF_EINVAL); }
+    if (c->smem_h > b->smem_h) b->smem_h = c->smem_h;
+    if (c->smem_e > b->smem_e) b->smem_e = c->smem_e;
+  }
+  rh[nmodels] = (int)h;
+  re[nmodels] = (int)ev;
+  auto alloc_copy = [&](void** dst, const void* src, size_t n) {
+    cudaError_t r = cudaMalloc(dst, n);
+    if (r == cudaSuccess) r = cudaMemcpy(*dst, src, n, cudaMemcpyHostToDevice);
+    return r;
+  };
+  if ((e = alloc_copy((void**)&b->d_models, sp.data(), sizeof(StepParams) * nmodels)) != cudaSuccess ||
+      (e = alloc_copy((void**)&b->d_rx, rp.data(), sizeof(RxParams) * nmodels)) != cudaSuccess ||
+      (e = alloc_copy((void**)&b->d_rangeH, rh.data(), sizeof(int) * (nmodels + 1))) != cudaSuccess ||
+      (e = alloc_copy((void**)&b->d_rangeE, re.data(), sizeof(int) * (nmodels + 1))) != cudaSuccess) {
+    bfail(nullptr, e == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA, "gbf_batch_create: %s", cudaGetErrorString(e));
+    return cleanup(GBF_ECUDA);
+  }
+  batch_kernels(pk, m0->d.maxpoles, m0->idp, &b->hk, &b->ek);
+  const size_t sh = b->smem_h, se = b->smem_e;
+  b->grid_h = persistent_blocks((const void*)b->hk, sh);
+  b->grid_e = persistent_blocks((const void*)b->ek, se);
+  *out = b;
+  return GBF_OK;
+}
+
+void gbf_batch_destroy(gbf_batch* b) {
+  if (!b) return;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  cudaFree(b->d_models);
+  cudaFree(b->d_rx);
+  cudaFree(b->d_rangeH);
+  cudaFree(b->d_rangeE);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int gbf_batch_last_error(gbf_batch* b, char* buf, size_t n) {
+  if (!buf || n == 0) return GBF_EINVAL;
+  snprintf(buf, n, "%s", b ? b->err.c_str() : g_create_err.c_str());
+  return GBF_OK;
+}
+
+int gbf_batch_run(gbf_batch* b, int32_t nsteps, uint32_t flags) {
+  if (!b) return GBF_EINVAL;
+  int rc = check_batch_steps(b, nsteps);
+  if (rc) return rc;
+  if (nsteps == 0) return GBF_OK;
+  if (flags & GBF_RUN_GRAPH) {
+    rc = ensure_batch_graph(b, nsteps);
+    if (rc) return rc;
+    BK(cudaGraphLaunch(b->gexec, b->stream));
+  } else {
+    for (int s = 0; s < nsteps; ++s) batch_step(b);
+  }
+  BK(cudaGetLastError());
+  b->it += nsteps;
+  for (gbf_ctx* c : b->models) c->it += nsteps;
+  return GBF_OK;
+}
+
+int gbf_batch_run_timed(gbf_batch* b, int32_t nsteps, uint32_t flags, float* ms) {
+  if (!b || !ms) return GBF_EINVAL;
+  int rc0 = check_batch_steps(b, nsteps);
+  if (rc0) return rc0;
+  if ((flags & GBF_RUN_GRAPH) && nsteps > 0) {   // capture before the timed region
+    rc0 = ensure_batch_graph(b, nsteps);
+    if (rc0) return rc0;
+  }
+  cudaEvent_t a, z;
+  BK(cudaEventCreate(&a));
+  BK(cudaEventCreate(&z));
+  BK(cudaEventRecord(a, b->stream));
+  int rc = gbf_batch_run(b, nsteps, flags);
+  if (rc) { cudaEventDestroy(a); cudaEventDestroy(z); return rc; }
+  BK(cudaEventRecord(z, b->stream));
+  BK(cudaEventSynchronize(z));
+  BK(cudaEventElapsedTime(ms, a, z));
+  cudaEventDestroy(a);
+  cudaEventDestroy(z);
+  return GBF_OK;
+}
+
+int gbf_batch_synchronize(gbf_batch* b) {
+  if (!b) return GBF_EINVAL;
+  BK(cudaStreamSynchronize(b->stream));
+  return GBF_OK;
+}
+
+}  // extern "C"

@@ -34,4 +34,26 @@ void GBF_CAT(kernels_pk, GBF_PK)(int np, int idp, HKernFn* h, EKernFn* e) {
   }
 }
 
+template <int IDP>
+static BKernFn eb_for(int np) {
+  switch (np) {
+    case 1: return e_half_step_batch<GBF_PK, 1, IDP>;
+    case 2: return e_half_step_batch<GBF_PK, 2, IDP>;
+    case 3: return e_half_step_batch<GBF_PK, 3, IDP>;
+    case 4: return e_half_step_batch<GBF_PK, 4, IDP>;
+    default: return e_half_step_batch<GBF_PK, 0, IDP>;
+  }
+}
+
+// Batched kernels for PML kind GBF_PK (see kernels_pk*).
+void GBF_CAT(batch_kernels_pk, GBF_PK)(int np, int idp, BKernFn* h, BKernFn* e) {
+  if (idp == 1) {
+    *h = h_half_step_batch<GBF_PK, 1>;
+    *e = eb_for<1>(np);
+  } else {
+    *h = h_half_step_batch<GBF_PK, 3>;
+    *e = eb_for<3>(np);
+  }
+}
+
 }  // namespace gbf

@@ -236,6 +236,93 @@ class DeviceModel:
                 G.Tx, G.Ty, G.Tz = T[0], T[1], T[2]
 
 
+class BatchModel:
+    """Many models advanced together: one persistent launch per half-step walks every model
+    (``gbf_batch_*`` in the C ABI), and the requested time loop is replayed from one CUDA graph.
+    The models may differ in size, geometry, sources and receivers; they must share the PML
+    formulation and order, the pole count and the material-ID layout, and have no snapshots."""
+
+    def __init__(self, grids, options=0):
+        self.lib = _native.lib()
+        self.models = []
+        self.b = ctypes.c_void_p(0)
+        try:
+            for G in grids:
+                self.models.append(DeviceModel(G, options))
+            arr = (ctypes.c_void_p * len(self.models))(*[m.ctx.value for m in self.models])
+            rc = self.lib.gbf_batch_create(arr, len(self.models), ctypes.byref(self.b))
+            self._check(rc, created=False)
+        except Exception:
+            self.close()
+            raise
+
+    def _check(self, rc, created=True):
+        if rc != 0:
+            buf = ctypes.create_string_buffer(1024)
+            self.lib.gbf_batch_last_error(self.b if created else None, buf, 1024)
+            raise SolverError('libgbfdtd batch error {}: {}'.format(rc, buf.value.decode()))
+
+    def iteration(self):
+        return self.models[0].iteration()
+
+    def run(self, nsteps=None, graph=True):
+        """Advance every model ``nsteps`` iterations (default: to the end of the shortest)."""
+        if nsteps is None:
+            nsteps = min(m.G.iterations for m in self.models) - self.iteration()
+        flags = _native.GBF_RUN_GRAPH if graph else 0
+        self._check(self.lib.gbf_batch_run(self.b, int(nsteps), flags))
+
+    def run_timed(self, nsteps, graph=True):
+        """Run ``nsteps`` iterations; device milliseconds from CUDA events on the batch stream
+        (the graph is captured before the timed region)."""
+        ms = ctypes.c_float(0)
+        flags = _native.GBF_RUN_GRAPH if graph else 0
+        self._check(self.lib.gbf_batch_run_timed(self.b, int(nsteps), flags, ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._check(self.lib.gbf_batch_synchronize(self.b))
+
+    def receivers(self):
+        """Per model, fp32 [9][iterations][nrx] receiver samples."""
+        self.synchronize()
+        return [m.receivers() for m in self.models]
+
+    def store_results(self, fields=False):
+        self.synchronize()
+        for m in self.models:
+            m.store_results(fields=fields)
+
+    def close(self):
+        if self.b and self.b.value:
+            self.lib.gbf_batch_destroy(self.b)
+        self.b = ctypes.c_void_p(0)
+        for m in self.models:
+            m.close()
+        self.models = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_gb300_batch(grids, fields=False):
+    """Run every grid of a B-scan or parameter sweep to its end in one batch; returns the solve
+    seconds. Each grid's receiver outputs are stored as ``solve_gb300`` stores them."""
+    bm = BatchModel(grids)
+    try:
+        t0 = time.perf_counter()
+        bm.run()
+        bm.synchronize()
+        tsolve = time.perf_counter() - t0
+        bm.store_results(fields=fields)
+    finally:
+        bm.close()
+    return tsolve
+
+
 def solve_gb300(currentmodelrun, modelend, G, fields=True):
     """Run all iterations of ``G`` on the GPU; returns (tsolve seconds, device bytes)."""
     dm = DeviceModel(G)

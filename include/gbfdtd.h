@@ -162,6 +162,25 @@ int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n);
 /* Library version string. */
 const char* gbf_version(void);
 
+/* ---- batches: many models advanced together ----------------------------------------
+ * A batch borrows contexts that are fully set up (materials, PML rows, sources, receivers
+ * uploaded; no snapshots; all at the same iteration, with the same PML kind, pole count and
+ * material-ID layout) and advances all of them with one persistent launch per half-step plus
+ * one end-of-step launch, replaying the requested time loop from one CUDA graph. Results are
+ * read from each context as usual (gbf_download_rx ...). While a batch exists, its contexts
+ * must not be run or re-uploaded on their own; destroy the batch before the contexts.
+ * Replaces: the task farm of independent model runs for B-scans and parameter sweeps
+ * (gprMax/gprMax.py:run_std_sim, run_mpi_sim and model_build_run.py:84-405 per model). */
+typedef struct gbf_batch gbf_batch;
+int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out);
+void gbf_batch_destroy(gbf_batch* batch);
+/* Advance every model nsteps iterations (flags: GBF_RUN_GRAPH). */
+int gbf_batch_run(gbf_batch* batch, int32_t nsteps, uint32_t flags);
+/* The same, timed with CUDA events on the batch's stream (graph capture outside the timing). */
+int gbf_batch_run_timed(gbf_batch* batch, int32_t nsteps, uint32_t flags, float* ms);
+int gbf_batch_synchronize(gbf_batch* batch);
+int gbf_batch_last_error(gbf_batch* batch, char* buf, size_t n);
+
 /* 1 if, for this cell size, the PML kernels may form dF/d as the product with the rounded
  * reciprocal corrected once by the exact residual, because that equals the IEEE quotient for
  * every dF; 0 otherwise (the kernels then divide). Host only, no device needed; gbf_create

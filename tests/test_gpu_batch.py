@@ -1,0 +1,86 @@
+"""GPU: the batched form (one launch per half-step over many models) against the plain
+solver model by model. Both run the same per-node code, so the traces and fields must be
+bit-identical; the plain solver is pinned to the oracle by test_gpu_parity.py."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FREE = """#domain: {x} {y} {z}
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: {steps}
+#pml_cells: {pml}
+#waveform: ricker 1 2e9 w
+#hertzian_dipole: z {sx} {sy} {sz} w
+#rx: {rx} {sy} {sz}
+#rx: {sx} {ry} {sz} r2 Ex Ey Ez Hx Hy Hz Ix Iy Iz
+"""
+
+SOIL = FREE + """#material: 6 0.005 1 0 soil
+#add_dispersion_debye: 1 10 1e-9 soil
+#box: 0 0 0 {x} {y} {surf} soil
+#sphere: {bx} {by} {bz} 0.004 pec
+"""
+
+
+def _grids(template, n, steps, pml='6'):
+    from gprmax_gb300.model import build_grid
+    rng = np.random.default_rng(3)
+    grids = []
+    for m in range(n):
+        x, y, z = (int(v) for v in rng.integers(24, 40, 3))
+        sx, sy, sz = x // 2 + m % 3, y // 2, z // 2 + 2
+        text = template.format(x=x / 1000, y=y / 1000, z=z / 1000, steps=steps, pml=pml,
+                               sx=sx / 1000, sy=sy / 1000, sz=sz / 1000, rx=(sx + 3) / 1000,
+                               ry=(sy - 4) / 1000, surf=(z // 2) / 1000, bx=x / 2000,
+                               by=y / 2000, bz=z / 4000)
+        grids.append(build_grid(text.splitlines(True), messages=False))
+    return grids
+
+
+def _plain(G):
+    from gprmax_gb300.solver import DeviceModel
+    dm = DeviceModel(G)
+    dm.run()
+    out = dm.receivers(), dm.fields()
+    dm.close()
+    return out
+
+
+@pytest.mark.parametrize('template,pml', [(FREE, '6'), (SOIL, '6'), (FREE, '0'),
+                                          (SOIL, '5 4 6 6 5 4')])
+def test_batch_matches_plain_runs(native, template, pml):
+    from gprmax_gb300.solver import BatchModel
+    grids = _grids(template, 4, 80, pml)
+    bm = BatchModel(grids)
+    bm.run()
+    rx = bm.receivers()
+    fields = [m.fields() for m in bm.models]
+    bm.close()
+    for n, G in enumerate(grids):
+        prx, pf = _plain(G)
+        np.testing.assert_array_equal(rx[n], prx, err_msg='model {} traces'.format(n))
+        np.testing.assert_array_equal(fields[n], pf, err_msg='model {} fields'.format(n))
+
+
+def test_batch_in_pieces_and_without_graph(native):
+    from gprmax_gb300.solver import BatchModel
+    grids = _grids(SOIL, 3, 60)
+    outs = []
+    for pieces, graph in (((60,), True), ((17, 25, 18), True), ((60,), False)):
+        bm = BatchModel(grids)
+        for n in pieces:
+            bm.run(n, graph=graph)
+        outs.append(bm.receivers())
+        bm.close()
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_batch_rejects_mixed_pml_kinds(native):
+    from gprmax_gb300.exceptions import SolverError
+    from gprmax_gb300.solver import BatchModel
+    grids = _grids(FREE, 1, 20, '6') + _grids(FREE, 1, 20, '0')
+    with pytest.raises(SolverError):
+        BatchModel(grids)
