@@ -102,3 +102,49 @@ def throughput_cube(n, iterations=2000, seed=0, pml=10, messages=False):
              '#hertzian_dipole: z {0:g} {0:g} {1:g} w'.format(c, L / 4 - 5 * d),
              '#rx: {0:g} {0:g} {1:g}'.format(c + 5 * d, L / 4 - 5 * d)]
     return build_grid([l + '\n' for l in lines], messages=messages)
+
+
+def bscan_input(shape, seed, position, dx=0.002, timewindow='10e-9', pml=10):
+    """Input-file lines of one model of an uneven B-scan: a seeded 3-layer soil (per layer
+    eps_r ~ U[3,15], sigma ~ logU[1e-4,1e-2] S/m) filling the lower 70 % of the domain, one
+    buried PEC sphere of radius U[15,30] mm at a random position in the soil, and a y-directed
+    Hertzian dipole with a receiver 40 mm away in x, 10 mm above the surface, moved 4 mm per
+    model along x (``position``); Ricker 1.5 GHz."""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(seed)
+    er = rng.uniform(3, 15, 3)
+    sig = 10 ** rng.uniform(-4, -2, 3)
+    surf = int(nz * 0.7)
+    cuts = np.sort(rng.choice(np.arange(int(surf * 0.2), int(surf * 0.9)), 2, replace=False))
+    lines = ['#domain: {:g} {:g} {:g}'.format(nx * dx, ny * dx, nz * dx),
+             '#dx_dy_dz: {0:g} {0:g} {0:g}'.format(dx), '#time_window: {}'.format(timewindow),
+             '#pml_cells: {}'.format(pml), '#waveform: ricker 1 1.5e9 w']
+    for layer in range(3):
+        lines.append('#material: {!r} {!r} 1 0 layer{}'.format(float(er[layer]), float(sig[layer]), layer))
+    z = [0, int(cuts[0]), int(cuts[1]), surf]
+    for layer in range(3):
+        lines.append('#box: 0 0 {:g} {:g} {:g} {:g} layer{}'.format(
+            z[layer] * dx, nx * dx, ny * dx, z[layer + 1] * dx, layer))
+    r = rng.uniform(0.015, 0.030)
+    c = (rng.uniform(0.2, 0.8) * nx * dx, rng.uniform(0.2, 0.8) * ny * dx,
+         rng.uniform(r + 0.03, surf * dx - r))
+    lines.append('#sphere: {:g} {:g} {:g} {:g} pec'.format(c[0], c[1], c[2], r))
+    x = 0.06 + 0.004 * position
+    zs = surf * dx + 0.01
+    lines.append('#hertzian_dipole: y {:g} {:g} {:g} w'.format(x, ny * dx / 2, zs))
+    lines.append('#rx: {:g} {:g} {:g}'.format(x + 0.04, ny * dx / 2, zs))
+    return [line + '\n' for line in lines]
+
+
+def bscan_models(nmodels=128, shapes=((200, 200, 100), (300, 300, 150)), seed=11,
+                 messages=False):
+    """The uneven B-scan: ``nmodels`` grids, the first half of the first shape and the second
+    half of the second, each with its own seed; the dipole/receiver pair of model m of each half
+    sits 4 mm * m along x."""
+    half = nmodels // 2
+    grids = []
+    for m in range(nmodels):
+        shape = shapes[0] if m < half else shapes[1]
+        pos = m if m < half else m - half
+        grids.append(build_grid(bscan_input(shape, seed + m, pos), messages=messages))
+    return grids
