@@ -11,7 +11,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
-SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fdtd_kernels.cuh']
+SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'adjoint.cu', 'fdtd_kernels.cuh']
 PML_KINDS = 5   # kernels_inst.cu is compiled once per PML kind
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -50,7 +50,8 @@ def build(force=False, verbose=False):
     objdir = os.path.join(CSRC, '_build')
     os.makedirs(objdir, exist_ok=True)
     compile_flags = [f for f in NVCC_FLAGS if f != '-shared']
-    jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), [])]
+    jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), []),
+            (os.path.join(CSRC, 'adjoint.cu'), os.path.join(objdir, 'adjoint.o'), [])]
     for pk in range(PML_KINDS):
         jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
                      os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
@@ -70,6 +71,15 @@ def build(force=False, verbose=False):
     subprocess.run(cmd, check=True, cwd=CSRC)
     os.replace(LIBPATH + '.tmp', LIBPATH)
     return LIBPATH
+
+
+class AdjDesc(ctypes.Structure):
+    _fields_ = [('nx', ctypes.c_int32), ('ny', ctypes.c_int32), ('nz', ctypes.c_int32),
+                ('iterations', ctypes.c_int32), ('d', ctypes.c_float), ('dt', ctypes.c_float),
+                ('dbd', ctypes.c_float), ('srcm', ctypes.c_float),
+                ('pml_thickness', ctypes.c_int32 * 6), ('nsrc', ctypes.c_int32),
+                ('nrx', ctypes.c_int32), ('checkpoint_interval', ctypes.c_int32),
+                ('reserved', ctypes.c_int32 * 3)]
 
 
 class GridDesc(ctypes.Structure):
@@ -110,6 +120,14 @@ _SIGS = {
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
+    'gbf_adj_create': (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    'gbf_adj_destroy': (None, [_P]),
+    'gbf_adj_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    'gbf_adj_upload_pml': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
+    'gbf_adj_upload_sources': (ctypes.c_int, [_P, _P, _P, _P]),
+    'gbf_adj_set_receivers': (ctypes.c_int, [_P, _P]),
+    'gbf_adj_forward': (ctypes.c_int, [_P, _P, _P, _P]),
+    'gbf_adj_backward': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     'gbf_batch_create': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
     'gbf_batch_destroy': (None, [_P]),
     'gbf_batch_run': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32]),

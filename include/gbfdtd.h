@@ -181,6 +181,45 @@ int gbf_batch_run_timed(gbf_batch* batch, int32_t nsteps, uint32_t flags, float*
 int gbf_batch_synchronize(gbf_batch* batch);
 int gbf_batch_last_error(gbf_batch* batch, char* buf, size_t n);
 
+/* ---- differentiable time loop (adjoint) ---------------------------------------------
+ * Receiver traces of a non-dispersive 3D model with one (CA, CB) pair per E edge, and the
+ * gradient of a misfit with respect to every CA and CB through the discrete adjoint
+ * (transposed updates in reverse time, recomputed from checkpoints every checkpoint_interval
+ * steps). The update, ranges, HORIPML order-1 slab corrections, Hertzian dipoles and receivers
+ * are the reference's (fields_updates_ext.pyx, pml_updates_*_HORIPML_ext.pyx order1_*,
+ * sources.py:163-193, fields_outputs.py:40-67); H uses free-space coefficients. CA, CB,
+ * traces and gradients are DEVICE pointers of the caller (e.g. torch tensors), laid out
+ * [3][nx+1][ny+1][nz+1] (CA, CB, gradients) and [nrx][iterations] (traces). No counterpart in
+ * the reference, which has no gradient path. */
+typedef struct gbf_adj_desc {
+    int32_t nx, ny, nz, iterations;
+    float d;                     /* cubic cell size */
+    float dt;
+    float dbd;                   /* H curl coefficient DB/d (fp32) */
+    float srcm;                  /* H PML coefficient DB (fp32) */
+    int32_t pml_thickness[6];    /* x0, y0, z0, xmax, ymax, zmax; HORIPML order 1 */
+    int32_t nsrc;                /* Hertzian dipoles, at most 16 */
+    int32_t nrx;                 /* receivers, at least 1 */
+    int32_t checkpoint_interval; /* steps between checkpoints; 0: ceil(sqrt(iterations)) */
+    int32_t reserved[3];         /* must be zero */
+} gbf_adj_desc;
+typedef struct gbf_adj gbf_adj;
+int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out);
+void gbf_adj_destroy(gbf_adj* adj);
+int gbf_adj_last_error(gbf_adj* adj, char* buf, size_t n);
+/* rows: ERA ERB ERE ERF HRA HRB HRE HRF of the slab's CFS term, thickness values each */
+int gbf_adj_upload_pml(gbf_adj* adj, int32_t slab, const float* const rows[8]);
+/* info [nsrc][4]: component (0..2), i, j, k; scale [nsrc]: dl/(dx dy dz);
+ * waves [nsrc][iterations]: the waveform at whole steps, zero where inactive */
+int gbf_adj_upload_sources(gbf_adj* adj, const int32_t* info, const float* scale, const float* waves);
+/* info [nrx][4]: component (0..2), i, j, k */
+int gbf_adj_set_receivers(gbf_adj* adj, const int32_t* info);
+/* run every iteration; writes traces and keeps the checkpoints for gbf_adj_backward */
+int gbf_adj_forward(gbf_adj* adj, const float* CA, const float* CB, float* traces);
+/* gCA, gCB (fp64, overwritten) = d(misfit)/d(CA, CB) given gtraces = d(misfit)/d(traces) */
+int gbf_adj_backward(gbf_adj* adj, const float* CA, const float* CB, const float* gtraces,
+                     double* gCA, double* gCB);
+
 /* 1 if, for this cell size, the PML kernels may form dF/d as the product with the rounded
  * reciprocal corrected once by the exact residual, because that equals the IEEE quotient for
  * every dF; 0 otherwise (the kernels then divide). Host only, no device needed; gbf_create
