@@ -401,6 +401,84 @@ def run_bscan(args):
     print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args):
+    """Gradient of a trace misfit with respect to per-cell eps_r and sigma on a 200x200x100 grid
+    at 2 mm, 8 ns (2079 iterations): GRF permittivity, random conductivity, 4 dipoles and 8
+    receivers, observed data from a model with a buried 40 mm box 5 % denser. Times the forward
+    (traces) and the checkpointed adjoint (gradient), and checks the gradient against central
+    finite differences of the same GPU forward (fp64 misfit) on 20 seeded cells among the most
+    sensitive 1 %."""
+    import torch
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.adjoint import AdjointModel, AdjointSolver, fdtd_traces
+    lines, eps, sig, true = workloads.adjoint_problem()
+    m = AdjointModel(lines)
+    solver = AdjointSolver(m)
+    dev = torch.device('cuda')
+    e = torch.tensor(eps, dtype=torch.float64, device=dev)
+    s = torch.tensor(sig, dtype=torch.float64, device=dev)
+    CAo, CBo = m.edge_coefficients(torch.tensor(true, dtype=torch.float64, device=dev), s)
+    obs = solver.forward(CAo.float().contiguous(), CBo.float().contiguous()).double()
+
+    def loss_of(ee):
+        CA, CB = m.edge_coefficients(ee, s)
+        tr = solver.forward(CA.float().contiguous(), CB.float().contiguous())
+        return float(0.5 * ((tr.double() - obs) ** 2).sum())
+    for _ in range(max(args.warmup - 2, 1)):
+        loss_of(e)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss_of(e)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    ee = e.clone().requires_grad_(True)
+    ss = s.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    CA, CB = m.edge_coefficients(ee, ss)
+    tr = fdtd_traces(CA, CB, solver)
+    L = 0.5 * ((tr.double() - obs) ** 2).sum()
+    L.backward()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    g = ee.grad
+    # finite differences on 20 cells drawn from the 1 % with the largest |gradient|
+    flat = g.abs().flatten()
+    top = torch.topk(flat, max(20, flat.numel() // 100)).indices.cpu().numpy()
+    rng = np.random.default_rng(5)
+    cells = rng.choice(top, 20, replace=False)
+    errs = []
+    for c in cells:
+        # fourth-order central difference, step 5 % of eps_r (the fp32 forward's rounding noise
+        # limits how small the step can be)
+        idx = np.unravel_index(int(c), eps.shape)
+        h = 0.05 * float(e[idx])
+        f = {}
+        for k in (-2, -1, 1, 2):
+            p = e.clone()
+            p[idx] += k * h
+            f[k] = loss_of(p)
+        fd = (8 * (f[1] - f[-1]) - (f[2] - f[-2])) / (12 * h)
+        errs.append(abs(fd - float(g[idx])) / max(abs(fd), 1e-300))
+    solver.close()
+    cells_n = m.nx * m.ny * m.nz
+    out = {'metric': 'adjoint_over_forward', 'value': round(t_grad / t_fwd, 3), 'unit': 'x',
+           'n_gpus': 1, 'steps': m.iterations, 'warmup': args.warmup,
+           'ms_per_step': t_fwd / m.iterations * 1e3, 'higher_is_better': False,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 fields, f64 misfit and gradient',
+           'data': 'synthetic (seeded Gaussian random field permittivity)',
+           'config': {'workload': 'adjoint_200x200x100_grf', 'grid': [m.nx, m.ny, m.nz],
+                      'iterations': m.iterations, 'sources': len(m.sources),
+                      'receivers': len(m.receivers)},
+           'forward_s': round(t_fwd, 4), 'gradient_s': round(t_grad, 4),
+           'forward_Mcells_per_s': round(cells_n * m.iterations / t_fwd / 1e6, 1),
+           'fd_check': {'cells': 20, 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',
+                        'median_rel_err': float(np.median(errs)),
+                        'max_rel_err': float(np.max(errs))},
+           'misfit': float(L.detach())}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -415,15 +493,18 @@ def main():
                     help='smaller soil grid (profiling runs); default 400 400 200')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
-    ap.add_argument('--workload', choices=['soil', 'bscan'], default='soil',
+    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint'], default='soil',
                     help='soil: the 400x400x200 Debye soil (default); bscan: the batched uneven '
-                         'B-scan against sequential plain runs')
+                         'B-scan against sequential plain runs; adjoint: gradient cost and '
+                         'finite-difference check of the differentiable time loop')
     ap.add_argument('--models', type=int, default=128, help='bscan: number of models')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.workload == 'bscan':
         run_bscan(args)
+    elif args.workload == 'adjoint':
+        run_adjoint(args)
     elif args.impl == 'reference':
         run_reference(args)
     else:

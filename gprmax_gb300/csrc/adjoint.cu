@@ -5,18 +5,20 @@
 // (fields_updates_ext.pyx update_electric/update_magnetic), HORIPML order-1 slab corrections
 // (pml_updates_{electric,magnetic}_HORIPML_ext.pyx order1_*), Hertzian dipoles
 // (sources.py:163-193) and field receivers (fields_outputs.py:40-67), with one (CA, CB) pair per
-// E edge instead of a material-ID lookup, free-space H coefficients and cubic cells. Phi state
-// lives in full-grid arrays (one per slab axis and tangential component); only slab nodes use
-// them.
+// E edge instead of a material-ID lookup, free-space H coefficients and cubic cells. Phi state is
+// stored per slab and tangential component ("pair": x (Ey, Ez), y (Ex, Ez), z (Ex, Ey) for E and
+// x (Hy, Hz), y (Hx, Hz), z (Hx, Hy) for H) in the main solver's compact layout.
 //
-// Adjoint of one iteration s_n -> s_{n+1} (H half-step, then E half-step and sources), given the
-// adjoint lambda of s_{n+1} and the forward E_n, H^{n+1/2}, PhiE_n of the segment being undone:
-//   adj_e_nodes   per E node: u = CB/d * lamE, lamE <- CA * lamE, PML: the Phi and dF adjoints,
-//                 gradients dL/dCA += lamE * E_n, dL/dCB += lamE * (curl/d, PML X, source)
-//   adj_e_to_h    per H node: lamH += transposed E curl of u, transposed PML differences
-//   adj_h_nodes   per H node: u = DB/d * lamH, PML Phi and dF adjoints
-//   adj_h_to_e    per E node: lamE += transposed H curl of u, transposed PML differences
-//   adj_receivers lamE at receivers += dL/d(trace sample n)
+// Backward pass, per segment of K steps (from the last): the forward is recomputed from the
+// segment's checkpoint straight into per-step slots (E_n, PhiE_n, H^{n+1/2}), then undone in
+// reverse with two kernels per step:
+//   adj_e_step(n)  per E node: finish the adjoint of E_{n+1} (transposed H curl of u_H and the
+//                  transposed H-PML differences of step n+1, receiver samples n+1), then undo
+//                  the E half-step n: u_E = CB/d lamE, lamE <- CA lamE, PML Phi/dF adjoints,
+//                  gradient partials dL/dCA += lamE E_n, dL/dCB += lamE (curl/d, PML X, source)
+//   adj_h_step(n)  per H node: lamH += transposed E curl of u_E and transposed E-PML
+//                  differences, then undo the H half-step n: u_H = DB/d lamH, PML adjoints
+// The gradient partials are fp32 within a segment and folded into fp64 at its end.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -34,18 +36,25 @@ namespace {
 
 constexpr int kAdjThreads = 256;
 constexpr int kAdjSrcMax = 16;
+constexpr int kAdjRxMax = 64;
+
+struct AdjSlab {
+  int T;            // thickness (0: absent)
+  int ocount;       // Phi values per pair
+  const float* R;   // [8][T]: ERA ERB ERE ERF HRA HRB HRE HRF (CFS term 0)
+};
+
+// Phi-shaped arrays of one field type: [slab][pair] (nullptr for absent slabs)
+struct PhiSet {
+  float* p[6][2];
+};
 
 struct AdjParams {
   int nx, ny, nz, sx, sy, ncomp;
   float rd;      // 1 / d
   float dbd;     // H curl coefficient DB / d
   float srcm;    // H PML coefficient DB
-  int T[6];      // slab thickness, x0 y0 z0 xmax ymax zmax
-  const float* R[6];  // per slab [8][T]: ERA ERB ERE ERF HRA HRB HRE HRF (CFS term 0)
-  float* E;      // [3][ncomp] working state
-  float* H;
-  float* phiE;   // [6][ncomp]: pairs x:(Ey,Ez) y:(Ex,Ez) z:(Ex,Ey)
-  float* phiH;   // [6][ncomp]: pairs x:(Hy,Hz) y:(Hx,Hz) z:(Hx,Hy)
+  AdjSlab slab[6];
   const float* CA;   // [3][ncomp]
   const float* CB;
   int nsrc;
@@ -54,50 +63,42 @@ struct AdjParams {
   const float* waves;    // [nsrc][iterations]
   int iterations;
   int nrx;
-  const int* rx;         // [nrx][2]: component, node index
+  int rx_comp[kAdjRxMax], rx_idx[kAdjRxMax];
 };
 
-struct AdjBuffers {
-  float* lE;     // [3][ncomp] adjoint of E
-  float* lH;
-  float* lphiE;  // [6][ncomp]
-  float* lphiH;
-  float* uE;     // [3][ncomp] CB/d * lamE on updated edges
-  float* uH;
-  float* dFE;    // [6][ncomp] adjoint of the PML differences
-  float* dFH;
-  const float* En;    // forward E_n        [3][ncomp]
-  const float* Hh;    // forward H^{n+1/2}  [3][ncomp]
-  const float* PEn;   // forward PhiE_n     [6][ncomp]
-  double* gCA;        // [3][ncomp]
-  double* gCB;
+// Node walk of a persistent grid over all (nx+1)(ny+1)(nz+1) nodes (as the main kernels).
+struct Walk {
+  int i, j, k, si, sj, sk;
+  __device__ __forceinline__ Walk(int q, int stride, const AdjParams& p) {
+    i = q / p.sx;
+    int r = q - i * p.sx;
+    j = r / p.sy;
+    k = r - j * p.sy;
+    si = stride / p.sx;
+    r = stride - si * p.sx;
+    sj = r / p.sy;
+    sk = r - sj * p.sy;
+  }
+  __device__ __forceinline__ void advance(const AdjParams& p) {
+    k += sk;
+    if (k >= p.sy) { k -= p.sy; ++j; }
+    j += sj;
+    if (j > p.ny) { j -= p.ny + 1; ++i; }
+    i += si;
+  }
 };
 
-struct Node {
-  int i, j, k, idx;
-};
-
-__device__ __forceinline__ Node node_of(int q, const AdjParams& p) {
-  Node n;
-  n.i = q / p.sx;
-  const int r = q - n.i * p.sx;
-  n.j = r / p.sy;
-  n.k = r - n.j * p.sy;
-  n.idx = q;
-  return n;
-}
-
-// pair index and sign of slab axis AX for field component C (electric or magnetic); -1 if C is
-// not tangential to AX. E: x (Ey -, Ez +), y (Ex +, Ez -), z (Ex -, Ey +); H opposite signs.
+// pair index (0: first, 1: second tangential component) of component C on slab axis AX, -1 if
+// C is not tangential; the sign of the correction (E: x Ey -, Ez +; y Ex +, Ez -; z Ex -, Ey +;
+// H the opposite); the component whose difference drives it.
 __host__ __device__ constexpr int pair_of(int AX, int C) {
   return AX == 0 ? (C == 1 ? 0 : C == 2 ? 1 : -1)
-       : AX == 1 ? (C == 0 ? 2 : C == 2 ? 3 : -1)
-                 : (C == 0 ? 4 : C == 1 ? 5 : -1);
+       : AX == 1 ? (C == 0 ? 0 : C == 2 ? 1 : -1)
+                 : (C == 0 ? 0 : C == 1 ? 1 : -1);
 }
 __host__ __device__ constexpr float pair_sign(bool electric, int AX, int C) {
   return (electric != ((AX == 0) ? (C == 1) : (AX == 1) ? (C == 2) : (C == 0))) ? 1.f : -1.f;
 }
-// the component whose difference drives the pair (E pairs use H, H pairs use E)
 __host__ __device__ constexpr int pair_driver(int AX, int C) {
   return AX == 0 ? (C == 1 ? 2 : 1) : AX == 1 ? (C == 0 ? 2 : 0) : (C == 0 ? 1 : 0);
 }
@@ -106,36 +107,26 @@ __device__ __forceinline__ int axis_stride(int AX, const AdjParams& p) {
   return AX == 0 ? p.sx : AX == 1 ? p.sy : 1;
 }
 
-// slab membership along an axis (0 out, 1 minus, 2 plus) and the profile index
-template <bool ELECTRIC>
-__device__ __forceinline__ int member(int c, int n, int Tm, int Tp, int& pr) {
-  return axis_member<ELECTRIC>(c, n, Tm, Tp, pr);
-}
-
-__device__ __forceinline__ const float* slab_rows(const AdjParams& p, int AX, int where, int& T) {
+// Slab of axis AX holding node (i, j, k) (E ranges if ELECTRIC, else H ranges; every coordinate
+// below its cell count): slab index (-1 if none), profile index and Phi index.
+template <bool ELECTRIC, int AX>
+__device__ __forceinline__ int slab_of(const AdjParams& p, int i, int j, int k, int& pr,
+                                       int& pidx) {
+  if (i < 0 || j < 0 || k < 0 || i >= p.nx || j >= p.ny || k >= p.nz) return -1;
+  const int c = AX == 0 ? i : AX == 1 ? j : k;
+  const int n = AX == 0 ? p.nx : AX == 1 ? p.ny : p.nz;
+  const int where = axis_member<ELECTRIC>(c, n, p.slab[AX].T, p.slab[AX + 3].T, pr);
+  if (!where) return -1;
   const int s = AX + (where == 2 ? 3 : 0);
-  T = p.T[s];
-  return p.R[s];
+  pidx = phi_index<AX>(i, j, k, pr, p.slab[s].T, p.ny, p.nz);
+  return s;
 }
 
-// E node inside the E domain and in the slab of axis AX? (E ranges)
-__device__ __forceinline__ bool e_in_slab(const AdjParams& p, int AX, int i, int j, int k,
-                                          int& where, int& pr) {
-  if (i < 0 || j < 0 || k < 0 || i >= p.nx || j >= p.ny || k >= p.nz) return false;
-  const int c = AX == 0 ? i : AX == 1 ? j : k;
-  const int n = AX == 0 ? p.nx : AX == 1 ? p.ny : p.nz;
-  where = member<true>(c, n, p.T[AX], p.T[AX + 3], pr);
-  return where != 0;
-}
-
-// H node inside the H PML domain (all coordinates < n) and in the slab of axis AX? (H ranges)
-__device__ __forceinline__ bool h_in_slab(const AdjParams& p, int AX, int i, int j, int k,
-                                          int& where, int& pr) {
-  if (i < 0 || j < 0 || k < 0 || i >= p.nx || j >= p.ny || k >= p.nz) return false;
-  const int c = AX == 0 ? i : AX == 1 ? j : k;
-  const int n = AX == 0 ? p.nx : AX == 1 ? p.ny : p.nz;
-  where = member<false>(c, n, p.T[AX], p.T[AX + 3], pr);
-  return where != 0;
+// Is the node within one cell of any slab (so that it or a neighbour may be in one)?
+__device__ __forceinline__ bool near_slab(const AdjParams& p, int i, int j, int k) {
+  return i <= p.slab[0].T + 1 || i >= p.nx - p.slab[3].T - 1 ||
+         j <= p.slab[1].T + 1 || j >= p.ny - p.slab[4].T - 1 ||
+         k <= p.slab[2].T + 1 || k >= p.nz - p.slab[5].T - 1;
 }
 
 __device__ __forceinline__ bool e_updated(int C, int i, int j, int k, const AdjParams& p) {
@@ -150,7 +141,7 @@ __device__ __forceinline__ bool h_updated(int C, int i, int j, int k, const AdjP
   return i < p.nx && j < p.ny && k >= 1;
 }
 
-// E curl term of component C at idx from H (the bracket multiplied by CB/d)
+// E curl bracket of component C at idx (multiplied by CB/d in the update)
 __device__ __forceinline__ float e_curl(int C, int idx, const float* H, const AdjParams& p) {
   const float* Hx = H;
   const float* Hy = H + p.ncomp;
@@ -160,307 +151,327 @@ __device__ __forceinline__ float e_curl(int C, int idx, const float* H, const Ad
   return (Hy[idx] - Hy[idx - p.sx]) - (Hx[idx] - Hx[idx - p.sy]);
 }
 
-// Apply the slab corrections of component C in the reference's slab order (x0 y0 z0 xmax ymax
-// zmax): with one slab per axis, axis b comes before a (a < b) only when a is on its plus side
-// and b on its minus side.
+// slab corrections of component C in the reference's slab order (x0 y0 z0 xmax ymax zmax):
+// axis b before a (a < b) only when a's slab is a plus slab and b's a minus slab
 template <int C>
-__device__ __forceinline__ float apply_terms(float F, const int* where, const float* t) {
+__device__ __forceinline__ float apply_terms(float F, const int* s, const float* t) {
   constexpr int a = C == 0 ? 1 : 0;
   constexpr int b = C == 2 ? 1 : 2;
-  if (where[a] && where[b] && where[a] == 2 && where[b] == 1) {
+  if (s[a] >= 3 && s[b] >= 0 && s[b] < 3) {
     F = F + t[b];
     F = F + t[a];
   } else {
-    if (where[a]) F = F + t[a];
-    if (where[b]) F = F + t[b];
+    if (s[a] >= 0) F = F + t[a];
+    if (s[b] >= 0) F = F + t[b];
   }
   return F;
 }
 
 // ---- forward --------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAdjThreads) adj_fwd_h(const __grid_constant__ AdjParams p) {
+// H half-step: Hout = update(Hin, E); Phi_H in place. Hin may equal Hout.
+__global__ void __launch_bounds__(kAdjThreads)
+adj_fwd_h(const __grid_constant__ AdjParams p, const float* __restrict__ E, const float* Hin,
+          float* Hout, const __grid_constant__ PhiSet phi) {
   const int stride = gridDim.x * blockDim.x;
-  const float* Ex = p.E;
-  const float* Ey = p.E + p.ncomp;
-  const float* Ez = p.E + 2 * (size_t)p.ncomp;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int idx = n.idx;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.ncomp) return;
+  Walk w(q, stride, p);
+  const float* Ex = E;
+  const float* Ey = E + p.ncomp;
+  const float* Ez = E + 2 * (size_t)p.ncomp;
+  for (; q < p.ncomp; q += stride, w.advance(p)) {
+    const int i = w.i, j = w.j, k = w.k, idx = q;
     float h[3];
-    for (int C = 0; C < 3; ++C) h[C] = p.H[C * (size_t)p.ncomp + idx];
-    if (h_updated(0, n.i, n.j, n.k, p))
+#pragma unroll
+    for (int C = 0; C < 3; ++C) h[C] = Hin[C * (size_t)p.ncomp + idx];
+    if (h_updated(0, i, j, k, p))
       h[0] = h[0] - p.dbd * (Ez[idx + p.sy] - Ez[idx]) + p.dbd * (Ey[idx + 1] - Ey[idx]);
-    if (h_updated(1, n.i, n.j, n.k, p))
+    if (h_updated(1, i, j, k, p))
       h[1] = h[1] - p.dbd * (Ex[idx + 1] - Ex[idx]) + p.dbd * (Ez[idx + p.sx] - Ez[idx]);
-    if (h_updated(2, n.i, n.j, n.k, p))
+    if (h_updated(2, i, j, k, p))
       h[2] = h[2] - p.dbd * (Ey[idx + p.sx] - Ey[idx]) + p.dbd * (Ex[idx + p.sy] - Ex[idx]);
-    int where[3] = {0, 0, 0};
-    float t[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // [component][axis]
-    bool any = false;
+    if (near_slab(p, i, j, k)) {
+      int s[3], pr[3], pidx[3];
+      s[0] = slab_of<false, 0>(p, i, j, k, pr[0], pidx[0]);
+      s[1] = slab_of<false, 1>(p, i, j, k, pr[1], pidx[1]);
+      s[2] = slab_of<false, 2>(p, i, j, k, pr[2], pidx[2]);
+      float t[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // [component][axis]
 #pragma unroll
-    for (int AX = 0; AX < 3; ++AX) {
-      int pr = 0;
-      if (!h_in_slab(p, AX, n.i, n.j, n.k, where[AX], pr)) { where[AX] = 0; continue; }
-      any = true;
-      int T;
-      const float* R = slab_rows(p, AX, where[AX], T);
-      const float RA = R[4 * T + pr], RB = R[5 * T + pr], RE = R[6 * T + pr], RF = R[7 * T + pr];
-      const int st = axis_stride(AX, p);
+      for (int AX = 0; AX < 3; ++AX) {
+        if (s[AX] < 0) continue;
+        const AdjSlab& sl = p.slab[s[AX]];
+        const int T = sl.T, r = pr[AX];
+        const float RA = sl.R[4 * T + r], RB = sl.R[5 * T + r], RE = sl.R[6 * T + r], RF = sl.R[7 * T + r];
+        const int st = axis_stride(AX, p);
 #pragma unroll
-      for (int C = 0; C < 3; ++C) {
-        const int q2 = pair_of(AX, C);
-        if (q2 < 0) continue;
-        const float* D = p.E + pair_driver(AX, C) * (size_t)p.ncomp;
-        const float dF = (D[idx + st] - D[idx]) * p.rd;
-        float* phi = p.phiH + q2 * (size_t)p.ncomp + idx;
-        const float ph = *phi;
-        const float X = (RA - 1.0f) * dF + RB * ph;
-        *phi = RE * ph - RF * dF;
-        t[C][AX] = pair_sign(false, AX, C) * (p.srcm * X);
+        for (int C = 0; C < 3; ++C) {
+          const int pw = pair_of(AX, C);
+          if (pw < 0) continue;
+          const float* D = E + pair_driver(AX, C) * (size_t)p.ncomp;
+          const float dF = (D[idx + st] - D[idx]) * p.rd;
+          float* ph = phi.p[s[AX]][pw] + pidx[AX];
+          const float v = *ph;
+          const float X = (RA - 1.0f) * dF + RB * v;
+          *ph = RE * v - RF * dF;
+          t[C][AX] = pair_sign(false, AX, C) * (p.srcm * X);
+        }
       }
+      h[0] = apply_terms<0>(h[0], s, t[0]);
+      h[1] = apply_terms<1>(h[1], s, t[1]);
+      h[2] = apply_terms<2>(h[2], s, t[2]);
     }
-    if (any) {
-      h[0] = apply_terms<0>(h[0], where, t[0]);
-      h[1] = apply_terms<1>(h[1], where, t[1]);
-      h[2] = apply_terms<2>(h[2], where, t[2]);
-    }
-    for (int C = 0; C < 3; ++C) p.H[C * (size_t)p.ncomp + idx] = h[C];
+#pragma unroll
+    for (int C = 0; C < 3; ++C) Hout[C * (size_t)p.ncomp + idx] = h[C];
   }
 }
 
-__global__ void __launch_bounds__(kAdjThreads) adj_fwd_e(const __grid_constant__ AdjParams p, int it) {
+// E half-step n: Eout = update(Ein, H); Phi_E read from phin, written to phout; sources.
+// Ein may equal Eout and phin phout.
+__global__ void __launch_bounds__(kAdjThreads)
+adj_fwd_e(const __grid_constant__ AdjParams p, const float* Ein, float* Eout,
+          const float* __restrict__ H, const __grid_constant__ PhiSet phin,
+          const __grid_constant__ PhiSet phout, int it) {
   const int stride = gridDim.x * blockDim.x;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int idx = n.idx;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.ncomp) return;
+  Walk w(q, stride, p);
+  for (; q < p.ncomp; q += stride, w.advance(p)) {
+    const int i = w.i, j = w.j, k = w.k, idx = q;
     float e[3], cb[3];
+#pragma unroll
     for (int C = 0; C < 3; ++C) {
-      e[C] = p.E[C * (size_t)p.ncomp + idx];
-      cb[C] = p.CB[C * (size_t)p.ncomp + idx];
-      if (e_updated(C, n.i, n.j, n.k, p))
-        e[C] = p.CA[C * (size_t)p.ncomp + idx] * e[C] + (cb[C] * p.rd) * e_curl(C, idx, p.H, p);
+      const size_t o = C * (size_t)p.ncomp + idx;
+      e[C] = Ein[o];
+      cb[C] = p.CB[o];
+      if (e_updated(C, i, j, k, p)) e[C] = p.CA[o] * e[C] + (cb[C] * p.rd) * e_curl(C, idx, H, p);
     }
-    int where[3] = {0, 0, 0};
-    float t[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    bool any = false;
+    if (near_slab(p, i, j, k)) {
+      int s[3], pr[3], pidx[3];
+      s[0] = slab_of<true, 0>(p, i, j, k, pr[0], pidx[0]);
+      s[1] = slab_of<true, 1>(p, i, j, k, pr[1], pidx[1]);
+      s[2] = slab_of<true, 2>(p, i, j, k, pr[2], pidx[2]);
+      float t[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
-    for (int AX = 0; AX < 3; ++AX) {
-      int pr = 0;
-      if (!e_in_slab(p, AX, n.i, n.j, n.k, where[AX], pr)) { where[AX] = 0; continue; }
-      any = true;
-      int T;
-      const float* R = slab_rows(p, AX, where[AX], T);
-      const float RA = R[pr], RB = R[T + pr], RE = R[2 * T + pr], RF = R[3 * T + pr];
-      const int st = axis_stride(AX, p);
+      for (int AX = 0; AX < 3; ++AX) {
+        if (s[AX] < 0) continue;
+        const AdjSlab& sl = p.slab[s[AX]];
+        const int T = sl.T, r = pr[AX];
+        const float RA = sl.R[r], RB = sl.R[T + r], RE = sl.R[2 * T + r], RF = sl.R[3 * T + r];
+        const int st = axis_stride(AX, p);
 #pragma unroll
-      for (int C = 0; C < 3; ++C) {
-        const int q2 = pair_of(AX, C);
-        if (q2 < 0) continue;
-        const float* D = p.H + pair_driver(AX, C) * (size_t)p.ncomp;
-        const float dF = (D[idx] - D[idx - st]) * p.rd;
-        float* phi = p.phiE + q2 * (size_t)p.ncomp + idx;
-        const float ph = *phi;
-        const float X = (RA - 1.0f) * dF + RB * ph;
-        *phi = RE * ph - RF * dF;
-        t[C][AX] = pair_sign(true, AX, C) * (cb[C] * X);
+        for (int C = 0; C < 3; ++C) {
+          const int pw = pair_of(AX, C);
+          if (pw < 0) continue;
+          const float* D = H + pair_driver(AX, C) * (size_t)p.ncomp;
+          const float dF = (D[idx] - D[idx - st]) * p.rd;
+          const float v = phin.p[s[AX]][pw][pidx[AX]];
+          const float X = (RA - 1.0f) * dF + RB * v;
+          phout.p[s[AX]][pw][pidx[AX]] = RE * v - RF * dF;
+          t[C][AX] = pair_sign(true, AX, C) * (cb[C] * X);
+        }
       }
+      e[0] = apply_terms<0>(e[0], s, t[0]);
+      e[1] = apply_terms<1>(e[1], s, t[1]);
+      e[2] = apply_terms<2>(e[2], s, t[2]);
     }
-    if (any) {
-      e[0] = apply_terms<0>(e[0], where, t[0]);
-      e[1] = apply_terms<1>(e[1], where, t[1]);
-      e[2] = apply_terms<2>(e[2], where, t[2]);
-    }
-    for (int s = 0; s < p.nsrc; ++s)
-      if (p.src_idx[s] == idx) {
-        const int C = p.src_comp[s];
-        e[C] = e[C] - cb[C] * p.waves[(size_t)s * p.iterations + it] * p.src_scale[s];
+    for (int n = 0; n < p.nsrc; ++n)
+      if (p.src_idx[n] == idx) {
+        const int C = p.src_comp[n];
+        e[C] = e[C] - cb[C] * p.waves[(size_t)n * p.iterations + it] * p.src_scale[n];
       }
-    for (int C = 0; C < 3; ++C) p.E[C * (size_t)p.ncomp + idx] = e[C];
+#pragma unroll
+    for (int C = 0; C < 3; ++C) Eout[C * (size_t)p.ncomp + idx] = e[C];
   }
 }
 
-__global__ void adj_fwd_rx(const __grid_constant__ AdjParams p, float* traces, int it) {
-  for (int r = threadIdx.x; r < p.nrx; r += blockDim.x) {
-    const int C = p.rx[2 * r], idx = p.rx[2 * r + 1];
-    traces[(size_t)r * p.iterations + it] = p.E[C * (size_t)p.ncomp + idx];
-  }
+__global__ void adj_fwd_rx(const __grid_constant__ AdjParams p, const float* E, float* traces, int it) {
+  for (int r = threadIdx.x; r < p.nrx; r += blockDim.x)
+    traces[(size_t)r * p.iterations + it] = E[p.rx_comp[r] * (size_t)p.ncomp + p.rx_idx[r]];
 }
 
 // ---- adjoint --------------------------------------------------------------------------
+struct AdjStep {
+  float* lE;          // [3][ncomp] adjoint of E (in place)
+  float* lH;          // [3][ncomp] adjoint of H (in place)
+  float* uE;          // [3][ncomp]
+  float* uH;          // [3][ncomp]
+  PhiSet lphiE, lphiH, dFE, dFH;
+  const float* En;    // forward E_n
+  const float* Hh;    // forward H^{n+1/2}
+  PhiSet PEn;         // forward Phi_E at step n
+  float* gCA;         // [3][ncomp] fp32 partials of the segment
+  float* gCB;
+  const float* gtr;   // [nrx][iterations] d(misfit)/d(traces)
+  int it;             // step being undone (n)
+  int finish;         // 1: lamE still needs the step n+1 terms (n + 1 < iterations)
+};
+
+__device__ __forceinline__ float at(const float* a, int C, int i, int j, int k, const AdjParams& p) {
+  if (i < 0 || j < 0 || k < 0 || i > p.nx || j > p.ny || k > p.nz) return 0.f;
+  return a[C * (size_t)p.ncomp + i * p.sx + j * p.sy + k];
+}
+
+template <bool ELECTRIC, int AX>
+__device__ __forceinline__ float dF_at(const PhiSet& d, int C, int i, int j, int k,
+                                       const AdjParams& p) {
+  int pr, pidx;
+  const int s = slab_of<ELECTRIC, AX>(p, i, j, k, pr, pidx);
+  return s < 0 ? 0.f : d.p[s][pair_of(AX, C)][pidx];
+}
+
 __global__ void __launch_bounds__(kAdjThreads)
-adj_e_nodes(const __grid_constant__ AdjParams p, const __grid_constant__ AdjBuffers b, int it) {
+adj_e_step(const __grid_constant__ AdjParams p, const __grid_constant__ AdjStep b) {
   const int stride = gridDim.x * blockDim.x;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int idx = n.idx;
-    float lam[3], cb[3];
-    double gcb[3] = {0.0, 0.0, 0.0};
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.ncomp) return;
+  Walk w(q, stride, p);
+  const float rd = p.rd;
+  for (; q < p.ncomp; q += stride, w.advance(p)) {
+    const int i = w.i, j = w.j, k = w.k, idx = q;
+    float lam[3];
+#pragma unroll
+    for (int C = 0; C < 3; ++C) lam[C] = b.lE[C * (size_t)p.ncomp + idx];
+    const bool near = near_slab(p, i, j, k);
+    if (b.finish) {
+      // adjoint of E_{n+1}: transposed H curl of u_H (Hx -= DB/d (Ez(j+1) - Ez) - DB/d (Ey(k+1) - Ey) ...)
+      const float* u = b.uH;
+      lam[0] += at(u, 1, i, j, k, p) - at(u, 1, i, j, k - 1, p) + at(u, 2, i, j - 1, k, p) - at(u, 2, i, j, k, p);
+      lam[1] += at(u, 0, i, j, k - 1, p) - at(u, 0, i, j, k, p) - at(u, 2, i - 1, j, k, p) + at(u, 2, i, j, k, p);
+      lam[2] += -at(u, 0, i, j - 1, k, p) + at(u, 0, i, j, k, p) + at(u, 1, i - 1, j, k, p) - at(u, 1, i, j, k, p);
+      if (near) {
+        // H-PML differences dF(h) = (E(h + a) - E(h)) / d feed E at h + a and h
+        lam[2] += rd * (dF_at<false, 0>(b.dFH, 1, i - 1, j, k, p) - dF_at<false, 0>(b.dFH, 1, i, j, k, p) +
+                        dF_at<false, 1>(b.dFH, 0, i, j - 1, k, p) - dF_at<false, 1>(b.dFH, 0, i, j, k, p));
+        lam[1] += rd * (dF_at<false, 0>(b.dFH, 2, i - 1, j, k, p) - dF_at<false, 0>(b.dFH, 2, i, j, k, p) +
+                        dF_at<false, 2>(b.dFH, 0, i, j, k - 1, p) - dF_at<false, 2>(b.dFH, 0, i, j, k, p));
+        lam[0] += rd * (dF_at<false, 1>(b.dFH, 2, i, j - 1, k, p) - dF_at<false, 1>(b.dFH, 2, i, j, k, p) +
+                        dF_at<false, 2>(b.dFH, 1, i, j, k - 1, p) - dF_at<false, 2>(b.dFH, 1, i, j, k, p));
+      }
+      for (int r = 0; r < p.nrx; ++r)
+        if (p.rx_idx[r] == idx) lam[p.rx_comp[r]] += b.gtr[(size_t)r * p.iterations + b.it + 1];
+    }
+    // undo the E half-step n
+    float gcb[3] = {0.f, 0.f, 0.f};
+    float cb[3];
+#pragma unroll
     for (int C = 0; C < 3; ++C) {
       const size_t o = C * (size_t)p.ncomp + idx;
-      lam[C] = b.lE[o];
       cb[C] = p.CB[o];
       float u = 0.f, lnew = lam[C];
-      if (e_updated(C, n.i, n.j, n.k, p)) {
-        u = (cb[C] * p.rd) * lam[C];
+      if (e_updated(C, i, j, k, p)) {
+        u = (cb[C] * rd) * lam[C];
         lnew = p.CA[o] * lam[C];
-        b.gCA[o] += (double)lam[C] * (double)b.En[o];
-        gcb[C] += (double)lam[C] * (double)(p.rd * e_curl(C, idx, b.Hh, p));
+        b.gCA[o] += lam[C] * b.En[o];
+        gcb[C] = lam[C] * (rd * e_curl(C, idx, b.Hh, p));
       }
       b.uE[o] = u;
       b.lE[o] = lnew;
     }
+    if (near) {
+      int s[3], pr[3], pidx[3];
+      s[0] = slab_of<true, 0>(p, i, j, k, pr[0], pidx[0]);
+      s[1] = slab_of<true, 1>(p, i, j, k, pr[1], pidx[1]);
+      s[2] = slab_of<true, 2>(p, i, j, k, pr[2], pidx[2]);
 #pragma unroll
-    for (int AX = 0; AX < 3; ++AX) {
-      int where = 0, pr = 0;
-      if (!e_in_slab(p, AX, n.i, n.j, n.k, where, pr)) continue;
-      int T;
-      const float* R = slab_rows(p, AX, where, T);
-      const float RA = R[pr], RB = R[T + pr], RE = R[2 * T + pr], RF = R[3 * T + pr];
-      const int st = axis_stride(AX, p);
+      for (int AX = 0; AX < 3; ++AX) {
+        if (s[AX] < 0) continue;
+        const AdjSlab& sl = p.slab[s[AX]];
+        const int T = sl.T, r = pr[AX];
+        const float RA = sl.R[r], RB = sl.R[T + r], RE = sl.R[2 * T + r], RF = sl.R[3 * T + r];
+        const int st = axis_stride(AX, p);
 #pragma unroll
-      for (int C = 0; C < 3; ++C) {
-        const int q2 = pair_of(AX, C);
-        if (q2 < 0) continue;
-        const size_t o = q2 * (size_t)p.ncomp + idx;
-        const float s = pair_sign(true, AX, C);
-        const float Xb = s * cb[C] * lam[C];
-        const float lph = b.lphiE[o];
-        b.dFE[o] = (RA - 1.0f) * Xb - RF * lph;
-        b.lphiE[o] = RB * Xb + RE * lph;
-        const float* D = b.Hh + pair_driver(AX, C) * (size_t)p.ncomp;
-        const float dF = (D[idx] - D[idx - st]) * p.rd;
-        const float X = (RA - 1.0f) * dF + RB * b.PEn[o];
-        gcb[C] += (double)s * (double)X * (double)lam[C];
+        for (int C = 0; C < 3; ++C) {
+          const int pw = pair_of(AX, C);
+          if (pw < 0) continue;
+          const int o = pidx[AX];
+          const float sg = pair_sign(true, AX, C);
+          const float Xb = sg * cb[C] * lam[C];
+          float* lph = b.lphiE.p[s[AX]][pw] + o;
+          const float l0 = *lph;
+          b.dFE.p[s[AX]][pw][o] = (RA - 1.0f) * Xb - RF * l0;
+          *lph = RB * Xb + RE * l0;
+          const float* D = b.Hh + pair_driver(AX, C) * (size_t)p.ncomp;
+          const float dF = (D[idx] - D[idx - st]) * rd;
+          const float X = (RA - 1.0f) * dF + RB * b.PEn.p[s[AX]][pw][o];
+          gcb[C] += sg * X * lam[C];
+        }
       }
     }
-    for (int s = 0; s < p.nsrc; ++s)
-      if (p.src_idx[s] == idx) {
-        const int C = p.src_comp[s];
-        gcb[C] -= (double)p.waves[(size_t)s * p.iterations + it] * (double)p.src_scale[s] *
-                  (double)lam[C];
+    for (int n = 0; n < p.nsrc; ++n)
+      if (p.src_idx[n] == idx) {
+        const int C = p.src_comp[n];
+        gcb[C] -= p.waves[(size_t)n * p.iterations + b.it] * p.src_scale[n] * lam[C];
       }
+#pragma unroll
     for (int C = 0; C < 3; ++C) b.gCB[C * (size_t)p.ncomp + idx] += gcb[C];
   }
 }
 
-// u of E component C at node (i, j, k), 0 outside the arrays
-__device__ __forceinline__ float u_at(const float* u, int C, int i, int j, int k,
-                                      const AdjParams& p) {
-  if (i < 0 || j < 0 || k < 0 || i > p.nx || j > p.ny || k > p.nz) return 0.f;
-  return u[C * (size_t)p.ncomp + i * p.sx + j * p.sy + k];
-}
-
-// adjoint of the PML difference of pair (AX, C) at E node (i, j, k), 0 off the slab
-__device__ __forceinline__ float dFE_at(const AdjBuffers& b, const AdjParams& p, int AX, int C,
-                                        int i, int j, int k) {
-  int where, pr;
-  if (!e_in_slab(p, AX, i, j, k, where, pr)) return 0.f;
-  return b.dFE[pair_of(AX, C) * (size_t)p.ncomp + i * p.sx + j * p.sy + k];
-}
-
-__device__ __forceinline__ float dFH_at(const AdjBuffers& b, const AdjParams& p, int AX, int C,
-                                        int i, int j, int k) {
-  int where, pr;
-  if (!h_in_slab(p, AX, i, j, k, where, pr)) return 0.f;
-  return b.dFH[pair_of(AX, C) * (size_t)p.ncomp + i * p.sx + j * p.sy + k];
-}
-
 __global__ void __launch_bounds__(kAdjThreads)
-adj_e_to_h(const __grid_constant__ AdjParams p, const __grid_constant__ AdjBuffers b) {
+adj_h_step(const __grid_constant__ AdjParams p, const __grid_constant__ AdjStep b) {
   const int stride = gridDim.x * blockDim.x;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.ncomp) return;
+  Walk w(q, stride, p);
+  const float rd = p.rd;
   const float* u = b.uE;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int i = n.i, j = n.j, k = n.k;
-    // transposed E curl (E update: Ex += u-terms of Hz(j), Hz(j-1), Hy(k), Hy(k-1) ...)
-    float gx = u_at(u, 1, i, j, k, p) - u_at(u, 1, i, j, k + 1, p) - u_at(u, 2, i, j, k, p) +
-               u_at(u, 2, i, j + 1, k, p);
-    float gy = -u_at(u, 0, i, j, k, p) + u_at(u, 0, i, j, k + 1, p) + u_at(u, 2, i, j, k, p) -
-               u_at(u, 2, i + 1, j, k, p);
-    float gz = u_at(u, 0, i, j, k, p) - u_at(u, 0, i, j + 1, k, p) - u_at(u, 1, i, j, k, p) +
-               u_at(u, 1, i + 1, j, k, p);
-    // transposed PML differences: dF(e) = (H(e) - H(e - a)) / d feeds H at e and e - a
-    const float rd = p.rd;
-    gz += rd * (dFE_at(b, p, 0, 1, i, j, k) - dFE_at(b, p, 0, 1, i + 1, j, k) +
-                dFE_at(b, p, 1, 0, i, j, k) - dFE_at(b, p, 1, 0, i, j + 1, k));
-    gy += rd * (dFE_at(b, p, 0, 2, i, j, k) - dFE_at(b, p, 0, 2, i + 1, j, k) +
-                dFE_at(b, p, 2, 0, i, j, k) - dFE_at(b, p, 2, 0, i, j, k + 1));
-    gx += rd * (dFE_at(b, p, 1, 2, i, j, k) - dFE_at(b, p, 1, 2, i, j + 1, k) +
-                dFE_at(b, p, 2, 1, i, j, k) - dFE_at(b, p, 2, 1, i, j, k + 1));
-    b.lH[n.idx] += gx;
-    b.lH[p.ncomp + (size_t)n.idx] += gy;
-    b.lH[2 * (size_t)p.ncomp + n.idx] += gz;
-  }
-}
-
-__global__ void __launch_bounds__(kAdjThreads)
-adj_h_nodes(const __grid_constant__ AdjParams p, const __grid_constant__ AdjBuffers b) {
-  const int stride = gridDim.x * blockDim.x;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int idx = n.idx;
+  for (; q < p.ncomp; q += stride, w.advance(p)) {
+    const int i = w.i, j = w.j, k = w.k, idx = q;
     float lam[3];
+#pragma unroll
+    for (int C = 0; C < 3; ++C) lam[C] = b.lH[C * (size_t)p.ncomp + idx];
+    // transposed E curl (Ex += CB/d ((Hz - Hz(j-1)) - (Hy - Hy(k-1))) ...)
+    lam[0] += at(u, 1, i, j, k, p) - at(u, 1, i, j, k + 1, p) - at(u, 2, i, j, k, p) + at(u, 2, i, j + 1, k, p);
+    lam[1] += -at(u, 0, i, j, k, p) + at(u, 0, i, j, k + 1, p) + at(u, 2, i, j, k, p) - at(u, 2, i + 1, j, k, p);
+    lam[2] += at(u, 0, i, j, k, p) - at(u, 0, i, j + 1, k, p) - at(u, 1, i, j, k, p) + at(u, 1, i + 1, j, k, p);
+    const bool near = near_slab(p, i, j, k);
+    if (near) {
+      // E-PML differences dF(e) = (H(e) - H(e - a)) / d feed H at e and e - a
+      lam[2] += rd * (dF_at<true, 0>(b.dFE, 1, i, j, k, p) - dF_at<true, 0>(b.dFE, 1, i + 1, j, k, p) +
+                      dF_at<true, 1>(b.dFE, 0, i, j, k, p) - dF_at<true, 1>(b.dFE, 0, i, j + 1, k, p));
+      lam[1] += rd * (dF_at<true, 0>(b.dFE, 2, i, j, k, p) - dF_at<true, 0>(b.dFE, 2, i + 1, j, k, p) +
+                      dF_at<true, 2>(b.dFE, 0, i, j, k, p) - dF_at<true, 2>(b.dFE, 0, i, j, k + 1, p));
+      lam[0] += rd * (dF_at<true, 1>(b.dFE, 2, i, j, k, p) - dF_at<true, 1>(b.dFE, 2, i, j + 1, k, p) +
+                      dF_at<true, 2>(b.dFE, 1, i, j, k, p) - dF_at<true, 2>(b.dFE, 1, i, j, k + 1, p));
+    }
+    // undo the H half-step n (DA = 1: lamH passes through)
+#pragma unroll
     for (int C = 0; C < 3; ++C) {
       const size_t o = C * (size_t)p.ncomp + idx;
-      lam[C] = b.lH[o];
-      b.uH[o] = h_updated(C, n.i, n.j, n.k, p) ? p.dbd * lam[C] : 0.f;
+      b.lH[o] = lam[C];
+      b.uH[o] = h_updated(C, i, j, k, p) ? p.dbd * lam[C] : 0.f;
     }
+    if (near) {
+      int s[3], pr[3], pidx[3];
+      s[0] = slab_of<false, 0>(p, i, j, k, pr[0], pidx[0]);
+      s[1] = slab_of<false, 1>(p, i, j, k, pr[1], pidx[1]);
+      s[2] = slab_of<false, 2>(p, i, j, k, pr[2], pidx[2]);
 #pragma unroll
-    for (int AX = 0; AX < 3; ++AX) {
-      int where = 0, pr = 0;
-      if (!h_in_slab(p, AX, n.i, n.j, n.k, where, pr)) continue;
-      int T;
-      const float* R = slab_rows(p, AX, where, T);
-      const float RA = R[4 * T + pr], RB = R[5 * T + pr], RE = R[6 * T + pr], RF = R[7 * T + pr];
+      for (int AX = 0; AX < 3; ++AX) {
+        if (s[AX] < 0) continue;
+        const AdjSlab& sl = p.slab[s[AX]];
+        const int T = sl.T, r = pr[AX];
+        const float RA = sl.R[4 * T + r], RB = sl.R[5 * T + r], RE = sl.R[6 * T + r], RF = sl.R[7 * T + r];
 #pragma unroll
-      for (int C = 0; C < 3; ++C) {
-        const int q2 = pair_of(AX, C);
-        if (q2 < 0) continue;
-        const size_t o = q2 * (size_t)p.ncomp + idx;
-        const float Xb = pair_sign(false, AX, C) * p.srcm * lam[C];
-        const float lph = b.lphiH[o];
-        b.dFH[o] = (RA - 1.0f) * Xb - RF * lph;
-        b.lphiH[o] = RB * Xb + RE * lph;
+        for (int C = 0; C < 3; ++C) {
+          const int pw = pair_of(AX, C);
+          if (pw < 0) continue;
+          const int o = pidx[AX];
+          const float Xb = pair_sign(false, AX, C) * p.srcm * lam[C];
+          float* lph = b.lphiH.p[s[AX]][pw] + o;
+          const float l0 = *lph;
+          b.dFH.p[s[AX]][pw][o] = (RA - 1.0f) * Xb - RF * l0;
+          *lph = RB * Xb + RE * l0;
+        }
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(kAdjThreads)
-adj_h_to_e(const __grid_constant__ AdjParams p, const __grid_constant__ AdjBuffers b) {
-  const int stride = gridDim.x * blockDim.x;
-  const float* u = b.uH;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.ncomp; q += stride) {
-    const Node n = node_of(q, p);
-    const int i = n.i, j = n.j, k = n.k;
-    // transposed H curl (Hx -= DB/d (Ez(j+1) - Ez) - DB/d (Ey(k+1) - Ey) ...)
-    float gx = u_at(u, 1, i, j, k, p) - u_at(u, 1, i, j, k - 1, p) + u_at(u, 2, i, j - 1, k, p) -
-               u_at(u, 2, i, j, k, p);
-    float gy = u_at(u, 0, i, j, k - 1, p) - u_at(u, 0, i, j, k, p) - u_at(u, 2, i - 1, j, k, p) +
-               u_at(u, 2, i, j, k, p);
-    float gz = -u_at(u, 0, i, j - 1, k, p) + u_at(u, 0, i, j, k, p) + u_at(u, 1, i - 1, j, k, p) -
-               u_at(u, 1, i, j, k, p);
-    // transposed PML differences: dF(h) = (E(h + a) - E(h)) / d feeds E at h + a and h
-    const float rd = p.rd;
-    gz += rd * (dFH_at(b, p, 0, 1, i - 1, j, k) - dFH_at(b, p, 0, 1, i, j, k) +
-                dFH_at(b, p, 1, 0, i, j - 1, k) - dFH_at(b, p, 1, 0, i, j, k));
-    gy += rd * (dFH_at(b, p, 0, 2, i - 1, j, k) - dFH_at(b, p, 0, 2, i, j, k) +
-                dFH_at(b, p, 2, 0, i, j, k - 1) - dFH_at(b, p, 2, 0, i, j, k));
-    gx += rd * (dFH_at(b, p, 1, 2, i, j - 1, k) - dFH_at(b, p, 1, 2, i, j, k) +
-                dFH_at(b, p, 2, 1, i, j, k - 1) - dFH_at(b, p, 2, 1, i, j, k));
-    b.lE[n.idx] += gx;
-    b.lE[p.ncomp + (size_t)n.idx] += gy;
-    b.lE[2 * (size_t)p.ncomp + n.idx] += gz;
-  }
-}
-
-__global__ void adj_receivers(const __grid_constant__ AdjParams p, AdjBuffers b,
-                              const float* gtraces, int it) {
-  if (threadIdx.x != 0) return;
-  for (int r = 0; r < p.nrx; ++r) {
-    const int C = p.rx[2 * r], idx = p.rx[2 * r + 1];
-    b.lE[C * (size_t)p.ncomp + idx] += gtraces[(size_t)r * p.iterations + it];
-  }
+__global__ void adj_fold(const float* __restrict__ a, double* __restrict__ g, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    g[q] += (double)a[q];
 }
 
 }  // namespace
@@ -471,18 +482,22 @@ struct gbf_adj {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  long long ncomp = 0;
-  int K = 1;                 // checkpoint interval (steps)
+  long long N = 0;           // nodes per component
+  int K = 1;                 // checkpoint interval
   int nck = 0;               // checkpoints
+  size_t phi_len = 0;        // floats of one PhiSet (every slab, both pairs)
+  size_t off[6] = {0, 0, 0, 0, 0, 0};
   AdjParams p{};
   std::vector<void*> allocs;
-  float* state = nullptr;    // working E, H, phiE, phiH: 18 * ncomp
-  float* ckpt = nullptr;     // nck * 18 * ncomp
-  float* seg = nullptr;      // K * 12 * ncomp: E_n, H^{n+1/2}, PhiE_n of each step of a segment
-  float* adj = nullptr;      // lE lH (3 each) lphiE lphiH (6 each) uE uH (3 each) dFE dFH (6 each)
-  float* pml_rows = nullptr; // 6 * 8 * Tmax
+  float* pml_rows = nullptr; // 6 x 8 x Tmax
   float* waves = nullptr;
-  int* rx = nullptr;
+  float *E = nullptr, *H = nullptr, *phiE = nullptr, *phiH = nullptr;   // forward state
+  float* ckpt = nullptr;     // nck x (6N + 2 phi_len)
+  float *segE = nullptr, *segPhiE = nullptr, *segH = nullptr;         // recompute slots
+  float *recH = nullptr, *recPhiH = nullptr;
+  float *lE = nullptr, *lH = nullptr, *uE = nullptr, *uH = nullptr;
+  float *lphiE = nullptr, *lphiH = nullptr, *dFE = nullptr, *dFH = nullptr;
+  float *gCA = nullptr, *gCB = nullptr;                                // fp32 segment partials
   bool forward_done = false;
   int grid = 0;
 };
@@ -508,40 +523,19 @@ static int afail(gbf_adj* a, int code, const char* fmt, ...) {
                    "%s failed: %s", #call, cudaGetErrorString(e_));                       \
   } while (0)
 
-static int adj_alloc(gbf_adj* a, void** ptr, size_t bytes) {
-  AK(cudaMalloc(ptr, bytes));
-  a->allocs.push_back(*ptr);
-  AK(cudaMemsetAsync(*ptr, 0, bytes, a->stream));
+static PhiSet phiset(const gbf_adj* a, float* base) {
+  PhiSet ps;
+  for (int s = 0; s < 6; ++s) {
+    const int oc = a->p.slab[s].ocount;
+    ps.p[s][0] = (a->p.slab[s].T && base) ? base + a->off[s] : nullptr;
+    ps.p[s][1] = (a->p.slab[s].T && base) ? base + a->off[s] + oc : nullptr;
+  }
+  return ps;
+}
+
+static int copy_d2d(gbf_adj* a, float* dst, const float* src, size_t n) {
+  if (n) AK(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, a->stream));
   return GBF_OK;
-}
-
-static void set_state_ptrs(gbf_adj* a) {
-  const size_t N = a->ncomp;
-  a->p.E = a->state;
-  a->p.H = a->state + 3 * N;
-  a->p.phiE = a->state + 6 * N;
-  a->p.phiH = a->state + 12 * N;
-}
-
-static AdjBuffers buffers(gbf_adj* a, int step_in_seg, double* gCA, double* gCB) {
-  const size_t N = a->ncomp;
-  AdjBuffers b;
-  float* q = a->adj;
-  b.lE = q; q += 3 * N;
-  b.lH = q; q += 3 * N;
-  b.lphiE = q; q += 6 * N;
-  b.lphiH = q; q += 6 * N;
-  b.uE = q; q += 3 * N;
-  b.uH = q; q += 3 * N;
-  b.dFE = q; q += 6 * N;
-  b.dFH = q;
-  const float* s = a->seg + (size_t)step_in_seg * 12 * N;
-  b.En = s;
-  b.Hh = s + 3 * N;
-  b.PEn = s + 6 * N;
-  b.gCA = gCA;
-  b.gCB = gCB;
-  return b;
 }
 
 extern "C" {
@@ -554,10 +548,10 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
     return afail(nullptr, GBF_EINVAL, "gbf_adj_create: 3D grid and at least one iteration needed");
   if (!(d.d > 0.f) || !(d.dt > 0.f))
     return afail(nullptr, GBF_EINVAL, "gbf_adj_create: cell size and time step must be positive");
-  if (d.nsrc < 0 || d.nsrc > kAdjSrcMax || d.nrx < 1)
-    return afail(nullptr, GBF_EINVAL, "gbf_adj_create: 0..%d sources and at least one receiver", kAdjSrcMax);
-  if (d.reserved[0] || d.reserved[1] || d.reserved[2])
-    return afail(nullptr, GBF_EINVAL, "gbf_adj_create: reserved fields must be zero");
+  if (d.nsrc < 0 || d.nsrc > kAdjSrcMax || d.nrx < 1 || d.nrx > kAdjRxMax)
+    return afail(nullptr, GBF_EINVAL, "gbf_adj_create: 0..%d sources and 1..%d receivers", kAdjSrcMax, kAdjRxMax);
+  if (d.checkpoint_interval < 0 || d.reserved[0] || d.reserved[1] || d.reserved[2])
+    return afail(nullptr, GBF_EINVAL, "gbf_adj_create: bad checkpoint interval or reserved fields");
   const int n3[3] = {d.nx, d.ny, d.nz};
   for (int s = 0; s < 6; ++s)
     if (d.pml_thickness[s] < 0 || 2 * d.pml_thickness[s] >= n3[s % 3])
@@ -566,7 +560,7 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
   if (N > (1LL << 31) - 1) return afail(nullptr, GBF_EINVAL, "gbf_adj_create: more than 2^31 nodes");
   gbf_adj* a = new gbf_adj();
   a->d = d;
-  a->ncomp = N;
+  a->N = N;
   a->K = d.checkpoint_interval > 0 ? d.checkpoint_interval : (int)ceil(sqrt((double)d.iterations));
   if (a->K > d.iterations) a->K = d.iterations;
   a->nck = (d.iterations + a->K - 1) / a->K;
@@ -577,22 +571,6 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
     delete a;
     return GBF_ECUDA;
   }
-  int Tmax = 1;
-  for (int s = 0; s < 6; ++s) Tmax = d.pml_thickness[s] > Tmax ? d.pml_thickness[s] : Tmax;
-  int rc = GBF_OK;
-  auto A = [&](void** ptr, size_t bytes) { if (rc == GBF_OK) rc = adj_alloc(a, ptr, bytes); };
-  A((void**)&a->state, sizeof(float) * 18 * (size_t)N);
-  A((void**)&a->ckpt, sizeof(float) * 18 * (size_t)N * a->nck);
-  A((void**)&a->seg, sizeof(float) * 12 * (size_t)N * a->K);
-  A((void**)&a->adj, sizeof(float) * 36 * (size_t)N);
-  A((void**)&a->pml_rows, sizeof(float) * 6 * 8 * Tmax);
-  A((void**)&a->waves, sizeof(float) * (size_t)(d.nsrc + 1) * d.iterations);
-  A((void**)&a->rx, sizeof(int) * 2 * d.nrx);
-  if (rc != GBF_OK) {
-    g_adj_err = a->err;
-    gbf_adj_destroy(a);
-    return rc;
-  }
   AdjParams& p = a->p;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.sy = d.nz + 1;
@@ -601,20 +579,66 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
   p.rd = 1.0f / d.d;
   p.dbd = d.dbd;
   p.srcm = d.srcm;
-  for (int s = 0; s < 6; ++s) {
-    p.T[s] = d.pml_thickness[s];
-    p.R[s] = a->pml_rows + (size_t)s * 8 * Tmax;
-  }
-  set_state_ptrs(a);
-  p.nsrc = 0;
-  p.waves = a->waves;
   p.iterations = d.iterations;
-  p.nrx = 0;
-  p.rx = a->rx;
+  int Tmax = 1;
+  for (int s = 0; s < 6; ++s) {
+    const int t = d.pml_thickness[s];
+    Tmax = t > Tmax ? t : Tmax;
+    const int ax = s % 3;
+    const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
+    p.slab[s].T = t;
+    p.slab[s].ocount = t ? (int)(t * nu * nv) : 0;
+    a->off[s] = a->phi_len;
+    a->phi_len += 2 * (size_t)p.slab[s].ocount;
+  }
+  const size_t PL = a->phi_len, K = a->K;
+  const size_t ck = 6 * (size_t)N + 2 * PL;
+  int rc = GBF_OK;
+  auto A = [&](float** ptr, size_t floats) {
+    if (rc != GBF_OK) return;
+    cudaError_t r = cudaMalloc((void**)ptr, sizeof(float) * (floats ? floats : 1));
+    if (r != cudaSuccess) {
+      rc = afail(a, r == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA, "gbf_adj_create: allocation of %zu bytes failed: %s",
+                 sizeof(float) * floats, cudaGetErrorString(r));
+      return;
+    }
+    a->allocs.push_back(*ptr);
+    r = cudaMemsetAsync(*ptr, 0, sizeof(float) * (floats ? floats : 1), a->stream);
+    if (r != cudaSuccess) rc = afail(a, GBF_ECUDA, "gbf_adj_create: %s", cudaGetErrorString(r));
+  };
+  A(&a->pml_rows, 6 * 8 * (size_t)Tmax);
+  A(&a->waves, (size_t)(d.nsrc + 1) * d.iterations);
+  A(&a->E, 3 * (size_t)N);
+  A(&a->H, 3 * (size_t)N);
+  A(&a->phiE, PL);
+  A(&a->phiH, PL);
+  A(&a->ckpt, ck * a->nck);
+  A(&a->segE, 3 * (size_t)N * (K + 1));
+  A(&a->segPhiE, PL * (K + 1));
+  A(&a->segH, 3 * (size_t)N * K);
+  A(&a->recH, 3 * (size_t)N);
+  A(&a->recPhiH, PL);
+  A(&a->lE, 3 * (size_t)N);
+  A(&a->lH, 3 * (size_t)N);
+  A(&a->uE, 3 * (size_t)N);
+  A(&a->uH, 3 * (size_t)N);
+  A(&a->lphiE, PL);
+  A(&a->lphiH, PL);
+  A(&a->dFE, PL);
+  A(&a->dFH, PL);
+  A(&a->gCA, 3 * (size_t)N);
+  A(&a->gCB, 3 * (size_t)N);
+  if (rc != GBF_OK) {
+    g_adj_err = a->err;
+    gbf_adj_destroy(a);
+    return rc;
+  }
+  for (int s = 0; s < 6; ++s) p.slab[s].R = a->pml_rows + (size_t)s * 8 * Tmax;
+  p.waves = a->waves;
   int dev = 0, sms = 1, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, adj_e_nodes, kAdjThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, adj_e_step, kAdjThreads, 0);
   a->grid = sms * (per > 0 ? per : 1);
   *out = a;
   return GBF_OK;
@@ -640,8 +664,8 @@ int gbf_adj_upload_pml(gbf_adj* a, int32_t slab, const float* const rows[8]) {
   if (!T) return afail(a, GBF_EINVAL, "gbf_adj_upload_pml: slab %d has zero thickness", slab);
   for (int r = 0; r < 8; ++r) {
     if (!rows[r]) return afail(a, GBF_EINVAL, "gbf_adj_upload_pml: row %d missing", r);
-    AK(cudaMemcpyAsync(const_cast<float*>(a->p.R[slab]) + (size_t)r * T, rows[r], sizeof(float) * T,
-                       cudaMemcpyHostToDevice, a->stream));
+    AK(cudaMemcpyAsync(const_cast<float*>(a->p.slab[slab].R) + (size_t)r * T, rows[r],
+                       sizeof(float) * T, cudaMemcpyHostToDevice, a->stream));
   }
   AK(cudaStreamSynchronize(a->stream));
   return GBF_OK;
@@ -670,41 +694,40 @@ int gbf_adj_upload_sources(gbf_adj* a, const int32_t* info, const float* scale, 
 int gbf_adj_set_receivers(gbf_adj* a, const int32_t* info) {
   if (!a || !info) return GBF_EINVAL;
   const gbf_adj_desc& d = a->d;
-  std::vector<int> rx(2 * d.nrx);
   for (int r = 0; r < d.nrx; ++r) {
     const int C = info[4 * r], i = info[4 * r + 1], j = info[4 * r + 2], k = info[4 * r + 3];
     if (C < 0 || C > 2 || i < 0 || j < 0 || k < 0 || i > d.nx || j > d.ny || k > d.nz)
       return afail(a, GBF_EINVAL, "gbf_adj_set_receivers: receiver %d out of the grid", r);
-    rx[2 * r] = C;
-    rx[2 * r + 1] = i * a->p.sx + j * a->p.sy + k;
+    a->p.rx_comp[r] = C;
+    a->p.rx_idx[r] = i * a->p.sx + j * a->p.sy + k;
   }
-  AK(cudaMemcpyAsync(a->rx, rx.data(), sizeof(int) * rx.size(), cudaMemcpyHostToDevice, a->stream));
-  AK(cudaStreamSynchronize(a->stream));
   a->p.nrx = d.nrx;
   return GBF_OK;
 }
 
-}  // extern "C"
-
-static void fwd_step(gbf_adj* a, int it, float* traces) {
-  if (traces) adj_fwd_rx<<<1, 32, 0, a->stream>>>(a->p, traces, it);
-  adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p);
-  adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, it);
-}
-
-extern "C" {
-
 int gbf_adj_forward(gbf_adj* a, const float* CA, const float* CB, float* traces) {
   if (!a || !CA || !CB || !traces) return GBF_EINVAL;
-  const size_t N = a->ncomp;
+  if (!a->p.nrx) return afail(a, GBF_ESTATE, "gbf_adj_forward: receivers not set");
+  const size_t N = a->N, PL = a->phi_len, ck = 6 * N + 2 * PL;
   a->p.CA = CA;
   a->p.CB = CB;
-  AK(cudaMemsetAsync(a->state, 0, sizeof(float) * 18 * N, a->stream));
+  AK(cudaMemsetAsync(a->E, 0, sizeof(float) * 3 * N, a->stream));
+  AK(cudaMemsetAsync(a->H, 0, sizeof(float) * 3 * N, a->stream));
+  if (PL) AK(cudaMemsetAsync(a->phiE, 0, sizeof(float) * PL, a->stream));
+  if (PL) AK(cudaMemsetAsync(a->phiH, 0, sizeof(float) * PL, a->stream));
+  const PhiSet pE = phiset(a, a->phiE), pH = phiset(a, a->phiH);
   for (int it = 0; it < a->d.iterations; ++it) {
-    if (it % a->K == 0)
-      AK(cudaMemcpyAsync(a->ckpt + (size_t)(it / a->K) * 18 * N, a->state, sizeof(float) * 18 * N,
-                         cudaMemcpyDeviceToDevice, a->stream));
-    fwd_step(a, it, traces);
+    if (it % a->K == 0) {
+      float* c = a->ckpt + (size_t)(it / a->K) * ck;
+      int rc = copy_d2d(a, c, a->E, 3 * N);
+      if (!rc) rc = copy_d2d(a, c + 3 * N, a->H, 3 * N);
+      if (!rc) rc = copy_d2d(a, c + 6 * N, a->phiE, PL);
+      if (!rc) rc = copy_d2d(a, c + 6 * N + PL, a->phiH, PL);
+      if (rc) return rc;
+    }
+    adj_fwd_rx<<<1, 64, 0, a->stream>>>(a->p, a->E, traces, it);
+    adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, a->E, a->H, a->H, pH);
+    adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, a->E, a->E, a->H, pE, pE, it);
   }
   AK(cudaGetLastError());
   AK(cudaStreamSynchronize(a->stream));
@@ -716,36 +739,63 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
                      double* gCA, double* gCB) {
   if (!a || !CA || !CB || !gtraces || !gCA || !gCB) return GBF_EINVAL;
   if (!a->forward_done) return afail(a, GBF_ESTATE, "gbf_adj_backward: run gbf_adj_forward first");
-  const size_t N = a->ncomp;
+  const size_t N = a->N, PL = a->phi_len, ck = 6 * N + 2 * PL;
+  const int T = a->d.iterations;
   a->p.CA = CA;
   a->p.CB = CB;
-  AK(cudaMemsetAsync(a->adj, 0, sizeof(float) * 36 * N, a->stream));
+  for (float* z : {a->lE, a->lH, a->uE, a->uH})
+    AK(cudaMemsetAsync(z, 0, sizeof(float) * 3 * N, a->stream));
+  if (PL)
+    for (float* z : {a->lphiE, a->lphiH, a->dFE, a->dFH})
+      AK(cudaMemsetAsync(z, 0, sizeof(float) * PL, a->stream));
   AK(cudaMemsetAsync(gCA, 0, sizeof(double) * 3 * N, a->stream));
   AK(cudaMemsetAsync(gCB, 0, sizeof(double) * 3 * N, a->stream));
-  const int T = a->d.iterations;
+  AdjStep b;
+  b.lE = a->lE; b.lH = a->lH; b.uE = a->uE; b.uH = a->uH;
+  b.lphiE = phiset(a, a->lphiE);
+  b.lphiH = phiset(a, a->lphiH);
+  b.dFE = phiset(a, a->dFE);
+  b.dFH = phiset(a, a->dFH);
+  b.gCA = a->gCA;
+  b.gCB = a->gCB;
+  b.gtr = gtraces;
+  const PhiSet recPH = phiset(a, a->recPhiH);
+  const int fold_blocks = a->grid;
   for (int c = a->nck - 1; c >= 0; --c) {
     const int n0 = c * a->K;
     const int n1 = (n0 + a->K < T) ? n0 + a->K : T;
-    // recompute the segment from its checkpoint, keeping what the adjoint steps read
-    AK(cudaMemcpyAsync(a->state, a->ckpt + (size_t)c * 18 * N, sizeof(float) * 18 * N,
-                       cudaMemcpyDeviceToDevice, a->stream));
+    const float* src = a->ckpt + (size_t)c * ck;
+    int rc = copy_d2d(a, a->segE, src, 3 * N);
+    if (!rc) rc = copy_d2d(a, a->recH, src + 3 * N, 3 * N);
+    if (!rc) rc = copy_d2d(a, a->segPhiE, src + 6 * N, PL);
+    if (!rc) rc = copy_d2d(a, a->recPhiH, src + 6 * N + PL, PL);
+    if (rc) return rc;
+    // recompute the segment into its slots: E_m, PhiE_m (m = 0..K) and H^{m+1/2} (m = 0..K-1)
     for (int it = n0; it < n1; ++it) {
-      float* s = a->seg + (size_t)(it - n0) * 12 * N;
-      AK(cudaMemcpyAsync(s, a->p.E, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, a->stream));
-      AK(cudaMemcpyAsync(s + 6 * N, a->p.phiE, sizeof(float) * 6 * N, cudaMemcpyDeviceToDevice, a->stream));
-      adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p);
-      AK(cudaMemcpyAsync(s + 3 * N, a->p.H, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, a->stream));
-      adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, it);
+      const int m = it - n0;
+      float* Em = a->segE + (size_t)m * 3 * N;
+      float* Hm = a->segH + (size_t)m * 3 * N;
+      const float* Hprev = m == 0 ? a->recH : a->segH + (size_t)(m - 1) * 3 * N;
+      adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, Em, Hprev, Hm, recPH);
+      adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(
+          a->p, Em, a->segE + (size_t)(m + 1) * 3 * N, Hm, phiset(a, a->segPhiE + (size_t)m * PL),
+          phiset(a, a->segPhiE + (size_t)(m + 1) * PL), it);
     }
+    AK(cudaMemsetAsync(a->gCA, 0, sizeof(float) * 3 * N, a->stream));
+    AK(cudaMemsetAsync(a->gCB, 0, sizeof(float) * 3 * N, a->stream));
     // undo the segment's steps in reverse
     for (int it = n1 - 1; it >= n0; --it) {
-      const AdjBuffers b = buffers(a, it - n0, gCA, gCB);
-      adj_e_nodes<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b, it);
-      adj_e_to_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
-      adj_h_nodes<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
-      adj_h_to_e<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
-      adj_receivers<<<1, 32, 0, a->stream>>>(a->p, b, gtraces, it);
+      const int m = it - n0;
+      b.En = a->segE + (size_t)m * 3 * N;
+      b.Hh = a->segH + (size_t)m * 3 * N;
+      b.PEn = phiset(a, a->segPhiE + (size_t)m * PL);
+      b.it = it;
+      b.finish = it + 1 < T ? 1 : 0;
+      adj_e_step<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
+      adj_h_step<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
     }
+    adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCA, gCA, 3 * (long long)N);
+    adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCB, gCB, 3 * (long long)N);
     AK(cudaGetLastError());
   }
   AK(cudaStreamSynchronize(a->stream));

@@ -148,3 +148,45 @@ def bscan_models(nmodels=128, shapes=((200, 200, 100), (300, 300, 150)), seed=11
         pos = m if m < half else m - half
         grids.append(build_grid(bscan_input(shape, seed + m, pos), messages=messages))
     return grids
+
+
+def gaussian_random_field(shape, corr_cells, seed, lo=1.0, hi=20.0, mean=8.0, std=4.0):
+    """Seeded smooth Gaussian random field: white noise filtered in Fourier space by a Gaussian
+    of correlation length ``corr_cells``, scaled to ``mean`` +/- ``std`` and clipped to
+    [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    noise = rng.standard_normal(shape)
+    k = [np.fft.fftfreq(n) for n in shape]
+    kk = sum(np.meshgrid(*[(2 * np.pi * x) ** 2 for x in k], indexing='ij'))
+    field = np.real(np.fft.ifftn(np.fft.fftn(noise) * np.exp(-0.5 * kk * corr_cells ** 2)))
+    field = (field - field.mean()) / (field.std() + 1e-30)
+    return np.clip(mean + std * field, lo, hi)
+
+
+def adjoint_problem(shape=(200, 200, 100), dx=0.002, timewindow='8e-9', seed=21, pml=10):
+    """The gradient workload: per-cell eps_r from a seeded Gaussian random field (correlation
+    20 mm, clipped to [1, 20]), sigma ~ U[0, 0.01] S/m, four z-directed dipoles and eight
+    receivers on a plane 5 cells below the top PML, Ricker 1 GHz. Returns the input lines,
+    eps_r and sigma [nx][ny][nz], and the 'true' eps_r of the observed data (eps_r with a
+    buried 40 mm box raised by 5 %)."""
+    nx, ny, nz = shape
+    rng = np.random.default_rng(seed)
+    eps = gaussian_random_field(shape, 0.020 / dx, seed)
+    sig = rng.uniform(0, 0.01, shape)
+    top = (nz - pml - 5) * dx
+    lines = ['#domain: {:g} {:g} {:g}'.format(nx * dx, ny * dx, nz * dx),
+             '#dx_dy_dz: {0:g} {0:g} {0:g}'.format(dx), '#time_window: {}'.format(timewindow),
+             '#pml_cells: {}'.format(pml), '#waveform: ricker 1 1e9 w']
+    for s in range(4):
+        x = (0.3 + 0.4 * (s % 2)) * nx * dx
+        y = (0.3 + 0.4 * (s // 2)) * ny * dx
+        lines.append('#hertzian_dipole: z {:g} {:g} {:g} w'.format(x, y, top))
+    for r in range(8):
+        x = (0.2 + 0.6 * (r % 4) / 3) * nx * dx
+        y = (0.35 + 0.3 * (r // 4)) * ny * dx
+        lines.append('#rx: {:g} {:g} {:g}'.format(x, y, top))
+    true = eps.copy()
+    b = int(round(0.040 / dx))
+    c = (nx // 2, ny // 2, nz // 2 - b)
+    true[c[0] - b // 2:c[0] + b // 2, c[1] - b // 2:c[1] + b // 2, c[2] - b // 2:c[2] + b // 2] *= 1.05
+    return [line + '\n' for line in lines], eps, sig, true

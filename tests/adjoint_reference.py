@@ -44,25 +44,26 @@ def forward(model, CA, CB, dtype=torch.float64):
     n3 = (nx, ny, nz)
     d = model.d
     shape = (nx + 1, ny + 1, nz + 1)
+    dev = CA.device
     CA = CA.to(dtype)
     CB = CB.to(dtype)
     CBd = CB / d
     dbd = model.dbd
     srcm = model.srcm
-    F = [torch.zeros(shape, dtype=dtype) for _ in range(6)]   # Ex Ey Ez Hx Hy Hz
+    F = [torch.zeros(shape, dtype=dtype, device=dev) for _ in range(6)]   # Ex Ey Ez Hx Hy Hz
     slabs = []
     for s in range(6):
         T = model.thickness[s]
         if not T:
             continue
-        rows = [torch.tensor(r, dtype=dtype) for r in model.pml_rows[s]]
+        rows = [torch.tensor(r, dtype=dtype, device=dev) for r in model.pml_rows[s]]
         axis, minus = s % 3, s < 3
         eb, ep = _box(axis, minus, T, n3, True)
         hb, hp = _box(axis, minus, T, n3, False)
         box_shape = lambda b: tuple(x.stop - x.start for x in b)
         slabs.append({'axis': axis, 'rows': rows, 'eb': eb, 'ep': ep, 'hb': hb, 'hp': hp,
-                      'phiE': [torch.zeros(box_shape(eb), dtype=dtype) for _ in range(2)],
-                      'phiH': [torch.zeros(box_shape(hb), dtype=dtype) for _ in range(2)]})
+                      'phiE': [torch.zeros(box_shape(eb), dtype=dtype, device=dev) for _ in range(2)],
+                      'phiH': [torch.zeros(box_shape(hb), dtype=dtype, device=dev) for _ in range(2)]})
     traces = [[] for _ in model.receivers]
     for n in range(model.iterations):
         for r, (c, i, j, k) in enumerate(model.receivers):
@@ -81,7 +82,7 @@ def forward(model, CA, CB, dtype=torch.float64):
         Hn = [nHx, nHy, nHz]
         for sd in slabs:
             axis, rows = sd['axis'], sd['rows']
-            RA, RB, RE, RF = (_bcast(rows[4 + q][sd['hp']], axis) for q in range(4))
+            RA, RB, RE, RF = (_bcast(rows[4 + q][sd['hp'].to(dev)], axis) for q in range(4))
             for which, (comp, dcomp, sign) in enumerate(H_SLAB[axis]):
                 b = tuple(sd['hb'])
                 dF = (F[dcomp][_shift(b, axis, 1)] - F[dcomp][b]) / d
@@ -107,7 +108,7 @@ def forward(model, CA, CB, dtype=torch.float64):
         Hall = [None, None, None, Hx, Hy, Hz]
         for sd in slabs:
             axis, rows = sd['axis'], sd['rows']
-            RA, RB, RE, RF = (_bcast(rows[q][sd['ep']], axis) for q in range(4))
+            RA, RB, RE, RF = (_bcast(rows[q][sd['ep'].to(dev)], axis) for q in range(4))
             for which, (comp, dcomp, sign) in enumerate(E_SLAB[axis]):
                 b = tuple(sd['eb'])
                 dF = (Hall[3 + dcomp][b] - Hall[3 + dcomp][_shift(b, axis, -1)]) / d

@@ -1,7 +1,7 @@
 """GPU: the differentiable time loop (gbf_adj_*) against the pure-torch restatement of the same
 model (tests/adjoint_reference.py, fp64 on the CPU): forward traces, and the checkpointed
 discrete-adjoint gradient with respect to per-cell eps_r and sigma against torch's autograd
-gradient; the gradient must not depend on the checkpoint interval."""
+gradient; the gradient must not depend on the checkpoint interval beyond the rounding of its sums."""
 import numpy as np
 import pytest
 
@@ -49,7 +49,7 @@ def test_adjoint_gradient_matches_torch_autograd(native):
     loss.backward()
     gl, ge, gs = _gpu_gradient(m, solver, eps, sig, obs)
     solver.close()
-    assert abs(gl - float(loss)) <= 1e-4 * float(loss)
+    assert abs(gl - float(loss.detach())) <= 1e-4 * float(loss.detach())
     for got, want in ((ge, e.grad), (gs, s.grad)):
         err = float((got - want).norm() / want.norm())
         assert err <= 1e-3, err
@@ -64,6 +64,62 @@ def test_gradient_independent_of_checkpoint_interval(native):
         obs = torch.zeros((len(m.receivers), m.iterations), dtype=torch.float64)
         grads.append(_gpu_gradient(m, solver, eps, sig, obs))
         solver.close()
+    # the forward is the same; the gradient partials are summed in fp32 within a segment and in
+    # fp64 across segments, so the interval changes only the rounding of the sums
     for g in grads[1:]:
         assert g[0] == grads[0][0]
-        assert torch.equal(g[1], grads[0][1]) and torch.equal(g[2], grads[0][2])
+        for a, b in ((g[1], grads[0][1]), (g[2], grads[0][2])):
+            assert float((a - b).abs().max()) <= 1e-5 * float(b.abs().max())
+
+
+CROP = """#domain: 0.064 0.064 0.064
+#dx_dy_dz: 0.002 0.002 0.002
+#time_window: 240
+#pml_cells: 6
+#waveform: ricker 1 3e9 w
+#hertzian_dipole: z 0.032 0.032 0.044 w
+#rx: 0.020 0.032 0.044
+#rx: 0.044 0.032 0.044
+"""
+
+
+def test_adjoint_on_a_crop_of_the_gradient_workload(native):
+    """A 32^3 crop of the 200x200x100 Gaussian-random-field model. The misfit's residual r
+    (GPU traces minus data from the crop of the 'true' model) is small here, so fp32 rounding
+    in the forward moves it; the adjoint is therefore checked on the residual it was given:
+    the GPU gradient J^T r against torch's fp64 autograd of sum(traces * r) of the pure-torch
+    model, and against fp64 central finite differences of that sum on 20 seeded cells."""
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.adjoint import AdjointModel, AdjointSolver
+    _, eps, sig, true = workloads.adjoint_problem()
+    crop = (slice(84, 116), slice(84, 116), slice(34, 66))
+    dev = torch.device('cuda')
+    e0 = torch.tensor(eps[crop], dtype=torch.float64, device=dev)
+    s0 = torch.tensor(sig[crop], dtype=torch.float64, device=dev)
+    et = torch.tensor(true[crop], dtype=torch.float64, device=dev)
+    m = AdjointModel(CROP.splitlines(True))
+    solver = AdjointSolver(m)
+    obs = ar.forward(m, *m.edge_coefficients(et, s0)).detach()
+    _, ge, _ = _gpu_gradient(m, solver, e0.cpu(), s0.cpu(), obs.cpu())
+    CA, CB = m.edge_coefficients(e0, s0)
+    r = (solver.forward(CA.float().contiguous(), CB.float().contiguous()).double() - obs).detach()
+    solver.close()
+    e = e0.clone().requires_grad_(True)
+    (ar.forward(m, *m.edge_coefficients(e, s0)) * r).sum().backward()
+    want = e.grad.cpu()
+    assert float((ge - want).norm() / want.norm()) <= 1e-3
+
+    def L(ee):
+        return float((ar.forward(m, *m.edge_coefficients(ee, s0)) * r).sum())
+    flat = want.abs().flatten()
+    top = torch.topk(flat, flat.numel() // 10).indices.numpy()
+    cells = np.random.default_rng(9).choice(top, 20, replace=False)
+    for c in cells:
+        idx = np.unravel_index(int(c), want.shape)
+        h = 1e-4 * float(e0[idx])
+        p = e0.clone()
+        p[idx] += h
+        up = L(p)
+        p[idx] -= 2 * h
+        fd = (up - L(p)) / (2 * h)
+        assert abs(float(ge[idx]) - fd) <= 1e-3 * abs(fd), (idx, float(ge[idx]), fd)
