@@ -479,6 +479,58 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sweep(args):
+    """Throughput sweep: cubic grids N^3 at 1 mm with a seeded dielectric block in the central
+    half and a 10-cell PML, N in {100, ..., 600}. Per N: device-timed Mcells/s of the fused
+    kernels, achieved GB/s of the half-steps (algorithmic bytes over the profiled kernel
+    times), and the reference's own compiled CPU kernels on all host cores over a bounded
+    number of steps."""
+    import ref_cpu
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.solver import DeviceModel
+    K, W = args.steps, args.warmup
+    rows = []
+    peak, peak_kind = load_peaks()
+    for n in args.sizes:
+        G = workloads.throughput_cube(n)
+        cells = G.nx * G.ny * G.nz
+        dm = DeviceModel(G)
+        dm.run(W)
+        dm.synchronize()
+        ms = dm.run_timed(K)
+        ms_h, ms_e, _ = dm.profile(5)
+        dm.close()
+        bh, be = algorithmic_bytes(G)
+        gbs = (bh + be) / ((ms_h + ms_e) / 5 / 1e3) / 1e9
+        row = {'N': n, 'Mcells_per_s': round(cells * K / (ms / 1e3) / 1e6, 1),
+               'ms_per_step': ms / K, 'GBps_half_steps': round(gbs, 1),
+               'frac_of_peak': round(gbs / peak, 4)}
+        if args.cpu_baseline:
+            solver, kind = ref_cpu.make_solver(G, os.cpu_count() or 1)
+            solver.step()
+            t0 = time.perf_counter()
+            steps = 0
+            while (time.perf_counter() - t0 < args.cpu_budget / len(args.sizes) or steps < 2) \
+                    and steps < G.iterations - 2:
+                solver.step()
+                steps += 1
+            t = time.perf_counter() - t0
+            row['cpu'] = {'Mcells_per_s': round(cells * steps / t / 1e6, 1), 'steps': steps,
+                          'kind': kind, 'cores': os.cpu_count() or 1}
+            row['speedup_vs_cpu'] = round(row['Mcells_per_s'] / row['cpu']['Mcells_per_s'], 1)
+            del solver
+        rows.append(row)
+        del G
+    out = {'metric': 'Mcells/s', 'value': rows[-1]['Mcells_per_s'], 'unit': 'Mcells/s',
+           'n_gpus': 1, 'steps': K, 'warmup': W, 'ms_per_step': rows[-1]['ms_per_step'],
+           'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+           'data': 'synthetic (seeded dielectric block)',
+           'config': {'workload': 'throughput_sweep_cubes_1mm_pml10', 'sizes': args.sizes,
+                      'peak_GBps': peak, 'peak_source': peak_kind},
+           'sweep': rows}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -493,11 +545,14 @@ def main():
                     help='smaller soil grid (profiling runs); default 400 400 200')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
-    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint'], default='soil',
+    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint', 'sweep'], default='soil',
                     help='soil: the 400x400x200 Debye soil (default); bscan: the batched uneven '
                          'B-scan against sequential plain runs; adjoint: gradient cost and '
-                         'finite-difference check of the differentiable time loop')
+                         'finite-difference check of the differentiable time loop; sweep: '
+                         'cubes of 100^3 to 600^3 cells')
     ap.add_argument('--models', type=int, default=128, help='bscan: number of models')
+    ap.add_argument('--sizes', type=int, nargs='+', default=[100, 200, 300, 400, 500, 600],
+                    help='sweep: cube edge lengths in cells')
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -505,6 +560,8 @@ def main():
         run_bscan(args)
     elif args.workload == 'adjoint':
         run_adjoint(args)
+    elif args.workload == 'sweep':
+        run_sweep(args)
     elif args.impl == 'reference':
         run_reference(args)
     else:

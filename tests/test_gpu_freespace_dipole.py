@@ -1,0 +1,80 @@
+"""GPU: the 100^3 free-space Hertzian dipole (1 mm cells, 10-cell CFS PML, Ricker 1.5 GHz,
+3 ns = 1559 iterations, Ez/Hx/Hy receiver 10 mm from the dipole).
+
+* bit-exact against the oracle (the reference's time loop restated in C);
+* the error of the fp32 fields against an fp64 run of the same grid (the pure-torch
+  restatement of the update, tests/adjoint_reference.py, in fp64 on the GPU);
+* against the analytical dipole field (tests/analytical_dipole.py), to the level the FDTD
+  discretisation allows.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MODEL = """#domain: 0.1 0.1 0.1
+#dx_dy_dz: 1e-3 1e-3 1e-3
+#time_window: 3e-9
+#pml_cells: 10
+#waveform: ricker 1 1.5e9 w
+#hertzian_dipole: z 0.050 0.050 0.050 w
+#rx: 0.060 0.050 0.050 rx1 Ez Hx Hy
+"""
+
+
+@pytest.fixture(scope='module')
+def gpu_run():
+    from gprmax_gb300.model import build_grid
+    from gprmax_gb300.solver import DeviceModel
+    G = build_grid(MODEL.splitlines(True), messages=False)
+    dm = DeviceModel(G)
+    dm.run()
+    rx = dm.receivers()
+    dm.close()
+    return G, rx
+
+
+def test_matches_oracle_bit_for_bit(native, gpu_run):
+    import oracle
+    G, rx = gpu_run
+    ref = oracle.OracleSolver(G).run().receivers()
+    np.testing.assert_array_equal(rx, ref)
+
+
+def test_error_against_fp64_run(native, gpu_run):
+    torch = pytest.importorskip('torch')
+    import adjoint_reference as ar
+    from gprmax_gb300.adjoint import AdjointModel
+    G, rx = gpu_run
+    m = AdjointModel(MODEL.splitlines(True))
+    eps = torch.ones((m.nx, m.ny, m.nz), dtype=torch.float64, device='cuda')
+    with torch.no_grad():
+        tr = ar.forward(m, *m.edge_coefficients(eps, torch.zeros_like(eps))).cpu().numpy()
+    ez = rx[2, :, 0].astype(np.float64)
+    err = np.abs(ez - tr[0]).max() / np.abs(tr[0]).max()
+    print('\nfp32 GPU against fp64 run: max |Ez error| / peak = {:.3e}'.format(err))
+    assert err <= 1e-4
+
+
+def test_against_analytical_dipole(native, gpu_run):
+    from analytical_dipole import dipole_ez
+    G, rx = gpu_run
+    w = G.waveforms[0]
+    src = G.hertziandipoles[0]
+    dt = G.dt
+    t = dt * np.arange(G.iterations)
+
+    def current(tt):
+        # the update at step n uses w(n dt) for the current of the half step (n + 1/2) dt
+        out = np.zeros_like(tt)
+        on = tt - dt / 2 >= 0
+        out[on] = w.values(tt[on] - dt / 2, dt)
+        return out
+    x = (G.rxs[0].xcoord - src.xcoord) * G.dx
+    y = (G.rxs[0].ycoord - src.ycoord) * G.dy
+    z = (G.rxs[0].zcoord - src.zcoord) * G.dz
+    ana = dipole_ez(current, t, src.dl, x, y, z)
+    ez = rx[2, :, 0].astype(np.float64)
+    err = np.abs(ez - ana).max() / np.abs(ana).max()
+    print('\nGPU against analytical dipole: max |Ez error| / peak = {:.3e}'.format(err))
+    assert err <= 0.05
