@@ -18,10 +18,10 @@
 // compiled the same way.
 //
 // Thread mapping: a persistent grid sweeps the nodes box by box (consecutive threads on
-// consecutive nodes), one node per thread per pass: first the core box, where no PML slab and no
-// domain face is near and the update has no branches, then the five shell boxes that hold the
-// PML slabs and the faces, so their warps run the PML code densely. The coefficient tables are staged in shared memory when they fit (the reference
-// keeps them in __constant__ memory, model_build_run.py:512-519).
+// consecutive nodes), one node per thread per pass: first the core box (whole rows away from the
+// x and y slabs and faces, where only the z-slab test remains), then the x and y slab planes and
+// rows, whose warps run the PML code densely. The coefficient tables are staged in shared memory
+// when they fit (the reference keeps them in __constant__ memory, model_build_run.py:512-519).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -96,6 +96,7 @@ struct StepParams {
   const uint32_t* PH;     // packed H IDs per node: x | y << 10 | z << 20
   int ncomp;              // nodes per component (< 2^31)
   int nx, ny, nz;
+  int two_d;              // 1: a dimension of one cell (TMx, TMy, TMz): 2D magnetic ranges
   int sy, sx;             // strides: j -> nz+1, i -> (ny+1)(nz+1)
   const float4* cE4;      // [nmat] CA, CBx, CBy, CBz
   const float* cEs;       // [nmat] srce
@@ -364,6 +365,11 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const bool iin = CORE || i < nx, jin = CORE || j < ny, kin = k < nz;
   const bool ipos = CORE || i >= 1, jpos = CORE || j >= 1;
+  // 2D grids (update_magnetic's 2D branch, fields_updates_ext.pyx:377-400): Hx only when ny or
+  // nz is one cell and only below i = nx; Hy, Hz likewise along j and k
+  const bool hx2 = !p.two_d || ((ny == 1 || nz == 1) && iin);
+  const bool hy2 = !p.two_d || ((nx == 1 || nz == 1) && jin);
+  const bool hz2 = !p.two_d || ((nx == 1 || ny == 1) && kin);
   float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
   if (PK != PML_NONE) {
     if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0]);
@@ -372,7 +378,7 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   }
   // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
-    const bool mainu = ipos && jin && kin;
+    const bool mainu = ipos && jin && kin && hx2;
     const bool pml = PK != PML_NONE && (where[1] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
     const float4 c = C4[mx];
@@ -385,7 +391,7 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   }
   // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
   {
-    const bool mainu = iin && jpos && kin;
+    const bool mainu = iin && jpos && kin && hy2;
     const bool pml = PK != PML_NONE && (where[0] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
     const float4 c = C4[my];
@@ -398,7 +404,7 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
   }
   // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs along x and y
   {
-    const bool mainu = iin && jin && (k >= 1);
+    const bool mainu = iin && jin && (k >= 1) && hz2;
     const bool pml = PK != PML_NONE && (where[0] || where[1]);
     // the main update is formed on every node and kept where it applies (no branch)
     const float4 c = C4[mz];

@@ -222,8 +222,11 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   if (!desc || !out) return fail(nullptr, GBF_EINVAL, "gbf_create: NULL argument");
   *out = nullptr;
   const gbf_grid_desc& d = *desc;
-  if (d.nx < 2 || d.ny < 2 || d.nz < 2)
-    return fail(nullptr, GBF_EINVAL, "gbf_create: 2D grids (a dimension of one cell) are not supported yet (nx=%d ny=%d nz=%d)", d.nx, d.ny, d.nz);
+  // 3D, or 2D with exactly one dimension of one cell (TMx, TMy, TMz)
+  const int ones = (d.nx == 1) + (d.ny == 1) + (d.nz == 1);
+  if (d.nx < 1 || d.ny < 1 || d.nz < 1 || ones > 1 ||
+      (d.nx < 2 && d.nx != 1) || (d.ny < 2 && d.ny != 1) || (d.nz < 2 && d.nz != 1))
+    return fail(nullptr, GBF_EINVAL, "gbf_create: grid must be 3D or 2D with one dimension of one cell (nx=%d ny=%d nz=%d)", d.nx, d.ny, d.nz);
   if (d.iterations < 1 || d.nmat < 1 || d.maxpoles < 0 || d.maxpoles > kMaxPoles)
     return fail(nullptr, GBF_EINVAL, "gbf_create: bad iterations/nmat/maxpoles (%d/%d/%d; poles <= %d)", d.iterations, d.nmat, d.maxpoles, kMaxPoles);
   if (d.pml_order < 1 || d.pml_order > 2 || (d.pml_formulation != 0 && d.pml_formulation != 1))
@@ -305,6 +308,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   for (int q = 0; q < kSrcInline; ++q) p.srcqE[q] = p.srcqH[q] = -1;
   p.ncomp = (int)npts;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
+  p.two_d = (d.nx == 1 || d.ny == 1 || d.nz == 1) ? 1 : 0;
   p.sy = d.nz + 1;
   p.sx = (d.ny + 1) * (d.nz + 1);
   p.cE4 = ctx->cE4; p.cEs = ctx->cEs; p.cH4 = ctx->cH4; p.cHs = ctx->cHs;

@@ -37,7 +37,8 @@ sys.path.insert(0, os.path.join(ROOT, 'tests'))
 sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 
 REFERENCE_MODELS = ['hertzian_dipole_fs', 'hertzian_dipole_dispersive', 'hertzian_dipole_hs',
-                    'magnetic_dipole_fs']
+                    'magnetic_dipole_fs', '2D_ExHyHz', '2D_EyHxHz', '2D_EzHxHy',
+                    'cylinder_Ascan_2D']
 HDF5_FIXTURE = 'hertzian_dipole_dispersive_ref.out'
 
 CHILD = r'''

@@ -85,6 +85,35 @@ MODELS = {
 #box: 0.026 0.024 0.020 0.034 0.030 0.028 ax ay az
 #snapshot: 0.004 0.004 0.004 0.036 0.032 0.028 0.002 0.002 0.002 60 snap1
 """,
+    # 2D TMz (one cell in z): Debye block, z dipole, PML in x and y
+    'tmz': BASE.format(dom='0.060 0.050 0.001', steps=160) + """#pml_cells: 8 8 0 8 8 0
+#material: 5 0.002 1 0 soil
+#add_dispersion_debye: 1 6 1e-9 soil
+#box: 0 0 0 0.060 0.020 0.001 soil
+#cylinder: 0.030 0.012 0 0.030 0.012 0.001 0.004 pec
+#waveform: ricker 1 3e9 w
+#hertzian_dipole: z 0.030 0.030 0 w
+#rx: 0.036 0.030 0
+#rx: 0.012 0.040 0 r2 Ez Hx Hy Ix Iy Iz
+""",
+    # 2D TMx (one cell in x): x dipole, unequal PML, a magnetic dipole
+    'tmx': BASE.format(dom='0.001 0.044 0.052', steps=150) + """#pml_cells: 0 6 7 0 5 8
+#material: 4 0.01 1 0 half
+#box: 0 0 0 0.001 0.044 0.018 half
+#waveform: gaussiandot 1 4e9 w
+#hertzian_dipole: x 0 0.022 0.030 w
+#rx: 0 0.030 0.030
+#rx: 0 0.015 0.040 r2 Ex Hy Hz
+""",
+    # 2D TMy (one cell in y): y dipole, MRIPML order 2
+    'tmy': BASE.format(dom='0.048 0.001 0.046', steps=150) + """#pml_cells: 6 0 5 7 0 6
+#pml_formulation: MRIPML
+#pml_cfs: constant forward 0 0 constant forward 1 1 sextic forward 0 0.5836
+#pml_cfs: constant forward 0.05 0.05 cubic forward 1 8 quadratic forward 0 5.8357
+#waveform: ricker 1 3e9 w
+#hertzian_dipole: y 0.024 0 0.023 w
+#rx: 0.030 0 0.023
+""",
     # sources on the upper domain faces and a receiver on a face (boundary index paths)
     'faces': BASE.format(dom='0.020 0.018 0.016', steps=90) + """#pml_cells: 0
 #waveform: gaussiandot 1 2e9 w
