@@ -62,3 +62,34 @@ def merge_files(paths, outputfile):
         for comp in traces[0][rx]:
             f['/rxs/{}/{}'.format(rx, comp)] = np.stack([t[rx][comp] for t in traces], axis=1)
     f.close()
+
+
+def write_merged_outputfile(outputfile, grids):
+    """One merged ``.out`` file straight from the grids of a B-scan whose receiver outputs are
+    filled (for example by ``solver.solve_gb300_batch``): root attributes of the first model,
+    and per receiver and output one fp32 [iterations][nmodels] dataset, the layout that merging
+    the per-model files gives (``merge_files``, the reference's ``tools/outputfiles_merge.py``).
+    Every model must have the same iterations, receivers and outputs."""
+    G0 = grids[0]
+    for G in grids[1:]:
+        if G.iterations != G0.iterations or len(G.rxs) != len(G0.rxs) or any(
+                list(a.outputs) != list(b.outputs) for a, b in zip(G.rxs, G0.rxs)):
+            raise ValueError('B-scan models differ in iterations, receivers or outputs')
+    f = hdf5.File(outputfile, 'w')
+    f.attrs['gprMax'] = VERSION
+    f.attrs['Title'] = G0.title
+    f.attrs['Iterations'] = np.int64(G0.iterations)
+    f.attrs['nx_ny_nz'] = np.array((G0.nx, G0.ny, G0.nz), dtype=np.int64)
+    f.attrs['dx_dy_dz'] = np.array((G0.dx, G0.dy, G0.dz), dtype=np.float64)
+    f.attrs['dt'] = np.float64(G0.dt)
+    nsrc = len(G0.voltagesources + G0.hertziandipoles + G0.magneticdipoles + G0.transmissionlines)
+    f.attrs['nsrc'] = np.int64(nsrc)
+    f.attrs['nrx'] = np.int64(len(G0.rxs))
+    f.attrs['srcsteps'] = np.array(G0.srcsteps, dtype=np.int64)
+    f.attrs['rxsteps'] = np.array(G0.rxsteps, dtype=np.int64)
+    for n, rx in enumerate(G0.rxs):
+        for output in rx.outputs:
+            f['/rxs/rx{}/{}'.format(n + 1, output)] = np.stack(
+                [np.asarray(G.rxs[n].outputs[output], dtype=np.float32) for G in grids], axis=1)
+    f.close()
+

@@ -308,9 +308,11 @@ class BatchModel:
             pass
 
 
-def solve_gb300_batch(grids, fields=False):
+def solve_gb300_batch(grids, fields=False, outputfile=None):
     """Run every grid of a B-scan or parameter sweep to its end in one batch; returns the solve
-    seconds. Each grid's receiver outputs are stored as ``solve_gb300`` stores them."""
+    seconds. Each grid's receiver outputs are stored as ``solve_gb300`` stores them; with
+    ``outputfile`` the traces are also written as one merged ``.out`` file
+    ([iterations][nmodels] per receiver output)."""
     bm = BatchModel(grids)
     try:
         t0 = time.perf_counter()
@@ -320,6 +322,9 @@ def solve_gb300_batch(grids, fields=False):
         bm.store_results(fields=fields)
     finally:
         bm.close()
+    if outputfile:
+        from .outputs import write_merged_outputfile
+        write_merged_outputfile(outputfile, grids)
     return tsolve
 
 
