@@ -89,7 +89,8 @@ class GridDesc(ctypes.Structure):
                 ('pml_order', ctypes.c_int32), ('pml_thickness', ctypes.c_int32 * 6),
                 ('dx', ctypes.c_float), ('dy', ctypes.c_float), ('dz', ctypes.c_float),
                 ('nsrc', ctypes.c_int32), ('nrx', ctypes.c_int32), ('nsnap', ctypes.c_int32),
-                ('options', ctypes.c_int32), ('reserved', ctypes.c_int32 * 3)]
+                ('options', ctypes.c_int32), ('ntl', ctypes.c_int32),
+                ('reserved', ctypes.c_int32 * 2)]
 
 
 GBF_RUN_GRAPH = 1
@@ -120,6 +121,8 @@ _SIGS = {
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
+    'gbf_upload_tls': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    'gbf_download_tls': (ctypes.c_int, [_P, _P]),
     'gbf_adj_create': (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     'gbf_adj_destroy': (None, [_P]),
     'gbf_adj_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),

@@ -3,7 +3,7 @@
 Single-use commands follow ``gprMax/input_cmds_singleuse.py:41-336``, multi-use commands
 ``input_cmds_multiuse.py:45-851`` and geometry commands ``input_cmds_geometry.py:51-1527`` for
 the commands this solver core supports. Parameter checks raise :class:`CmdInputError` with the
-reference's messages. Transmission lines and the fractal/surface/grass commands are rejected
+reference's messages. The fractal/surface/grass commands are rejected
 with an explicit error.
 """
 import decimal as d
@@ -13,13 +13,13 @@ import os
 import numpy as np
 from scipy import interpolate
 
-from .constants import c, floattype
+from .constants import c, floattype, z0
 from .exceptions import CmdInputError
 from .materials import Material
 from .pml import CFS, CFSParameter, PML
 from .receivers import Rx, allocate_outputs
 from .snapshots import Snapshot
-from .sources import HertzianDipole, MagneticDipole, VoltageSource
+from .sources import HertzianDipole, MagneticDipole, TransmissionLine, VoltageSource
 from .utilities import round_value
 from .waveforms import Waveform
 from . import geometry as geo
@@ -333,8 +333,22 @@ def process_multicmds(multicmds, G):
         m.calculate_waveform_values(G)
         G.magneticdipoles.append(m)
 
-    if multicmds['#transmission_line']:
-        raise CmdInputError('#transmission_line is not supported by the GB300 solver core')
+    cmdname = '#transmission_line'
+    for cmdinstance in multicmds[cmdname]:
+        tmp, t = _simple_source(G, cmdname, cmdinstance, TransmissionLine, 6)
+        resistance = float(tmp[4])
+        if resistance <= 0 or resistance >= z0:
+            raise _err(cmdname, tmp, ' requires a resistance greater than zero and less than the '
+                                     'impedance of free space, i.e. 376.73 Ohms')
+        if not any(x.ID == tmp[5] for x in G.waveforms):
+            raise _err(cmdname, tmp, ' there is no waveform with the identifier {}'.format(tmp[5]))
+        t.bind(G)
+        t.resistance = resistance
+        t.waveformID = tmp[5]
+        _start_stop(G, cmdname, tmp, t, 6)
+        t.calculate_waveform_values(G)
+        t.calculate_incident_V_I(G)
+        G.transmissionlines.append(t)
 
     cmdname = '#rx'
     for cmdinstance in multicmds[cmdname]:

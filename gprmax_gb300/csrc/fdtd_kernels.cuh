@@ -560,14 +560,19 @@ h_half_step_batch(const __grid_constant__ BatchParams bp) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Electric sources at one node/component, in list order (voltage sources, then Hertzian
-// dipoles): sources.py:81-120 and :163-193 with numpy-2 fp32 operation order.
+// Electric sources at one node/component, in list order (voltage sources, transmission lines,
+// Hertzian dipoles; model_build_run.py:459-461): sources.py:81-120, :396-424 and :163-193 with
+// numpy-2 fp32 operation order.
 __device__ __forceinline__ float apply_e_sources(float F, int comp, int i, int j, int k, int it,
                                                  float c4, const StepParams& p) {
   for (int s = 0; s < p.nsrcE; ++s) {
     const Src& q = p.srcE[s];
     if (q.comp != comp || q.i != i || q.j != j || q.k != k) continue;
     if (it < q.first || it > q.last) continue;
+    if (q.kind == 4) {        // transmission line: -V/d from the line (tl_step), w -> that value
+      F = *q.w;
+      continue;
+    }
     const float w = __ldg(q.w + it);
     if (q.kind == 0) {        // Hertzian dipole
       F = __fsub_rn(F, __fmul_rn(__fmul_rn(__fmul_rn(c4, w), q.s0), q.s1));
@@ -814,6 +819,25 @@ e_half_step_batch(const __grid_constant__ BatchParams bp) {
 // End of an iteration: electric sources on nodes outside the E kernel's domain, then the
 // receiver samples that the next iteration starts from (fields_outputs.py:40-67, grid.py:
 // 413-461), then the iteration counter advances.
+// A transmission line attached to one E edge (sources.py:286-451). The connected line has
+// antpos + 1 cells; its updates are the reference's numpy expressions, which evaluate in float64
+// (the step ratios are float64 scalars) and round to float32 on assignment.
+constexpr int kTLCells = 16;
+struct TLine {
+  int comp, i, j, k, first, last, nl, srcpos, antpos;
+  float d;            // cell size along the edge (fp32)
+  double s_iv;        // (1/R) c dt / dl
+  double s_vi;        // R c dt / dl
+  double r;           // c dt / dl
+  double h;           // absorbing end: (c dt - dl) / (c dt + dl)
+  float v[kTLCells];  // line voltage
+  float c[kTLCells];  // line current
+  float abcv0, abcv1;
+  float eset;         // -V(antpos)/d for this iteration's E half-step
+  const float* whole; // waveform at whole and half steps [iterations]
+  const float* half;
+};
+
 struct RxParams {
   const int* coords;   // [nrx][3]
   float* out;          // [9][iterations][nrx]
@@ -822,6 +846,9 @@ struct RxParams {
   float dx, dy, dz;
   int nsrcOut;
   const Src* srcOut;
+  const TLine* tls;    // [ntl]
+  int ntl;
+  float* tl_out;       // [ntl][2][iterations]: Vtotal, Itotal
 };
 
 __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxParams& r, int* d_it) {
@@ -832,6 +859,10 @@ __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxPa
       if (it < q.first || it > q.last) continue;
       const long long idx = (long long)q.i * p.sx + (long long)q.j * p.sy + q.k;
       float* E = p.E[q.comp];
+      if (q.kind == 4) {
+        E[idx] = *q.w;
+        continue;
+      }
       const uint32_t m = p.ID[q.comp][idx];
       const float c4 = p.cEs[m];
       const float w = q.w[it];
@@ -845,6 +876,11 @@ __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxPa
   __syncthreads();
   const int sample = it + 1;
   if (sample < r.iterations) {
+    for (int n = threadIdx.x; n < r.ntl; n += blockDim.x) {
+      const TLine& t = r.tls[n];
+      r.tl_out[(size_t)(2 * n) * r.iterations + sample] = t.v[t.antpos];
+      r.tl_out[(size_t)(2 * n + 1) * r.iterations + sample] = t.c[t.antpos];
+    }
     for (int n = threadIdx.x; n < r.nrx; n += blockDim.x) {
       const int x = r.coords[3 * n], y = r.coords[3 * n + 1], z = r.coords[3 * n + 2];
       const long long idx = (long long)x * p.sx + (long long)y * p.sy + z;
@@ -869,6 +905,54 @@ __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxPa
   }
   __syncthreads();
   if (threadIdx.x == 0) *d_it = it + 1;
+}
+
+// The current around an E edge (grid.py:413-461): Ix, Iy or Iz at node (x, y, z), fp32.
+__device__ __forceinline__ float edge_current(const StepParams& p, int comp, int x, int y, int z,
+                                              float dx, float dy, float dz) {
+  const long long idx = (long long)x * p.sx + (long long)y * p.sy + z;
+  const float* Hx = p.H[0];
+  const float* Hy = p.H[1];
+  const float* Hz = p.H[2];
+  if (comp == 0)
+    return (y == 0 || z == 0) ? 0.f :
+        __fadd_rn(__fmul_rn(dy, __fsub_rn(Hy[idx - 1], Hy[idx])),
+                  __fmul_rn(dz, __fsub_rn(Hz[idx], Hz[idx - p.sy])));
+  if (comp == 1)
+    return (x == 0 || z == 0) ? 0.f :
+        __fadd_rn(__fmul_rn(dx, __fsub_rn(Hx[idx], Hx[idx - 1])),
+                  __fmul_rn(dz, __fsub_rn(Hz[idx - p.sx], Hz[idx])));
+  return (x == 0 || y == 0) ? 0.f :
+      __fadd_rn(__fmul_rn(dx, __fsub_rn(Hx[idx - p.sy], Hx[idx])),
+                __fmul_rn(dy, __fsub_rn(Hy[idx], Hy[idx - p.sx])));
+}
+
+// Transmission lines between the H and E half-steps (one thread per line): the magnetic part
+// (update_current, then the line current at the antenna cell from the grid's H; sources.py:
+// 426-451) and the voltage update of the electric part (update_voltage with its absorbing end;
+// :396-424), whose -V/d the E half-step writes into the edge.
+__global__ void tl_step(const __grid_constant__ StepParams p, TLine* tls, int ntl, float dx,
+                        float dy, float dz) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= ntl) return;
+  const int it = *p.d_it;
+  TLine& t = tls[n];
+  if (it < t.first || it > t.last) return;
+  const int nl = t.nl;
+  // current[0:nl-1] -= s_iv * (v[1:nl] - v[0:nl-1]); current[srcpos-1] += s_iv * half[it]
+  for (int m = 0; m < nl - 1; ++m)
+    t.c[m] = __double2float_rn(__dsub_rn((double)t.c[m], __dmul_rn(t.s_iv, (double)__fsub_rn(t.v[m + 1], t.v[m]))));
+  t.c[t.srcpos - 1] = __double2float_rn(__dadd_rn((double)t.c[t.srcpos - 1], __dmul_rn(t.s_iv, (double)t.half[it])));
+  t.c[t.antpos] = edge_current(p, t.comp, t.i, t.j, t.k, dx, dy, dz);
+  // voltage[1:nl] -= s_vi * (c[1:nl] - c[0:nl-1]); voltage[srcpos] += r * whole[it]
+  for (int m = nl - 1; m >= 1; --m)
+    t.v[m] = __double2float_rn(__dsub_rn((double)t.v[m], __dmul_rn(t.s_vi, (double)__fsub_rn(t.c[m], t.c[m - 1]))));
+  t.v[t.srcpos] = __double2float_rn(__dadd_rn((double)t.v[t.srcpos], __dmul_rn(t.r, (double)t.whole[it])));
+  // absorbing end: v[0] = h (v[1] - abcv0) + abcv1
+  t.v[0] = __double2float_rn(__dadd_rn(__dmul_rn(t.h, (double)__fsub_rn(t.v[1], t.abcv0)), (double)t.abcv1));
+  t.abcv0 = t.v[0];
+  t.abcv1 = t.v[1];
+  t.eset = __fdiv_rn(-t.v[t.antpos], t.d);
 }
 
 __global__ void end_of_step(const __grid_constant__ StepParams p, const __grid_constant__ RxParams r, int* d_it) {

@@ -48,6 +48,10 @@ struct gbf_ctx {
   int* rx_coords = nullptr;
   float* rxs = nullptr;
   int* d_it = nullptr;
+  TLine* tls = nullptr;        // transmission lines (device state)
+  std::vector<TLine> tls_init; // their state at the start of the run
+  float* tl_waves = nullptr;   // [ntl][2][iterations]
+  float* tl_out = nullptr;     // [ntl][2][iterations]: Vtotal, Itotal
   std::vector<float*> snaps;
   std::vector<int> snapdef;    // nsnap x 10
   int it = 0;                  // host copy of the iteration counter
@@ -233,7 +237,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~3) || d.reserved[0] || d.reserved[1] || d.reserved[2])
+  if ((d.options & ~3) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
@@ -290,6 +294,11 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   A((void**)&ctx->rx_coords, sizeof(int) * 3 * (d.nrx + 1));
   A((void**)&ctx->rxs, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
   A((void**)&ctx->d_it, sizeof(int));
+  if (d.ntl) {
+    A((void**)&ctx->tls, sizeof(TLine) * d.ntl);
+    A((void**)&ctx->tl_waves, sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
+    A((void**)&ctx->tl_out, sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
+  }
   if (rc != GBF_OK) {
     g_create_err = ctx->err;
     gbf_destroy(ctx);
@@ -359,6 +368,9 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   r.dx = d.dx; r.dy = d.dy; r.dz = d.dz;
   r.nsrcOut = 0;
   r.srcOut = ctx->srcs;
+  r.tls = ctx->tls;
+  r.ntl = 0;
+  r.tl_out = ctx->tl_out;
   e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     fail(nullptr, GBF_ECUDA, "gbf_create: %s", cudaGetErrorString(e));
@@ -442,6 +454,7 @@ int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, co
   if (d.nsrc == 0) return GBF_OK;
   if (!info || !scale || !waves) return fail(ctx, GBF_EINVAL, "gbf_upload_sources: NULL array");
   std::vector<Src> inE, inH, outE;
+  int ntl_seen = 0;
   for (int s = 0; s < d.nsrc; ++s) {
     const int32_t* q = info + 8 * s;
     Src v{};
@@ -449,7 +462,14 @@ int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, co
     v.first = q[5]; v.last = q[6];
     v.s0 = scale[2 * s]; v.s1 = scale[2 * s + 1];
     v.w = ctx->waves + (size_t)s * d.iterations;
-    if (v.kind < 0 || v.kind > 3 || v.comp < 0 || v.comp > 5 || v.i < 0 || v.i > d.nx ||
+    if (v.kind == GBF_SRC_TRANSMISSION_LINE) {
+      // the E half-step reads the line's -V/d; lines are numbered in source order
+      if (ntl_seen >= d.ntl)
+        return fail(ctx, GBF_EINVAL, "gbf_upload_sources: more transmission lines than desc.ntl");
+      v.w = &ctx->tls[ntl_seen].eset;
+      ++ntl_seen;
+    }
+    if (v.kind < 0 || v.kind > 4 || v.comp < 0 || v.comp > 5 || v.i < 0 || v.i > d.nx ||
         v.j < 0 || v.j > d.ny || v.k < 0 || v.k > d.nz)
       return fail(ctx, GBF_EINVAL, "gbf_upload_sources: source %d out of range", s);
     if ((v.kind == GBF_SRC_MAGNETIC) != (v.comp >= 3))
@@ -458,6 +478,8 @@ int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, co
     else if (v.i < d.nx && v.j < d.ny && v.k < d.nz) inE.push_back(v);
     else outE.push_back(v);
   }
+  if (ntl_seen != d.ntl)
+    return fail(ctx, GBF_EINVAL, "gbf_upload_sources: %d transmission lines, desc.ntl is %d", ntl_seen, d.ntl);
   std::vector<Src> all;
   all.insert(all.end(), inE.begin(), inE.end());
   all.insert(all.end(), inH.begin(), inH.end());
@@ -530,8 +552,67 @@ int gbf_reset(gbf_ctx* ctx) {
   if (phi_total) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * phi_total, ctx->stream));
   CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
+  if (d.ntl && (int)ctx->tls_init.size() == d.ntl) {
+    // line state after the incident-wave run; samples 0 of Vtotal/Itotal are that state
+    CK(cudaMemcpyAsync(ctx->tls, ctx->tls_init.data(), sizeof(TLine) * d.ntl,
+                       cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<float> out(2 * (size_t)d.ntl * d.iterations, 0.f);
+    for (int n = 0; n < d.ntl; ++n) {
+      const TLine& t = ctx->tls_init[n];
+      out[(size_t)(2 * n) * d.iterations] = t.v[t.antpos];
+      out[(size_t)(2 * n + 1) * d.iterations] = t.c[t.antpos];
+    }
+    CK(cudaMemcpyAsync(ctx->tl_out, out.data(), sizeof(float) * out.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->it = 0;
+  return GBF_OK;
+}
+
+int gbf_upload_tls(gbf_ctx* ctx, const int32_t* info, const double* coef, const float* state,
+                   const float* cell, const float* waves) {
+  if (!ctx) return GBF_EINVAL;
+  const gbf_grid_desc& d = ctx->d;
+  if (d.ntl == 0) return GBF_OK;
+  if (!info || !coef || !state || !cell || !waves)
+    return fail(ctx, GBF_EINVAL, "gbf_upload_tls: NULL array");
+  std::vector<TLine> tl(d.ntl);
+  for (int n = 0; n < d.ntl; ++n) {
+    const int32_t* q = info + 9 * n;
+    TLine& t = tl[n];
+    memset(&t, 0, sizeof(TLine));
+    t.comp = q[0]; t.i = q[1]; t.j = q[2]; t.k = q[3]; t.first = q[4]; t.last = q[5];
+    t.nl = q[6]; t.srcpos = q[7]; t.antpos = q[8];
+    if (t.comp < 0 || t.comp > 2 || t.i < 0 || t.i > d.nx || t.j < 0 || t.j > d.ny || t.k < 0 ||
+        t.k > d.nz || t.nl < 2 || t.nl > kTLCells || t.srcpos < 1 || t.srcpos >= t.nl ||
+        t.antpos < 0 || t.antpos >= t.nl)
+      return fail(ctx, GBF_EINVAL, "gbf_upload_tls: line %d out of range (at most %d cells)", n, kTLCells);
+    t.s_iv = coef[4 * n]; t.s_vi = coef[4 * n + 1]; t.r = coef[4 * n + 2]; t.h = coef[4 * n + 3];
+    const float* st = state + (size_t)n * (2 * kTLCells + 2);
+    for (int m = 0; m < kTLCells; ++m) {
+      t.v[m] = st[m];
+      t.c[m] = st[kTLCells + m];
+    }
+    t.abcv0 = st[2 * kTLCells];
+    t.abcv1 = st[2 * kTLCells + 1];
+    t.d = cell[n];
+    t.whole = ctx->tl_waves + (size_t)(2 * n) * d.iterations;
+    t.half = ctx->tl_waves + (size_t)(2 * n + 1) * d.iterations;
+  }
+  CK(cudaMemcpyAsync(ctx->tl_waves, waves, sizeof(float) * 2 * (size_t)d.ntl * d.iterations,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  ctx->tls_init = tl;
+  ctx->rp.ntl = d.ntl;
+  invalidate_graph(ctx);
+  return gbf_reset(ctx);
+}
+
+int gbf_download_tls(gbf_ctx* ctx, float* out) {
+  if (!ctx || !out) return GBF_EINVAL;
+  const size_t n = 2 * (size_t)ctx->d.ntl * ctx->d.iterations;
+  if (n) CK(cudaMemcpyAsync(out, ctx->tl_out, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
 
@@ -587,8 +668,15 @@ static void launch_end(gbf_ctx* ctx) {
   end_of_step<<<1, 256, 0, ctx->stream>>>(ctx->sp, ctx->rp, ctx->d_it);
 }
 
+static void launch_tl(gbf_ctx* ctx) {
+  if (ctx->rp.ntl)
+    tl_step<<<(ctx->rp.ntl + 31) / 32, 32, 0, ctx->stream>>>(ctx->sp, ctx->tls, ctx->rp.ntl,
+                                                           ctx->d.dx, ctx->d.dy, ctx->d.dz);
+}
+
 static void launch_step(gbf_ctx* ctx) {
   launch_h(ctx);
+  launch_tl(ctx);
   launch_e(ctx);
   launch_end(ctx);
 }
@@ -745,6 +833,7 @@ int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_to
   CK(cudaEventRecord(ev[0], ctx->stream));
   for (int s = 0; s < nsteps; ++s) {
     launch_h(ctx);
+    launch_tl(ctx);
     CK(cudaEventRecord(ev[3 * s + 1], ctx->stream));
     launch_e(ctx);
     CK(cudaEventRecord(ev[3 * s + 2], ctx->stream));
@@ -870,7 +959,8 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
     if (c->device != m0->device) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models on different devices");
     if (pml_kind(c->d) != pk || c->d.maxpoles != m0->d.maxpoles || c->idp != m0->idp)
       return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d differs in PML kind, poles or ID layout from model 0", m);
-    if (c->d.nsnap) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d has snapshots (run it alone)", m);
+    if (c->d.nsnap || c->d.ntl)
+      return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d has snapshots or transmission lines (run it alone)", m);
     if (c->it != m0->it) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models at different iterations");
   }
   gbf_batch* b = new gbf_batch();

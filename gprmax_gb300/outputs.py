@@ -1,6 +1,7 @@
 """The ``.out`` receiver file (``gprMax/fields_outputs.py:111-161``), written with the
 package's own HDF5 writer. Layout: root attributes gprMax, Title, Iterations, nx_ny_nz,
 dx_dy_dz, dt, nsrc, nrx, srcsteps, rxsteps; ``/srcs/srcN`` groups with Type and Position;
+``/tls/tlN`` groups with Position, Resistance, dl and fp32 Vinc, Iinc, Vtotal, Itotal;
 ``/rxs/rxN`` groups with Name and Position and one fp32 [iterations] dataset per output.
 """
 import numpy as np
@@ -27,6 +28,13 @@ def write_hdf5_outputfile(outputfile, G):
         grp = f.create_group('/srcs/src' + str(n + 1))
         grp.attrs['Type'] = type(src).__name__
         grp.attrs['Position'] = np.array((src.xcoord * G.dx, src.ycoord * G.dy, src.zcoord * G.dz))
+    for n, tl in enumerate(G.transmissionlines):
+        grp = f.create_group('/tls/tl' + str(n + 1))
+        grp.attrs['Position'] = np.array((tl.xcoord * G.dx, tl.ycoord * G.dy, tl.zcoord * G.dz))
+        grp.attrs['Resistance'] = np.float64(tl.resistance)
+        grp.attrs['dl'] = np.float64(tl.dl)
+        for name in ('Vinc', 'Iinc', 'Vtotal', 'Itotal'):
+            grp[name] = np.asarray(getattr(tl, name), dtype=np.float32)
     for n, rx in enumerate(G.rxs):
         grp = f.create_group('/rxs/rx' + str(n + 1))
         if rx.ID:

@@ -33,9 +33,50 @@ def pole_count(G):
 
 
 def source_list(G):
-    """Sources in the reference's application order: E sources (voltage sources, then
-    Hertzian dipoles; ``model_build_run.py:459-461``), then magnetic dipoles."""
-    return list(G.voltagesources) + list(G.hertziandipoles) + list(G.magneticdipoles)
+    """Sources in the reference's application order: E sources (voltage sources, transmission
+    lines, Hertzian dipoles; ``model_build_run.py:459-461``), then magnetic dipoles."""
+    return (list(G.voltagesources) + list(getattr(G, 'transmissionlines', []))
+            + list(G.hertziandipoles) + list(G.magneticdipoles))
+
+
+_TL_STENCIL = {'x': ((4, 0, 0, -1), (4, 0, 0, 0), (5, 0, 0, 0), (5, 0, -1, 0)),
+               'y': ((3, 0, 0, 0), (3, 0, 0, -1), (5, -1, 0, 0), (5, 0, 0, 0)),
+               'z': ((3, 0, -1, 0), (3, 0, 0, 0), (4, 0, 0, 0), (4, -1, 0, 0))}
+
+
+def tl_tables(G):
+    """The transmission lines' device tables: info int32 [n][9], coefficients float64 [n][4],
+    line state float32 [n][34], cell sizes float32 [n], waveforms float32 [n][2][iterations]."""
+    from .sources import active_range
+    tls = list(getattr(G, 'transmissionlines', []))
+    n = len(tls)
+    cells = 16
+    info = np.zeros((max(n, 1), 9), dtype=np.int32)
+    coef = np.zeros((max(n, 1), 4), dtype=np.float64)
+    state = np.zeros((max(n, 1), 2 * cells + 2), dtype=np.float32)
+    cell = np.zeros(max(n, 1), dtype=np.float32)
+    waves = np.zeros((max(n, 1), 2, G.iterations), dtype=np.float32)
+    for q, t in enumerate(tls):
+        comp = 'xyz'.index(t.polarisation)
+        first, last = active_range(t, G)
+        info[q] = (comp, t.xcoord, t.ycoord, t.zcoord, first, last, t.nl, t.srcpos, t.antpos)
+        coef[q] = t.ratios(G)
+        state[q, :t.nl] = t.voltage[:t.nl]
+        state[q, cells:cells + t.nl] = t.current[:t.nl]
+        state[q, 2 * cells] = np.float32(t.abcv0)
+        state[q, 2 * cells + 1] = np.float32(t.abcv1)
+        cell[q] = np.float32({'x': G.dx, 'y': G.dy, 'z': G.dz}[t.polarisation])
+        waves[q, 0] = t.waveformvalues_wholestep
+        waves[q, 1] = t.waveformvalues_halfstep
+        # the reference updates the lines before the magnetic dipoles: a dipole on an H value
+        # of the line's current loop would be seen in a different order here
+        for m in G.magneticdipoles:
+            mc = 3 + 'xyz'.index(m.polarisation)
+            for c, di, dj, dk in _TL_STENCIL[t.polarisation]:
+                if (mc, m.xcoord, m.ycoord, m.zcoord) == (c, t.xcoord + di, t.ycoord + dj, t.zcoord + dk):
+                    raise SolverError('a magnetic dipole on the current loop of a transmission line '
+                                      'is not supported')
+    return info, coef, state, cell, waves
 
 
 def source_tables(G):
@@ -58,8 +99,6 @@ def model_inputs(G, options=0):
     """Everything the C ABI receives for grid ``G``: the descriptor and the host arrays, in
     the reference's layouts. Reads only attributes that the reference's own grid object also
     carries, so a grid built by the reference's ``run_model`` can be handed over unchanged."""
-    if getattr(G, 'transmissionlines', None):
-        raise SolverError('transmission lines are not supported by the GB300 solver core')
     d = _native.GridDesc()
     d.nx, d.ny, d.nz = G.nx, G.ny, G.nz
     d.iterations = G.iterations
@@ -74,6 +113,7 @@ def model_inputs(G, options=0):
     d.nsrc = len(source_list(G))
     d.nrx = len(G.rxs)
     d.nsnap = len(G.snapshots)
+    d.ntl = len(getattr(G, 'transmissionlines', []))
     d.options = options
     inp = {'desc': d,
            'ID': np.ascontiguousarray(G.ID, dtype=np.uint32),
@@ -88,6 +128,7 @@ def model_inputs(G, options=0):
         inp['pml'].append((PML_SLABS.index(pml.ID), rows))
     if d.nsrc:
         inp['sources'] = source_tables(G)
+    inp['tls'] = tl_tables(G) if d.ntl else None
     if G.rxs:
         inp['rx'] = np.array([[r.xcoord, r.ycoord, r.zcoord] for r in G.rxs], dtype=np.int32)
     if G.snapshots:
@@ -129,6 +170,8 @@ class DeviceModel:
         if inp['sources'] is not None:
             info, scale, waves = inp['sources']
             self._check(self.lib.gbf_upload_sources(self.ctx, _ptr(info), _ptr(scale), _ptr(waves)))
+        if inp['tls'] is not None:
+            self._check(self.lib.gbf_upload_tls(self.ctx, *(_ptr(a) for a in inp['tls'])))
         if inp['rx'] is not None:
             self._check(self.lib.gbf_set_receivers(self.ctx, _ptr(inp['rx'])))
         if inp['snapshots'] is not None:
@@ -168,6 +211,14 @@ class DeviceModel:
         if self.G.rxs:
             self._check(self.lib.gbf_download_rx(self.ctx, _ptr(out)))
         return out[:, :, :len(self.G.rxs)]
+
+    def transmission_lines(self):
+        """fp32 [ntl][2][iterations]: each line's Vtotal and Itotal."""
+        n = self.desc.ntl
+        out = np.zeros((max(n, 1), 2, self.G.iterations), dtype=np.float32)
+        if n:
+            self._check(self.lib.gbf_download_tls(self.ctx, _ptr(out)))
+        return out[:n]
 
     def fields(self):
         """fp32 [6][nx+1][ny+1][nz+1] (Ex, Ey, Ez, Hx, Hy, Hz)."""
@@ -223,6 +274,12 @@ class DeviceModel:
         for n, r in enumerate(G.rxs):
             for name in r.outputs:
                 r.outputs[name] = rx[OUTPUT_INDEX[name], :, n].copy()
+        tls = list(getattr(G, 'transmissionlines', []))
+        if tls:
+            out = self.transmission_lines()
+            for q, t in enumerate(tls):
+                t.Vtotal = out[q, 0].copy()
+                t.Itotal = out[q, 1].copy()
         for s, snap in enumerate(G.snapshots):
             f = self.snapshot(s)
             # the VTK point layout the reference's Snapshot.store leaves (snapshots.py:129-130)

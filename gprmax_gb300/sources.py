@@ -21,6 +21,7 @@ KIND_HERTZIAN = 0
 KIND_VOLTAGE_RESISTIVE = 1
 KIND_VOLTAGE_HARD = 2
 KIND_MAGNETIC = 3
+KIND_TRANSMISSION_LINE = 4
 
 
 class Source:
@@ -117,8 +118,90 @@ def kernel_record(src, G):
         comp = 'xyz'.index(src.polarisation)
         scale = (np.float32(src.dl), np.float32(1 / (G.dx * G.dy * G.dz)))
         return KIND_HERTZIAN, comp, scale, src.waveformvalues_wholestep
+    if name == 'TransmissionLine':
+        comp = 'xyz'.index(src.polarisation)
+        d = {'x': G.dx, 'y': G.dy, 'z': G.dz}[src.polarisation]
+        # the E edge is set to -V/d from the line's state (the table is unused)
+        return KIND_TRANSMISSION_LINE, comp, (np.float32(d), np.float32(1)), src.waveformvalues_wholestep
     if name == 'MagneticDipole':
         comp = 3 + 'xyz'.index(src.polarisation)
         scale = (np.float32(1 / (G.dx * G.dy * G.dz)), np.float32(1))
         return KIND_MAGNETIC, comp, scale, src.waveformvalues_halfstep
     raise TypeError('source type {} is not supported by the GB300 solver core'.format(name))
+
+
+class TransmissionLine(Source):
+    """One-dimensional transmission line attached to one E edge (``sources.py:286-451``).
+
+    The line's own 1D update (voltage, current, a first-order absorbing end) runs on the host
+    once, unconnected and long, for the incident voltage and current (``calculate_incident_V_I``);
+    its end state seeds the short connected line (``antpos + 1`` cells) that the GPU then advances
+    every iteration: after the H half-step the line current is updated and its value at the
+    antenna cell replaced by the current around the edge (grid.py's Ix/Iy/Iz), then the line
+    voltage is updated and the edge's E set to -V/d. The arithmetic follows the reference's numpy
+    expressions: the line updates are evaluated in float64 (the step ratio is a float64 scalar)
+    and rounded to float32 on assignment."""
+
+    def __init__(self, G=None):
+        super().__init__()
+        self.resistance = None
+        self.abcv0 = 0
+        self.abcv1 = 0
+        if G is not None:
+            self.bind(G)
+
+    def bind(self, G):
+        """Line discretisation for grid ``G``."""
+        from .constants import c
+        from .utilities import round_value
+        self.dl = np.sqrt(3) * c * G.dt
+        self.nl = round_value(0.667 * G.iterations)
+        self.srcpos = 5
+        self.antpos = 10
+        self.voltage = np.zeros(self.nl, dtype=floattype)
+        self.current = np.zeros(self.nl, dtype=floattype)
+        self.Vtotal = np.zeros(G.iterations, dtype=floattype)
+        self.Itotal = np.zeros(G.iterations, dtype=floattype)
+
+    def ratios(self, G):
+        """float64 coefficients of the line updates: I/V (1/R c dt/dl), V/I (R c dt/dl), the
+        injection ratio c dt/dl and the absorbing end's h."""
+        from .constants import c
+        r = c * G.dt / self.dl
+        h = (c * G.dt - self.dl) / (c * G.dt + self.dl)
+        return (np.float64((1 / self.resistance) * r), np.float64(self.resistance * r),
+                np.float64(r), np.float64(h))
+
+    def update_abc(self, G):
+        from .constants import c
+        h = (c * G.dt - self.dl) / (c * G.dt + self.dl)
+        self.voltage[0] = h * (self.voltage[1] - self.abcv0) + self.abcv1
+        self.abcv0 = self.voltage[0]
+        self.abcv1 = self.voltage[1]
+
+    def update_voltage(self, iteration, G):
+        from .constants import c
+        nl = self.nl
+        self.voltage[1:nl] -= (self.resistance * (c * G.dt / self.dl)
+                               * (self.current[1:nl] - self.current[0:nl - 1]))
+        self.voltage[self.srcpos] += ((c * G.dt / self.dl) * self.waveformvalues_wholestep[iteration])
+        self.update_abc(G)
+
+    def update_current(self, iteration, G):
+        from .constants import c
+        nl = self.nl
+        self.current[0:nl - 1] -= ((1 / self.resistance) * (c * G.dt / self.dl)
+                                   * (self.voltage[1:nl] - self.voltage[0:nl - 1]))
+        self.current[self.srcpos - 1] += ((1 / self.resistance) * (c * G.dt / self.dl)
+                                          * self.waveformvalues_halfstep[iteration])
+
+    def calculate_incident_V_I(self, G):
+        """Incident voltage and current of the long, unconnected line; then shorten it."""
+        self.Vinc = np.zeros(G.iterations, dtype=floattype)
+        self.Iinc = np.zeros(G.iterations, dtype=floattype)
+        for iteration in range(G.iterations):
+            self.Iinc[iteration] = self.current[self.antpos]
+            self.Vinc[iteration] = self.voltage[self.antpos]
+            self.update_current(iteration, G)
+            self.update_voltage(iteration, G)
+        self.nl = self.antpos + 1

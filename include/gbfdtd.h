@@ -45,6 +45,7 @@ extern "C" {
 #define GBF_SRC_VOLTAGE_RESISTIVE 1 /* E -= (srce*w[it])*s0             sources.py:81-120  */
 #define GBF_SRC_VOLTAGE_HARD 2      /* E = (-w[it])/s0 while active     sources.py:81-120  */
 #define GBF_SRC_MAGNETIC 3          /* H -= (srcm*w[it])*s0             sources.py:202-232 */
+#define GBF_SRC_TRANSMISSION_LINE 4 /* E = -V(antpos)/d of the line      sources.py:396-424 */
 
 /* gbf_run flags */
 #define GBF_RUN_GRAPH 1u     /* replay the step sequence from a captured CUDA graph */
@@ -67,7 +68,8 @@ typedef struct gbf_grid_desc {
                                     of staging them in shared memory (tuning); bit 1: form the
                                     PML differences dF/d by division even where the reciprocal
                                     product is exact (gbf_check_cell_division); other bits 0 */
-    int32_t reserved[3];         /* must be zero */
+    int32_t ntl;                 /* transmission lines among the nsrc sources */
+    int32_t reserved[2];         /* must be zero */
 } gbf_grid_desc;
 
 typedef struct gbf_ctx gbf_ctx;
@@ -161,6 +163,18 @@ int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n);
 
 /* Library version string. */
 const char* gbf_version(void);
+
+/* Transmission lines (sources.py:286-451), after gbf_upload_sources (whose kind-4 entries are
+ * the lines, in order). info [ntl][9]: component, i, j, k, first and last active iteration,
+ * cells of the connected line, injector cell, antenna cell; coef [ntl][4] (float64): (1/R) c dt/dl,
+ * R c dt/dl, c dt/dl and the absorbing end's (c dt - dl)/(c dt + dl); state [ntl][34]: voltage
+ * [16], current [16], abcv0, abcv1 of the line after the incident-wave run
+ * (calculate_incident_V_I); cell [ntl]: the edge's cell size (fp32); waves [ntl][2][iterations]:
+ * the waveform at whole and half steps. Replaces: TransmissionLine.update_magnetic/_electric. */
+int gbf_upload_tls(gbf_ctx* ctx, const int32_t* info, const double* coef, const float* state,
+                   const float* cell, const float* waves);
+/* [ntl][2][iterations]: Vtotal, Itotal (fields_outputs.py:65-67, tl.Vtotal / tl.Itotal) */
+int gbf_download_tls(gbf_ctx* ctx, float* out);
 
 /* ---- batches: many models advanced together ----------------------------------------
  * A batch borrows contexts that are fully set up (materials, PML rows, sources, receivers

@@ -99,11 +99,17 @@ class OracleSolver:
         self.rx = np.zeros((9, G.iterations, max(len(G.rxs), 1)), dtype=np.float32)
         self.snaps = {}
         self.it = 0
+        # transmission lines advance on copies, so the model's own state stays untouched
+        import copy
+        self.tls = [copy.deepcopy(t) for t in G.transmissionlines]
 
     # -- receivers and snapshots -------------------------------------------------------
     def _store_outputs(self, it):
         G = self.G
         Hx, Hy, Hz = self.H
+        for tl in self.tls:
+            tl.Vtotal[it] = tl.voltage[tl.antpos]
+            tl.Itotal[it] = tl.current[tl.antpos]
         for n, r in enumerate(G.rxs):
             x, y, z = r.xcoord, r.ycoord, r.zcoord
             for c in range(3):
@@ -135,8 +141,28 @@ class OracleSolver:
         self.snaps[s] = out
 
     # -- sources (gprMax/sources.py, numpy fp32 scalar arithmetic) ----------------------
-    def _sources_magnetic(self, it):
+    def _tl_current(self, tl):
+        """The current around a transmission line's edge (grid.py Ix/Iy/Iz, fp32)."""
         G = self.G
+        Hx, Hy, Hz = self.H
+        x, y, z = tl.xcoord, tl.ycoord, tl.zcoord
+        f = np.float32
+        if tl.polarisation == 'x':
+            return 0 if (y == 0 or z == 0) else (
+                f(G.dy) * (Hy[x, y, z - 1] - Hy[x, y, z]) + f(G.dz) * (Hz[x, y, z] - Hz[x, y - 1, z]))
+        if tl.polarisation == 'y':
+            return 0 if (x == 0 or z == 0) else (
+                f(G.dx) * (Hx[x, y, z] - Hx[x, y, z - 1]) + f(G.dz) * (Hz[x - 1, y, z] - Hz[x, y, z]))
+        return 0 if (x == 0 or y == 0) else (
+            f(G.dx) * (Hx[x, y - 1, z] - Hx[x, y, z]) + f(G.dy) * (Hy[x, y, z] - Hy[x - 1, y, z]))
+
+    def _sources_magnetic(self, it):
+        """Transmission lines, then magnetic dipoles (model_build_run.py:440-442)."""
+        G = self.G
+        for tl in self.tls:
+            if it * G.dt >= tl.start and it * G.dt <= tl.stop:
+                tl.update_current(it, G)
+                tl.current[tl.antpos] = self._tl_current(tl)
         for m in G.magneticdipoles:
             if it * G.dt >= m.start and it * G.dt <= m.stop:
                 c = 'xyz'.index(m.polarisation)
@@ -157,6 +183,12 @@ class OracleSolver:
                 else:
                     d = {'x': G.dx, 'y': G.dy, 'z': G.dz}[v.polarisation]
                     self.E[c][i, j, k] = -v.waveformvalues_halfstep[it] / d
+        for tl in self.tls:
+            if it * G.dt >= tl.start and it * G.dt <= tl.stop:
+                c = 'xyz'.index(tl.polarisation)
+                d = {'x': G.dx, 'y': G.dy, 'z': G.dz}[tl.polarisation]
+                tl.update_voltage(it, G)
+                self.E[c][tl.xcoord, tl.ycoord, tl.zcoord] = - tl.voltage[tl.antpos] / d
         for h in G.hertziandipoles:
             if it * G.dt >= h.start and it * G.dt <= h.stop:
                 c = 'xyz'.index(h.polarisation)

@@ -9,6 +9,7 @@ through the reference's own driver (``oracle/ref_harness.py``: input parsing, gr
 * ``iterations``, ``dt``, ``nmat``, ``ID_sha256``, ``coeffE``, ``coeffH`` (and ``coeffD``):
   the reference's model build;
 * ``rx<n>_<output>``: receiver traces of the no-contraction build (bit-for-bit reproducible);
+* ``tl<n>_<Vinc|Iinc|Vtotal|Itotal>``: transmission-line voltages and currents of that build;
 * ``field_<C>_sha256`` and ``field_stats`` (sum, sum of |.|, max |.| in float64) of the final
   fields Ex..Hz of that build;
 * ``fma_rx<n>_<output>``: the same traces from the default (-march=native) build;
@@ -54,6 +55,9 @@ if G.maxpoles:
 for n, r in enumerate(G.rxs):
     for k, v in r.outputs.items():
         out['rx{{}}_{{}}'.format(n + 1, k)] = np.asarray(v, dtype=np.float32)
+for n, t in enumerate(G.transmissionlines):
+    for k in ('Vinc', 'Iinc', 'Vtotal', 'Itotal'):
+        out['tl{{}}_{{}}'.format(n + 1, k)] = np.asarray(getattr(t, k), dtype=np.float32)
 stats = []
 for c in ('Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz'):
     a = np.ascontiguousarray(getattr(G, c))

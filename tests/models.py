@@ -114,6 +114,21 @@ MODELS = {
 #hertzian_dipole: y 0.024 0 0.023 w
 #rx: 0.030 0 0.023
 """,
+    # transmission lines (one with a delayed, shortened drive), a Debye half-space, a
+    # Hertzian dipole and a voltage source alongside
+    'tline': BASE.format(dom='0.036 0.034 0.040', steps=140) + """#pml_cells: 6
+#material: 5 0.002 1 0 soil
+#add_dispersion_debye: 1 6 1e-9 soil
+#box: 0 0 0 0.036 0.034 0.014 soil
+#waveform: gaussian 1 3e9 g
+#waveform: ricker 1 4e9 r
+#transmission_line: z 0.018 0.017 0.020 50 g
+#transmission_line: x 0.012 0.022 0.026 73 r 2e-11 2e-10
+#hertzian_dipole: y 0.024 0.012 0.022 r
+#voltage_source: z 0.014 0.012 0.024 25 g
+#rx: 0.022 0.017 0.020
+#rx: 0.018 0.017 0.016 r2 Ez Hx Iz
+""",
     # sources on the upper domain faces and a receiver on a face (boundary index paths)
     'faces': BASE.format(dom='0.020 0.018 0.016', steps=90) + """#pml_cells: 0
 #waveform: gaussiandot 1 2e9 w

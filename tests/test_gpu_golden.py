@@ -1,7 +1,8 @@
 """GPU against the reference itself: every golden fixture (tests/golden, written by gprMax
 v3.1.7's own time loop compiled without floating-point contraction) is rebuilt from its input
 text by the front-end and run through the C ABI; receiver traces must equal the reference's bit
-for bit and the final fields must hash to the reference's."""
+for bit (transmission-line voltages and currents too) and the final fields must hash to the
+reference's."""
 import glob
 import hashlib
 import os
@@ -28,7 +29,11 @@ def test_gpu_reproduces_reference_run(native, name):
     rx = dm.receivers()
     f = dm.fields()
     snaps = [dm.snapshot(s) for s in range(len(G.snapshots))]
+    tls = dm.transmission_lines()
     dm.close()
+    for n in range(len(G.transmissionlines)):
+        np.testing.assert_array_equal(tls[n, 0], g['tl{}_Vtotal'.format(n + 1)])
+        np.testing.assert_array_equal(tls[n, 1], g['tl{}_Itotal'.format(n + 1)])
     checked = 0
     for n, r in enumerate(G.rxs):
         for out in r.outputs:

@@ -49,6 +49,9 @@ def _check_build(G, g):
     np.testing.assert_array_equal(np.asarray(G.updatecoeffsH), g['coeffH'])
     if 'coeffD' in g:
         np.testing.assert_array_equal(np.asarray(G.updatecoeffsdispersive), g['coeffD'])
+    for n, t in enumerate(G.transmissionlines):
+        for k in ('Vinc', 'Iinc'):
+            np.testing.assert_array_equal(getattr(t, k), g['tl{}_{}'.format(n + 1, k)])
 
 
 def _check_run(G, g):
@@ -63,6 +66,9 @@ def _check_run(G, g):
             np.testing.assert_array_equal(rx[OUTPUT_INDEX[name], :, n], g[key], err_msg=key)
             n_checked += 1
     assert n_checked > 0
+    for n, t in enumerate(ref.tls):
+        for k in ('Vtotal', 'Itotal'):
+            np.testing.assert_array_equal(getattr(t, k), g['tl{}_{}'.format(n + 1, k)])
     f = ref.fields()
     for c, name in enumerate(COMPONENTS):
         sha = hashlib.sha256(np.ascontiguousarray(f[c]).tobytes()).hexdigest()
