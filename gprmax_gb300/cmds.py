@@ -3,7 +3,8 @@
 Single-use commands follow ``gprMax/input_cmds_singleuse.py:41-336``, multi-use commands
 ``input_cmds_multiuse.py:45-851`` and geometry commands ``input_cmds_geometry.py:51-1527`` for
 the commands this solver core supports. Parameter checks raise :class:`CmdInputError` with the
-reference's messages. The fractal/surface/grass commands are rejected
+reference's messages. ``#fractal_box`` is built with its materials from ``#soil_peplinski`` (or
+the reference's errors); its rough-surface, surface-water and grass modifiers are rejected
 with an explicit error.
 """
 import decimal as d
@@ -15,6 +16,7 @@ from scipy import interpolate
 
 from .constants import c, floattype, z0
 from .exceptions import CmdInputError
+from .fractals import FractalVolume, PeplinskiSoil
 from .materials import Material
 from .pml import CFS, CFSParameter, PML
 from .receivers import Rx, allocate_outputs
@@ -512,8 +514,26 @@ def process_multicmds(multicmds, G):
                 if material.poles > G.maxpoles:
                     G.maxpoles = material.poles
 
-    if multicmds['#soil_peplinski']:
-        raise CmdInputError('#soil_peplinski is not supported by the GB300 solver core')
+    cmdname = '#soil_peplinski'
+    for cmdinstance in multicmds[cmdname] or []:
+        tmp = cmdinstance.split()
+        if len(tmp) != 7:
+            raise _err(cmdname, tmp, ' requires at exactly seven parameters')
+        for idx, what in ((0, 'sand fraction'), (1, 'clay fraction'), (2, 'bulk density'),
+                          (3, 'sand particle density'),
+                          (4, 'lower limit of the water volumetric fraction'),
+                          (5, 'upper limit of the water volumetric fraction')):
+            if float(tmp[idx]) < 0:
+                raise _err(cmdname, tmp, ' requires a positive value for the ' + what)
+        if any(x.ID == tmp[6] for x in G.mixingmodels):
+            raise _err(cmdname, tmp, ' with ID {} already exists'.format(tmp[6]))
+        s = PeplinskiSoil(tmp[6], float(tmp[0]), float(tmp[1]), float(tmp[2]), float(tmp[3]),
+                          (float(tmp[4]), float(tmp[5])))
+        _log(G, 'Mixing model (Peplinski) used to create {} with sand fraction {:g}, clay '
+                'fraction {:g}, bulk density {:g}g/cm3, sand particle density {:g}g/cm3, and '
+                'water volumetric fraction {:g} to {:g} created.'.format(
+                    s.ID, s.S, s.C, s.rb, s.rs, s.mu[0], s.mu[1]))
+        G.mixingmodels.append(s)
 
     cmdname = '#pml_cfs'
     if multicmds[cmdname]:
@@ -665,5 +685,93 @@ def process_geometrycmds(geometry, G):
             zf = round_value(float(tmp[6]) / G.dz)
             mats = _lookup_materials(G, tmp, requested)
             geo.build_plate(G, xs, xf, ys, yf, zs, zf, [m.numID for m in mats])
+        elif name == '#fractal_box:':
+            _fractal_box(G, tmp, geometry)
+        elif name in _FRACTAL_MODIFIERS:
+            # handled (and rejected) by the fractal box they name
+            continue
         else:
             raise CmdInputError('{} is not supported by the GB300 solver core'.format(name.rstrip(':')))
+
+
+_FRACTAL_MODIFIERS = ('#add_surface_roughness:', '#add_surface_water:', '#add_grass:')
+
+
+def _fractal_box(G, tmp, geometry):
+    """``#fractal_box`` without modifiers (``input_cmds_geometry.py:808-888`` and
+    ``1519-1527``): a seeded fractal volume binned into the materials of a Peplinski mixing
+    model and voxelised with ``build_voxels_from_array``. Rough surfaces, surface water and
+    grass are not supported and raise :class:`CmdInputError`."""
+    averaging = False
+    if len(tmp) < 14:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least thirteen parameters')
+    elif len(tmp) == 14:
+        seed = None
+    elif len(tmp) == 15:
+        seed = int(tmp[14])
+    elif len(tmp) == 16:
+        seed = int(tmp[14])
+        flag = tmp[15].lower()
+        if flag not in ('y', 'n'):
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires averaging to be either y or n')
+        averaging = flag == 'y'
+    else:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' too many parameters have been given')
+    xs = round_value(float(tmp[1]) / G.dx)
+    xf = round_value(float(tmp[4]) / G.dx)
+    ys = round_value(float(tmp[2]) / G.dy)
+    yf = round_value(float(tmp[5]) / G.dy)
+    zs = round_value(float(tmp[3]) / G.dz)
+    zf = round_value(float(tmp[6]) / G.dz)
+    for v, n, lu, ax, dl in ((xs, G.nx, 'lower', 'x', G.dx), (xf, G.nx, 'upper', 'x', G.dx),
+                             (ys, G.ny, 'lower', 'y', G.dy), (yf, G.ny, 'upper', 'y', G.dy),
+                             (zs, G.nz, 'lower', 'z', G.dz), (zf, G.nz, 'upper', 'z', G.dz)):
+        if v < 0 or v > n:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the {} {}-coordinate {:g}m is not within the model domain'.format(lu, ax, v * dl))
+    if xs >= xf or ys >= yf or zs >= zf:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the lower coordinates should be less than the upper coordinates')
+    if float(tmp[7]) < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the fractal dimension')
+    for idx, ax in ((8, 'x'), (9, 'y'), (10, 'z')):
+        if float(tmp[idx]) < 0:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the fractal weighting in the {} direction'.format(ax))
+    if round_value(tmp[11]) < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the number of bins')
+
+    mixingmodel = next((x for x in G.mixingmodels if x.ID == tmp[12]), None)
+    material = next((x for x in G.materials if x.ID == tmp[12]), None)
+    nbins = round_value(tmp[11])
+    if mixingmodel:
+        if nbins == 1:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' must be used with more than one material from the mixing model.')
+        mixingmodel.calculate_debye_properties(nbins, G, tmp[13])
+    elif not material:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' mixing model or material with ID {} does not exist'.format(tmp[12]))
+
+    volume = FractalVolume(xs, xf, ys, yf, zs, zf, float(tmp[7]), seed)
+    volume.ID = tmp[13]
+    volume.operatingonID = tmp[12]
+    volume.nbins = nbins
+    volume.weighting = np.array([float(tmp[8]), float(tmp[9]), float(tmp[10])])
+    volume.averaging = averaging
+    _log(G, 'Fractal box {} from {:g}m, {:g}m, {:g}m, to {:g}m, {:g}m, {:g}m with {}, fractal '
+            'dimension {:g}, fractal weightings {:g}, {:g}, {:g}, fractal seeding {}, with {} '
+            'material(s) created, dielectric smoothing is {}.'.format(
+                volume.ID, xs * G.dx, ys * G.dy, zs * G.dz, xf * G.dx, yf * G.dy, zf * G.dz,
+                volume.operatingonID, volume.dimension, volume.weighting[0],
+                volume.weighting[1], volume.weighting[2], volume.seed, volume.nbins,
+                'on' if averaging else 'off'))
+    G.fractalvolumes.append(volume)
+
+    for other in geometry:
+        m = other.split()
+        if m and m[0] in _FRACTAL_MODIFIERS and volume.ID in m[1:]:
+            raise CmdInputError('{} is not supported by the GB300 solver core'.format(m[0].rstrip(':')))
+
+    if nbins == 1:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' is being used with a single material and no modifications, therefore please use a #box command instead.')
+    if not mixingmodel:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' needs a mixing model to bin {} materials from; {} is a single material'.format(nbins, tmp[12]))
+    vol = volume.generate_fractal_volume()
+    vol += mixingmodel.startmaterialnum
+    geo.build_voxels_array(G, (xs, ys, zs), vol.astype('int16', order='C'), averaging)

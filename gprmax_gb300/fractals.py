@@ -1,0 +1,126 @@
+"""Fractal volumes for ``#fractal_box`` (``gprMax/fractals.py:141-194``) and the Peplinski soil
+mixing model for ``#soil_peplinski`` (``gprMax/materials.py:244-330``).
+
+The volume is generated with the same library calls and the same floating-point operations as
+the reference, so the binned material numbers (and hence the material-ID array) agree bit for
+bit: seeded standard normals (``numpy.random.default_rng``), ``scipy.fftpack`` FFTs and shifts,
+the 1/r^D filter of ``fractals_generate_ext.pyx:56-86`` (rr = (dx^2 + dy^2 + dz^2)^(1/2) and
+B = rr^D, every power through the C library's ``pow`` in float64, D rounded to float32 as the
+extension's ``float D`` argument, B = 0.9 where it is zero, the complex value divided by the
+real B component-wise), the DC term
+zeroed, the real part of the inverse FFT in float32, and ``numpy.digitize`` into ``nbins``
+bins row by row.
+"""
+import math
+
+import numpy as np
+from scipy import fftpack
+
+from .constants import floattype
+from .materials import Material
+
+
+class FractalVolume:
+    """A box whose cells take one of ``nbins`` materials from a seeded fractal field."""
+
+    def __init__(self, xs, xf, ys, yf, zs, zf, dimension, seed):
+        self.ID = None
+        self.operatingonID = None
+        self.xs, self.xf, self.ys, self.yf, self.zs, self.zf = xs, xf, ys, yf, zs, zf
+        self.nx = xf - xs
+        self.ny = yf - ys
+        self.nz = zf - zs
+        self.averaging = False
+        self.seed = seed
+        self.dimension = dimension
+        self.weighting = np.array([1, 1, 1], dtype=np.float64)
+        self.nbins = 0
+
+    def generate_fractal_volume(self):
+        """Bin numbers (float32 array [nx][ny][nz], values 0..nbins-1) of the fractal field."""
+        n = np.array([self.nx, self.ny, self.nz])
+        if self.nx == 1:
+            scaling = np.insert(np.amin(n[1:]) / n[1:], 0, 1)
+        elif self.ny == 1:
+            scaling = np.insert(np.amin(n[[0, 2]]) / n[[0, 2]], 1, 1)
+        elif self.nz == 1:
+            scaling = np.insert(np.amin(n[:2]) / n[:2], 2, 1)
+        else:
+            scaling = np.amin(n) / n
+        self.weighting = np.multiply(self.weighting, scaling)
+        w = self.weighting
+        v1 = np.array([w[0] * self.nx / 2, w[1] * self.ny / 2, w[2] * self.nz / 2])
+        rng = np.random.default_rng(seed=self.seed)
+        A = rng.standard_normal(size=(self.nx, self.ny, self.nz))
+        A = fftpack.fftshift(fftpack.fftn(A))
+        # 1/r^D filter. Every power goes through the C library's pow (math.pow), as the
+        # compiled filter does: numpy's vectorised power differs from it in the last bit.
+        cpow = np.frompyfunc(math.pow, 2, 1)
+        d = [cpow(w[a] * np.arange(n[a], dtype=np.float64) - v1[a], 2.0).astype(np.float64)
+             for a in range(3)]
+        rr = cpow(d[0][:, None, None] + d[1][None, :, None] + d[2][None, None, :], 0.5)
+        B = cpow(rr, float(np.float32(self.dimension))).astype(np.float64)
+        B[B == 0] = 0.9
+        vol = np.empty(A.shape, dtype=np.complex128)
+        vol.real = A.real / B
+        vol.imag = A.imag / B
+        vol = fftpack.ifftshift(vol)
+        vol[0, 0, 0] = 0
+        vol = np.real(fftpack.ifftn(vol)).astype(floattype, copy=False)
+        bins = np.linspace(np.amin(vol), np.amax(vol), self.nbins)
+        for j in range(self.ny):
+            for k in range(self.nz):
+                vol[:, j, k] = np.digitize(vol[:, j, k], bins, right=True)
+        self.fractalvolume = vol
+        return vol
+
+
+class PeplinskiSoil:
+    """Soil whose materials come from the Peplinski mixing model
+    (http://dx.doi.org/10.1109/36.387598): one single-pole Debye material per bin of the
+    volumetric water fraction."""
+
+    def __init__(self, ID, sandfraction, clayfraction, bulkdensity, sandpartdensity,
+                 watervolfraction):
+        self.ID = ID
+        self.S = sandfraction
+        self.C = clayfraction
+        self.rb = bulkdensity
+        self.rs = sandpartdensity
+        self.mu = watervolfraction
+        self.startmaterialnum = 0
+
+    def calculate_debye_properties(self, nbins, G, fractalboxname):
+        """Append the ``nbins`` materials named ``|<box>_<n>|`` to ``G.materials``."""
+        self.startmaterialnum = len(G.materials)
+        f = 1.3e9
+        w = 2 * np.pi * f
+        erealw = Material.watereri + ((Material.waterdeltaer) / (1 + (w * Material.watertau) ** 2))
+        a = 0.65
+        es = (1.01 + 0.44 * self.rs) ** 2 - 0.062
+        b1 = 1.2748 - 0.519 * self.S - 0.152 * self.C
+        b2 = 1.33797 - 0.603 * self.S - 0.166 * self.C
+        sigf = 0.0467 + 0.2204 * self.rb - 0.411 * self.S + 0.6614 * self.C
+        mubins = np.linspace(self.mu[0], self.mu[1], nbins)
+        mumaterials = mubins + (mubins[1] - mubins[0]) / 2
+        digits = len(str(int(nbins)))
+        it = np.nditer(mumaterials, flags=['c_index'])
+        while not it.finished:
+            mu = it[0]
+            er = (1 + (self.rb / self.rs) * ((es ** a) - 1) + (mu ** b1 * erealw ** a) - mu) ** (1 / a)
+            er = 1.15 * er - 0.68
+            eri = er - (mu ** (b2 / a) * Material.waterdeltaer)
+            sig = mu ** (b2 / a) * ((sigf * (self.rs - self.rb)) / (self.rs * mu))
+            m = Material(len(G.materials), '|{}_{}|'.format(fractalboxname,
+                                                         str(it.index + 1).zfill(digits)))
+            m.type = 'debye'
+            m.averagable = False
+            m.poles = 1
+            if m.poles > G.maxpoles:
+                G.maxpoles = m.poles
+            m.er = eri
+            m.se = sig
+            m.deltaer.append(er - eri)
+            m.tau.append(Material.watertau)
+            G.materials.append(m)
+            it.iternext()

@@ -34,6 +34,7 @@ class FDTDGrid:
         self.materials = []
         self.maxpoles = 0
         self.mixingmodels = []
+        self.fractalvolumes = []
         self.averagevolumeobjects = True
         self.waveforms = []
         self.voltagesources = []

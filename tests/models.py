@@ -140,4 +140,18 @@ MODELS = {
 #rx: 0.010 0.009 0.000
 #rx: 0.011 0.010 0.009
 """,
+    # fractal soil from a Peplinski mixing model (no smoothing), a second box smoothed. The
+    # mixing-model parameters are ones whose water-fraction powers come out the same through
+    # numpy's vectorised pow and the C library's pow, so the material values do not depend
+    # on the machine that builds the model.
+    'fractal': BASE.format(dom='0.034 0.032 0.036', steps=120) + """#pml_cells: 6
+#soil_peplinski: 0.5 0.5 2.0 2.66 0.001 0.3 soil
+#soil_peplinski: 0.7 0.2 1.8 2.6 0.05 0.15 wet
+#fractal_box: 0 0 0 0.034 0.032 0.016 1.5 1 1 1 8 soil lower 7
+#fractal_box: 0.008 0.010 0.016 0.026 0.022 0.024 2.2 1 0.5 2 5 wet upper 3 y
+#waveform: ricker 1 2e9 w
+#hertzian_dipole: z 0.017 0.016 0.026 w
+#rx: 0.021 0.016 0.026
+#rx: 0.017 0.016 0.012 deep Ex Ey Ez Hx Hy Hz
+""",
 }

@@ -57,7 +57,7 @@ pickle.dump(inp, open({out!r}, 'wb'))
         return pickle.load(f)
 
 
-@pytest.mark.parametrize('name', ['mixed', 'debye1', 'hori2'])
+@pytest.mark.parametrize('name', ['mixed', 'debye1', 'hori2', 'fractal'])
 def test_reference_grid_gives_the_same_solver_inputs(name):
     from gprmax_gb300.model import build_grid
     from gprmax_gb300.solver import model_inputs
