@@ -131,6 +131,7 @@ _SIGS = {
     'gbf_adj_set_receivers': (ctypes.c_int, [_P, _P]),
     'gbf_adj_forward': (ctypes.c_int, [_P, _P, _P, _P]),
     'gbf_adj_backward': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    'gbf_adj_backward_static': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     'gbf_batch_create': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
     'gbf_batch_destroy': (None, [_P]),
     'gbf_batch_run': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_uint32]),

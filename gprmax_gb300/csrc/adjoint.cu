@@ -23,6 +23,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -800,6 +801,58 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
   }
   AK(cudaStreamSynchronize(a->stream));
   return GBF_OK;
+}
+
+// Fixed device scratch of gbf_adj_backward_static: the fp32 per-segment partial sums of the
+// two gradients (3N floats each), which gbf_adj_backward keeps in buffers of the context.
+// 16 MiB, enough for grids of up to kStaticScratchFloats / 6 = 699,050 nodes per component.
+constexpr size_t kStaticScratchFloats = (size_t)4 << 20;
+static __device__ __align__(256) float g_static_scratch[kStaticScratchFloats];
+constexpr int kStaticMaxDevices = 64;
+static float* g_static_scratch_addr[kStaticMaxDevices];
+static std::mutex g_static_scratch_lock;
+
+int gbf_adj_backward_static(gbf_adj* a, const float* CA, const float* CB, const float* gtraces,
+                            double* gCA, double* gCB) {
+  if (!a || !CA || !CB || !gtraces || !gCA || !gCB) return GBF_EINVAL;
+  const size_t need = 6 * (size_t)a->N;
+  if (need > kStaticScratchFloats)
+    return afail(a, GBF_EINVAL,
+                 "gbf_adj_backward_static: the grid has %lld nodes per component; the fixed "
+                 "scratch holds the partial sums of at most %zu (use gbf_adj_backward)",
+                 a->N, kStaticScratchFloats / 6);
+  if (a->device < 0 || a->device >= kStaticMaxDevices)
+    return afail(a, GBF_EINVAL, "gbf_adj_backward_static: device %d is beyond the %d supported",
+                 a->device, kStaticMaxDevices);
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != a->device)
+    return afail(a, GBF_ESTATE, "gbf_adj_backward_static: call with the context's device (%d) current",
+                 a->device);
+  float* base = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_static_scratch_lock);
+    base = g_static_scratch_addr[a->device];
+    if (!base) {
+      // once per device: the address of the array in this device's copy of the module
+      void* addr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&addr, g_static_scratch);
+      if (e != cudaSuccess)
+        return afail(a, GBF_ECUDA, "gbf_adj_backward_static: scratch address: %s",
+                     cudaGetErrorString(e));
+      base = static_cast<float*>(addr);
+      g_static_scratch_addr[a->device] = base;
+    }
+  }
+  // gbf_adj_backward zeroes the partials before each segment, so the scratch needs no
+  // particular contents on entry; only the two pointers are swapped for this call.
+  float* keepA = a->gCA;
+  float* keepB = a->gCB;
+  a->gCA = base;
+  a->gCB = base + 3 * (size_t)a->N;
+  const int rc = gbf_adj_backward(a, CA, CB, gtraces, gCA, gCB);
+  a->gCA = keepA;
+  a->gCB = keepB;
+  return rc;
 }
 
 }  // extern "C"

@@ -233,6 +233,15 @@ int gbf_adj_forward(gbf_adj* adj, const float* CA, const float* CB, float* trace
 /* gCA, gCB (fp64, overwritten) = d(misfit)/d(CA, CB) given gtraces = d(misfit)/d(traces) */
 int gbf_adj_backward(gbf_adj* adj, const float* CA, const float* CB, const float* gtraces,
                      double* gCA, double* gCB);
+/* gbf_adj_backward with its fp32 per-segment partial sums in a fixed 16 MiB device array of
+ * the library instead of buffers of the context; allocates nothing. Same arguments and
+ * results. Grids of more than 699,050 nodes per component ((nx+1)(ny+1)(nz+1)) are rejected
+ * with GBF_EINVAL. The first call on a device looks up the array's address (setup); make it
+ * before any stream capture. All contexts on a device share the array: overlapping calls, from
+ * two threads or two contexts, race on it and must be serialised by the caller. No counterpart
+ * in the reference. */
+int gbf_adj_backward_static(gbf_adj* adj, const float* CA, const float* CB, const float* gtraces,
+                            double* gCA, double* gCB);
 
 /* 1 if, for this cell size, the PML kernels may form dF/d as the product with the rounded
  * reciprocal corrected once by the exact residual, because that equals the IEEE quotient for
