@@ -531,6 +531,45 @@ def run_sweep(args):
     print(json.dumps(out), flush=True)
 
 
+def run_build(args):
+    """Model build (geometry primitives, voxel blocks, per-edge IDs with smoothing, material
+    tables, PML coefficients) on the host and in device memory, for the dispersive soil
+    (400x400x200, 50 materials, fractal voxel block and a PEC cylinder) and the largest
+    throughput cube (a box with smoothing). Wall seconds of ``build_grid`` each way, best of
+    ``--steps`` after ``--warmup`` (the device build includes its CUDA work, which every call
+    finishes before it returns)."""
+    from gprmax_gb300 import workloads
+    rows = []
+    cases = [('dispersive_soil_400x400x200', lambda dev: workloads.dispersive_soil(device_build=dev)),
+             ('throughput_cube_{}'.format(max(args.sizes)),
+              lambda dev: workloads.throughput_cube(max(args.sizes), device_build=dev))]
+    for name, make in cases:
+        row = {'workload': name}
+        for dev in (False, True):
+            best = None
+            for rep in range(args.warmup + args.steps):
+                t0 = time.perf_counter()
+                G = make(dev)
+                t = time.perf_counter() - t0
+                if dev:
+                    G.geom.close()
+                cells = G.nx * G.ny * G.nz
+                del G
+                if rep >= args.warmup:
+                    best = t if best is None else min(best, t)
+            row['device_s' if dev else 'host_s'] = round(best, 3)
+        row['cells'] = cells
+        row['speedup'] = round(row['host_s'] / row['device_s'], 2)
+        rows.append(row)
+    out = {'metric': 'model build time', 'value': rows[0]['device_s'], 'unit': 's',
+           'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup,
+           'ms_per_step': rows[0]['device_s'] * 1e3, 'higher_is_better': False,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'u32',
+           'data': 'synthetic (seeded fractal Debye soil; seeded dielectric block)',
+           'config': {'workload': rows[0]['workload'] + ' build'}, 'builds': rows}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split('\n')[0])
     ap.add_argument('--gpus', type=int, default=1)
@@ -545,11 +584,13 @@ def main():
                     help='smaller soil grid (profiling runs); default 400 400 200')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
-    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint', 'sweep'], default='soil',
+    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint', 'sweep', 'build'],
+                    default='soil',
                     help='soil: the 400x400x200 Debye soil (default); bscan: the batched uneven '
                          'B-scan against sequential plain runs; adjoint: gradient cost and '
                          'finite-difference check of the differentiable time loop; sweep: '
-                         'cubes of 100^3 to 600^3 cells')
+                         'cubes of 100^3 to 600^3 cells; build: model build on the host and '
+                         'in device memory')
     ap.add_argument('--models', type=int, default=128, help='bscan: number of models')
     ap.add_argument('--sizes', type=int, nargs='+', default=[100, 200, 300, 400, 500, 600],
                     help='sweep: cube edge lengths in cells')
@@ -560,6 +601,8 @@ def main():
         run_bscan(args)
     elif args.workload == 'adjoint':
         run_adjoint(args)
+    elif args.workload == 'build':
+        run_build(args)
     elif args.workload == 'sweep':
         run_sweep(args)
     elif args.impl == 'reference':

@@ -11,7 +11,7 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
-SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'adjoint.cu', 'fdtd_kernels.cuh']
+SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'adjoint.cu', 'geom.cu', 'fdtd_kernels.cuh']
 PML_KINDS = 5   # kernels_inst.cu is compiled once per PML kind
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -51,7 +51,8 @@ def build(force=False, verbose=False):
     os.makedirs(objdir, exist_ok=True)
     compile_flags = [f for f in NVCC_FLAGS if f != '-shared']
     jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), []),
-            (os.path.join(CSRC, 'adjoint.cu'), os.path.join(objdir, 'adjoint.o'), [])]
+            (os.path.join(CSRC, 'adjoint.cu'), os.path.join(objdir, 'adjoint.o'), []),
+            (os.path.join(CSRC, 'geom.cu'), os.path.join(objdir, 'geom.o'), [])]
     for pk in range(PML_KINDS):
         jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
                      os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
@@ -141,6 +142,21 @@ _SIGS = {
     'gbf_batch_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_sweep_boxes': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
                                        ctypes.c_int32, _P]),
+    'gbf_geom_create': (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.POINTER(_P)]),
+    'gbf_geom_destroy': (None, [_P]),
+    'gbf_geom_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    'gbf_geom_cells': (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32]),
+    'gbf_geom_box': (ctypes.c_int, [_P, _P, _P, ctypes.c_int32]),
+    'gbf_geom_voxels': (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32]),
+    'gbf_geom_edges': (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    'gbf_geom_components': (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    'gbf_geom_averaged_keys': (ctypes.c_int, [_P, _P]),
+    'gbf_geom_resolve': (ctypes.c_int, [_P, ctypes.c_int64, _P, _P]),
+    'gbf_geom_fill': (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_uint32]),
+    'gbf_geom_read': (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    'gbf_geom_max_id': (ctypes.c_int, [_P, _P]),
+    'gbf_upload_materials_geom': (ctypes.c_int, [_P, _P, _P, _P, _P]),
 }
 
 

@@ -381,18 +381,12 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   return GBF_OK;
 }
 
-int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
-                         const float* coeffH, const float* coeffD) {
-  if (!ctx) return GBF_EINVAL;
-  if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
-    return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
+}  // extern "C"
+
+// Coefficient tables, dispersive flags and packed IDs, once ctx->ID holds the ID array.
+static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
+                         const float* coeffD) {
   const int nmat = ctx->d.nmat;
-  // every ID must index the tables
-  const size_t n = 6 * (size_t)ctx->ncomp;
-  for (size_t q = 0; q < n; ++q)
-    if (ID[q] >= (uint32_t)nmat)
-      return fail(ctx, GBF_EINVAL, "gbf_upload_materials: ID[%zu] = %u >= nmat %d", q, ID[q], nmat);
-  CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -424,6 +418,68 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->materials = true;
   return GBF_OK;
+}
+
+namespace gbf {
+const uint32_t* geom_ids(const gbf_geom* g, int dims[3], int* device, cudaStream_t* stream);
+}
+
+__global__ void id_max_kernel(const uint32_t* a, long long n, unsigned int* mx) {
+  unsigned int m = 0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    m = a[q] > m ? a[q] : m;
+  for (int o = 16; o; o >>= 1) {
+    const unsigned int t = __shfl_xor_sync(0xffffffffu, m, o);
+    m = t > m ? t : m;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+extern "C" {
+
+int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
+                         const float* coeffH, const float* coeffD) {
+  if (!ctx) return GBF_EINVAL;
+  if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
+  const int nmat = ctx->d.nmat;
+  // every ID must index the tables
+  const size_t n = 6 * (size_t)ctx->ncomp;
+  for (size_t q = 0; q < n; ++q)
+    if (ID[q] >= (uint32_t)nmat)
+      return fail(ctx, GBF_EINVAL, "gbf_upload_materials: ID[%zu] = %u >= nmat %d", q, ID[q], nmat);
+  CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  return upload_tables(ctx, coeffE, coeffH, coeffD);
+}
+
+int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
+                              const float* coeffH, const float* coeffD) {
+  if (!ctx) return GBF_EINVAL;
+  if (!geom || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_geom: NULL argument");
+  int dims[3], gdev = -1;
+  cudaStream_t gstream = nullptr;
+  const uint32_t* gid = geom_ids(geom, dims, &gdev, &gstream);
+  if (dims[0] != ctx->d.nx || dims[1] != ctx->d.ny || dims[2] != ctx->d.nz || gdev != ctx->device)
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_geom: geometry %d x %d x %d on device %d "
+                "does not match the context's grid %d x %d x %d on device %d", dims[0], dims[1],
+                dims[2], gdev, ctx->d.nx, ctx->d.ny, ctx->d.nz, ctx->device);
+  const size_t n = 6 * (size_t)ctx->ncomp;
+  CK(cudaStreamSynchronize(gstream));
+  CK(cudaMemcpyAsync(ctx->ID, gid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  unsigned int* dmax = nullptr;
+  CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
+  CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
+  id_max_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->ID, (long long)n, dmax);
+  CK(cudaGetLastError());
+  unsigned int mx = 0;
+  CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaFreeAsync(dmax, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (mx >= (unsigned)ctx->d.nmat)
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_geom: ID %u >= nmat %d", mx, ctx->d.nmat);
+  return upload_tables(ctx, coeffE, coeffH, coeffD);
 }
 
 int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]) {

@@ -7,7 +7,8 @@ with smoothing it only writes the solid array and clears the rigid flags, and th
 derived later by :mod:`gprmax_gb300.yee_build`. Cell selection for spheres and cylinders uses
 the reference's fp32 geometry inputs (``build_sphere`` :873, ``build_cylinder`` :692).
 All writes here are whole-array numpy operations; one primitive writes one material, so the
-order of its cells does not matter.
+order of its cells does not matter. On a grid built in device memory (``G.geom``, see
+:mod:`gprmax_gb300.devgeom`) the same cell selections are handed to the device builders.
 """
 import numpy as np
 
@@ -45,6 +46,10 @@ def _set_cells(G, I, J, K, numID, numIDx, numIDy, numIDz, averaging):
 
 def build_voxels_mask(G, mask, origin, numID, numIDx, numIDy, numIDz, averaging):
     """Build every cell where ``mask`` (a box starting at ``origin``) is true."""
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        geom.cells(origin, mask.shape, mask, (numID, numIDx, numIDy, numIDz), averaging)
+        return
     I, J, K = np.nonzero(mask)
     I = I + origin[0]
     J = J + origin[1]
@@ -55,6 +60,11 @@ def build_voxels_mask(G, mask, origin, numID, numIDx, numIDy, numIDz, averaging)
 
 def build_box(G, xs, xf, ys, yf, zs, zf, numID, numIDx, numIDy, numIDz, averaging):
     """Axis-aligned box of cells [xs, xf) x [ys, yf) x [zs, zf) (``build_box`` :618-691)."""
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        geom.box((xs, ys, zs), (xf - xs, yf - ys, zf - zs), (numID, numIDx, numIDy, numIDz),
+                 averaging)
+        return
     G.solid[xs:xf, ys:yf, zs:zf] = numID
     if averaging:
         G.rigidE[:, xs:xf, ys:yf, zs:zf] = 0
@@ -185,6 +195,15 @@ def _oblique_cylinder_mask(xs, xf, ys, yf, zs, zf, dx, dy, dz, x1, y1, z1, x2, y
 
 def build_edge(G, xs, ys, zs, xf, yf, zf, numID):
     """Single-material line of edges (``input_cmds_geometry.py`` #edge; ``build_edge_*``)."""
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        if xs != xf:
+            geom.edges([(0, i, ys, zs, numID) for i in range(xs, xf)])
+        elif ys != yf:
+            geom.edges([(1, xs, j, zs, numID) for j in range(ys, yf)])
+        elif zs != zf:
+            geom.edges([(2, xs, ys, k, numID) for k in range(zs, zf)])
+        return
     if xs != xf:
         for i in range(xs, xf):
             _rigid_edge(G, 0, i, ys, zs)
@@ -233,6 +252,26 @@ def build_plate(G, xs, xf, ys, yf, zs, zf, numIDs):
     ``numIDs`` holds one or two material numbers (isotropic or anisotropic)."""
     a = numIDs[0]
     b = numIDs[-1]
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        recs = []
+        if xs == xf:
+            for j in range(ys, yf):
+                for k in range(zs, zf):
+                    recs += [(1, xs, j, k, a), (2, xs, j, k, b), (1, xs, j, k + 1, a),
+                             (2, xs, j + 1, k, b)]
+        elif ys == yf:
+            for i in range(xs, xf):
+                for k in range(zs, zf):
+                    recs += [(0, i, ys, k, a), (2, i, ys, k, b), (0, i, ys, k + 1, a),
+                             (2, i + 1, ys, k, b)]
+        elif zs == zf:
+            for i in range(xs, xf):
+                for j in range(ys, yf):
+                    recs += [(0, i, j, zs, a), (1, i, j, zs, b), (0, i, j + 1, zs, a),
+                             (1, i + 1, j, zs, b)]
+        geom.edges(recs)
+        return
     if xs == xf:
         for j in range(ys, yf):
             for k in range(zs, zf):
@@ -272,6 +311,10 @@ def build_voxels_array(G, origin, numids, averaging):
     xs, ys, zs = origin
     n = numids[:max(0, min(numids.shape[0], G.nx - xs)), :max(0, min(numids.shape[1], G.ny - ys)),
                :max(0, min(numids.shape[2], G.nz - zs))]
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        geom.voxels((xs, ys, zs), n, averaging)
+        return
     built = n >= 0
     if not built.any():
         return

@@ -61,8 +61,14 @@ class FDTDGrid:
         from .utilities import round_value
         return round_value(float(val) / getattr(self, 'd' + coord))
 
-    def initialise_geometry_arrays(self):
-        """solid and ID start as free_space (1); nothing is rigid (``grid.py:157-169``)."""
+    def initialise_geometry_arrays(self, device=False):
+        """solid and ID start as free_space (1); nothing is rigid (``grid.py:157-169``).
+        ``device``: the arrays live on the GPU instead (:mod:`gprmax_gb300.devgeom`)."""
+        if device:
+            from .devgeom import DeviceGeometry
+            self.geom = DeviceGeometry(self.nx, self.ny, self.nz)
+            self.solid = self.rigidE = self.rigidH = self.ID = None
+            return
         self.solid = np.ones((self.nx, self.ny, self.nz), dtype=np.uint32)
         self.rigidE = np.zeros((12, self.nx, self.ny, self.nz), dtype=np.int8)
         self.rigidH = np.zeros((6, self.nx, self.ny, self.nz), dtype=np.int8)

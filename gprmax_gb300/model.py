@@ -18,12 +18,13 @@ from .yee_build import build_electric_components, build_magnetic_components
 
 
 def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=None,
-               geometry_hook=None):
+               geometry_hook=None, device_build=False):
     """Build a model from input-file lines up to the coefficient tables (before solving).
 
     Follows the build sequence of ``run_model`` (``model_build_run.py:110-292``).
     ``geometry_hook(G)``, when given, runs before the geometry commands (used to place
-    programmatic voxel blocks, as ``#fractal_box`` would).
+    programmatic voxel blocks, as ``#fractal_box`` would). ``device_build``: the geometry
+    arrays are built in GPU memory (:mod:`gprmax_gb300.devgeom`) and handed to the solver there.
     """
     G = G or FDTDGrid()
     if usernamespace is None:
@@ -41,7 +42,7 @@ def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=Non
     if messages is not None:
         G.messages = messages
     cmds.process_multicmds(multicmds, G)
-    G.initialise_geometry_arrays()
+    G.initialise_geometry_arrays(device=device_build)
     if geometry_hook is not None:
         geometry_hook(G)
     cmds.process_geometrycmds(geometry, G)
@@ -59,7 +60,22 @@ def finish_build(G):
         G.pmls = []
     build_electric_components(G)
     build_magnetic_components(G)
-    if '2D TMx' in G.mode:
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        # PEC planes of the 2D modes (the same writes as below, on the device)
+        n1 = (G.nx + 1, G.ny + 1, G.nz + 1)
+        planes = {'2D TMx': ((1, 0), (2, 0)), '2D TMy': ((0, 1), (2, 1)),
+                  '2D TMz': ((0, 2), (1, 2))}
+        for mode, pairs in planes.items():
+            if mode in G.mode:
+                for comp, axis in pairs:
+                    for idx in (0, 1):
+                        origin = [0, 0, 0]
+                        shape = list(n1)
+                        origin[axis] = idx
+                        shape[axis] = 1
+                        geom.fill(2 + comp, origin, shape, 0)
+    elif '2D TMx' in G.mode:
         G.ID[1, 0, :, :] = 0
         G.ID[1, 1, :, :] = 0
         G.ID[2, 0, :, :] = 0
@@ -104,24 +120,30 @@ def step_sources_receivers(G, currentmodelrun, modelend):
             r.zcoord = r.zcoordorigin + (currentmodelrun - 1) * G.rxsteps[2]
 
 
-def build_model_file(inputfile, currentmodelrun=1, modelend=1, messages=None):
-    """Build the model of an ``.in`` file for one model run of a B-scan."""
+def build_model_file(inputfile, currentmodelrun=1, modelend=1, messages=None, device_build=False):
+    """Build the model of an ``.in`` file for one model run of a B-scan (``device_build``: the
+    geometry arrays in GPU memory)."""
     usernamespace = {'c': c, 'e0': e0, 'm0': m0, 'z0': z0, 'number_model_runs': modelend,
                      'inputfile': os.path.abspath(inputfile), 'current_model_run': currentmodelrun}
     with open(inputfile) as f:
         lines = f.readlines()
-    G = build_grid(lines, usernamespace=usernamespace, inputfilename=inputfile, messages=messages)
+    G = build_grid(lines, usernamespace=usernamespace, inputfilename=inputfile, messages=messages,
+                   device_build=device_build)
     step_sources_receivers(G, currentmodelrun, modelend)
     return G
 
 
 def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write_output=True,
-              messages=None):
-    """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid."""
+              messages=None, device_build=False):
+    """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid.
+    ``device_build``: build the geometry arrays in GPU memory, where the solver takes them."""
     from .solver import solve_gb300
     from .outputs import write_hdf5_outputfile
-    G = build_model_file(inputfile, currentmodelrun, modelend, messages=messages)
+    G = build_model_file(inputfile, currentmodelrun, modelend, messages=messages,
+                         device_build=device_build)
     tsolve, mem = solve_gb300(currentmodelrun, modelend, G)
+    if getattr(G, 'geom', None) is not None:
+        G.geom.close()
     G.tsolve = tsolve
     G.memsolve = mem
     if write_output:

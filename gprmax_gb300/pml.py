@@ -165,6 +165,18 @@ def _face_average(G, face):
     return float(sumer) / ids.size, float(summr) / ids.size
 
 
+def _solid_face(G, axis, index):
+    """One plane of the solid array (read from the device for a grid built there)."""
+    geom = getattr(G, 'geom', None)
+    if geom is None:
+        return G.solid[(slice(None),) * axis + (index,)]
+    origin = [0, 0, 0]
+    shape = [G.nx, G.ny, G.nz]
+    origin[axis] = index
+    shape[axis] = 1
+    return geom.read(0, origin, shape).squeeze(axis)
+
+
 def build_pmls(G):
     """Create the slabs of ``G.pmlthickness`` and their coefficients (``pml.py:367-429``)."""
     G.pmls = []
@@ -176,19 +188,19 @@ def build_pmls(G):
                 pml = PML(G, ID=key, direction='xminus', xf=value, yf=G.ny, zf=G.nz)
             else:
                 pml = PML(G, ID=key, direction='xplus', xs=G.nx - value, xf=G.nx, yf=G.ny, zf=G.nz)
-            face = G.solid[pml.xs, :, :]
+            face = _solid_face(G, 0, pml.xs)
         elif key[0] == 'y':
             if key == 'y0':
                 pml = PML(G, ID=key, direction='yminus', yf=value, xf=G.nx, zf=G.nz)
             else:
                 pml = PML(G, ID=key, direction='yplus', ys=G.ny - value, xf=G.nx, yf=G.ny, zf=G.nz)
-            face = G.solid[:, pml.ys, :]
+            face = _solid_face(G, 1, pml.ys)
         else:
             if key == 'z0':
                 pml = PML(G, ID=key, direction='zminus', zf=value, xf=G.nx, yf=G.ny)
             else:
                 pml = PML(G, ID=key, direction='zplus', zs=G.nz - value, xf=G.nx, yf=G.ny, zf=G.nz)
-            face = G.solid[:, :, pml.zs]
+            face = _solid_face(G, 2, pml.zs)
         G.pmls.append(pml)
         averageer, averagemr = _face_average(G, face)
         pml.calculate_update_coeffs(averageer, averagemr, G)

@@ -116,7 +116,8 @@ def model_inputs(G, options=0):
     d.ntl = len(getattr(G, 'transmissionlines', []))
     d.options = options
     inp = {'desc': d,
-           'ID': np.ascontiguousarray(G.ID, dtype=np.uint32),
+           'ID': (np.ascontiguousarray(G.ID, dtype=np.uint32)
+                  if getattr(G, 'geom', None) is None else None),
            'coeffE': np.ascontiguousarray(G.updatecoeffsE, dtype=np.float32),
            'coeffH': np.ascontiguousarray(G.updatecoeffsH, dtype=np.float32),
            'coeffD': None, 'pml': [], 'sources': None, 'rx': None, 'snapshots': None}
@@ -162,8 +163,15 @@ class DeviceModel:
 
     def _upload(self):
         inp = self.inputs
-        self._check(self.lib.gbf_upload_materials(self.ctx, _ptr(inp['ID']), _ptr(inp['coeffE']),
-                                                  _ptr(inp['coeffH']), _ptr(inp['coeffD'])))
+        if inp['ID'] is None:
+            # IDs built in device memory: copied device to device
+            self._check(self.lib.gbf_upload_materials_geom(
+                self.ctx, self.G.geom.h, _ptr(inp['coeffE']), _ptr(inp['coeffH']),
+                _ptr(inp['coeffD'])))
+        else:
+            self._check(self.lib.gbf_upload_materials(
+                self.ctx, _ptr(inp['ID']), _ptr(inp['coeffE']), _ptr(inp['coeffH']),
+                _ptr(inp['coeffD'])))
         for slab, rows in inp['pml']:
             arr = (ctypes.c_void_p * 8)(*[r.ctypes.data for r in rows])
             self._check(self.lib.gbf_upload_pml(self.ctx, slab, arr))

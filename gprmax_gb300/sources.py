@@ -62,7 +62,8 @@ class VoltageSource(Source):
             return
         i, j, k = self.xcoord, self.ycoord, self.zcoord
         comp = 'xyz'.index(self.polarisation)
-        requirednumID = G.ID[comp, i, j, k]
+        geom = getattr(G, 'geom', None)
+        requirednumID = G.ID[comp, i, j, k] if geom is None else geom.id_at(comp, i, j, k)
         material = next(x for x in G.materials if x.numID == requirednumID)
         newmaterial = deepcopy(material)
         newmaterial.ID = material.ID + '+' + self.ID
@@ -75,7 +76,10 @@ class VoltageSource(Source):
             newmaterial.se += G.dy / (self.resistance * G.dx * G.dz)
         else:
             newmaterial.se += G.dz / (self.resistance * G.dx * G.dy)
-        G.ID[comp, i, j, k] = newmaterial.numID
+        if geom is None:
+            G.ID[comp, i, j, k] = newmaterial.numID
+        else:
+            geom.set_id(comp, i, j, k, newmaterial.numID)
         G.materials.append(newmaterial)
 
 class HertzianDipole(Source):

@@ -52,7 +52,7 @@ def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
 
 
 def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
-                    timewindow='12e-9', cylinder=True, pml=10, messages=False):
+                    timewindow='12e-9', cylinder=True, pml=10, messages=False, device_build=False):
     """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
 
     Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
@@ -84,10 +84,11 @@ def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed
     def soil(G):
         bins = fractal_volume((nx, ny, surface), 1.5, seed, nmat)
         build_voxels_array(G, (0, 0, 0), bins + first_soil, averaging=False)
-    return build_grid([l + '\n' for l in lines], messages=messages, geometry_hook=soil)
+    return build_grid([l + '\n' for l in lines], messages=messages, geometry_hook=soil,
+                      device_build=device_build)
 
 
-def throughput_cube(n, iterations=2000, seed=0, pml=10, messages=False):
+def throughput_cube(n, iterations=2000, seed=0, pml=10, messages=False, device_build=False):
     """N^3 cube at 1 mm with a seeded dielectric block filling the central half."""
     rng = np.random.default_rng(seed)
     er = rng.uniform(2, 20)
@@ -101,7 +102,7 @@ def throughput_cube(n, iterations=2000, seed=0, pml=10, messages=False):
              '#box: {0:g} {0:g} {0:g} {1:g} {1:g} {1:g} block'.format(L / 4, 3 * L / 4),
              '#hertzian_dipole: z {0:g} {0:g} {1:g} w'.format(c, L / 4 - 5 * d),
              '#rx: {0:g} {0:g} {1:g}'.format(c + 5 * d, L / 4 - 5 * d)]
-    return build_grid([l + '\n' for l in lines], messages=messages)
+    return build_grid([l + '\n' for l in lines], messages=messages, device_build=device_build)
 
 
 def bscan_input(shape, seed, position, dx=0.002, timewindow='10e-9', pml=10):

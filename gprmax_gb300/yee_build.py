@@ -6,7 +6,9 @@ edge uses its 2 neighbouring cells. Averaged materials are looked up, or created
 reference's name-matching rule (``create_electric_average`` :31-68,
 ``create_magnetic_average`` :71-108), in the order the reference's (i, j, k) loops first meet
 each neighbour combination, so new materials receive identical numbers. The loops are done as
-whole-array numpy operations; only distinct combinations are resolved one by one.
+whole-array numpy operations; only distinct combinations are resolved one by one. On a grid
+built in device memory the device classifies the edges and lists the combinations in the same
+order (:meth:`gprmax_gb300.devgeom.DeviceGeometry.components`); their resolution is the same.
 """
 import numpy as np
 
@@ -102,6 +104,9 @@ def _assign(G, comp, region, rigid, neighbours, resolve):
 
 def build_electric_components(G):
     """E-edge IDs for Ex, Ey, Ez in that order."""
+    if getattr(G, 'geom', None) is not None:
+        G.geom.components(True, _electric_average, G)
+        return
     s = G.solid
     ex, ey, ez, _, _, _ = _rigid_edges(G)
     # Ex: i in [0,nx), j in [1,ny), k in [1,nz)
@@ -117,6 +122,9 @@ def build_electric_components(G):
 
 def build_magnetic_components(G):
     """H-edge IDs for Hx, Hy, Hz in that order."""
+    if getattr(G, 'geom', None) is not None:
+        G.geom.components(False, _magnetic_average, G)
+        return
     s = G.solid
     _, _, _, hx, hy, hz = _rigid_edges(G)
     _assign(G, 3, (slice(1, G.nx), slice(0, G.ny), slice(0, G.nz)), hx,

@@ -258,6 +258,61 @@ int gbf_check_cell_division(float d);
 int gbf_sweep_boxes(int32_t nx, int32_t ny, int32_t nz, const int32_t thickness[6],
                     int32_t electric, int32_t* boxes);
 
+/* ---- model geometry in device memory ------------------------------------------------
+ * The solid, rigid and ID arrays of a grid (grid.py:157-169: solid and ID start as
+ * free_space = 1, nothing rigid) built on the device by the geometry primitives, then the
+ * per-edge IDs of the non-rigid edges from their neighbouring cells
+ * (yee_cell_build_ext.pyx:110-257). A box is six int32: first cell (xs, ys, zs) and extent
+ * (sx, sy, sz), inside the grid. Host arrays are C order with k fastest. Every call finishes its
+ * device work before it returns. */
+typedef struct gbf_geom gbf_geom;
+int gbf_geom_create(int32_t nx, int32_t ny, int32_t nz, gbf_geom** out);
+void gbf_geom_destroy(gbf_geom* geom);
+int gbf_geom_last_error(gbf_geom* geom, char* buf, size_t n);
+/* build_voxel (geometry_primitives_ext.pyx:314-377) on the cells of `box` where mask (uint8
+ * [sx][sy][sz], NULL: every cell) is non-zero, with material numbers num = (numID, numIDx,
+ * numIDy, numIDz); averaging != 0 only sets solid and clears the rigid flags. Replaces the cell
+ * loops of build_sphere (:873-928) and build_cylinder (:692-871) once the host has selected
+ * their cells. */
+int gbf_geom_cells(gbf_geom* geom, const int32_t box[6], const uint8_t* mask, const uint32_t num[4],
+                   int32_t averaging);
+/* build_box (geometry_primitives_ext.pyx:618-691): the cells as gbf_geom_cells, the IDs over
+ * the box's per-component node ranges (which differ from its cells' build_voxel edges). */
+int gbf_geom_box(gbf_geom* geom, const int32_t box[6], const uint32_t num[4], int32_t averaging);
+/* build_voxels_from_array (geometry_primitives_ext.pyx:934-980) for a block already clipped to
+ * the grid: data int16 [sx][sy][sz], negative = leave the cell; cell material numexist + value.
+ * Edges shared by cells of different materials keep the value of the last cell in (i, j, k)
+ * order, as the reference's loop leaves them. */
+int gbf_geom_voxels(gbf_geom* geom, const int32_t box[6], const int16_t* data, int32_t numexist,
+                    int32_t averaging);
+/* Rigid E edges with their material: recs int32 [n][5] = (component 0..2, i, j, k, numID), the
+ * edge's cell inside the grid. Replaces the build_edge_x/y/z and build_face_* writes of #edge
+ * and #plate (geometry_primitives_ext.pyx:30-312; set_rigid_Ex/Ey/Ez,
+ * yee_cell_setget_rigid_ext.pyx:72-97). */
+int gbf_geom_edges(gbf_geom* geom, int32_t n, const int32_t* recs);
+/* build_electric_components (electric != 0) or build_magnetic_components: every non-rigid edge
+ * whose neighbouring cells share one material takes it; the others are collected, in the
+ * reference's loop order (components in order, i, j, k), with a key of their neighbours'
+ * material numbers (E: four 16-bit numbers, first in the top bits; H: two), counts[3] per
+ * component. Fetch the keys with gbf_geom_averaged_keys, resolve them to material numbers on the
+ * host (create_electric_average / create_magnetic_average, yee_cell_build_ext.pyx:31-108) and
+ * hand them back with gbf_geom_resolve. Material numbers must fit in 16 bits. */
+int gbf_geom_components(gbf_geom* geom, int32_t electric, int64_t counts[3]);
+int gbf_geom_averaged_keys(gbf_geom* geom, uint64_t* keys);
+/* table: the distinct keys, strictly increasing; numbers: their material numbers */
+int gbf_geom_resolve(gbf_geom* geom, int64_t m, const uint64_t* table, const uint32_t* numbers);
+/* Fill or read a box of one array: 0 solid, 1 rigid flags (bits 0-11 rigidE[0..11], 12-17
+ * rigidH[0..5]), 2 + c the IDs of component c (Ex..Hz; node boxes within [nx+1][ny+1][nz+1]).
+ * out: uint32 [sx][sy][sz]. */
+int gbf_geom_fill(gbf_geom* geom, int32_t array, const int32_t box[6], uint32_t value);
+int gbf_geom_read(gbf_geom* geom, int32_t array, const int32_t box[6], uint32_t* out);
+/* the largest material number in the ID array */
+int gbf_geom_max_id(gbf_geom* geom, uint32_t* out);
+/* gbf_upload_materials with the ID array of a geometry built on the same device (copied on the
+ * device; the geometry can be destroyed afterwards). Every ID must be below nmat. */
+int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
+                              const float* coeffH, const float* coeffD);
+
 #ifdef __cplusplus
 }
 #endif

@@ -154,4 +154,23 @@ MODELS = {
 #rx: 0.021 0.016 0.026
 #rx: 0.017 0.016 0.012 deep Ex Ey Ez Hx Hy Hz
 """,
+    # every geometry primitive, with and without smoothing: boxes (isotropic and anisotropic),
+    # a sphere, oblique and axis-aligned cylinders, an edge, a plate, a resistive voltage source
+    'smoothed': BASE.format(dom='0.024 0.022 0.020', steps=80) + """#pml_cells: 4
+#material: 3 0.001 1 0 a
+#material: 5 0.002 1.5 0.001 b
+#material: 8 0 1 0 c
+#box: 0.003 0.003 0.003 0.018 0.016 0.012 a
+#sphere: 0.012 0.011 0.010 0.005 b
+#cylinder: 0.004 0.010 0.004 0.020 0.010 0.016 0.003 c
+#cylinder: 0.006 0.004 0.002 0.006 0.004 0.018 0.002 b n
+#box: 0.014 0.002 0.014 0.020 0.008 0.019 a b c
+#edge: 0.002 0.002 0.002 0.010 0.002 0.002 pec
+#plate: 0.004 0.018 0.004 0.012 0.018 0.010 c
+#waveform: ricker 1 2e9 w
+#voltage_source: z 0.012 0.011 0.010 50 w
+#hertzian_dipole: x 0.008 0.014 0.015 w
+#rx: 0.010 0.010 0.010
+#rx: 0.016 0.012 0.006 r2 Ex Ey Ez Hx Hy Hz
+""",
 }

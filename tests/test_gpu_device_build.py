@@ -1,0 +1,92 @@
+"""GPU: the geometry built in device memory (``gbf_geom_*``). For every golden fixture the
+device-built ID array must hash to the reference's, with the same materials and coefficient
+tables, and the model solved from it must give the reference's traces bit for bit. For every
+test model and for scaled-down benchmark workloads, the device build must equal the host build
+array for array (solid, rigid flags, IDs, materials)."""
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from models import MODELS
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden')
+FIXTURES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, '*.npz')))
+
+
+@pytest.mark.parametrize('name', FIXTURES)
+def test_device_build_reproduces_reference_model(native, name):
+    from gprmax_gb300.model import build_grid
+    from gprmax_gb300.solver import DeviceModel
+    g = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
+    D = build_grid(str(g['input']).splitlines(True), messages=False, device_build=True)
+    try:
+        ids = np.ascontiguousarray(D.geom.ids())
+        assert hashlib.sha256(ids.tobytes()).hexdigest() == str(g['ID_sha256'])
+        assert len(D.materials) == int(g['nmat'])
+        np.testing.assert_array_equal(D.updatecoeffsE, g['coeffE'])
+        np.testing.assert_array_equal(D.updatecoeffsH, g['coeffH'])
+        dm = DeviceModel(D)
+        dm.run()
+        rx = dm.receivers()
+        dm.close()
+    finally:
+        D.geom.close()
+    from gprmax_gb300.receivers import OUTPUT_INDEX
+    checked = 0
+    for n, r in enumerate(D.rxs):
+        for out in r.outputs:
+            key = 'rx{}_{}'.format(n + 1, out)
+            if key in g:
+                np.testing.assert_array_equal(rx[OUTPUT_INDEX[out], :, n], g[key], err_msg=key)
+                checked += 1
+    assert checked == sum(1 for k in g if k.startswith('rx'))
+
+
+def _same(G, D):
+    assert [m.ID for m in G.materials] == [m.ID for m in D.materials]
+    np.testing.assert_array_equal(G.updatecoeffsE, D.updatecoeffsE)
+    np.testing.assert_array_equal(G.updatecoeffsH, D.updatecoeffsH)
+    np.testing.assert_array_equal(G.solid, D.geom.solid())
+    rE, rH = D.geom.rigid()
+    np.testing.assert_array_equal(G.rigidE, rE)
+    np.testing.assert_array_equal(G.rigidH, rH)
+    for c in range(6):
+        np.testing.assert_array_equal(G.ID[c], D.geom.ids(c))
+
+
+@pytest.mark.parametrize('name', sorted(MODELS))
+def test_device_build_equals_host_build(native, name):
+    from gprmax_gb300.model import build_grid
+    lines = MODELS[name].splitlines(True)
+    G = build_grid(lines, messages=False)
+    D = build_grid(lines, messages=False, device_build=True)
+    try:
+        _same(G, D)
+    finally:
+        D.geom.close()
+
+
+@pytest.mark.parametrize('which', ['soil', 'cube', 'bscan'])
+def test_device_build_equals_host_build_on_workloads(native, which):
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.model import build_grid
+    if which == 'soil':
+        kw = dict(nx=96, ny=88, nz=48, surface=36, timewindow=20)
+        G = workloads.dispersive_soil(**kw)
+        D = workloads.dispersive_soil(device_build=True, **kw)
+    elif which == 'cube':
+        G = workloads.throughput_cube(72, iterations=10)
+        D = workloads.throughput_cube(72, iterations=10, device_build=True)
+    else:
+        lines = workloads.bscan_input((90, 80, 60), seed=5, position=3)
+        G = build_grid(lines, messages=False)
+        D = build_grid(lines, messages=False, device_build=True)
+    try:
+        _same(G, D)
+    finally:
+        D.geom.close()
