@@ -60,11 +60,12 @@ typedef void (*HKernFn)(StepParams);
 typedef void (*EKernFn)(StepParams);
 typedef void (*BKernFn)(BatchParams);
 // per-kind kernel tables (kernels_inst.cu, one object per PML kind)
-void kernels_pk0(int np, int idp, HKernFn* h, EKernFn* e);
-void kernels_pk1(int np, int idp, HKernFn* h, EKernFn* e);
-void kernels_pk2(int np, int idp, HKernFn* h, EKernFn* e);
-void kernels_pk3(int np, int idp, HKernFn* h, EKernFn* e);
-void kernels_pk4(int np, int idp, HKernFn* h, EKernFn* e);
+// idp: material-ID layout (1 packed, 3 plain); uniform_h: every material has the same H row
+void kernels_pk0(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
+void kernels_pk1(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
+void kernels_pk2(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
+void kernels_pk3(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
+void kernels_pk4(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
 // batched forms (kernels_inst.cu)
 void batch_kernels_pk0(int np, int idp, BKernFn* h, BKernFn* e);
 void batch_kernels_pk1(int np, int idp, BKernFn* h, BKernFn* e);
@@ -351,13 +352,28 @@ __device__ __forceinline__ bool node_has_source(int idx, int n, const int* inl, 
   return hit;
 }
 
+// Coefficients of the H half-step: per-material rows (C4: DA, DBx, DBy, DBz; Cs: srcm) indexed
+// by the node's material numbers, or, with IDP == 0 (every material has the same H row, as in
+// any model without magnetic materials), that one row held in registers and no material
+// numbers loaded at all.
+struct HCoef {
+  const float4* C4;
+  const float* Cs;
+  float4 u;
+  float us;
+};
+template <int IDP>
+__device__ __forceinline__ float4 hrow(const HCoef& c, uint32_t m) { return IDP == 0 ? c.u : c.C4[m]; }
+template <int IDP>
+__device__ __forceinline__ float hsrcm(const HCoef& c, uint32_t m) { return IDP == 0 ? c.us : c.Cs[m]; }
+
 // H update of one node: main update (update_magnetic), slab corrections in slab order, sources.
 // where[a] / pr[a]: slab membership and profile index along each axis (axis_member; 0 outside
 // the PML). The X values of the node's slabs are formed first (they depend only on the E
 // differences and the Phi state), then each component takes its main update and its
 // corrections in the reference's order.
-template <int PK, bool CORE>
-__device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, const float* Cs,
+template <int PK, int IDP, bool CORE>
+__device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
                                        int i, int j, int k, bool src, int it, const int* where,
                                        const int* pr, float dEz_y, float dEy_z, float dEx_z,
                                        float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
@@ -381,12 +397,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
     const bool mainu = ipos && jin && kin && hx2;
     const bool pml = PK != PML_NONE && (where[1] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = C4[mx];
+    const float4 c = hrow<IDP>(hc, mx);
     const float Fo = hx;
     float F = c.x * Fo - c.z * dEz_y + c.w * dEy_z;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 0>(F, Cs[mx], where, XA, XB);
-    if (src) F = apply_h_sources(F, 3, i, j, k, it, Cs[mx], p);
+    if (pml) F = apply_pml<false, 0>(F, hsrcm<IDP>(hc, mx), where, XA, XB);
+    if (src) F = apply_h_sources(F, 3, i, j, k, it, hsrcm<IDP>(hc, mx), p);
     hx = F;
   }
   // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
@@ -394,12 +410,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
     const bool mainu = iin && jpos && kin && hy2;
     const bool pml = PK != PML_NONE && (where[0] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = C4[my];
+    const float4 c = hrow<IDP>(hc, my);
     const float Fo = hy;
     float F = c.x * Fo - c.w * dEx_z + c.y * dEz_x;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 1>(F, Cs[my], where, XA, XB);
-    if (src) F = apply_h_sources(F, 4, i, j, k, it, Cs[my], p);
+    if (pml) F = apply_pml<false, 1>(F, hsrcm<IDP>(hc, my), where, XA, XB);
+    if (src) F = apply_h_sources(F, 4, i, j, k, it, hsrcm<IDP>(hc, my), p);
     hy = F;
   }
   // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs along x and y
@@ -407,12 +423,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
     const bool mainu = iin && jin && (k >= 1) && hz2;
     const bool pml = PK != PML_NONE && (where[0] || where[1]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = C4[mz];
+    const float4 c = hrow<IDP>(hc, mz);
     const float Fo = hz;
     float F = c.x * Fo - c.y * dEy_x + c.z * dEx_y;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 2>(F, Cs[mz], where, XA, XB);
-    if (src) F = apply_h_sources(F, 5, i, j, k, it, Cs[mz], p);
+    if (pml) F = apply_pml<false, 2>(F, hsrcm<IDP>(hc, mz), where, XA, XB);
+    if (src) F = apply_h_sources(F, 5, i, j, k, it, hsrcm<IDP>(hc, mz), p);
     hz = F;
   }
 }
@@ -420,7 +436,7 @@ __device__ __forceinline__ void h_node(const StepParams& p, const float4* C4, co
 // One H node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j
 // in [1, n-1] and outside the x and y slabs), so only k decides neighbours and PML terms.
 template <int PK, int IDP, bool CORE>
-__device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, const float* Cs,
+__device__ __forceinline__ void h_site(const StepParams& p, const HCoef& hc,
                                        int i, int j, int k, int it) {
   const int nx = p.nx, ny = p.ny, nz = p.nz, sx = p.sx, sy = p.sy;
   const int idx = i * sx + j * sy + k;
@@ -439,8 +455,10 @@ __device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, co
   const float ey_k = kin ? __ldg(Ey + idx + 1) : 0.f;
   const float ey_n = iin ? __ldg(Ey + idx + sx) : 0.f;
   const float ez_n = iin ? __ldg(Ez + idx + sx) : 0.f;
-  uint32_t mx, my, mz;
-  if (IDP == 1) {
+  uint32_t mx = 0, my = 0, mz = 0;
+  if (IDP == 0) {
+    // one H row for every material: no material numbers needed
+  } else if (IDP == 1) {
     const uint32_t w = __ldg(p.PH + idx);
     mx = w & kPackMask;
     my = (w >> kPackBits) & kPackMask;
@@ -460,7 +478,7 @@ __device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, co
     where[2] = axis_member<false>(k, nz, p.slab[2].T, p.slab[5].T, pr[2]);
   }
   const bool src = p.nsrcH && node_has_source(idx, p.nsrcH, p.srcqH, p.srcH, sx, sy);
-  h_node<PK, CORE>(p, C4, Cs, i, j, k, src, it, where, pr, ez_j - ez_c, ey_k - ey_c, ex_k - ex_c,
+  h_node<PK, IDP, CORE>(p, hc, i, j, k, src, it, where, pr, ez_j - ez_c, ey_k - ey_c, ex_k - ex_c,
                    ez_n - ez_c, ey_n - ey_c, ex_j - ex_c, mx, my, mz, hx, hy, hz);
   Hx[idx] = hx;
   Hy[idx] = hy;
@@ -473,7 +491,7 @@ __device__ __forceinline__ void h_site(const StepParams& p, const float4* C4, co
 // node index and base the position of the model's first node there; returns q after the
 // model's last node.
 template <int PK, int IDP>
-__device__ __forceinline__ int h_sweep(const StepParams& p, const float4* C4, const float* Cs,
+__device__ __forceinline__ int h_sweep(const StepParams& p, const HCoef& hc,
                                        int q, int base, int stride, int it) {
   q -= base;
   {
@@ -482,7 +500,7 @@ __device__ __forceinline__ int h_sweep(const StepParams& p, const float4* C4, co
     if (q < end) {
       BoxWalk w(q - B.start, stride, B);
       for (; q < end; q += stride, w.advance(B))
-        h_site<PK, IDP, true>(p, C4, Cs, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
+        h_site<PK, IDP, true>(p, hc, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
   }
 #pragma unroll 1
@@ -492,7 +510,7 @@ __device__ __forceinline__ int h_sweep(const StepParams& p, const float4* C4, co
     if (q >= end) continue;
     BoxWalk w(q - B.start, stride, B);
     for (; q < end; q += stride, w.advance(B))
-      h_site<PK, IDP, false>(p, C4, Cs, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
+      h_site<PK, IDP, false>(p, hc, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
   return q + base;
 }
@@ -507,11 +525,14 @@ h_half_step(const __grid_constant__ StepParams p) {
     stage_tables(p, false, s4, ss, nullptr);
     __syncthreads();
   }
-  const float4* C4 = p.smem ? s4 : p.cH4;
-  const float* Cs = p.smem ? ss : p.cHs;
+  HCoef hc;
+  hc.C4 = p.smem ? s4 : p.cH4;
+  hc.Cs = p.smem ? ss : p.cHs;
+  hc.u = IDP == 0 ? hc.C4[0] : make_float4(0.f, 0.f, 0.f, 0.f);
+  hc.us = IDP == 0 ? hc.Cs[0] : 0.f;
   int it = 0;
   if (p.nsrcH) it = *p.d_it;
-  h_sweep<PK, IDP>(p, C4, Cs, blockIdx.x * blockDim.x + threadIdx.x, 0, gridDim.x * blockDim.x, it);
+  h_sweep<PK, IDP>(p, hc, blockIdx.x * blockDim.x + threadIdx.x, 0, gridDim.x * blockDim.x, it);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -551,10 +572,13 @@ h_half_step_batch(const __grid_constant__ BatchParams bp) {
     float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
     if (p.smem) stage_tables(p, false, s4, ss, nullptr);
     __syncthreads();
-    const float4* C4 = p.smem ? s4 : p.cH4;
-    const float* Cs = p.smem ? ss : p.cHs;
+    HCoef hc;
+    hc.C4 = p.smem ? s4 : p.cH4;
+    hc.Cs = p.smem ? ss : p.cHs;
+    hc.u = make_float4(0.f, 0.f, 0.f, 0.f);
+    hc.us = 0.f;
     const int it = p.nsrcH ? *p.d_it : 0;
-    q = h_sweep<PK, IDP>(p, C4, Cs, q, __ldg(bp.rangeH + m), stride, it);
+    q = h_sweep<PK, IDP>(p, hc, q, __ldg(bp.rangeH + m), stride, it);
     if (q < end) q += stride;   // past the model's last node, inside its padding
   }
 }

@@ -34,6 +34,7 @@ struct gbf_ctx {
   uint32_t* PH = nullptr;      // packed H IDs
   unsigned char* disp = nullptr;   // per material: has dispersive poles
   int idp = 3;                 // 1: packed IDs, 3: three ID arrays per half-step
+  int uniform_h = 0;           // every material has the same H row: the H half-step reads no IDs
   float4* cE4 = nullptr;       // [nmat] CA, CBx, CBy, CBz
   float* cEs = nullptr;        // [nmat] srce
   float4* cH4 = nullptr;
@@ -387,6 +388,13 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
 static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
                          const float* coeffD) {
   const int nmat = ctx->d.nmat;
+  // one H row for every material (no magnetic materials): the H half-step then needs no IDs
+  int uni = 1;
+  for (int m = 1; m < nmat && uni; ++m)
+    uni = memcmp(coeffH + 5 * m, coeffH, 5 * sizeof(float)) == 0;
+  ctx->uniform_h = uni;
+  ctx->grid_h = 0;
+  invalidate_graph(ctx);
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -679,13 +687,13 @@ typedef HKernFn HKern;
 typedef EKernFn EKern;
 
 static void pick_kernels(gbf_ctx* ctx, HKern* h, EKern* e) {
-  const int np = ctx->d.maxpoles, idp = ctx->idp;
+  const int np = ctx->d.maxpoles, idp = ctx->idp, uh = ctx->uniform_h;
   switch (pml_kind(ctx->d)) {
-    case PML_HORI1: kernels_pk1(np, idp, h, e); break;
-    case PML_HORI2: kernels_pk2(np, idp, h, e); break;
-    case PML_MRI1: kernels_pk3(np, idp, h, e); break;
-    case PML_MRI2: kernels_pk4(np, idp, h, e); break;
-    default: kernels_pk0(np, idp, h, e); break;
+    case PML_HORI1: kernels_pk1(np, idp, uh, h, e); break;
+    case PML_HORI2: kernels_pk2(np, idp, uh, h, e); break;
+    case PML_MRI1: kernels_pk3(np, idp, uh, h, e); break;
+    case PML_MRI2: kernels_pk4(np, idp, uh, h, e); break;
+    default: kernels_pk0(np, idp, uh, h, e); break;
   }
 }
 

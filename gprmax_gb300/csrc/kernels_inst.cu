@@ -23,8 +23,9 @@ static EKernFn e_for(int np) {
   }
 }
 
-// Kernels for PML kind GBF_PK, `np` dispersive poles and ID layout `idp` (1 packed, 3 plain).
-void GBF_CAT(kernels_pk, GBF_PK)(int np, int idp, HKernFn* h, EKernFn* e) {
+// Kernels for PML kind GBF_PK, `np` dispersive poles and ID layout `idp` (1 packed, 3 plain);
+// with `uniform_h` the H half-step takes the one H row of every material (no IDs).
+void GBF_CAT(kernels_pk, GBF_PK)(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e) {
   if (idp == 1) {
     *h = h_half_step<GBF_PK, 1>;
     *e = e_for<1>(np);
@@ -32,6 +33,7 @@ void GBF_CAT(kernels_pk, GBF_PK)(int np, int idp, HKernFn* h, EKernFn* e) {
     *h = h_half_step<GBF_PK, 3>;
     *e = e_for<3>(np);
   }
+  if (uniform_h) *h = h_half_step<GBF_PK, 0>;
 }
 
 template <int IDP>
