@@ -36,21 +36,34 @@ sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 
 METRIC = 'Mcells/s'
 WORKLOAD = 'dispersive_soil_400x400x200_debye50_pml10'
-# ncu summary of the E half-step on the soil workload; its `dram_bytes_per_cell:` line gives the
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch per cell
+# ncu summaries of the E half-step on the soil workload: the full-size capture's
+# `dram_bytes_per_launch:` line (dram__bytes_read.sum + dram__bytes_write.sum of one launch of
+# the 400x400x200 workload), else the small capture's `dram_bytes_per_cell:` line scaled by cells
+TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'half_step_traffic_dispersive_soil_400x400x200.md')
 TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'e_half_step_dispersive_soil_256x256x128.md')
 
 
-def measured_traffic(cells):
-    """DRAM bytes of one E half-step launch over `cells` cells, scaled from the ncu capture."""
+def _profile_value(path, key):
     try:
-        with open(TRAFFIC_PROFILE) as f:
+        with open(path) as f:
             for line in f:
-                if line.startswith('dram_bytes_per_cell:'):
-                    return int(round(float(line.split(':')[1]) * cells))
+                if line.startswith(key + ':'):
+                    return float(line.split(':')[1])
     except OSError:
         pass
     return None
+
+
+def measured_traffic(cells):
+    """DRAM bytes of one E half-step launch over `cells` cells (ncu), and where they came from."""
+    full = _profile_value(TRAFFIC_FULL, 'dram_bytes_per_launch')
+    full_cells = _profile_value(TRAFFIC_FULL, 'cells')
+    if full is not None and full_cells == cells:
+        return int(full), 'ncu, full-size launch'
+    per_cell = _profile_value(TRAFFIC_PROFILE, 'dram_bytes_per_cell')
+    if per_cell is not None:
+        return int(round(per_cell * cells)), 'ncu, 256x256x128 launch scaled by cells'
+    return None, None
 
 
 def load_peaks():
@@ -74,7 +87,8 @@ def algorithmic_bytes(G):
     """Bytes per launch each half-step must move, in the device representation: fp32 fields,
     the node's three material IDs packed in one 32-bit word (nmat <= 1024; otherwise three
     uint32 IDs), complex64 dispersive state. Per node: H half-step reads E and H and the ID word
-    and writes H (12 + 12 + 4 + 12 = 40 B); E half-step the same (40 B) plus, on nodes whose
+    and writes H (12 + 12 + 4 + 12 = 40 B; 36 B when every material has the same H row and no
+    ID is needed); E half-step the same (40 B) plus, on nodes whose
     materials have poles, 8 B per pole and component read and written (48 B per pole). PML adds
     per slab node and CFS order two Phi values read and written (16 B) in each half-step.
     Neighbour values along j, k and x are re-reads of the same arrays (cache hits)."""
@@ -82,7 +96,10 @@ def algorithmic_bytes(G):
     idb = 4 if len(G.materials) <= 1024 else 12
     order = max(len(G.cfs), 1)
     pml = slab_cells(G) * 16 * order
-    h = cells * (36 + idb) + pml
+    # the H half-step reads no IDs when every material has the same H row (no magnetic ones)
+    hrows = np.asarray(G.updatecoeffsH)
+    uniform_h = bool((hrows.view(np.uint32) == hrows[:1].view(np.uint32)).all())
+    h = cells * (36 + (0 if uniform_h else idb)) + pml
     e = cells * (36 + idb) + pml
     if G.maxpoles:
         disp = np.zeros(len(G.materials), dtype=bool)
@@ -260,7 +277,7 @@ def run_gb300(args):
     t_e = ms_e / npf / 1e3
     t_h = ms_h / npf / 1e3
     achieved = bytes_e / t_e / 1e9
-    traffic = measured_traffic(cells)
+    traffic, traffic_src = measured_traffic(cells)
     if rank != 0:
         return
     out = {
@@ -278,7 +295,7 @@ def run_gb300(args):
         'gpu_launches': 3 * K,
         'roofline': {'bound': 'hbm', 'kernel': 'e_half_step', 'achieved': round(achieved, 1),
                      'peak': peak, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
-                     'traffic': traffic, 'peak_source': peak_kind,
+                     'traffic': traffic, 'traffic_source': traffic_src, 'peak_source': peak_kind,
                      'bytes_per_launch': bytes_e, 'ms_per_launch': t_e * 1e3},
         'kernels': {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
                                     'GBps': round(bytes_h / t_h / 1e9, 1)},

@@ -134,7 +134,7 @@ def build_model_file(inputfile, currentmodelrun=1, modelend=1, messages=None, de
 
 
 def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write_output=True,
-              messages=None, device_build=False):
+              messages=None, device_build=True):
     """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid.
     ``device_build``: build the geometry arrays in GPU memory, where the solver takes them."""
     from .solver import solve_gb300

@@ -90,3 +90,24 @@ def test_device_build_equals_host_build_on_workloads(native, which):
         _same(G, D)
     finally:
         D.geom.close()
+
+
+@pytest.mark.parametrize('name', ['smoothed', 'fractal', 'debye1'])
+def test_run_model_writes_the_reference_traces(native, name, tmp_path):
+    """The public driver (``run_model``: device geometry build, solve, ``.out`` file) against
+    the reference's traces."""
+    from gprmax_gb300.model import run_model
+    from gprmax_gb300.outputs import read_outputfile
+    g = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
+    inputfile = tmp_path / (name + '.in')
+    inputfile.write_text(str(g['input']))
+    G = run_model(str(inputfile), messages=False)
+    rxs, attrs = read_outputfile(G.outputfile)
+    checked = 0
+    for n in range(len(G.rxs)):
+        for out, v in rxs['rx{}'.format(n + 1)].items():
+            key = 'rx{}_{}'.format(n + 1, out)
+            if key in g:
+                np.testing.assert_array_equal(v, g[key], err_msg=key)
+                checked += 1
+    assert checked == sum(1 for k in g if k.startswith('rx'))
