@@ -3,9 +3,9 @@
 Single-use commands follow ``gprMax/input_cmds_singleuse.py:41-336``, multi-use commands
 ``input_cmds_multiuse.py:45-851`` and geometry commands ``input_cmds_geometry.py:51-1527`` for
 the commands this solver core supports. Parameter checks raise :class:`CmdInputError` with the
-reference's messages. ``#fractal_box`` is built with its materials from ``#soil_peplinski`` (or
-the reference's errors); its rough-surface, surface-water and grass modifiers are rejected
-with an explicit error.
+reference's messages. ``#fractal_box`` is built with its materials from ``#soil_peplinski``,
+with ``#add_surface_roughness`` and ``#add_surface_water``; ``#add_grass`` is rejected with an
+explicit error.
 """
 import decimal as d
 import inspect
@@ -16,7 +16,7 @@ from scipy import interpolate
 
 from .constants import c, floattype, z0
 from .exceptions import CmdInputError
-from .fractals import FractalVolume, PeplinskiSoil
+from .fractals import FractalSurface, FractalVolume, PeplinskiSoil
 from .materials import Material
 from .pml import CFS, CFSParameter, PML
 from .receivers import Rx, allocate_outputs
@@ -765,9 +765,33 @@ def _fractal_box(G, tmp, geometry):
 
     for other in geometry:
         m = other.split()
-        if m and m[0] in _FRACTAL_MODIFIERS and volume.ID in m[1:]:
-            raise CmdInputError('{} is not supported by the GB300 solver core'.format(m[0].rstrip(':')))
+        if not m:
+            continue
+        if m[0] == '#add_surface_roughness:':
+            _surface_roughness(G, m, volume)
+        elif m[0] == '#add_surface_water:':
+            _surface_water(G, m, volume)
+        elif m[0] == '#add_grass:' and volume.ID in m[1:]:
+            raise CmdInputError('#add_grass is not supported by the GB300 solver core')
 
+    if volume.fractalsurfaces:
+        # the box grows to take in its rough surfaces; the mask picks soil, water or nothing
+        volume.extend_for_surfaces()
+        if nbins == 1:
+            vol = np.ones((volume.nx, volume.ny, volume.nz), dtype=floattype)
+            vol *= next(x.numID for x in G.materials if x.ID == volume.operatingonID)
+        else:
+            if not mixingmodel:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' needs a mixing model to bin {} materials from; {} is a single material'.format(nbins, tmp[12]))
+            vol = volume.generate_fractal_volume()
+            vol += mixingmodel.startmaterialnum
+        mask = volume.generate_volume_mask()
+        waternumID = next((x.numID for x in G.materials if x.ID == 'water'), 0)
+        data = vol.astype('int16', order='C')
+        cells = np.where(mask == 1, data, np.where(mask == 2, np.int16(waternumID), np.int16(-1)))
+        geo.build_voxels_array(G, (volume.xs, volume.ys, volume.zs), cells.astype(np.int16),
+                               averaging)
+        return
     if nbins == 1:
         raise CmdInputError("'" + ' '.join(tmp) + "'" + ' is being used with a single material and no modifications, therefore please use a #box command instead.')
     if not mixingmodel:
@@ -775,3 +799,133 @@ def _fractal_box(G, tmp, geometry):
     vol = volume.generate_fractal_volume()
     vol += mixingmodel.startmaterialnum
     geo.build_voxels_array(G, (xs, ys, zs), vol.astype('int16', order='C'), averaging)
+
+
+def _surface_extent(G, tmp):
+    xs = round_value(float(tmp[1]) / G.dx)
+    xf = round_value(float(tmp[4]) / G.dx)
+    ys = round_value(float(tmp[2]) / G.dy)
+    yf = round_value(float(tmp[5]) / G.dy)
+    zs = round_value(float(tmp[3]) / G.dz)
+    zf = round_value(float(tmp[6]) / G.dz)
+    for v, n, lu, ax, dl in ((xs, G.nx, 'lower', 'x', G.dx), (xf, G.nx, 'upper', 'x', G.dx),
+                             (ys, G.ny, 'lower', 'y', G.dy), (yf, G.ny, 'upper', 'y', G.dy),
+                             (zs, G.nz, 'lower', 'z', G.dz), (zf, G.nz, 'upper', 'z', G.dz)):
+        if v < 0 or v > n:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the {} {}-coordinate {:g}m is not within the model domain'.format(lu, ax, v * dl))
+    if xs > xf or ys > yf or zs > zf:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the lower coordinates should be less than the upper coordinates')
+    return xs, xf, ys, yf, zs, zf
+
+
+def _surface_face(tmp, volume, xs, xf, ys, yf, zs, zf):
+    """The face of the fractal box the surface lies on: (axis, side) with side 'minus'/'plus'."""
+    lo = (xs, ys, zs)
+    hi = (xf, yf, zf)
+    vlo = (volume.xs, volume.ys, volume.zs)
+    vhi = (volume.xf, volume.yf, volume.zf)
+    for axis in range(3):
+        if lo[axis] == hi[axis]:
+            others = [a for a in range(3) if a != axis]
+            if any(lo[a] == hi[a] for a in others):
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' dimensions are not specified correctly')
+            if lo[axis] != vlo[axis] and lo[axis] != vhi[axis]:
+                raise CmdInputError("'" + ' '.join(tmp) + "'" + ' can only be used on the external surfaces of a fractal box')
+            if lo[axis] == vlo[axis]:
+                return axis, 'minus'
+            if hi[axis] == vhi[axis]:
+                return axis, 'plus'
+            return axis, None
+    raise CmdInputError("'" + ' '.join(tmp) + "'" + ' dimensions are not specified correctly')
+
+
+def _surface_roughness(G, tmp, volume):
+    """``#add_surface_roughness`` on a face of ``volume`` (``input_cmds_geometry.py:893-1006``)."""
+    if len(tmp) < 13:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least twelve parameters')
+    elif len(tmp) == 13:
+        seed = None
+    elif len(tmp) == 14:
+        seed = int(tmp[13])
+    else:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' too many parameters have been given')
+    if tmp[12] != volume.ID:
+        return
+    xs, xf, ys, yf, zs, zf = _surface_extent(G, tmp)
+    if float(tmp[7]) < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the fractal dimension')
+    if float(tmp[8]) < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the fractal weighting in the first direction of the surface')
+    if float(tmp[9]) < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the fractal weighting in the second direction of the surface')
+    axis, side = _surface_face(tmp, volume, xs, xf, ys, yf, zs, zf)
+    dl = (G.dx, G.dy, G.dz)[axis]
+    ax = 'xyz'[axis]
+    n = (G.nx, G.ny, G.nz)[axis]
+    vlo = (volume.xs, volume.ys, volume.zs)[axis]
+    vhi = (volume.xf, volume.yf, volume.zf)[axis]
+    fractalrange = (round_value(float(tmp[10]) / dl), round_value(float(tmp[11]) / dl))
+    if side == 'minus':
+        # (the reference's message names the x direction for a z-minus surface too)
+        if fractalrange[0] < 0 or fractalrange[1] > vhi:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' cannot apply fractal surface to fractal box as it would exceed either the upper coordinates of the fractal box or the domain in the {} direction'.format('x' if ax == 'z' else ax))
+    elif side == 'plus':
+        if fractalrange[0] < vlo or fractalrange[1] > n:
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' cannot apply fractal surface to fractal box as it would exceed either the lower coordinates of the fractal box or the domain in the {} direction'.format(ax))
+    surface = FractalSurface(xs, xf, ys, yf, zs, zf, float(tmp[7]), seed)
+    surface.surfaceID = ax + side
+    surface.fractalrange = fractalrange
+    surface.operatingonID = volume.ID
+    surface.weighting = np.array([float(tmp[8]), float(tmp[9])])
+    if surface.surfaceID in [x.surfaceID for x in volume.fractalsurfaces]:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' has already been used on the {} surface'.format(surface.surfaceID))
+    surface.generate_fractal_surface()
+    volume.fractalsurfaces.append(surface)
+    _log(G, 'Fractal surface from {:g}m, {:g}m, {:g}m, to {:g}m, {:g}m, {:g}m with fractal '
+            'dimension {:g}, fractal weightings {:g}, {:g}, fractal seeding {}, and range {:g}m '
+            'to {:g}m, added to {}.'.format(xs * G.dx, ys * G.dy, zs * G.dz, xf * G.dx,
+                                           yf * G.dy, zf * G.dz, surface.dimension,
+                                           surface.weighting[0], surface.weighting[1],
+                                           surface.seed, float(tmp[10]), float(tmp[11]),
+                                           surface.operatingonID))
+
+
+def _surface_water(G, tmp, volume):
+    """``#add_surface_water`` on a rough surface of ``volume`` (``input_cmds_geometry.py:1008-1109``):
+    water (the built-in single-pole Debye material) up to a fill depth."""
+    if len(tmp) != 9:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires exactly eight parameters')
+    if tmp[8] != volume.ID:
+        return
+    xs, xf, ys, yf, zs, zf = _surface_extent(G, tmp)
+    depth = float(tmp[7])
+    if depth <= 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for the depth of water')
+    axis, side = _surface_face(tmp, volume, xs, xf, ys, yf, zs, zf)
+    dl = (G.dx, G.dy, G.dz)[axis]
+    filldepthcells = round_value(depth / dl)
+    filldepth = filldepthcells * dl
+    requested = 'xyz'[axis] + (side or '')
+    surface = next((x for x in volume.fractalsurfaces if x.surfaceID == requested), None)
+    if not surface:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' specified surface {} does not have a rough surface applied'.format(requested))
+    surface.filldepth = filldepthcells
+    if surface.filldepth < surface.fractalrange[0] or surface.filldepth > surface.fractalrange[1]:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a value for the depth of water that lies with the range of the requested surface roughness')
+    if not any(x.ID == 'water' for x in G.materials):
+        m = Material(len(G.materials), 'water')
+        m.averagable = False
+        m.type = 'builtin, debye'
+        m.er = Material.watereri
+        m.poles = 1
+        m.deltaer.append(Material.waterdeltaer)
+        m.tau.append(Material.watertau)
+        G.materials.append(m)
+        if G.maxpoles == 0:
+            G.maxpoles = 1
+    water = next(x for x in G.materials if x.ID == 'water')
+    if next((x for x in water.tau if x < G.dt), None):
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires the time step for the model to be less than the relaxation time required to model water.')
+    _log(G, 'Water on surface from {:g}m, {:g}m, {:g}m, to {:g}m, {:g}m, {:g}m with depth {:g}m, '
+            'added to {}.'.format(xs * G.dx, ys * G.dy, zs * G.dz, xf * G.dx, yf * G.dy,
+                                  zf * G.dz, filldepth, surface.operatingonID))

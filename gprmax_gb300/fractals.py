@@ -20,6 +20,75 @@ from .constants import floattype
 from .materials import Material
 
 
+def _fractal_filter(A, w, v1, dimension):
+    """A / r^D with r the weighted distance of each index from v1 (``fractals_generate_ext.pyx``
+    ``generate_fractal2D`` :24-50 and ``generate_fractal3D`` :53-86). Every power goes through
+    the C library's pow (math.pow), as the compiled filter does (numpy's vectorised power
+    differs from it in the last bit); D is rounded to float32 as the extension's ``float D``
+    argument; r^D = 0 becomes 0.9; the complex value is divided by the real B component-wise."""
+    cpow = np.frompyfunc(math.pow, 2, 1)
+    nd = A.ndim
+    d = [cpow(w[a] * np.arange(A.shape[a], dtype=np.float64) - v1[a], 2.0).astype(np.float64)
+         for a in range(nd)]
+    if nd == 3:
+        s = d[0][:, None, None] + d[1][None, :, None] + d[2][None, None, :]
+    else:
+        s = d[0][:, None] + d[1][None, :]
+    rr = cpow(s, 0.5)
+    B = cpow(rr, float(np.float32(dimension))).astype(np.float64)
+    B[B == 0] = 0.9
+    out = np.empty(A.shape, dtype=np.complex128)
+    out.real = A.real / B
+    out.imag = A.imag / B
+    return out
+
+
+class FractalSurface:
+    """A fractal surface on one face of a fractal box (``#add_surface_roughness``,
+    ``gprMax/fractals.py:29-111``): heights in cells, scaled into ``fractalrange``."""
+
+    surfaceIDs = ['xminus', 'xplus', 'yminus', 'yplus', 'zminus', 'zplus']
+
+    def __init__(self, xs, xf, ys, yf, zs, zf, dimension, seed):
+        self.ID = None
+        self.surfaceID = None
+        self.xs, self.xf, self.ys, self.yf, self.zs, self.zf = xs, xf, ys, yf, zs, zf
+        self.nx = xf - xs
+        self.ny = yf - ys
+        self.nz = zf - zs
+        self.seed = seed
+        self.dimension = dimension
+        self.weighting = np.array([1, 1], dtype=np.float64)
+        self.fractalrange = (0, 0)
+        self.filldepth = 0
+        self.operatingonID = None
+
+    def generate_fractal_surface(self):
+        """Heights (float32 [n1][n2]) of the surface."""
+        if self.xs == self.xf:
+            dims = (self.ny, self.nz)
+        elif self.ys == self.yf:
+            dims = (self.nx, self.nz)
+        else:
+            dims = (self.nx, self.ny)
+        w = self.weighting
+        v1 = np.array([w[0] * dims[0] / 2, w[1] * dims[1] / 2])
+        rng = np.random.default_rng(seed=self.seed)
+        A = rng.standard_normal(size=(dims[0], dims[1]))
+        A = fftpack.fftshift(fftpack.fftn(A))
+        surf = fftpack.ifftshift(_fractal_filter(A, w, v1, self.dimension))
+        surf[0, 0] = 0
+        surf = np.real(fftpack.ifftn(surf)).astype(floattype, copy=False)
+        # scaled to the requested range (the reference's expression, types as numpy gives them)
+        fmin = np.amin(surf)
+        fmax = np.amax(surf)
+        frange = fmax - fmin
+        r0, r1 = self.fractalrange
+        surf = surf * ((r1 - r0) / frange) + r0 - ((r1 - r0) / frange) * fmin
+        self.fractalsurface = surf
+        return surf
+
+
 class FractalVolume:
     """A box whose cells take one of ``nbins`` materials from a seeded fractal field."""
 
@@ -35,6 +104,74 @@ class FractalVolume:
         self.dimension = dimension
         self.weighting = np.array([1, 1, 1], dtype=np.float64)
         self.nbins = 0
+        self.fractalsurfaces = []
+
+    def extend_for_surfaces(self):
+        """Grow the box to take in the ranges of its rough surfaces, keeping the original
+        extent (``input_cmds_geometry.py:1266-1298``)."""
+        self.originalxs, self.originalxf = self.xs, self.xf
+        self.originalys, self.originalyf = self.ys, self.yf
+        self.originalzs, self.originalzf = self.zs, self.zf
+        for surface in self.fractalsurfaces:
+            lo, hi = surface.fractalrange
+            if surface.surfaceID == 'xminus' and lo < self.xs:
+                self.nx += self.xs - lo
+                self.xs = lo
+            elif surface.surfaceID == 'xplus' and hi > self.xf:
+                self.nx += hi - self.xf
+                self.xf = hi
+            elif surface.surfaceID == 'yminus' and lo < self.ys:
+                self.ny += self.ys - lo
+                self.ys = lo
+            elif surface.surfaceID == 'yplus' and hi > self.yf:
+                self.ny += hi - self.yf
+                self.yf = hi
+            elif surface.surfaceID == 'zminus' and lo < self.zs:
+                self.nz += self.zs - lo
+                self.zs = lo
+            elif surface.surfaceID == 'zplus' and hi > self.zf:
+                self.nz += hi - self.zf
+                self.zf = hi
+
+    def generate_volume_mask(self):
+        """1 inside the original box, 0 in the extension (``fractals.py:196-210``), then each
+        rough surface in order: 1 below (or above, on a plus face) the surface, 2 (water) where
+        it lies between the surface and the fill depth, 0 elsewhere in the surface's range
+        (``input_cmds_geometry.py:1312-1470`` without grass)."""
+        mask = np.zeros((self.nx, self.ny, self.nz), dtype=np.int8)
+        mx = self.originalxs - self.xs
+        my = self.originalys - self.ys
+        mz = self.originalzs - self.zs
+        mask[mx:mx + self.originalxf - self.originalxs, my:my + self.originalyf - self.originalys,
+             mz:mz + self.originalzf - self.originalzs] = 1
+        for s in self.fractalsurfaces:
+            lo, hi = s.fractalrange
+            axis = 'xyz'.index(s.surfaceID[0])
+            minus = s.surfaceID.endswith('minus')
+            pos = np.arange(lo, hi)
+            h = s.fractalsurface
+            if axis == 0:
+                P = pos[:, None, None]
+                H = h[None, :, :]
+                region = (slice(lo - self.xs, hi - self.xs), slice(s.ys - self.ys, s.yf - self.ys),
+                          slice(s.zs - self.zs, s.zf - self.zs))
+            elif axis == 1:
+                P = pos[None, :, None]
+                H = h[:, None, :]
+                region = (slice(s.xs - self.xs, s.xf - self.xs), slice(lo - self.ys, hi - self.ys),
+                          slice(s.zs - self.zs, s.zf - self.zs))
+            else:
+                P = pos[None, None, :]
+                H = h[:, :, None]
+                region = (slice(s.xs - self.xs, s.xf - self.xs), slice(s.ys - self.ys, s.yf - self.ys),
+                          slice(lo - self.zs, hi - self.zs))
+            below = (P > H) if minus else (P < H)
+            wet = (P > s.filldepth) if minus else (P < s.filldepth)
+            wet = wet & (s.filldepth > 0)
+            m = np.where(below, 1, np.where(wet, 2, 0)).astype(np.int8)
+            mask[region] = np.broadcast_to(m, mask[region].shape)
+        self.mask = mask
+        return mask
 
     def generate_fractal_volume(self):
         """Bin numbers (float32 array [nx][ny][nz], values 0..nbins-1) of the fractal field."""
@@ -53,18 +190,7 @@ class FractalVolume:
         rng = np.random.default_rng(seed=self.seed)
         A = rng.standard_normal(size=(self.nx, self.ny, self.nz))
         A = fftpack.fftshift(fftpack.fftn(A))
-        # 1/r^D filter. Every power goes through the C library's pow (math.pow), as the
-        # compiled filter does: numpy's vectorised power differs from it in the last bit.
-        cpow = np.frompyfunc(math.pow, 2, 1)
-        d = [cpow(w[a] * np.arange(n[a], dtype=np.float64) - v1[a], 2.0).astype(np.float64)
-             for a in range(3)]
-        rr = cpow(d[0][:, None, None] + d[1][None, :, None] + d[2][None, None, :], 0.5)
-        B = cpow(rr, float(np.float32(self.dimension))).astype(np.float64)
-        B[B == 0] = 0.9
-        vol = np.empty(A.shape, dtype=np.complex128)
-        vol.real = A.real / B
-        vol.imag = A.imag / B
-        vol = fftpack.ifftshift(vol)
+        vol = fftpack.ifftshift(_fractal_filter(A, w, v1, self.dimension))
         vol[0, 0, 0] = 0
         vol = np.real(fftpack.ifftn(vol)).astype(floattype, copy=False)
         bins = np.linspace(np.amin(vol), np.amax(vol), self.nbins)

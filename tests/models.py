@@ -173,4 +173,16 @@ MODELS = {
 #rx: 0.010 0.010 0.010
 #rx: 0.016 0.012 0.006 r2 Ex Ey Ez Hx Hy Hz
 """,
+    # a fractal soil box with rough top and x-minus faces and surface water on the top
+    'rough': BASE.format(dom='0.040 0.036 0.040', steps=110) + """#pml_cells: 6
+#soil_peplinski: 0.5 0.5 2.0 2.66 0.001 0.3 soil
+#fractal_box: 0 0 0 0.040 0.036 0.020 1.5 1 1 1 8 soil box 7
+#add_surface_roughness: 0 0 0.020 0.040 0.036 0.020 1.5 1 1 0.015 0.025 box 12
+#add_surface_water: 0 0 0.020 0.040 0.036 0.020 0.022 box
+#add_surface_roughness: 0 0 0 0 0.036 0.020 1.8 1 1 0 0.006 box 5
+#waveform: ricker 1 2e9 w
+#hertzian_dipole: z 0.020 0.018 0.030 w
+#rx: 0.024 0.018 0.030
+#rx: 0.020 0.018 0.021 wet Ex Ey Ez Hx Hy Hz
+""",
 }

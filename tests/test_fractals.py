@@ -124,3 +124,76 @@ def test_fractal_volume_matches_reference_bit_for_bit():
         v.weighting = np.array(wt, dtype=np.float64)
         v.nbins = nb
         np.testing.assert_array_equal(v.generate_fractal_volume(), ref['v%d' % n])
+
+
+ROUGH = HEAD + '#fractal_box: 0 0 0 0.020 0.020 0.010 1.5 1 1 1 6 soil box 5\n'
+
+
+@pytest.mark.parametrize('lines, msg', [
+    ('#add_surface_water: 0 0 0.010 0.020 0.020 0.010 0.012 box', 'does not have a rough surface'),
+    ('#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 0.014 box 3\n'
+     '#add_surface_water: 0 0 0.010 0.020 0.020 0.010 0.016 box', 'lies with the range'),
+    ('#add_surface_roughness: 0 0 0.006 0.020 0.020 0.006 1.5 1 1 0.004 0.012 box 3',
+     'external surfaces'),
+    ('#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 0.014 box 3\n'
+     '#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 0.014 box 4',
+     'already been used'),
+    ('#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 0.030 box 3',
+     'exceed either the lower coordinates'),
+    ('#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 0.014 box 3 9',
+     'too many parameters'),
+    ('#add_grass: 0 0 0.010 0.020 0.020 0.010 1.5 0.010 0.015 10 box 3', 'add_grass'),
+])
+def test_surface_modifier_errors(lines, msg):
+    with pytest.raises(CmdInputError, match=msg):
+        _build(ROUGH + lines + '\n')
+
+
+def test_rough_top_surface_extends_the_box_and_adds_water():
+    G = _build(ROUGH + '#add_surface_roughness: 0 0 0.010 0.020 0.020 0.010 1.5 1 1 0.008 '
+               '0.014 box 3\n#add_surface_water: 0 0 0.010 0.020 0.020 0.010 0.012 box\n')
+    water = next(m for m in G.materials if m.ID == 'water')
+    soil = [m.numID for m in G.materials if m.ID.startswith('|box_')]
+    top = G.solid[:, :, 10:14]
+    assert (G.solid[:, :, 14:] == 1).all()
+    assert np.isin(top, soil + [water.numID, 1]).all()
+    assert (top == water.numID).any() and np.isin(top, soil).any()
+    assert np.isin(G.solid[:, :, :8], soil).all()
+
+
+SURFACES = [((30, 24), 1.5, (1.0, 1.0), (3, 12), 7), ((17, 40), 2.2, (0.5, 2.0), (10, 20), 3)]
+
+SURF_CHILD = r'''
+import sys, numpy as np
+sys.path.insert(0, {oracle!r})
+import ref_harness as rh
+rh.load({src!r}, 'nofma')
+import gprMax.fractals as F
+class G: nthreads = 4
+out = {{}}
+for n, (dims, D, wt, rng, seed) in enumerate({cases!r}):
+    s = F.FractalSurface(0, 0, 0, dims[0], 0, dims[1], D, seed)
+    s.weighting = np.array(wt, dtype=np.float64)
+    s.fractalrange = rng
+    s.generate_fractal_surface(G)
+    out['s%d' % n] = s.fractalsurface
+np.savez({dest!r}, **out)
+'''
+
+
+@pytest.mark.skipif(not (os.path.isdir(os.path.join(SRC, 'gprMax')) and os.path.isdir(REF_BUILD)),
+                    reason='reference sources or compiled reference kernels absent')
+def test_fractal_surface_matches_reference_bit_for_bit():
+    from gprmax_gb300.fractals import FractalSurface
+    with tempfile.TemporaryDirectory() as tmp:
+        dest = os.path.join(tmp, 's.npz')
+        code = SURF_CHILD.format(oracle=ORACLE, src=SRC, cases=SURFACES, dest=dest)
+        subprocess.run([sys.executable, '-c', code], check=True)
+        ref = dict(np.load(dest))
+    for n, (dims, D, wt, rng, seed) in enumerate(SURFACES):
+        s = FractalSurface(0, 0, 0, dims[0], 0, dims[1], D, seed)
+        s.weighting = np.array(wt, dtype=np.float64)
+        s.fractalrange = rng
+        got = s.generate_fractal_surface()
+        assert got.dtype == ref['s%d' % n].dtype
+        np.testing.assert_array_equal(got, ref['s%d' % n])
