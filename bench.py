@@ -247,9 +247,14 @@ def run_gb300(args):
         dist.barrier()
     t0 = time.perf_counter()
     dm = DeviceModel(G)
+    t1 = time.perf_counter()
     dm.run(K)
+    dm.synchronize()
+    t2 = time.perf_counter()
     rx = dm.receivers()
     t_e2e = time.perf_counter() - t0
+    e2e_parts = {'model_upload_s': round(t1 - t0, 4), 'steps_s': round(t2 - t1, 4),
+                 'readback_s': round(t0 + t_e2e - t2, 4)}
     h2d = (G.ID.nbytes + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
            + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)
            + sum(8 * getattr(p, 'ERA').nbytes for p in G.pmls)
@@ -291,7 +296,8 @@ def run_gb300(args):
                        dm_bytes(G) / 1e9), 'replicas': world},
         'e2e': {'value': round(world * cells * K / t_e2e / 1e6, 1), 'unit': METRIC,
                 'h2d_bytes_per_step': int(h2d / K), 'd2h_bytes_per_step': int(d2h / K),
-                'what': 'DeviceModel(G) upload from host + {} steps + receiver read-back'.format(K)},
+                'what': 'DeviceModel(G) upload from host + {} steps + receiver read-back'.format(K),
+                'parts': e2e_parts},
         'gpu_launches': 3 * K,
         'roofline': {'bound': 'hbm', 'kernel': 'e_half_step', 'achieved': round(achieved, 1),
                      'peak': peak, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),

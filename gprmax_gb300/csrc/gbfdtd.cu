@@ -444,6 +444,23 @@ __global__ void id_max_kernel(const uint32_t* a, long long n, unsigned int* mx) 
   if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
 }
 
+// The largest ID in ctx->ID (on the device) must index the coefficient tables.
+static int check_ids(gbf_ctx* ctx, const char* who) {
+  const size_t n = 6 * (size_t)ctx->ncomp;
+  unsigned int* dmax = nullptr;
+  CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
+  CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
+  id_max_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->ID, (long long)n, dmax);
+  CK(cudaGetLastError());
+  unsigned int mx = 0;
+  CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaFreeAsync(dmax, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (mx >= (unsigned)ctx->d.nmat)
+    return fail(ctx, GBF_EINVAL, "%s: ID %u >= nmat %d", who, mx, ctx->d.nmat);
+  return GBF_OK;
+}
+
 extern "C" {
 
 int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
@@ -451,13 +468,11 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   if (!ctx) return GBF_EINVAL;
   if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
-  const int nmat = ctx->d.nmat;
-  // every ID must index the tables
   const size_t n = 6 * (size_t)ctx->ncomp;
-  for (size_t q = 0; q < n; ++q)
-    if (ID[q] >= (uint32_t)nmat)
-      return fail(ctx, GBF_EINVAL, "gbf_upload_materials: ID[%zu] = %u >= nmat %d", q, ID[q], nmat);
   CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  // every ID must index the tables (checked on the device)
+  const int rc = check_ids(ctx, "gbf_upload_materials");
+  if (rc != GBF_OK) return rc;
   return upload_tables(ctx, coeffE, coeffH, coeffD);
 }
 
@@ -476,17 +491,8 @@ int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
   const size_t n = 6 * (size_t)ctx->ncomp;
   CK(cudaStreamSynchronize(gstream));
   CK(cudaMemcpyAsync(ctx->ID, gid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-  unsigned int* dmax = nullptr;
-  CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
-  CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
-  id_max_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->ID, (long long)n, dmax);
-  CK(cudaGetLastError());
-  unsigned int mx = 0;
-  CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaFreeAsync(dmax, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  if (mx >= (unsigned)ctx->d.nmat)
-    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_geom: ID %u >= nmat %d", mx, ctx->d.nmat);
+  const int rc = check_ids(ctx, "gbf_upload_materials_geom");
+  if (rc != GBF_OK) return rc;
   return upload_tables(ctx, coeffE, coeffH, coeffD);
 }
 

@@ -111,3 +111,14 @@ def test_run_model_writes_the_reference_traces(native, name, tmp_path):
                 np.testing.assert_array_equal(v, g[key], err_msg=key)
                 checked += 1
     assert checked == sum(1 for k in g if k.startswith('rx'))
+
+
+def test_upload_rejects_an_id_beyond_the_tables(native):
+    """IDs are checked on the device after the copy; one past the last material is refused."""
+    from gprmax_gb300.exceptions import SolverError
+    from gprmax_gb300.model import build_grid
+    from gprmax_gb300.solver import DeviceModel
+    G = build_grid(MODELS['fs_hori1'].splitlines(True), messages=False)
+    G.ID[1, 3, 4, 5] = len(G.materials)
+    with pytest.raises(SolverError, match='nmat'):
+        DeviceModel(G)
