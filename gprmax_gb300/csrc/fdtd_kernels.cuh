@@ -67,11 +67,11 @@ void kernels_pk2(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
 void kernels_pk3(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
 void kernels_pk4(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
 // batched forms (kernels_inst.cu)
-void batch_kernels_pk0(int np, int idp, BKernFn* h, BKernFn* e);
-void batch_kernels_pk1(int np, int idp, BKernFn* h, BKernFn* e);
-void batch_kernels_pk2(int np, int idp, BKernFn* h, BKernFn* e);
-void batch_kernels_pk3(int np, int idp, BKernFn* h, BKernFn* e);
-void batch_kernels_pk4(int np, int idp, BKernFn* h, BKernFn* e);
+void batch_kernels_pk0(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
+void batch_kernels_pk1(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
+void batch_kernels_pk2(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
+void batch_kernels_pk3(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
+void batch_kernels_pk4(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
 
 struct Src {
   int kind, comp, i, j, k, first, last, pad;
@@ -575,8 +575,8 @@ h_half_step_batch(const __grid_constant__ BatchParams bp) {
     HCoef hc;
     hc.C4 = p.smem ? s4 : p.cH4;
     hc.Cs = p.smem ? ss : p.cHs;
-    hc.u = make_float4(0.f, 0.f, 0.f, 0.f);
-    hc.us = 0.f;
+    hc.u = IDP == 0 ? hc.C4[0] : make_float4(0.f, 0.f, 0.f, 0.f);
+    hc.us = IDP == 0 ? hc.Cs[0] : 0.f;
     const int it = p.nsrcH ? *p.d_it : 0;
     q = h_sweep<PK, IDP>(p, hc, q, __ldg(bp.rangeH + m), stride, it);
     if (q < end) q += stride;   // past the model's last node, inside its padding

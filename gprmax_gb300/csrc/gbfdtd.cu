@@ -969,13 +969,13 @@ static int bfail(gbf_batch* b, int code, const char* fmt, ...) {
                    "%s failed: %s", #call, cudaGetErrorString(e_));                       \
   } while (0)
 
-static void batch_kernels(int pk, int np, int idp, BKernFn* h, BKernFn* e) {
+static void batch_kernels(int pk, int np, int idp, int uh, BKernFn* h, BKernFn* e) {
   switch (pk) {
-    case PML_HORI1: batch_kernels_pk1(np, idp, h, e); break;
-    case PML_HORI2: batch_kernels_pk2(np, idp, h, e); break;
-    case PML_MRI1: batch_kernels_pk3(np, idp, h, e); break;
-    case PML_MRI2: batch_kernels_pk4(np, idp, h, e); break;
-    default: batch_kernels_pk0(np, idp, h, e); break;
+    case PML_HORI1: batch_kernels_pk1(np, idp, uh, h, e); break;
+    case PML_HORI2: batch_kernels_pk2(np, idp, uh, h, e); break;
+    case PML_MRI1: batch_kernels_pk3(np, idp, uh, h, e); break;
+    case PML_MRI2: batch_kernels_pk4(np, idp, uh, h, e); break;
+    default: batch_kernels_pk0(np, idp, uh, h, e); break;
   }
 }
 
@@ -1073,7 +1073,10 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
     bfail(nullptr, e == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA, "gbf_batch_create: %s", cudaGetErrorString(e));
     return cleanup(GBF_ECUDA);
   }
-  batch_kernels(pk, m0->d.maxpoles, m0->idp, &b->hk, &b->ek);
+  // the ID-free H half-step when every model has one H row
+  int uh = 1;
+  for (int m = 0; m < nmodels; ++m) uh = uh && b->models[m]->uniform_h;
+  batch_kernels(pk, m0->d.maxpoles, m0->idp, uh, &b->hk, &b->ek);
   const size_t sh = b->smem_h, se = b->smem_e;
   b->grid_h = persistent_blocks((const void*)b->hk, sh);
   b->grid_e = persistent_blocks((const void*)b->ek, se);

@@ -48,7 +48,7 @@ static BKernFn eb_for(int np) {
 }
 
 // Batched kernels for PML kind GBF_PK (see kernels_pk*).
-void GBF_CAT(batch_kernels_pk, GBF_PK)(int np, int idp, BKernFn* h, BKernFn* e) {
+void GBF_CAT(batch_kernels_pk, GBF_PK)(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e) {
   if (idp == 1) {
     *h = h_half_step_batch<GBF_PK, 1>;
     *e = eb_for<1>(np);
@@ -56,6 +56,7 @@ void GBF_CAT(batch_kernels_pk, GBF_PK)(int np, int idp, BKernFn* h, BKernFn* e) 
     *h = h_half_step_batch<GBF_PK, 3>;
     *e = eb_for<3>(np);
   }
+  if (uniform_h) *h = h_half_step_batch<GBF_PK, 0>;
 }
 
 }  // namespace gbf

@@ -138,7 +138,7 @@ def bscan_input(shape, seed, position, dx=0.002, timewindow='10e-9', pml=10):
 
 
 def bscan_models(nmodels=128, shapes=((200, 200, 100), (300, 300, 150)), seed=11,
-                 messages=False):
+                 messages=False, device_build=False):
     """The uneven B-scan: ``nmodels`` grids, the first half of the first shape and the second
     half of the second, each with its own seed; the dipole/receiver pair of model m of each half
     sits 4 mm * m along x."""
@@ -147,7 +147,8 @@ def bscan_models(nmodels=128, shapes=((200, 200, 100), (300, 300, 150)), seed=11
     for m in range(nmodels):
         shape = shapes[0] if m < half else shapes[1]
         pos = m if m < half else m - half
-        grids.append(build_grid(bscan_input(shape, seed + m, pos), messages=messages))
+        grids.append(build_grid(bscan_input(shape, seed + m, pos), messages=messages,
+                                device_build=device_build))
     return grids
 
 
