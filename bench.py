@@ -456,21 +456,29 @@ def run_adjoint(args):
         return float(0.5 * ((tr.double() - obs) ** 2).sum())
     for _ in range(max(args.warmup - 2, 1)):
         loss_of(e)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    loss_of(e)
-    torch.cuda.synchronize()
-    t_fwd = time.perf_counter() - t0
-    ee = e.clone().requires_grad_(True)
-    ss = s.clone().requires_grad_(True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    CA, CB = m.edge_coefficients(ee, ss)
-    tr = fdtd_traces(CA, CB, solver)
-    L = 0.5 * ((tr.double() - obs) ** 2).sum()
-    L.backward()
-    torch.cuda.synchronize()
-    t_grad = time.perf_counter() - t0
+    fwd_times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss_of(e)
+        torch.cuda.synchronize()
+        fwd_times.append(time.perf_counter() - t0)
+    t_fwd = float(np.median(fwd_times))
+    # the gradient (forward with checkpoints, then the adjoint), once untimed, then the median
+    # of three
+    grad_times = []
+    for rep in range(4):
+        ee = e.clone().requires_grad_(True)
+        ss = s.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        CA, CB = m.edge_coefficients(ee, ss)
+        tr = fdtd_traces(CA, CB, solver)
+        L = 0.5 * ((tr.double() - obs) ** 2).sum()
+        L.backward()
+        torch.cuda.synchronize()
+        grad_times.append(time.perf_counter() - t0)
+    t_grad = float(np.median(grad_times[1:]))
     g = ee.grad
     # finite differences on 20 cells drawn from the 1 % with the largest |gradient|
     flat = g.abs().flatten()
@@ -501,6 +509,8 @@ def run_adjoint(args):
                       'iterations': m.iterations, 'sources': len(m.sources),
                       'receivers': len(m.receivers)},
            'forward_s': round(t_fwd, 4), 'gradient_s': round(t_grad, 4),
+           'gradient_runs_s': [round(t, 4) for t in grad_times],
+           'forward_runs_s': [round(t, 4) for t in fwd_times],
            'forward_Mcells_per_s': round(cells_n * m.iterations / t_fwd / 1e6, 1),
            'fd_check': {'cells': 20, 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',
                         'median_rel_err': float(np.median(errs)),
