@@ -86,10 +86,11 @@ def slab_cells(G):
 def algorithmic_bytes(G):
     """Bytes per launch each half-step must move, in the device representation: fp32 fields,
     the node's three material IDs packed in one 32-bit word (nmat <= 1024; otherwise three
-    uint32 IDs), complex64 dispersive state. Per node: H half-step reads E and H and the ID word
+    uint32 IDs), complex64 (or real fp32) dispersive state. Per node: H half-step reads E and H and the ID word
     and writes H (12 + 12 + 4 + 12 = 40 B; 36 B when every material has the same H row and no
     ID is needed); E half-step the same (40 B) plus, on nodes whose
-    materials have poles, 8 B per pole and component read and written (48 B per pole). PML adds
+    materials have poles, 8 B per pole and component read and written (48 B per pole; 24 B when
+    only the real parts are kept, every pole being Debye-like). PML adds
     per slab node and CFS order two Phi values read and written (16 B) in each half-step.
     Neighbour values along j, k and x are re-reads of the same arrays (cache hits)."""
     cells = G.nx * G.ny * G.nz
@@ -107,7 +108,10 @@ def algorithmic_bytes(G):
         disp[:] = np.any(d != 0, axis=1)
         ids = G.ID[:3, :G.nx, :G.ny, :G.nz]
         dcells = int(np.count_nonzero(disp[ids[0]] | disp[ids[1]] | disp[ids[2]]))
-        e += dcells * 48 * G.maxpoles
+        # complex64 state read and written (48 B per pole), or its real parts only (24 B) when
+        # every pole is Debye-like and the device keeps just those
+        from gprmax_gb300.solver import real_dispersive_state
+        e += dcells * (24 if real_dispersive_state(G) else 48) * G.maxpoles
     return h, e
 
 

@@ -60,18 +60,19 @@ typedef void (*HKernFn)(StepParams);
 typedef void (*EKernFn)(StepParams);
 typedef void (*BKernFn)(BatchParams);
 // per-kind kernel tables (kernels_inst.cu, one object per PML kind)
-// idp: material-ID layout (1 packed, 3 plain); uniform_h: every material has the same H row
-void kernels_pk0(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
-void kernels_pk1(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
-void kernels_pk2(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
-void kernels_pk3(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
-void kernels_pk4(int np, int idp, int uniform_h, HKernFn* h, EKernFn* e);
+// idp: material-ID layout (1 packed, 3 plain); uniform_h: every material has the same H row;
+// treal: the dispersive state is stored as real parts (packed IDs only)
+void kernels_pk0(int np, int idp, int uniform_h, int treal, HKernFn* h, EKernFn* e);
+void kernels_pk1(int np, int idp, int uniform_h, int treal, HKernFn* h, EKernFn* e);
+void kernels_pk2(int np, int idp, int uniform_h, int treal, HKernFn* h, EKernFn* e);
+void kernels_pk3(int np, int idp, int uniform_h, int treal, HKernFn* h, EKernFn* e);
+void kernels_pk4(int np, int idp, int uniform_h, int treal, HKernFn* h, EKernFn* e);
 // batched forms (kernels_inst.cu)
-void batch_kernels_pk0(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
-void batch_kernels_pk1(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
-void batch_kernels_pk2(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
-void batch_kernels_pk3(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
-void batch_kernels_pk4(int np, int idp, int uniform_h, BKernFn* h, BKernFn* e);
+void batch_kernels_pk0(int np, int idp, int uniform_h, int treal, BKernFn* h, BKernFn* e);
+void batch_kernels_pk1(int np, int idp, int uniform_h, int treal, BKernFn* h, BKernFn* e);
+void batch_kernels_pk2(int np, int idp, int uniform_h, int treal, BKernFn* h, BKernFn* e);
+void batch_kernels_pk3(int np, int idp, int uniform_h, int treal, BKernFn* h, BKernFn* e);
+void batch_kernels_pk4(int np, int idp, int uniform_h, int treal, BKernFn* h, BKernFn* e);
 
 struct Src {
   int kind, comp, i, j, k, first, last, pad;
@@ -690,7 +691,7 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
 
 // One E node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j
 // >= 1 and outside the x and y slabs), so only k decides neighbours and PML terms.
-template <int PK, int NP, int IDP, bool CORE>
+template <int PK, int NP, int IDP, bool CORE, bool TR>
 __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, const float* Cs,
                                        const float2* CD, int i, int j, int k, int it) {
   const int sx = p.sx, sy = p.sy;
@@ -728,7 +729,11 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
   for (int comp = 0; comp < 3; ++comp) {
     e[comp] = p.E[comp][idx];
 #pragma unroll
-    for (int qq = 0; qq < NP; ++qq) t[comp][qq] = p.T[(comp * NP + qq) * (long long)p.ncomp + idx];
+    for (int qq = 0; qq < NP; ++qq) {
+      const long long o = (comp * NP + qq) * (long long)p.ncomp + idx;
+      // TR: the state is stored as its real part; its imaginary part is +0 at every step
+      t[comp][qq] = TR ? make_float2(reinterpret_cast<const float*>(p.T)[o], 0.f) : p.T[o];
+    }
   }
   int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
   if (PK != PML_NONE) {
@@ -746,7 +751,11 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
     p.E[comp][idx] = e[comp];
     if (disp) {
 #pragma unroll
-      for (int qq = 0; qq < NP; ++qq) p.T[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq];
+      for (int qq = 0; qq < NP; ++qq) {
+        const long long o = (comp * NP + qq) * (long long)p.ncomp + idx;
+        if (TR) reinterpret_cast<float*>(p.T)[o] = t[comp][qq].x;
+        else p.T[o] = t[comp][qq];
+      }
     }
   }
 }
@@ -754,7 +763,7 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
 // E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz), swept box by box (core
 // first) by one persistent grid. NP = dispersive poles.
 // The E sweep of one model over its boxes (see h_sweep).
-template <int PK, int NP, int IDP>
+template <int PK, int NP, int IDP, bool TR>
 __device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, const float* Cs,
                                        const float2* CD, int q, int base, int stride, int it) {
   q -= base;
@@ -764,7 +773,7 @@ __device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, co
     if (q < end) {
       BoxWalk w(q - B.start, stride, B);
       for (; q < end; q += stride, w.advance(B))
-        e_site<PK, NP, IDP, true>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
+        e_site<PK, NP, IDP, true, TR>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
   }
 #pragma unroll 1
@@ -774,7 +783,7 @@ __device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, co
     if (q >= end) continue;
     BoxWalk w(q - B.start, stride, B);
     for (; q < end; q += stride, w.advance(B))
-      e_site<PK, NP, IDP, false>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
+      e_site<PK, NP, IDP, false, TR>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
   return q + base;
 }
@@ -788,7 +797,12 @@ __device__ __forceinline__ void e_tables(const StepParams& p, float4* smem, floa
   sd = reinterpret_cast<float2*>(ss + (p.smem ? ((p.nmat + 1) & ~1) : 0));
 }
 
-template <int PK, int NP, int IDP>
+// TR: the dispersive state is stored as fp32 real parts ([3][P][ncomp] floats), possible when
+// every pole's eqt has imaginary part +0 and zt imaginary part +-0 (Debye poles): the update
+// then keeps every imaginary part at exactly +0 (it starts at +0, and each product and sum
+// forming it is a signed zero that adds to +0), and the real parts are computed from the same
+// operands as with the complex state, so the results are the same bit for bit.
+template <int PK, int NP, int IDP, bool TR>
 __global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
 e_half_step(const __grid_constant__ StepParams p) {
   extern __shared__ float4 smem_e[];
@@ -805,11 +819,11 @@ e_half_step(const __grid_constant__ StepParams p) {
   const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
   int it = 0;
   if (p.nsrcE) it = *p.d_it;
-  e_sweep<PK, NP, IDP>(p, C4, Cs, CD, blockIdx.x * blockDim.x + threadIdx.x, 0,
-                       gridDim.x * blockDim.x, it);
+  e_sweep<PK, NP, IDP, TR>(p, C4, Cs, CD, blockIdx.x * blockDim.x + threadIdx.x, 0,
+                           gridDim.x * blockDim.x, it);
 }
 
-template <int PK, int NP, int IDP>
+template <int PK, int NP, int IDP, bool TR>
 __global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
 e_half_step_batch(const __grid_constant__ BatchParams bp) {
   __shared__ StepParams p;
@@ -833,7 +847,7 @@ e_half_step_batch(const __grid_constant__ BatchParams bp) {
     const float* Cs = p.smem ? ss : p.cEs;
     const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
     const int it = p.nsrcE ? *p.d_it : 0;
-    q = e_sweep<PK, NP, IDP>(p, C4, Cs, CD, q, __ldg(bp.rangeE + m), stride, it);
+    q = e_sweep<PK, NP, IDP, TR>(p, C4, Cs, CD, q, __ldg(bp.rangeE + m), stride, it);
     if (q < end) q += stride;   // past the model's last node, inside its padding
   }
 }

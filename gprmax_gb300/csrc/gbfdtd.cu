@@ -35,6 +35,7 @@ struct gbf_ctx {
   unsigned char* disp = nullptr;   // per material: has dispersive poles
   int idp = 3;                 // 1: packed IDs, 3: three ID arrays per half-step
   int uniform_h = 0;           // every material has the same H row: the H half-step reads no IDs
+  int treal = 0;               // T stored as fp32 real parts (Debye poles, packed IDs)
   float4* cE4 = nullptr;       // [nmat] CA, CBx, CBy, CBz
   float* cEs = nullptr;        // [nmat] srce
   float4* cH4 = nullptr;
@@ -238,7 +239,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~3) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
+  if ((d.options & ~7) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
@@ -393,7 +394,25 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   for (int m = 1; m < nmat && uni; ++m)
     uni = memcmp(coeffH + 5 * m, coeffH, 5 * sizeof(float)) == 0;
   ctx->uniform_h = uni;
+  // real dispersive state: every pole's eqt has imaginary part +0 and zt imaginary part +-0
+  // (Debye poles; the E update reads only Re(T), and Im(T) then stays +0), packed IDs, and the
+  // complex layout not requested (option bit 2)
+  int tr = ctx->d.maxpoles > 0 && ctx->idp == 1 && !(ctx->d.options & 4);
+  for (int m = 0; m < nmat && tr; ++m)
+    for (int q = 0; q < ctx->d.maxpoles && tr; ++q) {
+      const float* c = coeffD + ((size_t)m * 3 * ctx->d.maxpoles + 3 * q) * 2;
+      uint32_t eqt_im, zt_im;
+      memcpy(&eqt_im, c + 3, 4);
+      memcpy(&zt_im, c + 5, 4);
+      tr = eqt_im == 0u && (zt_im & 0x7fffffffu) == 0u;
+    }
+  if (tr != ctx->treal && ctx->T) {
+    // the layout changes: start the state again from zero
+    CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)ctx->d.maxpoles * ctx->ncomp, ctx->stream));
+  }
+  ctx->treal = tr;
   ctx->grid_h = 0;
+  ctx->grid_e = 0;
   invalidate_graph(ctx);
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
@@ -693,13 +712,13 @@ typedef HKernFn HKern;
 typedef EKernFn EKern;
 
 static void pick_kernels(gbf_ctx* ctx, HKern* h, EKern* e) {
-  const int np = ctx->d.maxpoles, idp = ctx->idp, uh = ctx->uniform_h;
+  const int np = ctx->d.maxpoles, idp = ctx->idp, uh = ctx->uniform_h, tr = ctx->treal;
   switch (pml_kind(ctx->d)) {
-    case PML_HORI1: kernels_pk1(np, idp, uh, h, e); break;
-    case PML_HORI2: kernels_pk2(np, idp, uh, h, e); break;
-    case PML_MRI1: kernels_pk3(np, idp, uh, h, e); break;
-    case PML_MRI2: kernels_pk4(np, idp, uh, h, e); break;
-    default: kernels_pk0(np, idp, uh, h, e); break;
+    case PML_HORI1: kernels_pk1(np, idp, uh, tr, h, e); break;
+    case PML_HORI2: kernels_pk2(np, idp, uh, tr, h, e); break;
+    case PML_MRI1: kernels_pk3(np, idp, uh, tr, h, e); break;
+    case PML_MRI2: kernels_pk4(np, idp, uh, tr, h, e); break;
+    default: kernels_pk0(np, idp, uh, tr, h, e); break;
   }
 }
 
@@ -877,9 +896,20 @@ int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
 int gbf_download_dispersive(gbf_ctx* ctx, float* T) {
   if (!ctx || !T) return GBF_EINVAL;
   if (!ctx->T) return fail(ctx, GBF_ESTATE, "gbf_download_dispersive: model has no dispersive state");
-  CK(cudaMemcpyAsync(T, ctx->T, sizeof(float2) * 3 * (size_t)ctx->d.maxpoles * ctx->ncomp,
-                     cudaMemcpyDeviceToHost, ctx->stream));
+  const size_t n = 3 * (size_t)ctx->d.maxpoles * ctx->ncomp;
+  if (!ctx->treal) {
+    CK(cudaMemcpyAsync(T, ctx->T, sizeof(float2) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GBF_OK;
+  }
+  // real parts on the device: copy them into the first half, then spread them out in place
+  // from the end, each with its imaginary part +0
+  CK(cudaMemcpyAsync(T, ctx->T, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t q = n; q-- > 0;) {
+    T[2 * q] = T[q];
+    T[2 * q + 1] = 0.f;
+  }
   return GBF_OK;
 }
 
@@ -969,13 +999,13 @@ static int bfail(gbf_batch* b, int code, const char* fmt, ...) {
                    "%s failed: %s", #call, cudaGetErrorString(e_));                       \
   } while (0)
 
-static void batch_kernels(int pk, int np, int idp, int uh, BKernFn* h, BKernFn* e) {
+static void batch_kernels(int pk, int np, int idp, int uh, int tr, BKernFn* h, BKernFn* e) {
   switch (pk) {
-    case PML_HORI1: batch_kernels_pk1(np, idp, uh, h, e); break;
-    case PML_HORI2: batch_kernels_pk2(np, idp, uh, h, e); break;
-    case PML_MRI1: batch_kernels_pk3(np, idp, uh, h, e); break;
-    case PML_MRI2: batch_kernels_pk4(np, idp, uh, h, e); break;
-    default: batch_kernels_pk0(np, idp, uh, h, e); break;
+    case PML_HORI1: batch_kernels_pk1(np, idp, uh, tr, h, e); break;
+    case PML_HORI2: batch_kernels_pk2(np, idp, uh, tr, h, e); break;
+    case PML_MRI1: batch_kernels_pk3(np, idp, uh, tr, h, e); break;
+    case PML_MRI2: batch_kernels_pk4(np, idp, uh, tr, h, e); break;
+    default: batch_kernels_pk0(np, idp, uh, tr, h, e); break;
   }
 }
 
@@ -1029,6 +1059,9 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
     if (c->device != m0->device) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models on different devices");
     if (pml_kind(c->d) != pk || c->d.maxpoles != m0->d.maxpoles || c->idp != m0->idp)
       return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d differs in PML kind, poles or ID layout from model 0", m);
+    if (c->treal != m0->treal)
+      return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d stores its dispersive state %s, model 0 %s (set option bit 2 on every model)",
+                   m, c->treal ? "as real parts" : "complex", m0->treal ? "as real parts" : "complex");
     if (c->d.nsnap || c->d.ntl)
       return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: model %d has snapshots or transmission lines (run it alone)", m);
     if (c->it != m0->it) return bfail(nullptr, GBF_EINVAL, "gbf_batch_create: models at different iterations");
@@ -1076,7 +1109,7 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
   // the ID-free H half-step when every model has one H row
   int uh = 1;
   for (int m = 0; m < nmodels; ++m) uh = uh && b->models[m]->uniform_h;
-  batch_kernels(pk, m0->d.maxpoles, m0->idp, uh, &b->hk, &b->ek);
+  batch_kernels(pk, m0->d.maxpoles, m0->idp, uh, m0->treal, &b->hk, &b->ek);
   const size_t sh = b->smem_h, se = b->smem_e;
   b->grid_h = persistent_blocks((const void*)b->hk, sh);
   b->grid_e = persistent_blocks((const void*)b->ek, se);

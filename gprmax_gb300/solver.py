@@ -95,6 +95,17 @@ def source_tables(G):
     return info, scale, waves
 
 
+def real_dispersive_state(G):
+    """Whether the C ABI stores this model's dispersive state as real parts: poles present,
+    packed material IDs (at most 1024 materials) and every pole Debye-like (eqt with imaginary
+    part +0, zt with imaginary part +-0), the rule ``gbf_upload_materials`` applies."""
+    if not pole_count(G) or len(G.materials) > 1024:
+        return False
+    d = np.ascontiguousarray(G.updatecoeffsdispersive, dtype=np.complex64)
+    bits = d.view(np.float32).reshape(d.shape[0], -1, 3, 2).view(np.uint32)
+    return bool((bits[:, :, 1, 1] == 0).all() and ((bits[:, :, 2, 1] & 0x7fffffff) == 0).all())
+
+
 def model_inputs(G, options=0):
     """Everything the C ABI receives for grid ``G``: the descriptor and the host arrays, in
     the reference's layouts. Reads only attributes that the reference's own grid object also
@@ -311,6 +322,10 @@ class BatchModel:
         self.lib = _native.lib()
         self.models = []
         self.b = ctypes.c_void_p(0)
+        # one layout of the dispersive state for the whole batch: real parts only if every
+        # model allows it, else complex everywhere (option bit 2)
+        if any(pole_count(G) for G in grids) and not all(real_dispersive_state(G) for G in grids):
+            options |= 4
         try:
             for G in grids:
                 self.models.append(DeviceModel(G, options))

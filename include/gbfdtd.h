@@ -67,7 +67,11 @@ typedef struct gbf_grid_desc {
     int32_t options;             /* bit 0: read coefficient tables from global memory instead
                                     of staging them in shared memory (tuning); bit 1: form the
                                     PML differences dF/d by division even where the reciprocal
-                                    product is exact (gbf_check_cell_division); other bits 0 */
+                                    product is exact (gbf_check_cell_division); bit 2: keep the
+                                    dispersive state complex even when every pole is Debye
+                                    (otherwise only its real parts are stored then, the
+                                    imaginary parts being +0 throughout; needed to batch such a
+                                    model with others whose state is complex); other bits 0 */
     int32_t ntl;                 /* transmission lines among the nsrc sources */
     int32_t reserved[2];         /* must be zero */
 } gbf_grid_desc;
@@ -139,7 +143,9 @@ int gbf_download_rx(gbf_ctx* ctx, float* rxs);
 int gbf_download_fields(gbf_ctx* ctx, float* fields);
 int gbf_upload_fields(gbf_ctx* ctx, const float* fields);
 
-/* Dispersive state complex64 as fp32 pairs [3][maxpoles][nx+1][ny+1][nz+1] (Tx, Ty, Tz). */
+/* Dispersive state complex64 as fp32 pairs [3][maxpoles][nx+1][ny+1][nz+1] (Tx, Ty, Tz);
+ * when only real parts are stored (Debye poles, options bit 2 clear) they come back with
+ * imaginary parts +0, which is what the complex update holds there. */
 int gbf_download_dispersive(gbf_ctx* ctx, float* T);
 
 /* Snapshot s: fp32 [6][snx][sny][snz] cell-averaged Ex, Ey, Ez, Hx, Hy, Hz

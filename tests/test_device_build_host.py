@@ -57,3 +57,11 @@ def test_averaged_keys_resolve_in_first_occurrence_order(fake_lib):
     assert first, names
     G = build_grid(lines, messages=False)
     assert [m.ID for m in G.materials if m.ID.count('+') == 3] == first
+
+
+def test_real_dispersive_state_rule():
+    """The models whose pole state the C ABI keeps as real parts (every pole Debye-like)."""
+    from gprmax_gb300.solver import real_dispersive_state
+    got = {n for n in MODELS
+           if real_dispersive_state(build_grid(MODELS[n].splitlines(True), messages=False))}
+    assert got == {'debye1', 'fractal', 'rough', 'tline', 'tmz'}

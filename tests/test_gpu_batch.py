@@ -84,3 +84,34 @@ def test_batch_rejects_mixed_pml_kinds(native):
     grids = _grids(FREE, 1, 20, '6') + _grids(FREE, 1, 20, '0')
     with pytest.raises(SolverError):
         BatchModel(grids)
+
+
+LORENTZ = FREE + """#material: 4 0.002 1 0 wet
+#add_dispersion_lorentz: 1 3 2e9 1e8 wet
+#box: 0 0 0 {x} {y} {surf} wet
+"""
+
+
+def test_batch_of_debye_and_lorentz_models_keeps_complex_state(native):
+    """A Debye model alone keeps only the real part of its pole state; batched with a Lorentz
+    model both keep it complex (option bit 2), and the results do not change."""
+    from gprmax_gb300.solver import BatchModel, real_dispersive_state
+    grids = _grids(SOIL, 2, 70) + _grids(LORENTZ, 2, 70)
+    assert real_dispersive_state(grids[0]) and not real_dispersive_state(grids[2])
+    bm = BatchModel(grids)
+    bm.run()
+    rx = bm.receivers()
+    fields = [m.fields() for m in bm.models]
+    T = [m.dispersive() for m in bm.models]
+    bm.close()
+    for n, G in enumerate(grids):
+        prx, pf = _plain(G)
+        np.testing.assert_array_equal(rx[n], prx, err_msg='model {} traces'.format(n))
+        np.testing.assert_array_equal(fields[n], pf, err_msg='model {} fields'.format(n))
+    from gprmax_gb300.solver import DeviceModel
+    dm = DeviceModel(grids[0])
+    dm.run()
+    Treal = dm.dispersive()
+    dm.close()
+    # the real-part layout gives back the complex state with imaginary parts +0
+    np.testing.assert_array_equal(np.asarray(Treal).view(np.uint32), np.asarray(T[0]).view(np.uint32))
