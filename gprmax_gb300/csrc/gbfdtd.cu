@@ -15,6 +15,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gbfdtd.h"
@@ -121,15 +122,30 @@ static bool reciprocal_division_exact(float d) {
       if (c.first == bits) return c.second;
   }
   const float r = 1.0f / d;
+  // the 2^23 significands in slices over the host's cores, each slice without early exit
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = nt < 1 ? 1 : (nt > 64 ? 64 : nt);
+  std::vector<int> bad(nt, 0);
+  auto slice = [&](unsigned t) {
+    const uint32_t lo = (uint32_t)(((uint64_t)t << 23) / nt);
+    const uint32_t hi = (uint32_t)(((uint64_t)(t + 1) << 23) / nt);
+    int b = 0;
+    for (uint32_t m = lo; m < hi; ++m) {
+      const uint32_t xb = (127u << 23) | m;
+      float x;
+      memcpy(&x, &xb, 4);
+      const float q = x * r;
+      const float q1 = fmaf(fmaf(-q, d, x), r, q);
+      b |= (q1 != x / d);
+    }
+    bad[t] = b;
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(slice, t);
+  slice(0);
+  for (auto& th : pool) th.join();
   bool ok = true;
-  for (uint32_t m = 0; m < (1u << 23) && ok; ++m) {
-    const uint32_t xb = (127u << 23) | m;
-    float x;
-    memcpy(&x, &xb, 4);
-    const float q = x * r;
-    const float q1 = fmaf(fmaf(-q, d, x), r, q);
-    ok = (q1 == x / d);
-  }
+  for (int b : bad) ok = ok && !b;
   std::lock_guard<std::mutex> lock(mu);
   cache.emplace_back(bits, ok);
   return ok;
