@@ -222,12 +222,21 @@ def dist_setup(n_gpus):
 
 
 def barrier_max(dist, value):
+    """The largest `value` over the ranks (the slowest rank's time); the all-reduce is also the
+    barrier that closes the timed region."""
     if dist is None:
         return value
     import torch
-    t = torch.tensor([value], dtype=torch.float64, device='cuda')
+    device = 'cuda' if dist.get_backend() == 'nccl' else 'cpu'
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(world, cells, steps, seconds):
+    """Whole-job Mcells/s of `world` replicas, each advancing `cells` cells `steps` steps, when
+    the slowest took `seconds` (weak scaling: the work per GPU is fixed)."""
+    return world * cells * steps / seconds / 1e6
 
 
 def run_gb300(args):
@@ -279,7 +288,7 @@ def run_gb300(args):
     ms_h, ms_e, ms_t = dm.profile(max(args.profile_steps, 1))
     checksum = float(np.abs(dm.receivers()).sum())
     dm.close()
-    value = world * cells * K / (ms / 1e3) / 1e6
+    value = replica_rate(world, cells, K, ms / 1e3)
     bytes_h, bytes_e = algorithmic_bytes(G)
     peak, peak_kind = load_peaks()
     npf = max(args.profile_steps, 1)
@@ -298,7 +307,7 @@ def run_gb300(args):
                    'materials': len(G.materials), 'poles': G.maxpoles, 'pml_cells': 10,
                    'cells': cells, 'l2': 'working set {:.2f} GB > L2 (129 MB), no flush'.format(
                        dm_bytes(G) / 1e9), 'replicas': world},
-        'e2e': {'value': round(world * cells * K / t_e2e / 1e6, 1), 'unit': METRIC,
+        'e2e': {'value': round(replica_rate(world, cells, K, t_e2e), 1), 'unit': METRIC,
                 'h2d_bytes_per_step': int(h2d / K), 'd2h_bytes_per_step': int(d2h / K),
                 'what': 'DeviceModel(G) upload from host + {} steps + receiver read-back'.format(K),
                 'parts': e2e_parts},
