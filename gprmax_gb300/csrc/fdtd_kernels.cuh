@@ -613,7 +613,7 @@ __device__ __forceinline__ float apply_e_sources(float F, int comp, int i, int j
 // E update of one node for all three components: main update (update_electric, or part A of
 // the dispersive update), slab corrections in slab order, sources, dispersive part B.
 // where[a] / pr[a]: slab membership and profile index along each axis (0 outside the PML).
-template <int PK, int NP, bool CORE>
+template <int PK, int NP, bool CORE, bool TR>
 __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
                                        const float2* CD, int i, int j, int k, bool src, int it,
                                        const int* where, const int* pr, float dHz_y,
@@ -652,6 +652,21 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
     float F;
     if (NP == 0) {
       F = c.x * Eold + t1 - t2;
+    } else if (TR) {
+      // real pole state: per material and pole (Re(e0*eqt2), Re(eqt), Re(zt), srce). The
+      // complex update's Im(eqt)*Im(T) term is (+0)*(+0) = +0 here and x - (+0) == x, so it is
+      // left out; every other operation is the complex update's real part, in its order.
+      float phi = 0.f;
+      const float4* rec = reinterpret_cast<const float4*>(CD) + mm * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float4 r = rec[q];
+        const float Tx = t[comp][q].x;
+        phi = phi + r.x * Tx;
+        TA[q].x = r.y * Tx + r.z * Eold;
+        TA[q].y = 0.f;
+      }
+      F = c.x * Eold + t1 - t2 - rec[0].w * phi;
     } else {
       float phi = 0.f;
       const float2* cd = CD + mm * 3 * NP;
@@ -676,7 +691,14 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
     }
     if (src) F = apply_e_sources(F, comp, i, j, k, it, Cs[mm], p);
     e[comp] = F;
-    if (NP > 0) {
+    if (NP > 0 && TR) {
+      const float4* rec = reinterpret_cast<const float4*>(CD) + mm * NP;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float tx = TA[q].x - rec[q].z * F;
+        t[comp][q].x = mainu ? tx : t[comp][q].x;
+      }
+    } else if (NP > 0) {
       const float2* cd = CD + mm * 3 * NP;
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
@@ -744,7 +766,7 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
     where[2] = axis_member<true>(k, p.nz, p.slab[2].T, p.slab[5].T, pr[2]);
   }
   const bool src = p.nsrcE && node_has_source(idx, p.nsrcE, p.srcqE, p.srcE, sx, sy);
-  e_node<PK, NP, CORE>(p, C4, Cs, CD, i, j, k, src, it, where, pr, hz_c - hz_j, hy_c - hy_k,
+  e_node<PK, NP, CORE, TR>(p, C4, Cs, CD, i, j, k, src, it, where, pr, hz_c - hz_j, hy_c - hy_k,
                        hx_c - hx_k, hz_c - hz_p, hy_c - hy_p, hx_c - hx_j, m, e, t);
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
@@ -788,13 +810,13 @@ __device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, co
   return q + base;
 }
 
-// Shared-memory layout of the E tables: float4 rows, srce column (padded to 8 bytes), then the
-// dispersive coefficients.
+// Shared-memory layout of the E tables: float4 rows, srce column (padded to 16 bytes), then the
+// dispersive coefficients (complex [nmat][3P], or with the real pole state float4 [nmat][P]).
 __device__ __forceinline__ void e_tables(const StepParams& p, float4* smem, float4*& s4,
                                          float*& ss, float2*& sd) {
   s4 = smem;
   ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
-  sd = reinterpret_cast<float2*>(ss + (p.smem ? ((p.nmat + 1) & ~1) : 0));
+  sd = reinterpret_cast<float2*>(ss + (p.smem ? ((p.nmat + 3) & ~3) : 0));   // 16-byte aligned
 }
 
 // TR: the dispersive state is stored as fp32 real parts ([3][P][ncomp] floats), possible when

@@ -343,7 +343,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   p.nmat = d.nmat;
   // shared-memory coefficient tables when they are small
   ctx->smem_h = (size_t)d.nmat * (sizeof(float4) + sizeof(float));
-  ctx->smem_e = (size_t)d.nmat * sizeof(float4) + (size_t)((d.nmat + 1) & ~1) * sizeof(float) +
+  ctx->smem_e = (size_t)d.nmat * sizeof(float4) + (size_t)((d.nmat + 3) & ~3) * sizeof(float) +
                 (size_t)d.nmat * 3 * d.maxpoles * sizeof(float2);
   p.smem = (d.nmat <= kSmemCoefMax && ctx->smem_e <= 32768 && !(d.options & 1)) ? 1 : 0;
   if (!p.smem) ctx->smem_e = ctx->smem_h = 0;
@@ -445,9 +445,23 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   CK(cudaMemcpyAsync(ctx->cH4, h4.data(), sizeof(float4) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->cHs, hs.data(), sizeof(float) * nmat, cudaMemcpyHostToDevice, ctx->stream));
   std::vector<unsigned char> disp(nmat, 0);
-  if (ctx->d.maxpoles > 0) {
+  if (ctx->d.maxpoles > 0 && tr) {
+    // real pole state: one record per material and pole, (Re(e0*eqt2), Re(eqt), Re(zt), srce),
+    // in the space of the complex table
+    const int P = ctx->d.maxpoles;
+    std::vector<float4> rec((size_t)nmat * P);
+    for (int m = 0; m < nmat; ++m)
+      for (int q = 0; q < P; ++q) {
+        const float* c = coeffD + ((size_t)m * 3 * P + 3 * q) * 2;
+        rec[(size_t)m * P + q] = make_float4(c[0], c[2], c[4], coeffE[5 * m + 4]);
+      }
+    CK(cudaMemcpyAsync(ctx->cD, rec.data(), sizeof(float4) * rec.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  } else if (ctx->d.maxpoles > 0) {
     CK(cudaMemcpyAsync(ctx->cD, coeffD, sizeof(float2) * 3 * ctx->d.maxpoles * nmat,
                        cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (ctx->d.maxpoles > 0) {
     for (int m = 0; m < nmat; ++m)
       for (int q = 0; q < 6 * ctx->d.maxpoles; ++q)
         if (coeffD[(size_t)m * 6 * ctx->d.maxpoles + q] != 0.f) disp[m] = 1;
