@@ -518,7 +518,22 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
   const size_t n = 6 * (size_t)ctx->ncomp;
-  CK(cudaMemcpyAsync(ctx->ID, ID, sizeof(uint32_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+  // a large array is page-locked for the copy (registration is cheap next to the first copy of
+  // pageable memory); where that is refused the copy goes from pageable memory
+  const size_t bytes = sizeof(uint32_t) * n;
+  bool locked = false;
+  if (bytes >= ((size_t)64 << 20)) {
+    locked = cudaHostRegister(const_cast<uint32_t*>(ID), bytes, cudaHostRegisterReadOnly) == cudaSuccess;
+    if (!locked) (void)cudaGetLastError();
+  }
+  cudaError_t ce = cudaMemcpyAsync(ctx->ID, ID, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (locked) {
+    cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    cudaHostUnregister(const_cast<uint32_t*>(ID));
+    if (ce == cudaSuccess) ce = se;
+  }
+  if (ce != cudaSuccess)
+    return fail(ctx, GBF_ECUDA, "gbf_upload_materials: ID copy: %s", cudaGetErrorString(ce));
   // every ID must index the tables (checked on the device)
   const int rc = check_ids(ctx, "gbf_upload_materials");
   if (rc != GBF_OK) return rc;
