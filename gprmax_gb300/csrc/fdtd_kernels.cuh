@@ -118,6 +118,7 @@ struct StepParams {
   const int* d_it;
   Box boxE[kBoxes];       // sweep boxes of the E half-step (domain [0,nx) x [0,ny) x [0,nz))
   Box boxH[kBoxes];       // and of the H half-step (domain [0,nx] x [0,ny] x [0,nz])
+  float hrow[6];          // the H row shared by every material (DA, DBx, DBy, DBz, srcm), if any
 };
 
 // ---------------------------------------------------------------------------------------
@@ -355,18 +356,20 @@ __device__ __forceinline__ bool node_has_source(int idx, int n, const int* inl, 
 
 // Coefficients of the H half-step: per-material rows (C4: DA, DBx, DBy, DBz; Cs: srcm) indexed
 // by the node's material numbers, or, with IDP == 0 (every material has the same H row, as in
-// any model without magnetic materials), that one row held in registers and no material
-// numbers loaded at all.
+// any model without magnetic materials), that one row from the kernel parameters (constant
+// bank, no registers held) and no material numbers loaded at all.
 struct HCoef {
   const float4* C4;
   const float* Cs;
-  float4 u;
-  float us;
 };
 template <int IDP>
-__device__ __forceinline__ float4 hrow(const HCoef& c, uint32_t m) { return IDP == 0 ? c.u : c.C4[m]; }
+__device__ __forceinline__ float4 hrow(const StepParams& p, const HCoef& c, uint32_t m) {
+  return IDP == 0 ? make_float4(p.hrow[0], p.hrow[1], p.hrow[2], p.hrow[3]) : c.C4[m];
+}
 template <int IDP>
-__device__ __forceinline__ float hsrcm(const HCoef& c, uint32_t m) { return IDP == 0 ? c.us : c.Cs[m]; }
+__device__ __forceinline__ float hsrcm(const StepParams& p, const HCoef& c, uint32_t m) {
+  return IDP == 0 ? p.hrow[4] : c.Cs[m];
+}
 
 // H update of one node: main update (update_magnetic), slab corrections in slab order, sources.
 // where[a] / pr[a]: slab membership and profile index along each axis (axis_member; 0 outside
@@ -398,12 +401,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
     const bool mainu = ipos && jin && kin && hx2;
     const bool pml = PK != PML_NONE && (where[1] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = hrow<IDP>(hc, mx);
+    const float4 c = hrow<IDP>(p, hc, mx);
     const float Fo = hx;
     float F = c.x * Fo - c.z * dEz_y + c.w * dEy_z;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 0>(F, hsrcm<IDP>(hc, mx), where, XA, XB);
-    if (src) F = apply_h_sources(F, 3, i, j, k, it, hsrcm<IDP>(hc, mx), p);
+    if (pml) F = apply_pml<false, 0>(F, hsrcm<IDP>(p, hc, mx), where, XA, XB);
+    if (src) F = apply_h_sources(F, 3, i, j, k, it, hsrcm<IDP>(p, hc, mx), p);
     hx = F;
   }
   // Hy: main i in [0,nx), j in [1,ny], k in [0,nz); slabs along x and z
@@ -411,12 +414,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
     const bool mainu = iin && jpos && kin && hy2;
     const bool pml = PK != PML_NONE && (where[0] || where[2]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = hrow<IDP>(hc, my);
+    const float4 c = hrow<IDP>(p, hc, my);
     const float Fo = hy;
     float F = c.x * Fo - c.w * dEx_z + c.y * dEz_x;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 1>(F, hsrcm<IDP>(hc, my), where, XA, XB);
-    if (src) F = apply_h_sources(F, 4, i, j, k, it, hsrcm<IDP>(hc, my), p);
+    if (pml) F = apply_pml<false, 1>(F, hsrcm<IDP>(p, hc, my), where, XA, XB);
+    if (src) F = apply_h_sources(F, 4, i, j, k, it, hsrcm<IDP>(p, hc, my), p);
     hy = F;
   }
   // Hz: main i in [0,nx), j in [0,ny), k in [1,nz]; slabs along x and y
@@ -424,12 +427,12 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
     const bool mainu = iin && jin && (k >= 1) && hz2;
     const bool pml = PK != PML_NONE && (where[0] || where[1]);
     // the main update is formed on every node and kept where it applies (no branch)
-    const float4 c = hrow<IDP>(hc, mz);
+    const float4 c = hrow<IDP>(p, hc, mz);
     const float Fo = hz;
     float F = c.x * Fo - c.y * dEy_x + c.z * dEx_y;
     F = mainu ? F : Fo;
-    if (pml) F = apply_pml<false, 2>(F, hsrcm<IDP>(hc, mz), where, XA, XB);
-    if (src) F = apply_h_sources(F, 5, i, j, k, it, hsrcm<IDP>(hc, mz), p);
+    if (pml) F = apply_pml<false, 2>(F, hsrcm<IDP>(p, hc, mz), where, XA, XB);
+    if (src) F = apply_h_sources(F, 5, i, j, k, it, hsrcm<IDP>(p, hc, mz), p);
     hz = F;
   }
 }
@@ -529,8 +532,6 @@ h_half_step(const __grid_constant__ StepParams p) {
   HCoef hc;
   hc.C4 = p.smem ? s4 : p.cH4;
   hc.Cs = p.smem ? ss : p.cHs;
-  hc.u = IDP == 0 ? hc.C4[0] : make_float4(0.f, 0.f, 0.f, 0.f);
-  hc.us = IDP == 0 ? hc.Cs[0] : 0.f;
   int it = 0;
   if (p.nsrcH) it = *p.d_it;
   h_sweep<PK, IDP>(p, hc, blockIdx.x * blockDim.x + threadIdx.x, 0, gridDim.x * blockDim.x, it);
@@ -576,8 +577,6 @@ h_half_step_batch(const __grid_constant__ BatchParams bp) {
     HCoef hc;
     hc.C4 = p.smem ? s4 : p.cH4;
     hc.Cs = p.smem ? ss : p.cHs;
-    hc.u = IDP == 0 ? hc.C4[0] : make_float4(0.f, 0.f, 0.f, 0.f);
-    hc.us = IDP == 0 ? hc.Cs[0] : 0.f;
     const int it = p.nsrcH ? *p.d_it : 0;
     q = h_sweep<PK, IDP>(p, hc, q, __ldg(bp.rangeH + m), stride, it);
     if (q < end) q += stride;   // past the model's last node, inside its padding

@@ -410,6 +410,9 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   for (int m = 1; m < nmat && uni; ++m)
     uni = memcmp(coeffH + 5 * m, coeffH, 5 * sizeof(float)) == 0;
   ctx->uniform_h = uni;
+  // the shared row, read from the kernel parameters by the ID-free H half-step
+  for (int q = 0; q < 5; ++q) ctx->sp.hrow[q] = coeffH[q];
+  ctx->sp.hrow[5] = 0.f;
   // real dispersive state: every pole's eqt has imaginary part +0 and zt imaginary part +-0
   // (Debye poles; the E update reads only Re(T), and Im(T) then stays +0), packed IDs, and the
   // complex layout not requested (option bit 2)
