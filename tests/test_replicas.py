@@ -37,7 +37,7 @@ def _rank(rank, world, port, out):
 def test_two_replicas_take_the_slowest_rank_and_count_all_cells():
     world = 2
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context('spawn').Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
         res = dict(out)
