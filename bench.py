@@ -512,6 +512,24 @@ def run_adjoint(args):
         fd = (8 * (f[1] - f[-1]) - (f[2] - f[-2])) / (12 * h)
         errs.append(abs(fd - float(g[idx])) / max(abs(fd), 1e-300))
     solver.close()
+    # the same gradient with plain sqrt checkpointing (checkpoint_interval 0): a segment every
+    # ceil(sqrt(iterations)) steps, all but the last recomputed
+    rich = AdjointSolver(m, checkpoint_interval=0)
+    rich_times = []
+    for rep in range(4):
+        ee = e.clone().requires_grad_(True)
+        ss = s.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        CA, CB = m.edge_coefficients(ee, ss)
+        tr = fdtd_traces(CA, CB, rich)
+        L2 = 0.5 * ((tr.double() - obs) ** 2).sum()
+        L2.backward()
+        torch.cuda.synchronize()
+        rich_times.append(time.perf_counter() - t0)
+    t_rich = float(np.median(rich_times[1:]))
+    rich_dev = float((ee.grad - g).abs().max() / g.abs().max())
+    rich.close()
     cells_n = m.nx * m.ny * m.nz
     out = {'metric': 'adjoint_over_forward', 'value': round(t_grad / t_fwd, 3), 'unit': 'x',
            'n_gpus': 1, 'steps': m.iterations, 'warmup': args.warmup,
@@ -523,6 +541,13 @@ def run_adjoint(args):
                       'receivers': len(m.receivers)},
            'forward_s': round(t_fwd, 4), 'gradient_s': round(t_grad, 4),
            'gradient_runs_s': [round(t, 4) for t in grad_times],
+           'checkpointing': ('interval -1: the last segment as long as 60 % of the free device '
+                             'memory holds (kept from the forward, never recomputed), the steps '
+                             'before it in segments of ceil(sqrt(their count))'),
+           'sqrt_checkpointing': {'checkpoint_interval': 0, 'gradient_s': round(t_rich, 4),
+                                  'adjoint_over_forward': round(t_rich / t_fwd, 3),
+                                  'gradient_runs_s': [round(t, 4) for t in rich_times],
+                                  'max_rel_diff_vs_default': rich_dev},
            'forward_runs_s': [round(t, 4) for t in fwd_times],
            'forward_Mcells_per_s': round(cells_n * m.iterations / t_fwd / 1e6, 1),
            'fd_check': {'cells': 20, 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',

@@ -18,9 +18,13 @@ receivers). The model it differentiates is the reference's update with per-cell 
   component at the start of every iteration (``fields_outputs.py:40-67``).
 
 ``FDTDTraces`` is the ``torch.autograd.Function``: forward runs the time loop on the GPU
-(``gbf_adj_forward``) and keeps a checkpoint of the state every ~sqrt(T) steps; backward runs
-the transposed (reverse-time) updates (``gbf_adj_backward``), recomputing each segment's states
-from its checkpoint, and returns dL/dCA and dL/dCB per edge, accumulated in fp64. The map
+(``gbf_adj_forward``) and keeps a checkpoint at the start of every segment; backward runs the
+transposed (reverse-time) updates (``gbf_adj_backward``), recomputing each segment's states
+from its checkpoint, and returns dL/dCA and dL/dCB per edge, accumulated in fp64. By default
+(``checkpoint_interval=-1``) the last segment is as long as 60 % of the free device memory can
+hold and the forward leaves its states in place, so only the steps before it are recomputed
+(none when the whole run fits); ``checkpoint_interval=0`` gives segments of ceil(sqrt(T))
+steps. The map
 from (eps_r, sigma) to (CA, CB) is plain torch, so autograd carries the gradient to the cells.
 """
 import ctypes
@@ -127,7 +131,9 @@ class AdjointModel:
 class AdjointSolver:
     """GPU forward/adjoint engine of one ``AdjointModel`` (``gbf_adj_*`` in the C ABI)."""
 
-    def __init__(self, model, checkpoint_interval=0):
+    def __init__(self, model, checkpoint_interval=-1):
+        """checkpoint_interval: steps per segment; 0: ceil(sqrt(iterations)); -1: the last
+        segment sized to the free device memory (see the module docstring)."""
         self.model = model
         self.lib = _native.lib()
         self.h = ctypes.c_void_p(0)

@@ -484,8 +484,9 @@ struct gbf_adj {
   cudaStream_t stream = nullptr;
   std::string err;
   long long N = 0;           // nodes per component
-  int K = 1;                 // checkpoint interval
-  int nck = 0;               // checkpoints
+  int K = 1;                 // recompute slots (the longest segment)
+  int nck = 0;               // checkpoints (segments)
+  std::vector<int> seg;      // segment starts, nck + 1 entries (the last is iterations)
   size_t phi_len = 0;        // floats of one PhiSet (every slab, both pairs)
   size_t off[6] = {0, 0, 0, 0, 0, 0};
   AdjParams p{};
@@ -500,6 +501,7 @@ struct gbf_adj {
   float *lphiE = nullptr, *lphiH = nullptr, *dFE = nullptr, *dFH = nullptr;
   float *gCA = nullptr, *gCB = nullptr;                                // fp32 segment partials
   bool forward_done = false;
+  bool resident = false;     // the slots hold the last segment's states from the forward
   int grid = 0;
 };
 
@@ -551,7 +553,7 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
     return afail(nullptr, GBF_EINVAL, "gbf_adj_create: cell size and time step must be positive");
   if (d.nsrc < 0 || d.nsrc > kAdjSrcMax || d.nrx < 1 || d.nrx > kAdjRxMax)
     return afail(nullptr, GBF_EINVAL, "gbf_adj_create: 0..%d sources and 1..%d receivers", kAdjSrcMax, kAdjRxMax);
-  if (d.checkpoint_interval < 0 || d.reserved[0] || d.reserved[1] || d.reserved[2])
+  if (d.checkpoint_interval < -1 || d.reserved[0] || d.reserved[1] || d.reserved[2])
     return afail(nullptr, GBF_EINVAL, "gbf_adj_create: bad checkpoint interval or reserved fields");
   const int n3[3] = {d.nx, d.ny, d.nz};
   for (int s = 0; s < 6; ++s)
@@ -591,6 +593,35 @@ int gbf_adj_create(const gbf_adj_desc* desc, gbf_adj** out) {
     p.slab[s].ocount = t ? (int)(t * nu * nv) : 0;
     a->off[s] = a->phi_len;
     a->phi_len += 2 * (size_t)p.slab[s].ocount;
+  }
+  // segments: every K steps; with interval -1 the last segment is as long as the recompute
+  // slots (E, H and the E-side PML state per step) that fit in 60 % of the free device memory
+  // (the forward leaves it in the slots, so only the steps before it are ever recomputed), and
+  // the steps before it form segments of ceil(sqrt(their count))
+  {
+    const int T = d.iterations;
+    int last = T - (a->nck - 1) * a->K;
+    if (d.checkpoint_interval == -1) {
+      size_t freeb = 0, totalb = 0;
+      if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) freeb = 0;
+      const double per_step = 4.0 * (6.0 * (double)N + (double)a->phi_len);
+      long long l = (long long)(0.6 * (double)freeb / per_step);
+      if (l > T) l = T;
+      if (l < a->K) l = a->K < T ? a->K : T;
+      last = (int)l;
+      const int rest = T - last;
+      const int k0 = rest > 0 ? (int)ceil(sqrt((double)rest)) : 1;
+      a->seg.clear();
+      for (int s0 = 0; s0 < rest; s0 += k0) a->seg.push_back(s0);
+      a->seg.push_back(rest);
+      a->seg.push_back(T);
+      a->K = last > k0 ? last : k0;
+    } else {
+      a->seg.clear();
+      for (int s0 = 0; s0 < T; s0 += a->K) a->seg.push_back(s0);
+      a->seg.push_back(T);
+    }
+    a->nck = (int)a->seg.size() - 1;
   }
   const size_t PL = a->phi_len, K = a->K;
   const size_t ck = 6 * (size_t)N + 2 * PL;
@@ -717,9 +748,14 @@ int gbf_adj_forward(gbf_adj* a, const float* CA, const float* CB, float* traces)
   if (PL) AK(cudaMemsetAsync(a->phiE, 0, sizeof(float) * PL, a->stream));
   if (PL) AK(cudaMemsetAsync(a->phiH, 0, sizeof(float) * PL, a->stream));
   const PhiSet pE = phiset(a, a->phiE), pH = phiset(a, a->phiH);
-  for (int it = 0; it < a->d.iterations; ++it) {
-    if (it % a->K == 0) {
-      float* c = a->ckpt + (size_t)(it / a->K) * ck;
+  // the last segment runs straight into the recompute slots (out of place, as the backward
+  // would recompute it from its checkpoint), so the backward needs no recompute for it
+  const int T = a->d.iterations;
+  const int last0 = a->seg[a->nck - 1];
+  int sc = 0;   // next segment whose start takes a checkpoint
+  for (int it = 0; it < last0; ++it) {
+    if (it == a->seg[sc]) {
+      float* c = a->ckpt + (size_t)(sc++) * ck;
       int rc = copy_d2d(a, c, a->E, 3 * N);
       if (!rc) rc = copy_d2d(a, c + 3 * N, a->H, 3 * N);
       if (!rc) rc = copy_d2d(a, c + 6 * N, a->phiE, PL);
@@ -730,9 +766,34 @@ int gbf_adj_forward(gbf_adj* a, const float* CA, const float* CB, float* traces)
     adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, a->E, a->H, a->H, pH);
     adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, a->E, a->E, a->H, pE, pE, it);
   }
+  {
+    float* c = a->ckpt + (size_t)(a->nck - 1) * ck;
+    int rc = copy_d2d(a, c, a->E, 3 * N);
+    if (!rc) rc = copy_d2d(a, c + 3 * N, a->H, 3 * N);
+    if (!rc) rc = copy_d2d(a, c + 6 * N, a->phiE, PL);
+    if (!rc) rc = copy_d2d(a, c + 6 * N + PL, a->phiH, PL);
+    if (!rc) rc = copy_d2d(a, a->segE, a->E, 3 * N);
+    if (!rc) rc = copy_d2d(a, a->recH, a->H, 3 * N);
+    if (!rc) rc = copy_d2d(a, a->segPhiE, a->phiE, PL);
+    if (!rc) rc = copy_d2d(a, a->recPhiH, a->phiH, PL);
+    if (rc) return rc;
+    const PhiSet recPH = phiset(a, a->recPhiH);
+    for (int it = last0; it < T; ++it) {
+      const int m = it - last0;
+      float* Em = a->segE + (size_t)m * 3 * N;
+      float* Hm = a->segH + (size_t)m * 3 * N;
+      const float* Hprev = m == 0 ? a->recH : a->segH + (size_t)(m - 1) * 3 * N;
+      adj_fwd_rx<<<1, 64, 0, a->stream>>>(a->p, Em, traces, it);
+      adj_fwd_h<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, Em, Hprev, Hm, recPH);
+      adj_fwd_e<<<a->grid, kAdjThreads, 0, a->stream>>>(
+          a->p, Em, a->segE + (size_t)(m + 1) * 3 * N, Hm, phiset(a, a->segPhiE + (size_t)m * PL),
+          phiset(a, a->segPhiE + (size_t)(m + 1) * PL), it);
+    }
+  }
   AK(cudaGetLastError());
   AK(cudaStreamSynchronize(a->stream));
   a->forward_done = true;
+  a->resident = true;
   return GBF_OK;
 }
 
@@ -763,16 +824,18 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
   const PhiSet recPH = phiset(a, a->recPhiH);
   const int fold_blocks = a->grid;
   for (int c = a->nck - 1; c >= 0; --c) {
-    const int n0 = c * a->K;
-    const int n1 = (n0 + a->K < T) ? n0 + a->K : T;
+    const int n0 = a->seg[c];
+    const int n1 = a->seg[c + 1];
     const float* src = a->ckpt + (size_t)c * ck;
-    int rc = copy_d2d(a, a->segE, src, 3 * N);
-    if (!rc) rc = copy_d2d(a, a->recH, src + 3 * N, 3 * N);
-    if (!rc) rc = copy_d2d(a, a->segPhiE, src + 6 * N, PL);
-    if (!rc) rc = copy_d2d(a, a->recPhiH, src + 6 * N + PL, PL);
+    const bool have = a->resident && c == a->nck - 1;   // left in the slots by the forward
+    a->resident = false;
+    int rc = have ? 0 : copy_d2d(a, a->segE, src, 3 * N);
+    if (!rc && !have) rc = copy_d2d(a, a->recH, src + 3 * N, 3 * N);
+    if (!rc && !have) rc = copy_d2d(a, a->segPhiE, src + 6 * N, PL);
+    if (!rc && !have) rc = copy_d2d(a, a->recPhiH, src + 6 * N + PL, PL);
     if (rc) return rc;
     // recompute the segment into its slots: E_m, PhiE_m (m = 0..K) and H^{m+1/2} (m = 0..K-1)
-    for (int it = n0; it < n1; ++it) {
+    for (int it = have ? n1 : n0; it < n1; ++it) {
       const int m = it - n0;
       float* Em = a->segE + (size_t)m * 3 * N;
       float* Hm = a->segH + (size_t)m * 3 * N;

@@ -220,7 +220,13 @@ typedef struct gbf_adj_desc {
     int32_t pml_thickness[6];    /* x0, y0, z0, xmax, ymax, zmax; HORIPML order 1 */
     int32_t nsrc;                /* Hertzian dipoles, at most 16 */
     int32_t nrx;                 /* receivers, at least 1 */
-    int32_t checkpoint_interval; /* steps between checkpoints; 0: ceil(sqrt(iterations)) */
+    int32_t checkpoint_interval; /* steps between checkpoints; 0: ceil(sqrt(iterations));
+                                    -1: the last segment as long as its recompute slots fit in
+                                    60 % of the free device memory (all steps if they fit, when
+                                    nothing is recomputed) and the steps before it in segments
+                                    of ceil(sqrt(their count)). The forward leaves the last
+                                    segment in the slots, so the first backward after it
+                                    recomputes every segment but that one */
     int32_t reserved[3];         /* must be zero */
 } gbf_adj_desc;
 typedef struct gbf_adj gbf_adj;

@@ -58,7 +58,7 @@ def test_adjoint_gradient_matches_torch_autograd(native):
 
 def test_gradient_independent_of_checkpoint_interval(native):
     grads = []
-    for interval in (1, 9, 0, 70):
+    for interval in (1, 9, 0, 70, -1):
         m, solver = _setup(interval)
         eps, sig = materials(m, 6, torch.float64)
         obs = torch.zeros((len(m.receivers), m.iterations), dtype=torch.float64)
