@@ -16,6 +16,9 @@ through the reference's own driver (``oracle/ref_harness.py``: input parsing, gr
 * ``refout_rx<n>_<output>``: for the reference's own test models, the traces stored in their
   ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote.
 
+The reference's own test models come from ``tests/models_basic`` (with ``_ref.out`` files) and
+``tests/models_pmls`` (the PML slab-by-slab and thin-plate models, which have none).
+
 It also copies one of those ``_ref.out`` files here as a fixture for the HDF5 reader.
 
 Usage: python tests/golden/make_golden.py [--src /root/reference] [--only NAME ...]
@@ -40,6 +43,11 @@ sys.path.insert(0, os.path.join(ROOT, 'oracle'))
 REFERENCE_MODELS = ['hertzian_dipole_fs', 'hertzian_dipole_dispersive', 'hertzian_dipole_hs',
                     'magnetic_dipole_fs', '2D_ExHyHz', '2D_EyHxHz', '2D_EzHxHy',
                     'cylinder_Ascan_2D']
+# the reference's PML test models (tests/models_pmls; no stored outputs: golden from the run)
+PML_MODELS = ['pml_off.in'] + ['pml_{0}/pml_{0}.in'.format(s) for s in
+                               ('x0', 'y0', 'z0', 'xmax', 'ymax', 'zmax')] + \
+    ['pml_3D_pec_plate/pml_3D_pec_plate_{}.in'.format(f) for f in
+     ('CFS-PML', 'HORIPML-1', 'HORIPML-2', 'MRIPML-1', 'MRIPML-2')]
 HDF5_FIXTURE = 'hertzian_dipole_dispersive_ref.out'
 
 CHILD = r'''
@@ -114,6 +122,10 @@ def main():
             text = f.read()
         ref = os.path.join(d, n + '_ref.out')
         todo['ref_' + n] = (text, ref if os.path.exists(ref) else None)
+    for rel in PML_MODELS:
+        with open(os.path.join(a.src, 'tests', 'models_pmls', rel)) as f:
+            text = f.read()
+        todo['ref_' + os.path.splitext(os.path.basename(rel))[0]] = (text, None)
     for name, (text, ref) in sorted(todo.items()):
         if a.only and name not in a.only:
             continue
