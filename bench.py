@@ -381,19 +381,21 @@ def run_bscan(args):
     another through the plain solver. Both arms upload every model from host memory, advance
     it K steps and read its receiver trace back; traces/s scales the K-step times to the full
     2598 iterations (the per-step work does not change with the step index). The host model
-    build (input parsing and material-ID build, identical for both arms) is timed separately."""
+    build (input parsing and material-ID build, identical for both arms) is timed separately.
+    ``--shapes`` replaces the two model shapes (many small models: the case batching is for)."""
     from gprmax_gb300 import workloads
     from gprmax_gb300.solver import BatchModel, DeviceModel
     K, W = args.steps, args.warmup
+    shapes = tuple(tuple(int(v) for v in s.split('x')) for s in args.shapes)
     # the same 128 models built with their geometry in device memory (timed, then freed)
     t0 = time.perf_counter()
-    dgrids = workloads.bscan_models(args.models, device_build=True)
+    dgrids = workloads.bscan_models(args.models, shapes, device_build=True)
     t_build_dev = time.perf_counter() - t0
     for G in dgrids:
         G.geom.close()
     del dgrids
     t0 = time.perf_counter()
-    grids = workloads.bscan_models(args.models)
+    grids = workloads.bscan_models(args.models, shapes)
     t_build = time.perf_counter() - t0
     iters = min(G.iterations for G in grids)
     cells = sum(G.nx * G.ny * G.nz for G in grids)
@@ -431,7 +433,7 @@ def run_bscan(args):
            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
            'data': 'synthetic (seeded 3-layer soils with buried PEC spheres)',
            'config': {'workload': 'bscan_uneven_{}_models'.format(len(grids)),
-                      'shapes': [[200, 200, 100], [300, 300, 150]], 'iterations': iters,
+                      'shapes': [list(s) for s in shapes], 'iterations': iters,
                       'cells_total': cells},
            'plain_sequential': {'value': round(len(grids) / full_plain, 4), 'unit': 'traces/s',
                                 'ms_per_step_all_models': dev_plain / K,
@@ -670,6 +672,8 @@ def main():
                          'cubes of 100^3 to 600^3 cells; build: model build on the host and '
                          'in device memory')
     ap.add_argument('--models', type=int, default=128, help='bscan: number of models')
+    ap.add_argument('--shapes', nargs=2, default=['200x200x100', '300x300x150'],
+                    help='bscan: the two model shapes, NXxNYxNZ cells at 2 mm')
     ap.add_argument('--sizes', type=int, nargs='+', default=[100, 200, 300, 400, 500, 600],
                     help='sweep: cube edge lengths in cells')
     args = ap.parse_args()

@@ -110,7 +110,8 @@ def bscan_input(shape, seed, position, dx=0.002, timewindow='10e-9', pml=10):
     eps_r ~ U[3,15], sigma ~ logU[1e-4,1e-2] S/m) filling the lower 70 % of the domain, one
     buried PEC sphere of radius U[15,30] mm at a random position in the soil, and a y-directed
     Hertzian dipole with a receiver 40 mm away in x, 10 mm above the surface, moved 4 mm per
-    model along x (``position``); Ricker 1.5 GHz."""
+    model along x (``position``, wrapped to the positions that keep the pair 30 mm clear of the
+    far side); Ricker 1.5 GHz."""
     nx, ny, nz = shape
     rng = np.random.default_rng(seed)
     er = rng.uniform(3, 15, 3)
@@ -128,9 +129,9 @@ def bscan_input(shape, seed, position, dx=0.002, timewindow='10e-9', pml=10):
             z[layer] * dx, nx * dx, ny * dx, z[layer + 1] * dx, layer))
     r = rng.uniform(0.015, 0.030)
     c = (rng.uniform(0.2, 0.8) * nx * dx, rng.uniform(0.2, 0.8) * ny * dx,
-         rng.uniform(r + 0.03, surf * dx - r))
+         rng.uniform(r + 0.03, max(surf * dx - r, r + 0.03)))
     lines.append('#sphere: {:g} {:g} {:g} {:g} pec'.format(c[0], c[1], c[2], r))
-    x = 0.06 + 0.004 * position
+    x = 0.06 + 0.004 * (position % max(1, int((nx * dx - 0.13) / 0.004 + 1e-9) + 1))
     zs = surf * dx + 0.01
     lines.append('#hertzian_dipole: y {:g} {:g} {:g} w'.format(x, ny * dx / 2, zs))
     lines.append('#rx: {:g} {:g} {:g}'.format(x + 0.04, ny * dx / 2, zs))
