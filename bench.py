@@ -189,7 +189,8 @@ def build_workload(iterations, grid=None):
 
 
 def cpu_baseline(G, budget_s=20.0, max_steps=60):
-    """Bounded CPU run of the same model: reference kernels on all host cores."""
+    """Bounded CPU run of the same model: reference kernels on all host cores, one warm-up
+    step and then at most ``max_steps`` (the model must have ``max_steps + 1`` iterations)."""
     import ref_cpu
     cores = os.cpu_count() or 1
     solver, kind = ref_cpu.make_solver(G, cores)
@@ -268,10 +269,7 @@ def run_gb300(args):
     t_e2e = time.perf_counter() - t0
     e2e_parts = {'model_upload_s': round(t1 - t0, 4), 'steps_s': round(t2 - t1, 4),
                  'readback_s': round(t0 + t_e2e - t2, 4)}
-    h2d = (G.ID.nbytes + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
-           + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)
-           + sum(8 * getattr(p, 'ERA').nbytes for p in G.pmls)
-           + len(G.hertziandipoles + G.voltagesources + G.magneticdipoles) * G.iterations * 4)
+    h2d = upload_bytes(G)
     d2h = rx.nbytes
     t_e2e = barrier_max(dist, t_e2e)
 
@@ -331,6 +329,15 @@ def run_gb300(args):
 
 def dm_bytes(G):
     return G.memory_estimate()
+
+
+def upload_bytes(G):
+    """Host bytes a model's upload copies to the device: material IDs, coefficient tables,
+    PML profiles and the sources' waveform tables."""
+    return (G.ID.nbytes + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
+            + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)
+            + sum(8 * getattr(p, 'ERA').nbytes for p in G.pmls)
+            + len(G.hertziandipoles + G.voltagesources + G.magneticdipoles) * G.iterations * 4)
 
 
 def run_reference(args):
@@ -443,6 +450,90 @@ def run_bscan(args):
                        'Mcells_per_s': round(cells * K / (dev_batch / 1e3) / 1e6, 1)},
            'speedup_vs_plain': round(full_plain / full_batch, 3),
            'host_build_s': round(t_build, 2), 'device_build_s': round(t_build_dev, 2)}
+    print(json.dumps(out), flush=True)
+
+
+def run_bscan2d(args):
+    """2D B-scan (``workloads.bscan_2d_models``: TMz, 120x105 cells at 2 mm, a dielectric
+    half-space with a buried PEC cylinder, 637 iterations, ``--traces`` traces with the antenna
+    pair stepped one cell per trace). Every trace runs to its last iteration in both arms, with
+    the upload of each model from host memory and the read-back of its trace inside the timed
+    region (wall clock around the public API): the batched form (one launch per half-step over
+    every trace, the time loop replayed from one CUDA graph) against the traces run one after
+    another through the plain solver. Median of three runs of each arm after a warm-up of each.
+    The whole B-scan's state (about 2 MB per trace) stays in L2, as in any run of this model, so
+    no flush is done. The host model build (the same for both arms) is timed separately; the
+    reference's own kernels on the host cores time one trace."""
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.solver import BatchModel, DeviceModel
+    W = args.warmup
+    t0 = time.perf_counter()
+    grids = workloads.bscan_2d_models(args.traces)
+    t_build = time.perf_counter() - t0
+    n = len(grids)
+    iters = grids[0].iterations
+    cells = grids[0].nx * grids[0].ny * grids[0].nz
+    warm = DeviceModel(grids[0])
+    warm.run(W)
+    warm.synchronize()
+    warm.close()
+    warm = BatchModel(grids[:2])
+    warm.run(W)
+    warm.synchronize()
+    warm.close()
+
+    def plain():
+        t0 = time.perf_counter()
+        dev, traces = 0.0, []
+        for G in grids:
+            dm = DeviceModel(G)
+            dev += dm.run_timed(iters)
+            traces.append(dm.receivers())
+            dm.close()
+        return time.perf_counter() - t0, dev, traces
+
+    def batched():
+        t0 = time.perf_counter()
+        bm = BatchModel(grids)
+        dev = bm.run_timed(iters)
+        traces = bm.receivers()
+        bm.close()
+        return time.perf_counter() - t0, dev, traces
+
+    runs_p = [plain() for _ in range(3)]
+    runs_b = [batched() for _ in range(3)]
+    identical = all(np.array_equal(a, b) for a, b in zip(runs_p[0][2], runs_b[0][2]))
+    wall_p = float(np.median([r[0] for r in runs_p]))
+    dev_p = float(np.median([r[1] for r in runs_p]))
+    wall_b = float(np.median([r[0] for r in runs_b]))
+    dev_b = float(np.median([r[1] for r in runs_b]))
+    rx_bytes = sum(int(np.asarray(t).nbytes) for t in runs_b[0][2])
+    out = {'metric': 'traces/s', 'value': round(n / wall_b, 2), 'unit': 'traces/s',
+           'n_gpus': 1, 'steps': iters, 'warmup': W, 'ms_per_step': dev_b / iters,
+           'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+           'data': 'synthetic (seeded half-space with a buried PEC cylinder)',
+           'config': {'workload': 'bscan_2d_cylinder_{}_traces'.format(n),
+                      'shape': [grids[0].nx, grids[0].ny, grids[0].nz], 'iterations': iters,
+                      'cells_per_trace': cells,
+                      'l2': 'no flush: the B-scan state fits in L2 in any run of this model'},
+           'e2e': {'value': round(n / wall_b, 2), 'unit': 'traces/s',
+                   'h2d_bytes_per_step': round(sum(upload_bytes(G) for G in grids) / iters, 1),
+                   'd2h_bytes_per_step': round(rx_bytes / iters, 1),
+                   'note': 'whole B-scan per timed run: every model uploaded, run and read back'},
+           'plain_sequential': {'value': round(n / wall_p, 2), 'unit': 'traces/s',
+                                'device_ms_all_traces': round(dev_p, 3)},
+           'batched': {'device_ms_all_traces': round(dev_b, 3),
+                       'Mcells_per_s': round(cells * n * iters / (dev_b / 1e3) / 1e6, 1)},
+           'speedup_vs_plain': round(wall_p / wall_b, 3),
+           'traces_identical': bool(identical),
+           'gpu_launches': 3 * iters,
+           'host_build_s': round(t_build, 3)}
+    if args.cpu_baseline:
+        cb = cpu_baseline(grids[0], budget_s=min(args.cpu_budget, 20.0), max_steps=iters - 1)
+        cb['value'] = round(cb['value'] * 1e6 / (cells * iters), 2)
+        cb['unit'] = 'traces/s'
+        cb['sample'] = 'one trace, ' + cb['sample']
+        out['cpu_baseline'] = cb
     print(json.dumps(out), flush=True)
 
 
@@ -664,14 +755,16 @@ def main():
                     help='smaller soil grid (profiling runs); default 400 400 200')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
-    ap.add_argument('--workload', choices=['soil', 'bscan', 'adjoint', 'sweep', 'build'],
+    ap.add_argument('--workload', choices=['soil', 'bscan', 'bscan2d', 'adjoint', 'sweep', 'build'],
                     default='soil',
                     help='soil: the 400x400x200 Debye soil (default); bscan: the batched uneven '
-                         'B-scan against sequential plain runs; adjoint: gradient cost and '
+                         'B-scan against sequential plain runs; bscan2d: a whole 2D B-scan, '
+                         'batched against sequential; adjoint: gradient cost and '
                          'finite-difference check of the differentiable time loop; sweep: '
                          'cubes of 100^3 to 600^3 cells; build: model build on the host and '
                          'in device memory')
     ap.add_argument('--models', type=int, default=128, help='bscan: number of models')
+    ap.add_argument('--traces', type=int, default=60, help='bscan2d: number of traces')
     ap.add_argument('--shapes', nargs=2, default=['200x200x100', '300x300x150'],
                     help='bscan: the two model shapes, NXxNYxNZ cells at 2 mm')
     ap.add_argument('--sizes', type=int, nargs='+', default=[100, 200, 300, 400, 500, 600],
@@ -681,6 +774,8 @@ def main():
         args.warmup = 3
     if args.workload == 'bscan':
         run_bscan(args)
+    elif args.workload == 'bscan2d':
+        run_bscan2d(args)
     elif args.workload == 'adjoint':
         run_adjoint(args)
     elif args.workload == 'build':

@@ -153,6 +153,46 @@ def bscan_models(nmodels=128, shapes=((200, 200, 100), (300, 300, 150)), seed=11
     return grids
 
 
+def bscan_2d_input(shape=(120, 105), dx=0.002, timewindow='3e-9', seed=31):
+    """Input-file lines of a 2D (TMz, one cell in z) B-scan: a seeded dielectric half-space
+    (eps_r ~ U[4, 9], sigma ~ logU[1e-4, 1e-2] S/m) filling the lower 80 % of the domain, a PEC
+    cylinder along z of radius U[8, 14] mm buried in it, and a z-directed Hertzian dipole with a
+    receiver 40 mm away in x, 10 mm above the surface, both stepped one cell in x per trace
+    (``#src_steps`` / ``#rx_steps``); Ricker 1.5 GHz; the default 10-cell PML (none along z)."""
+    nx, ny = shape
+    rng = np.random.default_rng(seed)
+    er = rng.uniform(4, 9)
+    sig = 10 ** rng.uniform(-4, -2)
+    surf = int(ny * 0.8)
+    r = rng.uniform(0.008, 0.014)
+    cx = rng.uniform(0.4, 0.6) * nx * dx
+    cy = rng.uniform(0.3, 0.6) * surf * dx
+    ys = surf * dx + 0.01
+    return [line + '\n' for line in (
+        '#domain: {:g} {:g} {:g}'.format(nx * dx, ny * dx, dx),
+        '#dx_dy_dz: {0:g} {0:g} {0:g}'.format(dx), '#time_window: {}'.format(timewindow),
+        '#material: {!r} {!r} 1 0 half_space'.format(float(er), float(sig)),
+        '#waveform: ricker 1 1.5e9 w',
+        '#hertzian_dipole: z {:g} {:g} 0 w'.format(0.04, ys),
+        '#rx: {:g} {:g} 0'.format(0.08, ys),
+        '#src_steps: {:g} 0 0'.format(dx), '#rx_steps: {:g} 0 0'.format(dx),
+        '#box: 0 0 0 {:g} {:g} {:g} half_space'.format(nx * dx, surf * dx, dx),
+        '#cylinder: {0:g} {1:g} 0 {0:g} {1:g} {2:g} {3:g} pec'.format(cx, cy, dx, r))]
+
+
+def bscan_2d_models(ntraces=60, shape=(120, 105), seed=31, messages=False, device_build=False):
+    """The grids of every trace of the 2D B-scan, each stepped to its model run as the
+    reference's ``-n`` loop steps them (``model_build_run.py:308-324``)."""
+    from .model import step_sources_receivers
+    lines = bscan_2d_input(shape, seed=seed)
+    grids = []
+    for m in range(ntraces):
+        G = build_grid(lines, messages=messages, device_build=device_build)
+        step_sources_receivers(G, m + 1, ntraces)
+        grids.append(G)
+    return grids
+
+
 def gaussian_random_field(shape, corr_cells, seed, lo=1.0, hi=20.0, mean=8.0, std=4.0):
     """Seeded smooth Gaussian random field: white noise filtered in Fourier space by a Gaussian
     of correlation length ``corr_cells``, scaled to ``mean`` +/- ``std`` and clipped to

@@ -115,3 +115,36 @@ def test_batch_of_debye_and_lorentz_models_keeps_complex_state(native):
     dm.close()
     # the real-part layout gives back the complex state with imaginary parts +0
     np.testing.assert_array_equal(np.asarray(Treal).view(np.uint32), np.asarray(T[0]).view(np.uint32))
+
+
+def test_batch_of_2d_bscan_traces(native, tmp_path):
+    """A 2D (TMz) B-scan as one batch, the antenna pair stepped one cell per trace: every
+    trace and final field equals the plain solver's bit for bit, the first and last traces
+    equal the oracle's, and the merged ``.out`` file holds the traces in model order."""
+    import oracle
+    from gprmax_gb300 import workloads
+    from gprmax_gb300.outputs import read_outputfile
+    from gprmax_gb300.solver import BatchModel, solve_gb300_batch
+    grids = workloads.bscan_2d_models(8)
+    assert grids[0].nz == 1 and grids[0].mode == '2D TMz'
+    assert grids[-1].rxs[0].xcoord == grids[0].rxs[0].xcoord + 7
+    bm = BatchModel(grids)
+    bm.run()
+    rx = bm.receivers()
+    fields = [m.fields() for m in bm.models]
+    bm.close()
+    for n, G in enumerate(grids):
+        prx, pf = _plain(G)
+        np.testing.assert_array_equal(rx[n], prx, err_msg='trace {}'.format(n))
+        np.testing.assert_array_equal(fields[n], pf, err_msg='trace {} fields'.format(n))
+    for n in (0, len(grids) - 1):
+        ref = oracle.OracleSolver(grids[n]).run()
+        np.testing.assert_array_equal(rx[n], ref.receivers(), err_msg='trace {} oracle'.format(n))
+    out = str(tmp_path / 'bscan2d_merged.out')
+    solve_gb300_batch(grids, outputfile=out)
+    merged, _ = read_outputfile(out)
+    from gprmax_gb300.receivers import OUTPUT_INDEX
+    ez = merged['rx1']['Ez']
+    assert ez.shape == (grids[0].iterations, len(grids))
+    for n in range(len(grids)):
+        np.testing.assert_array_equal(ez[:, n], rx[n][OUTPUT_INDEX['Ez'], :, 0])

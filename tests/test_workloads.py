@@ -31,3 +31,13 @@ def test_antenna_pair_inside_the_pml_free_region(shape):
         assert min(xs) == pytest.approx(0.06) and max(xs) == pytest.approx(0.06 + 0.004 * 63)
     else:
         assert 1 <= len(xs) < 64
+
+
+def test_2d_bscan_models_step_the_antenna_pair():
+    grids = workloads.bscan_2d_models(4)
+    for n, G in enumerate(grids):
+        assert G.mode == '2D TMz' and G.nz == 1
+        assert G.pmlthickness['z0'] == 0 and G.pmlthickness['x0'] == 10
+        assert G.hertziandipoles[0].xcoord == grids[0].hertziandipoles[0].xcoord + n
+        assert G.rxs[0].xcoord == grids[0].rxs[0].xcoord + n
+        assert G.rxs[0].xcoord - G.hertziandipoles[0].xcoord == 20
