@@ -347,7 +347,7 @@ def run_reference(args):
         return
     import ref_cpu
     K, W = args.steps, args.warmup
-    G = build_workload(3117)
+    G = build_workload(3117, args.grid)
     cores = os.cpu_count() or 1
     solver, kind = ref_cpu.make_solver(G, cores)
     t0 = time.perf_counter()
