@@ -526,7 +526,9 @@ def run_bscan2d(args):
                        'Mcells_per_s': round(cells * n * iters / (dev_b / 1e3) / 1e6, 1)},
            'speedup_vs_plain': round(wall_p / wall_b, 3),
            'traces_identical': bool(identical),
-           'gpu_launches': 3 * iters,
+           # per batched B-scan: H, E and end-of-step kernels per iteration, and per model
+           # upload the ID packing and the ID range check
+           'gpu_launches': 3 * iters + 2 * n,
            'host_build_s': round(t_build, 3)}
     if args.cpu_baseline:
         cb = cpu_baseline(grids[0], budget_s=min(args.cpu_budget, 20.0), max_steps=iters - 1)
