@@ -188,6 +188,25 @@ def build_workload(iterations, grid=None):
     return G
 
 
+def cpu_model():
+    """The host CPU's model name (``/proc/cpuinfo``; the architecture when it names none)."""
+    import platform
+    part = None
+    try:
+        with open('/proc/cpuinfo') as f:
+            for line in f:
+                key = line.split(':')[0].strip().lower()
+                if key in ('model name', 'hardware', 'cpu model'):
+                    return line.split(':', 1)[1].strip()
+                if key == 'cpu part' and part is None:
+                    part = line.split(':', 1)[1].strip()
+    except OSError:
+        pass
+    if part:   # Arm cores name themselves by part number only (0xd4f: Neoverse V2, as in Grace)
+        return {'0xd4f': 'Arm Neoverse V2'}.get(part.lower(), 'Arm CPU part ' + part)
+    return platform.machine()
+
+
 def cpu_baseline(G, budget_s=20.0, max_steps=60):
     """Bounded CPU run of the same model: reference kernels on all host cores, one warm-up
     step and then at most ``max_steps`` (the model must have ``max_steps + 1`` iterations)."""
@@ -205,7 +224,7 @@ def cpu_baseline(G, budget_s=20.0, max_steps=60):
     t = time.perf_counter() - t0
     cells = G.nx * G.ny * G.nz
     return {'value': cells * n / t / 1e6, 'unit': METRIC, 'cores': cores, 'kind': kind,
-            'sample': '{} steps (after 1 warm-up step) of the full {}x{}x{} model, {} OpenMP '
+            'cpu': cpu_model(), 'sample': '{} steps (after 1 warm-up step) of the full {}x{}x{} model, {} OpenMP '
                       'threads'.format(n, G.nx, G.ny, G.nz, cores)}
 
 
@@ -373,7 +392,7 @@ def run_reference(args):
            'data': 'synthetic (seeded fractal Debye soil)', 'impl': 'reference',
            'config': {'workload': WORKLOAD if not args.grid else 'dispersive_soil_{}x{}x{}'.format(*args.grid), 'grid': [G.nx, G.ny, G.nz], 'cells': cells},
            'cpu_baseline': {'value': round(value, 2), 'unit': METRIC, 'cores': cores,
-                            'kind': kind, 'sample': sample},
+                            'kind': kind, 'cpu': cpu_model(), 'sample': sample},
            'e2e': {'value': round(value, 2), 'unit': METRIC, 'h2d_bytes_per_step': 0,
                    'd2h_bytes_per_step': 0},
            'gpu_launches': 0}
