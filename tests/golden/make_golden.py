@@ -14,7 +14,10 @@ through the reference's own driver (``oracle/ref_harness.py``: input parsing, gr
   fields Ex..Hz of that build;
 * ``fma_rx<n>_<output>``: the same traces from the default (-march=native) build;
 * ``refout_rx<n>_<output>``: for the reference's own test models, the traces stored in their
-  ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote.
+  ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote;
+* ``model_run``, ``model_end``: for the B-scan fixtures, the model run (of ``model_end``) that
+  the reference's ``-n`` loop built and solved, its sources and receivers stepped by
+  ``#src_steps`` / ``#rx_steps``.
 
 The reference's own test models come from ``tests/models_basic`` (with ``_ref.out`` files) and
 ``tests/models_pmls`` (the PML slab-by-slab and thin-plate models, which have none).
@@ -54,7 +57,8 @@ CHILD = r'''
 import sys, hashlib, numpy as np
 sys.path.insert(0, {oracle!r})
 import ref_harness as rh
-G = rh.run_reference({inputfile!r}, src={src!r}, nthreads=8, variant={variant!r})
+G = rh.run_reference({inputfile!r}, src={src!r}, currentmodelrun={run}, modelend={end},
+                     nthreads=8, variant={variant!r})
 out = {{'iterations': G.iterations, 'dt': G.dt, 'nmat': len(G.materials),
         'ID_sha256': hashlib.sha256(np.ascontiguousarray(G.ID).tobytes()).hexdigest(),
         'coeffE': G.updatecoeffsE, 'coeffH': G.updatecoeffsH}}
@@ -80,22 +84,25 @@ np.savez({dest!r}, **out)
 '''
 
 
-def run_child(inputfile, src, variant, dest):
+def run_child(inputfile, src, variant, dest, run=1, end=1):
     code = CHILD.format(oracle=os.path.join(ROOT, 'oracle'), inputfile=inputfile, src=src,
-                        variant=variant, dest=dest)
+                        variant=variant, dest=dest, run=run, end=end)
     subprocess.run([sys.executable, '-c', code], check=True, cwd=ROOT)
     return dict(np.load(dest, allow_pickle=False))
 
 
-def make(name, text, src, refout=None):
+def make(name, text, src, refout=None, run=1, end=1):
     with tempfile.TemporaryDirectory() as tmp:
         inputfile = os.path.join(tmp, name + '.in')
         with open(inputfile, 'w') as f:
             f.write(text)
-        exact = run_child(inputfile, src, 'nofma', os.path.join(tmp, 'exact.npz'))
-        fma = run_child(inputfile, src, '', os.path.join(tmp, 'fma.npz'))
+        exact = run_child(inputfile, src, 'nofma', os.path.join(tmp, 'exact.npz'), run, end)
+        fma = run_child(inputfile, src, '', os.path.join(tmp, 'fma.npz'), run, end)
     out = dict(exact)
     out['input'] = np.array(text)
+    if end > 1:
+        out['model_run'] = np.int64(run)
+        out['model_end'] = np.int64(end)
     for k, v in fma.items():
         if k.startswith('rx'):
             out['fma_' + k] = v
@@ -115,7 +122,11 @@ def main():
     ap.add_argument('--only', nargs='*')
     a = ap.parse_args()
     from models import MODELS
+    from gprmax_gb300.workloads import bscan_2d_input
     todo = {n: (t, None) for n, t in MODELS.items()}
+    # the first and last model runs of a 6-trace 2D B-scan (antenna pair stepped per run)
+    bscan = ''.join(bscan_2d_input())
+    runs = {'bscan2d_run1': 1, 'bscan2d_run6': 6}
     for n in REFERENCE_MODELS:
         d = os.path.join(a.src, 'tests', 'models_basic', n)
         with open(os.path.join(d, n + '.in')) as f:
@@ -130,6 +141,10 @@ def main():
         if a.only and name not in a.only:
             continue
         make(name, text, a.src, ref)
+    for name, run in runs.items():
+        if a.only and name not in a.only:
+            continue
+        make(name, bscan, a.src, None, run, 6)
     shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
                              HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
     with open(os.path.join(HERE, 'README.txt'), 'w') as f:

@@ -186,3 +186,13 @@ MODELS = {
 #rx: 0.020 0.018 0.021 wet Ex Ey Ez Hx Hy Hz
 """,
 }
+
+
+def build_fixture(g, **kw):
+    """The grid of a golden fixture: its input text through the front-end and, for a B-scan
+    fixture, its sources and receivers stepped to the recorded model run."""
+    from gprmax_gb300.model import build_grid, step_sources_receivers
+    G = build_grid(str(g['input']).splitlines(True), messages=False, **kw)
+    if 'model_run' in g:
+        step_sources_receivers(G, int(g['model_run']), int(g['model_end']))
+    return G

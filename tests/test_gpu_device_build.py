@@ -20,10 +20,10 @@ FIXTURES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDE
 
 @pytest.mark.parametrize('name', FIXTURES)
 def test_device_build_reproduces_reference_model(native, name):
-    from gprmax_gb300.model import build_grid
+    from models import build_fixture
     from gprmax_gb300.solver import DeviceModel
     g = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
-    D = build_grid(str(g['input']).splitlines(True), messages=False, device_build=True)
+    D = build_fixture(g, device_build=True)
     try:
         ids = np.ascontiguousarray(D.geom.ids())
         assert hashlib.sha256(ids.tobytes()).hexdigest() == str(g['ID_sha256'])

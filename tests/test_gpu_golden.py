@@ -19,11 +19,11 @@ COMPONENTS = ('Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz')
 
 @pytest.mark.parametrize('name', NAMES)
 def test_gpu_reproduces_reference_run(native, name):
-    from gprmax_gb300.model import build_grid
+    from models import build_fixture
     from gprmax_gb300.receivers import OUTPUT_INDEX
     from gprmax_gb300.solver import DeviceModel
     g = dict(np.load(os.path.join(GOLDEN, name + '.npz'), allow_pickle=False))
-    G = build_grid(str(g['input']).splitlines(True), messages=False)
+    G = build_fixture(g)
     dm = DeviceModel(G)
     dm.run()
     rx = dm.receivers()

@@ -34,9 +34,8 @@ def _load(name):
 
 
 def _build(g):
-    from gprmax_gb300.model import build_grid
-    text = str(g['input'])
-    return build_grid(text.splitlines(True), messages=False)
+    from models import build_fixture
+    return build_fixture(g)
 
 
 def _check_build(G, g):
