@@ -15,6 +15,10 @@ through the reference's own driver (``oracle/ref_harness.py``: input parsing, gr
 * ``fma_rx<n>_<output>``: the same traces from the default (-march=native) build;
 * ``refout_rx<n>_<output>``: for the reference's own test models, the traces stored in their
   ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote;
+* ``src<n>_whole``, ``src<n>_half``: the waveform tables of every voltage source, Hertzian
+  dipole and magnetic dipole, in that order (the reference's ``calculate_waveform_values``);
+* ``file_<name>``: the text of a file the input reads (an ``#excitation_file``), to be written
+  beside the input before it is built;
 * ``model_run``, ``model_end``: for the B-scan fixtures, the model run (of ``model_end``) that
   the reference's ``-n`` loop built and solved, its sources and receivers stepped by
   ``#src_steps`` / ``#rx_steps``.
@@ -53,6 +57,33 @@ PML_MODELS = ['pml_off.in'] + ['pml_{0}/pml_{0}.in'.format(s) for s in
      ('CFS-PML', 'HORIPML-1', 'HORIPML-2', 'MRIPML-1', 'MRIPML-2')]
 HDF5_FIXTURE = 'hertzian_dipole_dispersive_ref.out'
 
+# every waveform type of the reference, two user waveforms from an excitation file (with a time
+# column), delayed and cut-off sources, a magnetic dipole and a resistive voltage source
+_TYPES = ['gaussian', 'gaussiandot', 'gaussiandotnorm', 'gaussiandotdot', 'gaussiandotdotnorm',
+          'gaussianprime', 'gaussiandoubleprime', 'ricker', 'sine', 'contsine', 'impulse']
+WAVEFORMS = '\n'.join(
+    ['#title: every waveform type', '#domain: 0.020 0.020 0.020', '#dx_dy_dz: 0.001 0.001 0.001',
+     '#time_window: 300', '#pml_cells: 0', '#excitation_file: exc.txt'] +
+    ['#waveform: {} 1.3 2e9 w{}'.format(t, n) for n, t in enumerate(_TYPES)] +
+    ['#hertzian_dipole: z {:.3f} 0.010 0.010 w{}'.format(0.004 + 0.001 * n, n)
+     for n in range(len(_TYPES))] +
+    ['#hertzian_dipole: x 0.010 0.006 0.010 u1 0 4e-10',
+     '#hertzian_dipole: y 0.010 0.008 0.010 u2 1e-10 4e-10',
+     '#hertzian_dipole: z 0.016 0.010 0.014 w7 1e-10 3e-10',
+     '#magnetic_dipole: z 0.010 0.012 0.012 w8',
+     '#voltage_source: y 0.012 0.014 0.010 50 w9',
+     '#rx: 0.010 0.010 0.016', '#rx: 0.015 0.015 0.005']) + '\n'
+
+
+def excitation_text():
+    """An excitation file with a time column and two user waveforms (101 samples over 1 ns)."""
+    t = np.linspace(0, 1e-9, 101)
+    u1 = np.sin(2 * np.pi * 3e9 * t) * np.exp(-((t - 2e-10) / 8e-11) ** 2)
+    u2 = np.where(t < 3e-10, t / 3e-10, 0.0)
+    rows = ['time u1 u2'] + ['{!r} {!r} {!r}'.format(float(a), float(b), float(c))
+                             for a, b, c in zip(t, u1, u2)]
+    return '\n'.join(rows) + '\n'
+
 CHILD = r'''
 import sys, hashlib, numpy as np
 sys.path.insert(0, {oracle!r})
@@ -67,6 +98,9 @@ if G.maxpoles:
 for n, r in enumerate(G.rxs):
     for k, v in r.outputs.items():
         out['rx{{}}_{{}}'.format(n + 1, k)] = np.asarray(v, dtype=np.float32)
+for n, s in enumerate(G.voltagesources + G.hertziandipoles + G.magneticdipoles):
+    out['src{{}}_whole'.format(n + 1)] = np.asarray(s.waveformvalues_wholestep, dtype=np.float32)
+    out['src{{}}_half'.format(n + 1)] = np.asarray(s.waveformvalues_halfstep, dtype=np.float32)
 for n, t in enumerate(G.transmissionlines):
     for k in ('Vinc', 'Iinc', 'Vtotal', 'Itotal'):
         out['tl{{}}_{{}}'.format(n + 1, k)] = np.asarray(getattr(t, k), dtype=np.float32)
@@ -91,11 +125,14 @@ def run_child(inputfile, src, variant, dest, run=1, end=1):
     return dict(np.load(dest, allow_pickle=False))
 
 
-def make(name, text, src, refout=None, run=1, end=1):
+def make(name, text, src, refout=None, run=1, end=1, files=None):
     with tempfile.TemporaryDirectory() as tmp:
         inputfile = os.path.join(tmp, name + '.in')
         with open(inputfile, 'w') as f:
             f.write(text)
+        for fname, ftext in (files or {}).items():
+            with open(os.path.join(tmp, fname), 'w') as f:
+                f.write(ftext)
         exact = run_child(inputfile, src, 'nofma', os.path.join(tmp, 'exact.npz'), run, end)
         fma = run_child(inputfile, src, '', os.path.join(tmp, 'fma.npz'), run, end)
     out = dict(exact)
@@ -103,6 +140,8 @@ def make(name, text, src, refout=None, run=1, end=1):
     if end > 1:
         out['model_run'] = np.int64(run)
         out['model_end'] = np.int64(end)
+    for fname, ftext in (files or {}).items():
+        out['file_' + fname] = np.array(ftext)
     for k, v in fma.items():
         if k.startswith('rx'):
             out['fma_' + k] = v
@@ -145,6 +184,8 @@ def main():
         if a.only and name not in a.only:
             continue
         make(name, bscan, a.src, None, run, 6)
+    if not a.only or 'waveforms' in a.only:
+        make('waveforms', WAVEFORMS, a.src, files={'exc.txt': excitation_text()})
     shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
                              HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
     with open(os.path.join(HERE, 'README.txt'), 'w') as f:

@@ -189,10 +189,19 @@ MODELS = {
 
 
 def build_fixture(g, **kw):
-    """The grid of a golden fixture: its input text through the front-end and, for a B-scan
-    fixture, its sources and receivers stepped to the recorded model run."""
+    """The grid of a golden fixture: its input text through the front-end (with the files it
+    reads, such as an excitation file, written beside it first) and, for a B-scan fixture, its
+    sources and receivers stepped to the recorded model run."""
+    import os
+    import tempfile
     from gprmax_gb300.model import build_grid, step_sources_receivers
-    G = build_grid(str(g['input']).splitlines(True), messages=False, **kw)
+    files = {k[len('file_'):]: str(v) for k, v in g.items() if k.startswith('file_')}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, text in files.items():
+            with open(os.path.join(tmp, name), 'w') as f:
+                f.write(text)
+        G = build_grid(str(g['input']).splitlines(True), messages=False,
+                       inputfilename=os.path.join(tmp, 'model.in') if files else '', **kw)
     if 'model_run' in g:
         step_sources_receivers(G, int(g['model_run']), int(g['model_end']))
     return G

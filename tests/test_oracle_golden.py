@@ -80,6 +80,23 @@ def test_front_end_matches_reference_build(name):
     _check_build(_build(g), g)
 
 
+def test_source_waveform_tables_match_reference():
+    """Every waveform type, user waveforms from an excitation file, delayed and cut-off sources:
+    the whole-step and half-step tables of every source equal the reference's bit for bit."""
+    g = _load('waveforms')
+    G = _build(g)
+    sources = G.voltagesources + G.hertziandipoles + G.magneticdipoles
+    assert len(sources) == sum(1 for k in g if k.endswith('_whole')) == 16
+    types = {w.ID: w.type for w in G.waveforms}
+    assert {types[s.waveformID] for s in sources} >= {'user', 'impulse', 'contsine', 'sine',
+                                                      'gaussiandoubleprime', 'gaussiandotdotnorm'}
+    for n, s in enumerate(sources):
+        np.testing.assert_array_equal(s.waveformvalues_wholestep, g['src{}_whole'.format(n + 1)],
+                                      err_msg='source {} ({})'.format(n + 1, s.waveformID))
+        np.testing.assert_array_equal(s.waveformvalues_halfstep, g['src{}_half'.format(n + 1)],
+                                      err_msg='source {} ({})'.format(n + 1, s.waveformID))
+
+
 @pytest.mark.parametrize('name', SMALL)
 def test_oracle_matches_reference_run(name):
     g = _load(name)
