@@ -185,6 +185,19 @@ MODELS = {
 #rx: 0.024 0.018 0.030
 #rx: 0.020 0.018 0.021 wet Ex Ey Ez Hx Hy Hz
 """,
+    # a receiver array (4 x 3 x 1, zero step along z) after a single receiver
+    'rxarray': """#title: receiver array
+#domain: 0.030 0.028 0.026
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: 80
+#pml_cells: 5
+#material: 4 0.001 1 0 block
+#box: 0.010 0.008 0.006 0.020 0.020 0.014 block
+#waveform: gaussiandot 1 3e9 w
+#hertzian_dipole: y 0.015 0.014 0.018 w
+#rx: 0.012 0.014 0.018
+#rx_array: 0.008 0.010 0.012 0.022 0.016 0.012 0.004 0.003 0
+""",
 }
 
 
