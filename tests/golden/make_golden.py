@@ -75,6 +75,32 @@ WAVEFORMS = '\n'.join(
      '#rx: 0.010 0.010 0.016', '#rx: 0.015 0.015 0.005']) + '\n'
 
 
+# materials and geometry from an #include_file (with ## comments and blank lines, which the
+# reference drops), placed between commands of the main file
+INCLUDE = """#title: include file
+#domain: 0.030 0.026 0.024
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: 90
+#pml_cells: 5
+#material: 3 0 1 0 base
+#box: 0 0 0 0.030 0.026 0.010 base
+#include_file: parts.txt
+#waveform: ricker 1 3e9 w
+#hertzian_dipole: z 0.015 0.013 0.016 w
+#rx: 0.019 0.013 0.016
+"""
+INCLUDED = """## shapes for the include-file model
+
+#material: 7 0.002 1 0 rock
+#add_dispersion_debye: 1 5 2e-10 rock
+#sphere: 0.012 0.012 0.008 0.004 rock
+##   a comment between commands
+#cylinder: 0.020 0.006 0.004 0.020 0.020 0.004 0.002 pec
+
+#box: 0.004 0.016 0.002 0.010 0.022 0.012 rock n
+"""
+
+
 def excitation_text():
     """An excitation file with a time column and two user waveforms (101 samples over 1 ns)."""
     t = np.linspace(0, 1e-9, 101)
@@ -186,6 +212,8 @@ def main():
         make(name, bscan, a.src, None, run, 6)
     if not a.only or 'waveforms' in a.only:
         make('waveforms', WAVEFORMS, a.src, files={'exc.txt': excitation_text()})
+    if not a.only or 'include' in a.only:
+        make('include', INCLUDE, a.src, files={'parts.txt': INCLUDED})
     shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
                              HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
     with open(os.path.join(HERE, 'README.txt'), 'w') as f:
