@@ -134,9 +134,11 @@ def build_model_file(inputfile, currentmodelrun=1, modelend=1, messages=None, de
 
 
 def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write_output=True,
-              messages=None, device_build=True):
-    """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid.
-    ``device_build``: build the geometry arrays in GPU memory, where the solver takes them."""
+              messages=None, device_build=True, append_number=False):
+    """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid. The model
+    number is appended to the file name when more than one model runs or ``append_number``
+    (task and restart runs, ``model_build_run.py:107``). ``device_build``: build the geometry
+    arrays in GPU memory, where the solver takes them."""
     from .solver import solve_gb300
     from .outputs import write_hdf5_outputfile
     G = build_model_file(inputfile, currentmodelrun, modelend, messages=messages,
@@ -147,7 +149,7 @@ def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write
     G.tsolve = tsolve
     G.memsolve = mem
     if write_output:
-        append = '' if numbermodelruns == 1 else str(currentmodelrun)
+        append = '' if numbermodelruns == 1 and not append_number else str(currentmodelrun)
         outdir = G.outputdirectory or G.inputdirectory
         if not os.path.isabs(outdir):
             outdir = os.path.join(G.inputdirectory, outdir)
@@ -181,5 +183,5 @@ def api(inputfile, n=1, task=None, restart=None, gpu=None, geometry_fixed=False,
         start, end = 1, 1 + n
     results = []
     for run in range(start, end):
-        results.append(run_model(inputfile, run, end - 1, n))
+        results.append(run_model(inputfile, run, end - 1, n, append_number=bool(task or restart)))
     return results
