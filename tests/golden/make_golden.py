@@ -15,6 +15,8 @@ through the reference's own driver (``oracle/ref_harness.py``: input parsing, gr
 * ``fma_rx<n>_<output>``: the same traces from the default (-march=native) build;
 * ``refout_rx<n>_<output>``: for the reference's own test models, the traces stored in their
   ``_ref.out`` files (read with ``gprmax_gb300.hdf5``), which older gprMax versions wrote;
+* ``snap<n>_electric``, ``snap<n>_magnetic``, ``snap<n>_vti``: each snapshot's arrays and the
+  bytes of the ``.vti`` file the reference writes from them;
 * ``src<n>_whole``, ``src<n>_half``: the waveform tables of every voltage source, Hertzian
   dipole and magnetic dipole, in that order (the reference's ``calculate_waveform_values``);
 * ``file_<name>``: the text of a file the input reads (an ``#excitation_file``), to be written
@@ -140,6 +142,21 @@ out['field_stats'] = np.array(stats)
 for s, snap in enumerate(G.snapshots):
     out['snap{{}}_electric'.format(s)] = snap.electric
     out['snap{{}}_magnetic'.format(s)] = snap.magnetic
+
+
+class _Bar:
+    def update(self, n=1):
+        pass
+
+
+import os, tempfile
+for s, snap in enumerate(G.snapshots):
+    fd, path = tempfile.mkstemp(suffix='.vti')
+    os.close(fd)
+    snap.filename = path
+    snap.write_vtk_imagedata(_Bar(), G)
+    out['snap{{}}_vti'.format(s)] = np.fromfile(path, dtype=np.uint8)
+    os.remove(path)
 np.savez({dest!r}, **out)
 '''
 

@@ -58,3 +58,21 @@ def test_reference_output_file_reads():
     rxs, attrs = read_outputfile(here)
     assert 'rx1' in rxs and {'Ex', 'Ey', 'Ez', 'Hx', 'Hy', 'Hz'} <= set(rxs['rx1'])
     assert rxs['rx1']['Ez'].shape == (int(attrs['Iterations']),)
+
+
+def test_snapshot_vti_file_equals_the_reference_byte_for_byte(tmp_path):
+    """The ``.vti`` writer, given the snapshot arrays of the ``mixed`` fixture, writes the same
+    bytes as the reference's ``Snapshot.write_vtk_imagedata`` (``snapshots.py:132-165``)."""
+    from models import build_fixture
+    g = dict(np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden',
+                                  'mixed.npz'), allow_pickle=False))
+    G = build_fixture(g)
+    assert len(G.snapshots) == 1
+    snap = G.snapshots[0]
+    snap.electric = g['snap0_electric']
+    snap.magnetic = g['snap0_magnetic']
+    out = str(tmp_path / 'snap.vti')
+    snap.write_vtk_imagedata(out, G)
+    with open(out, 'rb') as f:
+        data = f.read()
+    assert data == g['snap0_vti'].tobytes()
