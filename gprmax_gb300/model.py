@@ -134,17 +134,26 @@ def build_model_file(inputfile, currentmodelrun=1, modelend=1, messages=None, de
 
 
 def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write_output=True,
-              messages=None, device_build=True, append_number=False):
+              messages=None, device_build=True, append_number=False, G=None,
+              keep_geometry=False):
     """Build, solve on the GPU and write ``<name>[n].out``; returns the solved grid. The model
     number is appended to the file name when more than one model runs or ``append_number``
     (task and restart runs, ``model_build_run.py:107``). ``device_build``: build the geometry
-    arrays in GPU memory, where the solver takes them."""
+    arrays in GPU memory, where the solver takes them.
+
+    ``G``: the grid of an earlier run of a B-scan whose geometry is fixed (the reference's
+    ``--geometry-fixed``, ``model_build_run.py:108, 286-300, 402``): it is not rebuilt, only its
+    sources and receivers are stepped to this run; the solve starts from zero fields as a new
+    grid's would. ``keep_geometry``: leave a device-built geometry open for a following run."""
     from .solver import solve_gb300
     from .outputs import write_hdf5_outputfile
-    G = build_model_file(inputfile, currentmodelrun, modelend, messages=messages,
-                         device_build=device_build)
+    if G is None:
+        G = build_model_file(inputfile, currentmodelrun, modelend, messages=messages,
+                             device_build=device_build)
+    else:
+        step_sources_receivers(G, currentmodelrun, modelend)
     tsolve, mem = solve_gb300(currentmodelrun, modelend, G)
-    if getattr(G, 'geom', None) is not None:
+    if getattr(G, 'geom', None) is not None and not keep_geometry:
         G.geom.close()
     G.tsolve = tsolve
     G.memsolve = mem
@@ -168,7 +177,10 @@ def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write
 
 
 def api(inputfile, n=1, task=None, restart=None, gpu=None, geometry_fixed=False, **unused):
-    """Run ``n`` models of an input file on the GPU (``gprMax/gprMax.py:72-108``).
+    """Run ``n`` models of an input file on the GPU (``gprMax/gprMax.py:72-108``); returns the
+    solved grids. With ``geometry_fixed`` the input is built once and every later run reuses that
+    grid with its sources and receivers stepped, so the returned entries are that one grid
+    (holding the last run's outputs; each run's traces are in its ``.out`` file).
 
     MPI task farming, Taguchi optimisation and benchmark mode are not part of the solver core.
     """
@@ -182,6 +194,10 @@ def api(inputfile, n=1, task=None, restart=None, gpu=None, geometry_fixed=False,
     else:
         start, end = 1, 1 + n
     results = []
+    G = None
     for run in range(start, end):
-        results.append(run_model(inputfile, run, end - 1, n, append_number=bool(task or restart)))
+        G = run_model(inputfile, run, end - 1, n, append_number=bool(task or restart),
+                      G=G if geometry_fixed else None,
+                      keep_geometry=bool(geometry_fixed) and run < end - 1)
+        results.append(G)
     return results

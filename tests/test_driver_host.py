@@ -84,3 +84,38 @@ def test_output_dir_is_relative_to_the_input_file(stubbed, tmp_path, monkeypatch
     api(_write(tmp_path, MODEL + '#output_dir: results\n'))
     assert os.listdir(tmp_path / 'results') == ['model.out']
     assert os.listdir(elsewhere) == []
+
+
+def test_fixed_geometry_builds_once_and_steps_the_same_grid(stubbed, tmp_path, monkeypatch):
+    """``geometry_fixed``: one build for the whole B-scan; later runs step the same grid's sources
+    and receivers, keep its device geometry open and close it after the last run."""
+    import gprmax_gb300.model as model
+    builds = []
+    real = model.build_model_file
+
+    def counting(*a, **k):
+        builds.append(a[1] if len(a) > 1 else k.get('currentmodelrun'))
+        return real(*a, **k)
+    monkeypatch.setattr(model, 'build_model_file', counting)
+    grids = api(_write(tmp_path, MODEL), n=3, geometry_fixed=True)
+    assert builds == [1]
+    assert grids[0] is grids[1] is grids[2]
+    assert stubbed == [(1, 3, 12), (2, 3, 13), (3, 3, 14)]
+    assert grids[0].hertziandipoles[0].xcoord == 10
+    assert not grids[0].geom.h.value   # closed after the last run
+    assert sorted(f for f in os.listdir(tmp_path) if f.endswith('.out')) == \
+        ['model1.out', 'model2.out', 'model3.out']
+
+
+def test_fixed_geometry_runs_equal_rebuilt_runs(stubbed, tmp_path):
+    """The grid a fixed-geometry run solves has the inputs a rebuilt grid of that run has."""
+    from gprmax_gb300.model import build_model_file
+    from gprmax_gb300.solver import model_inputs
+    path = _write(tmp_path, MODEL)
+    fixed = api(path, n=3, geometry_fixed=True)[0]
+    fresh = build_model_file(path, 3, 3, messages=False)
+    a, b = model_inputs(fixed), model_inputs(fresh)
+    for k in ('coeffE', 'coeffH', 'rx'):
+        assert (a[k] == b[k]).all(), k
+    for x, y in zip(a['sources'], b['sources']):
+        assert (x == y).all()

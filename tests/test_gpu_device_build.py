@@ -122,3 +122,23 @@ def test_upload_rejects_an_id_beyond_the_tables(native):
     G.ID[1, 3, 4, 5] = len(G.materials)
     with pytest.raises(SolverError, match='nmat'):
         DeviceModel(G)
+
+
+@pytest.mark.parametrize('geometry_fixed', [False, True])
+def test_bscan_driver_writes_the_reference_traces(native, tmp_path, geometry_fixed):
+    """A 6-run 2D B-scan through the public driver (``api``: model runs, source and receiver
+    stepping, device geometry build, ``.out`` files), rebuilt per run or with its geometry fixed:
+    either way, runs 1 and 6 equal the reference's own runs bit for bit."""
+    from gprmax_gb300.model import api
+    from gprmax_gb300.outputs import read_outputfile
+    g1 = dict(np.load(os.path.join(GOLDEN, 'bscan2d_run1.npz'), allow_pickle=False))
+    g6 = dict(np.load(os.path.join(GOLDEN, 'bscan2d_run6.npz'), allow_pickle=False))
+    inputfile = tmp_path / 'bscan.in'
+    inputfile.write_text(str(g1['input']))
+    api(str(inputfile), n=6, geometry_fixed=geometry_fixed)
+    for run, g in ((1, g1), (6, g6)):
+        rxs, _ = read_outputfile(str(tmp_path / 'bscan{}.out'.format(run)))
+        keys = [k for k in g if k.startswith('rx1_')]
+        assert keys
+        for k in keys:
+            np.testing.assert_array_equal(rxs['rx1'][k[4:]], g[k], err_msg='run {} {}'.format(run, k))
