@@ -685,6 +685,8 @@ def process_geometrycmds(geometry, G):
             zf = round_value(float(tmp[6]) / G.dz)
             mats = _lookup_materials(G, tmp, requested)
             geo.build_plate(G, xs, xf, ys, yf, zs, zf, [m.numID for m in mats])
+        elif name == '#triangle:':
+            _triangle(G, tmp)
         elif name == '#fractal_box:':
             _fractal_box(G, tmp, geometry)
         elif name in _FRACTAL_MODIFIERS:
@@ -695,6 +697,45 @@ def process_geometrycmds(geometry, G):
 
 
 _FRACTAL_MODIFIERS = ('#add_surface_roughness:', '#add_surface_water:', '#add_grass:')
+
+
+def _triangle(G, tmp):
+    """#triangle: three vertices on one grid plane, a thickness and one material (with an
+    optional smoothing flag) or three (uniaxial) (``input_cmds_geometry.py``, #triangle)."""
+    if len(tmp) < 12:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least eleven parameters')
+    requested, avg = _average_option(G, tmp, 12, 12)
+    v = []
+    for q in range(3):
+        v.append((round_value(float(tmp[1 + 3 * q]) / G.dx) * G.dx,
+                  round_value(float(tmp[2 + 3 * q]) / G.dy) * G.dy,
+                  round_value(float(tmp[3 + 3 * q]) / G.dz) * G.dz))
+    thickness = float(tmp[10])
+    for ax, n, d in ((0, G.nx, G.dx), (1, G.ny, G.dy), (2, G.nz, G.dz)):
+        if any(p[ax] < 0 or p[ax] > n * d for p in v):
+            raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the one of the {}-coordinates is '
+                                'not within the model domain'.format('xyz'[ax]))
+    if thickness < 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires a positive value for thickness')
+    normal = None
+    for ax in range(3):
+        if v[0][ax] == v[1][ax] and v[1][ax] == v[2][ax]:
+            normal = 'xyz'[ax]
+            break
+    if normal is None:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the triangle is not specified correctly')
+    mats = _lookup_materials(G, tmp, requested)
+    if thickness > 0:
+        numID, nx_, ny_, nz_, averaging = _volume_material(G, tmp, mats, avg)
+    elif len(mats) == 1:
+        numID = nx_ = ny_ = nz_ = mats[0].numID
+        averaging = False
+    else:
+        # the reference passes no material number for a zero-thickness uniaxial triangle and
+        # its builder refuses the call
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' a zero-thickness triangle takes one '
+                            'material')
+    geo.build_triangle(G, v, normal, thickness, numID, nx_, ny_, nz_, averaging)
 
 
 def _fractal_box(G, tmp, geometry):

@@ -292,6 +292,85 @@ def build_plate(G, xs, xf, ys, yf, zs, zf, numIDs):
                     G.ID[comp, ii, jj, zs] = val
 
 
+def _triangle_cells(v, normal, d):
+    """Cells (i, j) of the triangle's plane whose centres lie strictly inside it, with the plane
+    index ``level`` and the axes (a, b) that i and j count along (``build_triangle``,
+    ``geometry_primitives_ext.pyx:378-486``). The arithmetic keeps the reference's C types:
+    vertices, cell sizes, the area and the two barycentric sums are fp32, the cell centres
+    (i + 1/2) * d are fp64 and promote the sums they enter, as the compiled reference does."""
+    f32, f64 = np.float32, np.float64
+    a, b = {'x': (1, 2), 'y': (0, 2), 'z': (0, 1)}[normal]
+    n = 'xyz'.index(normal)
+    P = [[f32(c) for c in p] for p in v]
+    A1, B1 = P[0][a], P[0][b]
+    A2, B2 = P[1][a], P[1][b]
+    A3, B3 = P[2][a], P[2][b]
+    da, db, dn = f32(d[a]), f32(d[b]), f32(d[n])
+    area = f32(f64(0.5) * f64(-B2 * A3 + B1 * (-A2 + A3) + A1 * (B2 - B3) + A2 * B3))
+    sign = int(np.sign(float(area)))
+    i1 = round_value(float(min(A1, A2, A3)) / float(da)) - 1
+    i2 = round_value(float(max(A1, A2, A3)) / float(da)) + 1
+    j1 = round_value(float(min(B1, B2, B3)) / float(db)) - 1
+    j2 = round_value(float(max(B1, B2, B3)) / float(db)) + 1
+    level = round_value(float(P[0][n] / dn))
+    I, J = np.meshgrid(np.arange(i1, i2), np.arange(j1, j2), indexing='ij')
+    ir = (I + 0.5) * f64(da)
+    jr = (J + 0.5) * f64(db)
+    s = (f64(sign) * (f64(B1 * A3 - A1 * B3) + f64(B3 - B1) * ir + f64(A1 - A3) * jr)).astype(f32)
+    t = (f64(sign) * (f64(A1 * B2 - B1 * A2) + f64(B1 - B2) * ir + f64(A2 - A1) * jr)).astype(f32)
+    bound = f32(f32(2) * area) * f32(sign)
+    inside = (s > 0) & (t > 0) & ((s + t) < bound)
+    return I[inside], J[inside], level, (a, b, n), dn
+
+
+def build_triangle(G, v, normal, thickness, numID, numIDx, numIDy, numIDz, averaging):
+    """#triangle: a triangle in a grid plane (zero thickness: the faces of the cells inside it,
+    ``build_face_*``) or a triangular prism of ``thickness`` metres (``build_voxel`` on those
+    cells of every layer from the triangle's plane up), ``geometry_primitives_ext.pyx:378-486``.
+    ``v``: the three vertices in metres (on grid nodes)."""
+    d = (G.dx, G.dy, G.dz)
+    I, J, level, (a, b, n), dn = _triangle_cells(v, normal, d)
+    if I.size == 0:
+        return
+    thicknesscells = round_value(float(np.float32(thickness) / dn))
+    shape = (G.nx, G.ny, G.nz)
+    if thicknesscells == 0:
+        # face numbers: the two in-plane components (yz face: Ey, Ez; xz: Ex, Ez; xy: Ex, Ey)
+        ca, cb = a, b
+        va, vb = (numIDx, numIDy, numIDz)[ca], (numIDx, numIDy, numIDz)[cb]
+        recs = []
+        for i, j in zip(I.tolist(), J.tolist()):
+            for (ii, jj, comp, val) in ((i, j, ca, va), (i, j, cb, vb), (i, j + 1, ca, va),
+                                        (i + 1, j, cb, vb)):
+                idx = [0, 0, 0]
+                idx[a], idx[b], idx[n] = ii, jj, level
+                recs.append((comp, idx[0], idx[1], idx[2], val))
+        geom = getattr(G, 'geom', None)
+        if geom is not None:
+            geom.edges(recs)
+            return
+        for comp, x, y, z, val in recs:
+            _rigid_edge(G, comp, x, y, z)
+            G.ID[comp, x, y, z] = val
+        return
+    ks = np.arange(level, min(level + thicknesscells, shape[n]))
+    if ks.size == 0:
+        return
+    lo = [0, 0, 0]
+    hi = [0, 0, 0]
+    lo[a], hi[a] = int(I.min()), int(I.max()) + 1
+    lo[b], hi[b] = int(J.min()), int(J.max()) + 1
+    lo[n], hi[n] = int(ks[0]), int(ks[-1]) + 1
+    mask = np.zeros([hi[q] - lo[q] for q in range(3)], dtype=bool)
+    sel = [None, None, None]
+    sel[a] = I - lo[a]
+    sel[b] = J - lo[b]
+    for k in ks:
+        sel[n] = np.full(I.shape, k - lo[n])
+        mask[sel[0], sel[1], sel[2]] = True
+    build_voxels_mask(G, mask, tuple(lo), numID, numIDx, numIDy, numIDz, averaging)
+
+
 # Edge offsets written by ``build_voxel`` for one cell, per component (E and H alike):
 # x-directed components take (0,0,0), (0,1,1), (0,1,0), (0,0,1) and so on.
 _VOXEL_EDGE_OFFSETS = {

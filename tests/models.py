@@ -198,6 +198,26 @@ MODELS = {
 #rx: 0.012 0.014 0.018
 #rx_array: 0.008 0.010 0.012 0.022 0.016 0.012 0.004 0.003 0
 """,
+    # triangles on all three grid planes: zero-thickness PEC faces, prisms with and without
+    # smoothing, a uniaxial prism of three materials, vertices in both windings
+    'triangles': """#title: triangles
+#domain: 0.040 0.036 0.032
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: 90
+#pml_cells: 5
+#material: 4 0.001 1 0 d1
+#material: 7 0.002 1 0 d2
+#material: 2.5 0 1 0 d3
+#triangle: 0.008 0.008 0.006 0.020 0.010 0.006 0.012 0.024 0.006 0 pec
+#triangle: 0.030 0.006 0.010 0.030 0.026 0.014 0.030 0.012 0.026 0.004 d1
+#triangle: 0.006 0.028 0.008 0.024 0.028 0.024 0.010 0.028 0.026 0.003 d2 n
+#triangle: 0.014 0.006 0.020 0.033 0.018 0.020 0.016 0.030 0.020 0.002 d1 d2 d3
+#triangle: 0.022 0.012 0.006 0.022 0.022 0.016 0.022 0.008 0.018 0 pec
+#waveform: gaussiandot 1 4e9 w
+#hertzian_dipole: z 0.018 0.017 0.016 w
+#rx: 0.021 0.015 0.014
+#rx: 0.026 0.020 0.022 r2 Ex Ey Ez Hx Hy Hz
+""",
 }
 
 
