@@ -687,6 +687,8 @@ def process_geometrycmds(geometry, G):
             geo.build_plate(G, xs, xf, ys, yf, zs, zf, [m.numID for m in mats])
         elif name == '#triangle:':
             _triangle(G, tmp)
+        elif name == '#cylindrical_sector:':
+            _cylindrical_sector(G, tmp)
         elif name == '#fractal_box:':
             _fractal_box(G, tmp, geometry)
         elif name in _FRACTAL_MODIFIERS:
@@ -697,6 +699,47 @@ def process_geometrycmds(geometry, G):
 
 
 _FRACTAL_MODIFIERS = ('#add_surface_roughness:', '#add_surface_water:', '#add_grass:')
+
+
+def _cylindrical_sector(G, tmp):
+    """#cylindrical_sector: normal axis, centre (two in-plane coordinates), the extent along the
+    normal, radius, start and sector angles in degrees, one material (with an optional smoothing
+    flag) or three (``input_cmds_geometry.py``, #cylindrical_sector)."""
+    if len(tmp) < 10:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' requires at least nine parameters')
+    requested, avg = _average_option(G, tmp, 10, 10)
+    normal = tmp[1].lower()
+    ctr1, ctr2 = float(tmp[2]), float(tmp[3])
+    extent1, extent2 = float(tmp[4]), float(tmp[5])
+    thickness = extent2 - extent1
+    r = float(tmp[6])
+    sectorstartangle = 2 * np.pi * (float(tmp[7]) / 360)
+    sectorangle = 2 * np.pi * (float(tmp[8]) / 360)
+    if normal not in ('x', 'y', 'z'):
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the normal direction must be either x, y or z.')
+    if r <= 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the radius {:g} should be a positive value.'.format(r))
+    if sectorstartangle < 0 or sectorangle <= 0:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the starting angle and sector angle should be a positive values.')
+    if sectorstartangle >= 2 * np.pi or sectorangle >= 2 * np.pi:
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' the starting angle and sector angle must be less than 360 degrees.')
+    mats = _lookup_materials(G, tmp, requested)
+    if thickness > 0:
+        numID, nx_, ny_, nz_, averaging = _volume_material(G, tmp, mats, avg)
+    elif len(mats) == 1:
+        numID = nx_ = ny_ = nz_ = mats[0].numID
+        averaging = False
+    else:
+        # the reference passes no material number for a zero-thickness uniaxial sector and its
+        # builder refuses the call
+        raise CmdInputError("'" + ' '.join(tmp) + "'" + ' a zero-thickness cylindrical sector '
+                            'takes one material')
+    d1, d2, dn = {'x': (G.dy, G.dz, G.dx), 'y': (G.dx, G.dz, G.dy), 'z': (G.dx, G.dy, G.dz)}[normal]
+    ctr1 = round_value(ctr1 / d1) * d1
+    ctr2 = round_value(ctr2 / d2) * d2
+    level = round_value(extent1 / dn)
+    geo.build_cylindrical_sector(G, ctr1, ctr2, level, sectorstartangle, sectorangle, r, normal,
+                                 thickness, numID, nx_, ny_, nz_, averaging)
 
 
 def _triangle(G, tmp):

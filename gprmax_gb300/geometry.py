@@ -329,10 +329,70 @@ def build_triangle(G, v, normal, thickness, numID, numIDx, numIDy, numIDz, avera
     cells of every layer from the triangle's plane up), ``geometry_primitives_ext.pyx:378-486``.
     ``v``: the three vertices in metres (on grid nodes)."""
     d = (G.dx, G.dy, G.dz)
-    I, J, level, (a, b, n), dn = _triangle_cells(v, normal, d)
-    if I.size == 0:
-        return
+    I, J, level, axes, dn = _triangle_cells(v, normal, d)
     thicknesscells = round_value(float(np.float32(thickness) / dn))
+    _build_in_plane(G, I, J, level, axes, thicknesscells, numID, numIDx, numIDy, numIDz,
+                    averaging)
+
+
+def _sector_cells(ctr1, ctr2, sectorstartangle, sectorangle, radius, normal, d, shape):
+    """Cells (i, j) of the sector's plane whose centres are inside the sector
+    (``build_cylindrical_sector`` :489-617 and ``is_inside_sector`` :73-110): anticlockwise of
+    the start arm, clockwise of the end arm and within the radius. fp32 like the reference: the
+    centre, radius, angles and cell sizes, each cell centre (i * d in fp32, plus d / 2 in fp64,
+    rounded to fp32), the arm end points (radius times the fp64 cosine and sine, rounded to fp32)
+    and both arm tests and the radius test."""
+    f32, f64 = np.float32, np.float64
+    a, b = {'x': (1, 2), 'y': (0, 2), 'z': (0, 1)}[normal]
+    c1, c2, r = f32(ctr1), f32(ctr2), f32(radius)
+    sa, ang = f32(sectorstartangle), f32(sectorangle)
+    da, db = f32(d[a]), f32(d[b])
+    i1 = max(round_value(float((c1 - r) / da)), 0)
+    i2 = min(round_value(float((c1 + r) / da)), shape[a])
+    j1 = max(round_value(float((c2 - r) / db)), 0)
+    j2 = min(round_value(float((c2 + r) / db)), shape[b])
+    if i1 >= i2 or j1 >= j2:
+        return np.zeros(0, int), np.zeros(0, int), (a, b)
+    I, J = np.meshgrid(np.arange(i1, i2), np.arange(j1, j2), indexing='ij')
+    px = (f64(I.astype(f32) * da) + f64(0.5) * f64(da)).astype(f32)
+    py = (f64(J.astype(f32) * db) + f64(0.5) * f64(db)).astype(f32)
+    s1 = f32(f64(r) * np.cos(f64(sa)))
+    s2 = f32(f64(r) * np.sin(f64(sa)))
+    e1 = f32(f64(r) * np.cos(f64(f32(sa + ang))))
+    e2 = f32(f64(r) * np.sin(f64(f32(sa + ang))))
+    v1 = px - c1
+    v2 = py - c2
+
+    def clockwise(ux, uy):
+        return (-ux) * v2 + uy * v1 > 0
+
+    inside = ~clockwise(s1, s2) & clockwise(e1, e2) & (v1 * v1 + v2 * v2 <= r * r)
+    return I[inside], J[inside], (a, b)
+
+
+def build_cylindrical_sector(G, ctr1, ctr2, level, sectorstartangle, sectorangle, radius, normal,
+                             thickness, numID, numIDx, numIDy, numIDz, averaging):
+    """#cylindrical_sector: the cells of a circular sector in a grid plane (zero thickness: their
+    faces) or of a sector prism of ``thickness`` metres from plane ``level`` up
+    (``geometry_primitives_ext.pyx:489-617``). Centre in metres on grid nodes, angles in
+    radians, anticlockwise from the first in-plane axis."""
+    d = (G.dx, G.dy, G.dz)
+    I, J, (a, b) = _sector_cells(ctr1, ctr2, sectorstartangle, sectorangle, radius, normal, d,
+                                 (G.nx, G.ny, G.nz))
+    n = 'xyz'.index(normal)
+    thicknesscells = round_value(float(np.float32(thickness) / np.float32(d[n])))
+    _build_in_plane(G, I, J, level, (a, b, n), thicknesscells, numID, numIDx, numIDy, numIDz,
+                    averaging)
+
+
+def _build_in_plane(G, I, J, level, axes, thicknesscells, numID, numIDx, numIDy, numIDz,
+                    averaging):
+    """Cells (I, J) of a grid plane at ``level``: with no thickness the faces of those cells
+    (``build_face_yz/xz/xy`` :230-312: rigid edges and IDs of the two in-plane components),
+    otherwise ``build_voxel`` on them in every layer from ``level`` up."""
+    a, b, n = axes
+    if I.size == 0 or thicknesscells < 0:
+        return
     shape = (G.nx, G.ny, G.nz)
     if thicknesscells == 0:
         # face numbers: the two in-plane components (yz face: Ey, Ez; xz: Ex, Ez; xy: Ex, Ey)

@@ -218,6 +218,28 @@ MODELS = {
 #rx: 0.021 0.015 0.014
 #rx: 0.026 0.020 0.022 r2 Ex Ey Ez Hx Hy Hz
 """,
+    # cylindrical sectors on all three planes: a zero-thickness PEC sector, prisms with and
+    # without smoothing, a uniaxial prism, a sector crossing the 0/360 degree line and one
+    # clipped by the domain
+    'sectors': """#title: cylindrical sectors
+#domain: 0.040 0.036 0.032
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: 90
+#pml_cells: 5
+#material: 4 0.001 1 0 d1
+#material: 7 0.002 1 0 d2
+#material: 2.5 0 1 0 d3
+#cylindrical_sector: z 0.014 0.012 0.006 0.006 0.008 20 110 pec
+#cylindrical_sector: x 0.018 0.016 0.026 0.030 0.009 300 120 d1
+#cylindrical_sector: y 0.010 0.010 0.024 0.028 0.007 45 270 d2 n
+#cylindrical_sector: z 0.026 0.024 0.018 0.021 0.010 90 200 d1 d2 d3
+#cylindrical_sector: x 0.034 0.004 0.012 0.016 0.006 0 90 d3
+#cylindrical_sector: z 0.038 0.030 0.010 0.014 0.005 180 150 d2
+#waveform: gaussiandot 1 4e9 w
+#hertzian_dipole: z 0.020 0.019 0.015 w
+#rx: 0.023 0.017 0.013
+#rx: 0.026 0.022 0.022 r2 Ex Ey Ez Hx Hy Hz
+""",
 }
 
 
