@@ -12,6 +12,7 @@ order of its cells does not matter. On a grid built in device memory (``G.geom``
 """
 import numpy as np
 
+from .exceptions import CmdInputError
 from .utilities import round_value
 
 # rigidE holds 12 edge flags per cell, rigidH 6 (``yee_cell_setget_rigid_ext.pyx:24-157``)
@@ -395,6 +396,12 @@ def _build_in_plane(G, I, J, level, axes, thicknesscells, numID, numIDx, numIDy,
         return
     shape = (G.nx, G.ny, G.nz)
     if thicknesscells == 0:
+        # the rigid flags of a face's far edges sit one cell on; on the domain's last cell row
+        # or its upper boundary plane that is past the end of the (cell-sized) rigid arrays
+        if level >= shape[n] or int(I.max()) + 1 >= shape[a] or int(J.max()) + 1 >= shape[b]:
+            raise CmdInputError('a zero-thickness face on the last cell row or the upper '
+                                'boundary of the domain is not built: its rigid edge flags would '
+                                'lie outside the grid')
         # face numbers: the two in-plane components (yz face: Ey, Ez; xz: Ex, Ez; xy: Ex, Ey)
         ca, cb = a, b
         va, vb = (numIDx, numIDy, numIDz)[ca], (numIDx, numIDy, numIDz)[cb]
