@@ -119,6 +119,7 @@ _SIGS = {
     'gbf_profile': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     'gbf_device_bytes': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    'gbf_set_device': (ctypes.c_int, [ctypes.c_int32]),
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),

@@ -1008,6 +1008,19 @@ int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes) {
   return GBF_OK;
 }
 
+int gbf_set_device(int32_t device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess)
+    return fail(nullptr, GBF_ECUDA, "gbf_set_device: %s", cudaGetErrorString(e));
+  if (device < 0 || device >= n)
+    return fail(nullptr, GBF_EINVAL, "gbf_set_device: device %d, %d CUDA device(s) present", device, n);
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess)
+    return fail(nullptr, GBF_ECUDA, "gbf_set_device: %s", cudaGetErrorString(e));
+  return GBF_OK;
+}
+
 }  // extern "C"
 
 // ---- batches: many models advanced by one launch per half-step ------------------------

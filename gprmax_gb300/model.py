@@ -176,6 +176,23 @@ def run_model(inputfile, currentmodelrun=1, modelend=1, numbermodelruns=1, write
     return G
 
 
+def select_device(gpu):
+    """Run the models of this thread on one CUDA device: the first of the device IDs given (a
+    list, possibly of lists, as the reference's ``-gpu`` option collects them; none: device 0),
+    as the reference does for a standard run (``gprMax/gprMax.py:132-144``)."""
+    import ctypes
+    from . import _native
+    ids = gpu if isinstance(gpu, (list, tuple)) else [gpu]
+    flat = [v for x in ids for v in (x if isinstance(x, (list, tuple)) else [x])]
+    device = int(flat[0]) if flat else 0
+    lib = _native.lib()
+    if lib.gbf_set_device(device) != 0:
+        buf = ctypes.create_string_buffer(512)
+        lib.gbf_last_error(None, buf, 512)
+        raise GeneralError(buf.value.decode())
+    return device
+
+
 def api(inputfile, n=1, task=None, restart=None, gpu=None, geometry_fixed=False, **unused):
     """Run ``n`` models of an input file on the GPU (``gprMax/gprMax.py:72-108``); returns the
     solved grids. With ``geometry_fixed`` the input is built once and every later run reuses that
@@ -187,6 +204,8 @@ def api(inputfile, n=1, task=None, restart=None, gpu=None, geometry_fixed=False,
     for key in ('mpi', 'mpi_no_spawn', 'benchmark', 'opt_taguchi', 'geometry_only'):
         if unused.get(key):
             raise GeneralError('{} mode is not supported by the GB300 solver core'.format(key))
+    if gpu is not None:
+        select_device(gpu)
     if task:
         start, end = task, task + 1
     elif restart:

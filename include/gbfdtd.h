@@ -163,6 +163,13 @@ int gbf_run_timed(gbf_ctx* ctx, int nsteps, uint32_t flags, float* ms);
 /* Bytes of device memory the context holds. */
 int gbf_device_bytes(gbf_ctx* ctx, size_t* bytes);
 
+/* Make CUDA device `device` current for the calling host thread, so that the contexts it creates
+ * next live there. Replaces the device choice of the reference's -gpu option (gprMax/gprMax.py:
+ * 132-144: the first of the given device IDs for a standard run; the reference then opens its
+ * context on that device in solve_gpu, model_build_run.py:477-500). GBF_EINVAL for an index
+ * outside [0, device count); the failure message is read with gbf_last_error(NULL, ...). */
+int gbf_set_device(int32_t device);
+
 /* Copy the message of the last failure on `ctx` (or of the last gbf_create failure when ctx
  * is NULL) into buf. */
 int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n);

@@ -119,3 +119,36 @@ def test_fixed_geometry_runs_equal_rebuilt_runs(stubbed, tmp_path):
         assert (a[k] == b[k]).all(), k
     for x, y in zip(a['sources'], b['sources']):
         assert (x == y).all()
+
+
+class _DeviceLib(FakeGeomLib):
+    def __init__(self, count=2):
+        super().__init__()
+        self.count = count
+        self.devices = []
+
+    def gbf_set_device(self, device):
+        if device < 0 or device >= self.count:
+            return -2
+        self.devices.append(device)
+        return 0
+
+    def gbf_last_error(self, ctx, buf, n):
+        buf.value = b'gbf_set_device: no such device'
+        return 0
+
+
+@pytest.mark.parametrize('gpu,device', [([1], 1), ([[1, 0]], 1), ([], 0), (0, 0)])
+def test_gpu_option_selects_the_first_device(stubbed, tmp_path, monkeypatch, gpu, device):
+    lib = _DeviceLib()
+    monkeypatch.setattr(devgeom._native, 'lib', lambda: lib)
+    api(_write(tmp_path, MODEL), gpu=gpu)
+    assert lib.devices == [device]
+
+
+def test_gpu_option_rejects_a_missing_device(stubbed, tmp_path, monkeypatch):
+    from gprmax_gb300.exceptions import GeneralError
+    lib = _DeviceLib(count=1)
+    monkeypatch.setattr(devgeom._native, 'lib', lambda: lib)
+    with pytest.raises(GeneralError, match='no such device'):
+        api(_write(tmp_path, MODEL), gpu=[3])

@@ -142,3 +142,15 @@ def test_bscan_driver_writes_the_reference_traces(native, tmp_path, geometry_fix
         assert keys
         for k in keys:
             np.testing.assert_array_equal(rxs['rx1'][k[4:]], g[k], err_msg='run {} {}'.format(run, k))
+
+
+def test_set_device_takes_a_present_device_and_refuses_others(native):
+    """``gbf_set_device`` (the ``-gpu`` device choice): device 0 is accepted and a model then
+    runs there; an index past the device count is refused before any CUDA call uses it."""
+    import ctypes
+    assert native.gbf_set_device(0) == 0
+    assert native.gbf_set_device(4096) != 0
+    buf = ctypes.create_string_buffer(256)
+    native.gbf_last_error(None, buf, 256)
+    assert b'device 4096' in buf.value
+    assert native.gbf_set_device(-1) != 0
