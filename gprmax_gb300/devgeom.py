@@ -73,10 +73,10 @@ class DeviceGeometry:
                                              0, 1 if averaging else 0))
 
     def edges(self, records):
-        """Rigid E edges: rows (component, i, j, k, numID)."""
-        if not records:
+        """Rigid E edges: rows (component, i, j, k, numID), a list or an (n, 5) array."""
+        r = np.ascontiguousarray(np.asarray(records, dtype=np.int32).reshape(-1, 5))
+        if r.shape[0] == 0:
             return
-        r = np.ascontiguousarray(np.array(records, dtype=np.int32).reshape(-1, 5))
         bad = ((r[:, 1] < 0) | (r[:, 2] < 0) | (r[:, 3] < 0) | (r[:, 1] >= self.nx)
                | (r[:, 2] >= self.ny) | (r[:, 3] >= self.nz))
         if bad.any():

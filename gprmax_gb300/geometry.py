@@ -250,47 +250,18 @@ def _rigid_edge(G, comp, i, j, k):
 
 def build_plate(G, xs, xf, ys, yf, zs, zf, numIDs):
     """Zero-thickness plate of E edges on one grid plane (#plate; ``build_face_*`` :230-312).
-    ``numIDs`` holds one or two material numbers (isotropic or anisotropic)."""
-    a = numIDs[0]
-    b = numIDs[-1]
-    geom = getattr(G, 'geom', None)
-    if geom is not None:
-        recs = []
-        if xs == xf:
-            for j in range(ys, yf):
-                for k in range(zs, zf):
-                    recs += [(1, xs, j, k, a), (2, xs, j, k, b), (1, xs, j, k + 1, a),
-                             (2, xs, j + 1, k, b)]
-        elif ys == yf:
-            for i in range(xs, xf):
-                for k in range(zs, zf):
-                    recs += [(0, i, ys, k, a), (2, i, ys, k, b), (0, i, ys, k + 1, a),
-                             (2, i + 1, ys, k, b)]
-        elif zs == zf:
-            for i in range(xs, xf):
-                for j in range(ys, yf):
-                    recs += [(0, i, j, zs, a), (1, i, j, zs, b), (0, i, j + 1, zs, a),
-                             (1, i + 1, j, zs, b)]
-        geom.edges(recs)
-        return
+    ``numIDs`` holds one or two material numbers (isotropic or anisotropic): the first for the
+    lower in-plane component (Ey on an x plane, Ex otherwise), the last for the other."""
     if xs == xf:
-        for j in range(ys, yf):
-            for k in range(zs, zf):
-                for (jj, kk, comp, val) in ((j, k, 1, a), (j, k, 2, b), (j, k + 1, 1, a), (j + 1, k, 2, b)):
-                    _rigid_edge(G, comp, xs, jj, kk)
-                    G.ID[comp, xs, jj, kk] = val
+        axes, level, r1, r2 = (1, 2, 0), xs, range(ys, yf), range(zs, zf)
     elif ys == yf:
-        for i in range(xs, xf):
-            for k in range(zs, zf):
-                for (ii, kk, comp, val) in ((i, k, 0, a), (i, k, 2, b), (i, k + 1, 0, a), (i + 1, k, 2, b)):
-                    _rigid_edge(G, comp, ii, ys, kk)
-                    G.ID[comp, ii, ys, kk] = val
+        axes, level, r1, r2 = (0, 2, 1), ys, range(xs, xf), range(zs, zf)
     elif zs == zf:
-        for i in range(xs, xf):
-            for j in range(ys, yf):
-                for (ii, jj, comp, val) in ((i, j, 0, a), (i, j, 1, b), (i, j + 1, 0, a), (i + 1, j, 1, b)):
-                    _rigid_edge(G, comp, ii, jj, zs)
-                    G.ID[comp, ii, jj, zs] = val
+        axes, level, r1, r2 = (0, 1, 2), zs, range(xs, xf), range(ys, yf)
+    else:
+        return
+    I, J = np.meshgrid(np.arange(r1.start, r1.stop), np.arange(r2.start, r2.stop), indexing='ij')
+    _write_faces(G, I.ravel(), J.ravel(), level, axes, numIDs[0], numIDs[-1])
 
 
 def _triangle_cells(v, normal, d):
@@ -386,6 +357,49 @@ def build_cylindrical_sector(G, ctr1, ctr2, level, sectorstartangle, sectorangle
                     averaging)
 
 
+def _rigid_edges(G, comp, x, y, z):
+    """``_rigid_edge`` for arrays of edges of one component (the flags are only ever set)."""
+    r = G.rigidE
+    if comp == 0:
+        own, nb = 0, ((1, y != 0, (0, -1, 0)), (3, z != 0, (0, 0, -1)),
+                      (2, (y != 0) & (z != 0), (0, -1, -1)))
+    elif comp == 1:
+        own, nb = 4, ((7, x != 0, (-1, 0, 0)), (5, z != 0, (0, 0, -1)),
+                      (6, (x != 0) & (z != 0), (-1, 0, -1)))
+    else:
+        own, nb = 8, ((9, x != 0, (-1, 0, 0)), (11, y != 0, (0, -1, 0)),
+                      (10, (x != 0) & (y != 0), (-1, -1, 0)))
+    r[own, x, y, z] = 1
+    for flag, m, (ox, oy, oz) in nb:
+        r[flag, x[m] + ox, y[m] + oy, z[m] + oz] = 1
+
+
+def _write_faces(G, I, J, level, axes, va, vb):
+    """The faces of cells (I, J) of the grid plane ``level`` normal to axis ``axes[2]``
+    (``build_face_yz/xz/xy`` :230-312): per face the near and far edges of the two in-plane
+    components, component ``axes[0]`` taking ``va`` and ``axes[1]`` taking ``vb``, with their
+    rigid flags; in face order on a device-built grid."""
+    a, b, n = axes
+    m = I.size
+    if m == 0:
+        return
+    ii = np.stack([I, I, I, I + 1], axis=1).ravel()
+    jj = np.stack([J, J, J + 1, J], axis=1).ravel()
+    comp = np.tile(np.array([a, b, a, b]), m)
+    val = np.tile(np.array([va, vb, va, vb], dtype=np.int64), m)
+    idx = [None, None, None]
+    idx[a], idx[b], idx[n] = ii, jj, np.full(ii.shape, level)
+    geom = getattr(G, 'geom', None)
+    if geom is not None:
+        geom.edges(np.stack([comp, idx[0], idx[1], idx[2], val], axis=1))
+        return
+    for c in (a, b):
+        sel = comp == c
+        x, y, z = idx[0][sel], idx[1][sel], idx[2][sel]
+        _rigid_edges(G, c, x, y, z)
+        G.ID[c, x, y, z] = val[sel]
+
+
 def _build_in_plane(G, I, J, level, axes, thicknesscells, numID, numIDx, numIDy, numIDz,
                     averaging):
     """Cells (I, J) of a grid plane at ``level``: with no thickness the faces of those cells
@@ -403,22 +417,8 @@ def _build_in_plane(G, I, J, level, axes, thicknesscells, numID, numIDx, numIDy,
                                 'boundary of the domain is not built: its rigid edge flags would '
                                 'lie outside the grid')
         # face numbers: the two in-plane components (yz face: Ey, Ez; xz: Ex, Ez; xy: Ex, Ey)
-        ca, cb = a, b
-        va, vb = (numIDx, numIDy, numIDz)[ca], (numIDx, numIDy, numIDz)[cb]
-        recs = []
-        for i, j in zip(I.tolist(), J.tolist()):
-            for (ii, jj, comp, val) in ((i, j, ca, va), (i, j, cb, vb), (i, j + 1, ca, va),
-                                        (i + 1, j, cb, vb)):
-                idx = [0, 0, 0]
-                idx[a], idx[b], idx[n] = ii, jj, level
-                recs.append((comp, idx[0], idx[1], idx[2], val))
-        geom = getattr(G, 'geom', None)
-        if geom is not None:
-            geom.edges(recs)
-            return
-        for comp, x, y, z, val in recs:
-            _rigid_edge(G, comp, x, y, z)
-            G.ID[comp, x, y, z] = val
+        nums = (numIDx, numIDy, numIDz)
+        _write_faces(G, I, J, level, axes, nums[a], nums[b])
         return
     ks = np.arange(level, min(level + thicknesscells, shape[n]))
     if ks.size == 0:
