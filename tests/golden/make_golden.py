@@ -103,6 +103,24 @@ INCLUDED = """## shapes for the include-file model
 """
 
 
+# a #python block that places the source and receiver from the model run number (run 2 of 3)
+PYTHON_BSCAN = """#title: python B-scan
+#domain: 0.030 0.028 0.024
+#dx_dy_dz: 0.001 0.001 0.001
+#time_window: 80
+#pml_cells: 5
+#material: 5 0.001 1 0 ground
+#box: 0 0 0 0.030 0.028 0.012 ground
+#cylinder: 0.015 0 0.007 0.015 0.028 0.007 0.002 pec
+#waveform: ricker 1 4e9 w
+#python:
+x = 0.008 + 0.003 * (current_model_run - 1)
+print('#hertzian_dipole: z {:g} 0.014 0.015 w'.format(x))
+print('#rx: {:g} 0.014 0.015'.format(x + 0.004))
+#end_python:
+"""
+
+
 def excitation_text():
     """An excitation file with a time column and two user waveforms (101 samples over 1 ns)."""
     t = np.linspace(0, 1e-9, 101)
@@ -231,6 +249,8 @@ def main():
         make('waveforms', WAVEFORMS, a.src, files={'exc.txt': excitation_text()})
     if not a.only or 'include' in a.only:
         make('include', INCLUDE, a.src, files={'parts.txt': INCLUDED})
+    if not a.only or 'python_run2' in a.only:
+        make('python_run2', PYTHON_BSCAN, a.src, None, 2, 3)
     shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
                              HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
     with open(os.path.join(HERE, 'README.txt'), 'w') as f:

@@ -245,18 +245,27 @@ MODELS = {
 
 def build_fixture(g, **kw):
     """The grid of a golden fixture: its input text through the front-end (with the files it
-    reads, such as an excitation file, written beside it first) and, for a B-scan fixture, its
-    sources and receivers stepped to the recorded model run."""
+    reads, such as an excitation file, written beside it first) and, for a B-scan fixture, the
+    recorded model run in the namespace of its #python blocks and its sources and receivers
+    stepped to that run."""
     import os
     import tempfile
     from gprmax_gb300.model import build_grid, step_sources_receivers
+    from gprmax_gb300.constants import c, e0, m0, z0
     files = {k[len('file_'):]: str(v) for k, v in g.items() if k.startswith('file_')}
     with tempfile.TemporaryDirectory() as tmp:
         for name, text in files.items():
             with open(os.path.join(tmp, name), 'w') as f:
                 f.write(text)
-        G = build_grid(str(g['input']).splitlines(True), messages=False,
-                       inputfilename=os.path.join(tmp, 'model.in') if files else '', **kw)
+        inputfile = os.path.join(tmp, 'model.in') if files else ''
+        namespace = None
+        if 'model_run' in g:   # what #python blocks see for that model run
+            namespace = {'c': c, 'e0': e0, 'm0': m0, 'z0': z0,
+                         'number_model_runs': int(g['model_end']),
+                         'current_model_run': int(g['model_run']),
+                         'inputfile': os.path.abspath(inputfile) if inputfile else ''}
+        G = build_grid(str(g['input']).splitlines(True), messages=False, usernamespace=namespace,
+                       inputfilename=inputfile, **kw)
     if 'model_run' in g:
         step_sources_receivers(G, int(g['model_run']), int(g['model_end']))
     return G
