@@ -281,7 +281,13 @@ def _simple_source(G, cmdname, cmdinstance, cls, minparams):
 
 
 def process_multicmds(multicmds, G):
-    """Waveforms, sources, receivers, snapshots, materials, dispersion and CFS terms."""
+    """Waveforms, sources, receivers, snapshots, materials, dispersion and CFS terms. Geometry
+    views and geometry-object files are not written by this package (in the drop-in route the
+    reference writes them); their commands are accepted and, with messages on, noted."""
+    for cmdname in ('#geometry_view', '#geometry_objects_write'):
+        if multicmds.get(cmdname) and G.messages:
+            print('{} ({} given) is not written by the GB300 driver; the reference writes it '
+                  'when it builds the model'.format(cmdname, len(multicmds[cmdname])))
     cmdname = '#waveform'
     for cmdinstance in multicmds[cmdname]:
         tmp = cmdinstance.split()
