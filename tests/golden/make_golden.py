@@ -251,6 +251,13 @@ def main():
         make('include', INCLUDE, a.src, files={'parts.txt': INCLUDED})
     if not a.only or 'python_run2' in a.only:
         make('python_run2', PYTHON_BSCAN, a.src, None, 2, 3)
+    # the reference's own B-scan example (user_models), first and last of its 60 model runs
+    with open(os.path.join(a.src, 'user_models', 'cylinder_Bscan_2D.in')) as f:
+        example = f.read()
+    for run in (1, 60):
+        name = 'ref_cylinder_Bscan_2D_run{}'.format(run)
+        if not a.only or name in a.only:
+            make(name, example, a.src, None, run, 60)
     shutil.copy(os.path.join(a.src, 'tests', 'models_basic', 'hertzian_dipole_dispersive',
                              HDF5_FIXTURE), os.path.join(HERE, HDF5_FIXTURE))
     with open(os.path.join(HERE, 'README.txt'), 'w') as f:

@@ -126,6 +126,14 @@ def test_oracle_matches_reference_on_dispersive_test_model():
     _check_run(_build(g), g)
 
 
+@pytest.mark.parametrize('name', ['ref_cylinder_Bscan_2D_run1', 'ref_cylinder_Bscan_2D_run60'])
+def test_oracle_matches_reference_bscan_example(name):
+    """The reference's B-scan example (``user_models/cylinder_Bscan_2D.in``, 60 model runs with
+    ``#src_steps``/``#rx_steps``): runs 1 and 60 as the reference built and solved them."""
+    g = _load(name)
+    _check_run(_build(g), g)
+
+
 @pytest.mark.parametrize('name', REFERENCE)
 def test_reference_test_outputs_read_and_agree(name):
     """The ``_ref.out`` traces stored with the reference's test models (written by older gprMax
