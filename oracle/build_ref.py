@@ -36,6 +36,9 @@ import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# where this recipe reads the reference checkout from: $GPRMAX_REFERENCE, else the read-only
+# copy this build environment mounts; every other oracle script takes the location from here
+SOURCE = os.environ.get('GPRMAX_REFERENCE', '/root/reference')
 OUT = os.path.join(HERE, '_ref')
 CSRC = os.path.join(OUT, 'csrc')
 PKG = os.path.join(OUT, 'gprMax')
@@ -150,7 +153,7 @@ def build(src=None, jobs=8, modules=None, quiet=False, variant=''):
 
 if __name__ == '__main__':
     ap = argparse.ArgumentParser()
-    ap.add_argument('--src', default='/root/reference')
+    ap.add_argument('--src', default=SOURCE)
     ap.add_argument('--jobs', type=int, default=os.cpu_count() or 4)
     ap.add_argument('--kernels-only', action='store_true')
     ap.add_argument('--variant', choices=['', 'nofma'], default='')

@@ -18,77 +18,87 @@
  * magnetic HORIPML order1_xminus :26-88; MRIPML electric order1_xminus :26-89, order2 :91-162).
  *
  * Arrays use the reference's shapes and C order: fields [nx+1][ny+1][nz+1] fp32, ID
- * [6][nx+1][ny+1][nz+1] uint32, dispersive T [P][nx+1][ny+1][nz+1] complex64 (float pairs),
+ * [6][nx+1][ny+1][nz+1] uint32, dispersive T [P][nx+1][ny+1][nz+1] complex64 (real pairs),
  * coefficients [nmat][5] fp32 and [nmat][3P] complex64, Phi [order][n1][n2][n3] fp32.
  * Built with -ffp-contract=off so every product and sum is rounded as written.
+ *
+ * `real` is float (the reference's default fp32 build, constants.pxd floattype_t). Compiled
+ * with -DORACLE_F64 it is double and the complex state is double pairs: the same loops in
+ * fp64, the "fp64 run of the same grid" that fp32 results are measured against.
  */
 #include <stdint.h>
 #include <stddef.h>
 
+#ifdef ORACLE_F64
+typedef double real;
+#else
+typedef float real;
+#endif
+
 #define IDX(i, j, k) (((size_t)(i) * NY + (j)) * NZ + (k))
 
 /* electric update, standard materials: fields_updates_ext.pyx:30-110 */
-void oracle_update_electric(int nx, int ny, int nz, const float* cE, const uint32_t* ID,
-                            float* Ex, float* Ey, float* Ez,
-                            const float* Hx, const float* Hy, const float* Hz) {
+void oracle_update_electric(int nx, int ny, int nz, const real* cE, const uint32_t* ID,
+                            real* Ex, real* Ey, real* Ez,
+                            const real* Hx, const real* Hy, const real* Hz) {
   const size_t NY = ny + 1, NZ = nz + 1, NC = (size_t)(nx + 1) * NY * NZ;
   const uint32_t *IDx = ID, *IDy = ID + NC, *IDz = ID + 2 * NC;
   int i, j, k;
   if (nx == 1) {
     for (i = 0; i < nx; i++) for (j = 1; j < ny; j++) for (k = 1; k < nz; k++) {
-      const float* c = cE + 5 * (size_t)IDx[IDX(i, j, k)];
+      const real* c = cE + 5 * (size_t)IDx[IDX(i, j, k)];
       Ex[IDX(i, j, k)] = c[0] * Ex[IDX(i, j, k)] + c[2] * (Hz[IDX(i, j, k)] - Hz[IDX(i, j - 1, k)]) - c[3] * (Hy[IDX(i, j, k)] - Hy[IDX(i, j, k - 1)]);
     }
   } else if (ny == 1) {
     for (i = 1; i < nx; i++) for (j = 0; j < ny; j++) for (k = 1; k < nz; k++) {
-      const float* c = cE + 5 * (size_t)IDy[IDX(i, j, k)];
+      const real* c = cE + 5 * (size_t)IDy[IDX(i, j, k)];
       Ey[IDX(i, j, k)] = c[0] * Ey[IDX(i, j, k)] + c[3] * (Hx[IDX(i, j, k)] - Hx[IDX(i, j, k - 1)]) - c[1] * (Hz[IDX(i, j, k)] - Hz[IDX(i - 1, j, k)]);
     }
   } else if (nz == 1) {
     for (i = 1; i < nx; i++) for (j = 1; j < ny; j++) for (k = 0; k < nz; k++) {
-      const float* c = cE + 5 * (size_t)IDz[IDX(i, j, k)];
+      const real* c = cE + 5 * (size_t)IDz[IDX(i, j, k)];
       Ez[IDX(i, j, k)] = c[0] * Ez[IDX(i, j, k)] + c[1] * (Hy[IDX(i, j, k)] - Hy[IDX(i - 1, j, k)]) - c[2] * (Hx[IDX(i, j, k)] - Hx[IDX(i, j - 1, k)]);
     }
   } else {
 #pragma omp parallel for private(j, k) schedule(static)
     for (i = 1; i < nx; i++) for (j = 1; j < ny; j++) for (k = 1; k < nz; k++) {
-      const float* a = cE + 5 * (size_t)IDx[IDX(i, j, k)];
-      const float* b = cE + 5 * (size_t)IDy[IDX(i, j, k)];
-      const float* c = cE + 5 * (size_t)IDz[IDX(i, j, k)];
+      const real* a = cE + 5 * (size_t)IDx[IDX(i, j, k)];
+      const real* b = cE + 5 * (size_t)IDy[IDX(i, j, k)];
+      const real* c = cE + 5 * (size_t)IDz[IDX(i, j, k)];
       Ex[IDX(i, j, k)] = a[0] * Ex[IDX(i, j, k)] + a[2] * (Hz[IDX(i, j, k)] - Hz[IDX(i, j - 1, k)]) - a[3] * (Hy[IDX(i, j, k)] - Hy[IDX(i, j, k - 1)]);
       Ey[IDX(i, j, k)] = b[0] * Ey[IDX(i, j, k)] + b[3] * (Hx[IDX(i, j, k)] - Hx[IDX(i, j, k - 1)]) - b[1] * (Hz[IDX(i, j, k)] - Hz[IDX(i - 1, j, k)]);
       Ez[IDX(i, j, k)] = c[0] * Ez[IDX(i, j, k)] + c[1] * (Hy[IDX(i, j, k)] - Hy[IDX(i - 1, j, k)]) - c[2] * (Hx[IDX(i, j, k)] - Hx[IDX(i, j - 1, k)]);
     }
     /* Ex at i = 0 */
     for (j = 1; j < ny; j++) for (k = 1; k < nz; k++) {
-      const float* a = cE + 5 * (size_t)IDx[IDX(0, j, k)];
+      const real* a = cE + 5 * (size_t)IDx[IDX(0, j, k)];
       Ex[IDX(0, j, k)] = a[0] * Ex[IDX(0, j, k)] + a[2] * (Hz[IDX(0, j, k)] - Hz[IDX(0, j - 1, k)]) - a[3] * (Hy[IDX(0, j, k)] - Hy[IDX(0, j, k - 1)]);
     }
     /* Ey at j = 0 */
     for (i = 1; i < nx; i++) for (k = 1; k < nz; k++) {
-      const float* b = cE + 5 * (size_t)IDy[IDX(i, 0, k)];
+      const real* b = cE + 5 * (size_t)IDy[IDX(i, 0, k)];
       Ey[IDX(i, 0, k)] = b[0] * Ey[IDX(i, 0, k)] + b[3] * (Hx[IDX(i, 0, k)] - Hx[IDX(i, 0, k - 1)]) - b[1] * (Hz[IDX(i, 0, k)] - Hz[IDX(i - 1, 0, k)]);
     }
     /* Ez at k = 0 */
     for (i = 1; i < nx; i++) for (j = 1; j < ny; j++) {
-      const float* c = cE + 5 * (size_t)IDz[IDX(i, j, 0)];
+      const real* c = cE + 5 * (size_t)IDz[IDX(i, j, 0)];
       Ez[IDX(i, j, 0)] = c[0] * Ez[IDX(i, j, 0)] + c[1] * (Hy[IDX(i, j, 0)] - Hy[IDX(i - 1, j, 0)]) - c[2] * (Hx[IDX(i, j, 0)] - Hx[IDX(i, j - 1, 0)]);
     }
   }
 }
 
-/* complex helpers (complex64 stored as float pairs) */
-typedef struct { float re, im; } cf;
+/* complex helpers (complex64 stored as real pairs) */
+typedef struct { real re, im; } cf;
 static inline cf cmul(cf a, cf b) { cf r; r.re = a.re * b.re - a.im * b.im; r.im = a.re * b.im + a.im * b.re; return r; }
-static inline cf cscale(cf a, float x) { cf r; r.re = a.re * x; r.im = a.im * x; return r; }
+static inline cf cscale(cf a, real x) { cf r; r.re = a.re * x; r.im = a.im * x; return r; }
 static inline cf cadd(cf a, cf b) { cf r; r.re = a.re + b.re; r.im = a.im + b.im; return r; }
 static inline cf csub(cf a, cf b) { cf r; r.re = a.re - b.re; r.im = a.im - b.im; return r; }
 
 /* dispersive part A for one component: phi = sum Re(c0) Re(T); T = c1 T + c2 E; E update - srce*phi
  * (fields_updates_ext.pyx:113-181 multipole, :238-297 one pole) */
 static void disp_A_comp(int comp, int i0, int i1, int j0, int j1, int k0, int k1, int nx, int ny, int nz,
-                        int P, const float* cE, const cf* cD, const uint32_t* IDc, cf* T, float* F,
-                        const float* Ha, const float* Hb, int da_i, int da_j, int da_k,
+                        int P, const real* cE, const cf* cD, const uint32_t* IDc, cf* T, real* F,
+                        const real* Ha, const real* Hb, int da_i, int da_j, int da_k,
                         int db_i, int db_j, int db_k, int ca, int cb) {
   const size_t NY = ny + 1, NZ = nz + 1, NC = (size_t)(nx + 1) * NY * NZ;
   int i, j, k, p;
@@ -97,9 +107,9 @@ static void disp_A_comp(int comp, int i0, int i1, int j0, int j1, int k0, int k1
   for (i = i0; i < i1; i++) for (j = j0; j < j1; j++) for (k = k0; k < k1; k++) {
     const size_t q = IDX(i, j, k);
     const uint32_t m = IDc[q];
-    const float* c = cE + 5 * (size_t)m;
+    const real* c = cE + 5 * (size_t)m;
     const cf* d = cD + 3 * (size_t)P * m;
-    float phi = 0;
+    real phi = 0;
     for (p = 0; p < P; p++) {
       cf t = T[p * NC + q];
       phi = phi + d[3 * p].re * t.re;
@@ -109,10 +119,10 @@ static void disp_A_comp(int comp, int i0, int i1, int j0, int j1, int k0, int k1
   }
 }
 
-void oracle_update_dispersive_A(int nx, int ny, int nz, int P, const float* cE, const float* cDf,
-                                const uint32_t* ID, float* Txf, float* Tyf, float* Tzf,
-                                float* Ex, float* Ey, float* Ez,
-                                const float* Hx, const float* Hy, const float* Hz) {
+void oracle_update_dispersive_A(int nx, int ny, int nz, int P, const real* cE, const real* cDf,
+                                const uint32_t* ID, real* Txf, real* Tyf, real* Tzf,
+                                real* Ex, real* Ey, real* Ez,
+                                const real* Hx, const real* Hy, const real* Hz) {
   const size_t NC = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
   const cf* cD = (const cf*)cDf;
   if (ny != 1 || nz != 1)  /* Ex: CBy*(Hz - Hz[j-1]) - CBz*(Hy - Hy[k-1]) */
@@ -124,7 +134,7 @@ void oracle_update_dispersive_A(int nx, int ny, int nz, int P, const float* cE, 
 }
 
 static void disp_B_comp(int i0, int i1, int j0, int j1, int k0, int k1, int nx, int ny, int nz, int P,
-                        const cf* cD, const uint32_t* IDc, cf* T, const float* F) {
+                        const cf* cD, const uint32_t* IDc, cf* T, const real* F) {
   const size_t NY = ny + 1, NZ = nz + 1, NC = (size_t)(nx + 1) * NY * NZ;
   int i, j, k, p;
 #pragma omp parallel for private(j, k, p) schedule(static)
@@ -135,9 +145,9 @@ static void disp_B_comp(int i0, int i1, int j0, int j1, int k0, int k1, int nx, 
   }
 }
 
-void oracle_update_dispersive_B(int nx, int ny, int nz, int P, const float* cDf, const uint32_t* ID,
-                                float* Txf, float* Tyf, float* Tzf,
-                                const float* Ex, const float* Ey, const float* Ez) {
+void oracle_update_dispersive_B(int nx, int ny, int nz, int P, const real* cDf, const uint32_t* ID,
+                                real* Txf, real* Tyf, real* Tzf,
+                                const real* Ex, const real* Ey, const real* Ez) {
   const size_t NC = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
   const cf* cD = (const cf*)cDf;
   if (ny != 1 || nz != 1) disp_B_comp(0, nx, 1, ny, 1, nz, nx, ny, nz, P, cD, ID, (cf*)Txf, Ex);
@@ -146,34 +156,34 @@ void oracle_update_dispersive_B(int nx, int ny, int nz, int P, const float* cDf,
 }
 
 /* magnetic update: fields_updates_ext.pyx:352-412 */
-void oracle_update_magnetic(int nx, int ny, int nz, const float* cH, const uint32_t* ID,
-                            const float* Ex, const float* Ey, const float* Ez,
-                            float* Hx, float* Hy, float* Hz) {
+void oracle_update_magnetic(int nx, int ny, int nz, const real* cH, const uint32_t* ID,
+                            const real* Ex, const real* Ey, const real* Ez,
+                            real* Hx, real* Hy, real* Hz) {
   const size_t NY = ny + 1, NZ = nz + 1, NC = (size_t)(nx + 1) * NY * NZ;
   const uint32_t *IDx = ID + 3 * NC, *IDy = ID + 4 * NC, *IDz = ID + 5 * NC;
   int i, j, k;
   if (nx == 1 || ny == 1 || nz == 1) {
     if (ny == 1 || nz == 1)
       for (i = 1; i < nx; i++) for (j = 0; j < ny; j++) for (k = 0; k < nz; k++) {
-        const float* c = cH + 5 * (size_t)IDx[IDX(i, j, k)];
+        const real* c = cH + 5 * (size_t)IDx[IDX(i, j, k)];
         Hx[IDX(i, j, k)] = c[0] * Hx[IDX(i, j, k)] - c[2] * (Ez[IDX(i, j + 1, k)] - Ez[IDX(i, j, k)]) + c[3] * (Ey[IDX(i, j, k + 1)] - Ey[IDX(i, j, k)]);
       }
     if (nx == 1 || nz == 1)
       for (i = 0; i < nx; i++) for (j = 1; j < ny; j++) for (k = 0; k < nz; k++) {
-        const float* c = cH + 5 * (size_t)IDy[IDX(i, j, k)];
+        const real* c = cH + 5 * (size_t)IDy[IDX(i, j, k)];
         Hy[IDX(i, j, k)] = c[0] * Hy[IDX(i, j, k)] - c[3] * (Ex[IDX(i, j, k + 1)] - Ex[IDX(i, j, k)]) + c[1] * (Ez[IDX(i + 1, j, k)] - Ez[IDX(i, j, k)]);
       }
     if (nx == 1 || ny == 1)
       for (i = 0; i < nx; i++) for (j = 0; j < ny; j++) for (k = 1; k < nz; k++) {
-        const float* c = cH + 5 * (size_t)IDz[IDX(i, j, k)];
+        const real* c = cH + 5 * (size_t)IDz[IDX(i, j, k)];
         Hz[IDX(i, j, k)] = c[0] * Hz[IDX(i, j, k)] - c[1] * (Ey[IDX(i + 1, j, k)] - Ey[IDX(i, j, k)]) + c[2] * (Ex[IDX(i, j + 1, k)] - Ex[IDX(i, j, k)]);
       }
   } else {
 #pragma omp parallel for private(j, k) schedule(static)
     for (i = 0; i < nx; i++) for (j = 0; j < ny; j++) for (k = 0; k < nz; k++) {
-      const float* a = cH + 5 * (size_t)IDx[IDX(i + 1, j, k)];
-      const float* b = cH + 5 * (size_t)IDy[IDX(i, j + 1, k)];
-      const float* c = cH + 5 * (size_t)IDz[IDX(i, j, k + 1)];
+      const real* a = cH + 5 * (size_t)IDx[IDX(i + 1, j, k)];
+      const real* b = cH + 5 * (size_t)IDy[IDX(i, j + 1, k)];
+      const real* c = cH + 5 * (size_t)IDz[IDX(i, j, k + 1)];
       Hx[IDX(i + 1, j, k)] = a[0] * Hx[IDX(i + 1, j, k)] - a[2] * (Ez[IDX(i + 1, j + 1, k)] - Ez[IDX(i + 1, j, k)]) + a[3] * (Ey[IDX(i + 1, j, k + 1)] - Ey[IDX(i + 1, j, k)]);
       Hy[IDX(i, j + 1, k)] = b[0] * Hy[IDX(i, j + 1, k)] - b[3] * (Ex[IDX(i, j + 1, k + 1)] - Ex[IDX(i, j + 1, k)]) + b[1] * (Ez[IDX(i + 1, j + 1, k)] - Ez[IDX(i, j + 1, k)]);
       Hz[IDX(i, j, k + 1)] = c[0] * Hz[IDX(i, j, k + 1)] - c[1] * (Ey[IDX(i + 1, j, k + 1)] - Ey[IDX(i, j, k + 1)]) + c[2] * (Ex[IDX(i, j + 1, k + 1)] - Ex[IDX(i, j, k + 1)]);
@@ -192,38 +202,38 @@ typedef struct {
 } slab_t;
 
 /* one CFS correction; returns the bracketed term multiplied by the material coefficient */
-static inline float pml_step(int form, int order, float dF, float* ph1, float* ph2_order1,
-                             const float* RA, const float* RB, const float* RE, const float* RF,
+static inline real pml_step(int form, int order, real dF, real* ph1, real* ph2_order1,
+                             const real* RA, const real* RB, const real* RE, const real* RF,
                              int T, int p) {
   /* ph1: Phi[0,...], ph2_order1: Phi[1,...] (second CFS term) */
   if (form == 0 && order == 1) {
-    float RA01 = RA[p] - 1, RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
-    float X = RA01 * dF + RB0 * (*ph1);
+    real RA01 = RA[p] - 1, RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
+    real X = RA01 * dF + RB0 * (*ph1);
     *ph1 = RE0 * (*ph1) - RF0 * dF;
     return X;
   } else if (form == 0) {
-    float RA0 = RA[p], RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
-    float RA1 = RA[T + p], RB1 = RB[T + p], RE1 = RE[T + p], RF1 = RF[T + p];
-    float RA01 = RA[p] * RA[T + p] - 1;
-    float X = RA01 * dF + RA1 * RB0 * (*ph1) + RB1 * (*ph2_order1);
+    real RA0 = RA[p], RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
+    real RA1 = RA[T + p], RB1 = RB[T + p], RE1 = RE[T + p], RF1 = RF[T + p];
+    real RA01 = RA[p] * RA[T + p] - 1;
+    real X = RA01 * dF + RA1 * RB0 * (*ph1) + RB1 * (*ph2_order1);
     *ph2_order1 = RE1 * (*ph2_order1) - RF1 * (RA0 * dF + RB0 * (*ph1));
     *ph1 = RE0 * (*ph1) - RF0 * dF;
     return X;
   } else if (order == 1) {
-    float IRA = 1 / RA[p];
-    float IRA1 = IRA - 1;
-    float RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
-    float RC0 = IRA * RB0 * RF0;
-    float X = IRA1 * dF - IRA * (*ph1);
+    real IRA = 1 / RA[p];
+    real IRA1 = IRA - 1;
+    real RB0 = RB[p], RE0 = RE[p], RF0 = RF[p];
+    real RC0 = IRA * RB0 * RF0;
+    real X = IRA1 * dF - IRA * (*ph1);
     *ph1 = RE0 * (*ph1) + RC0 * dF - RC0 * (*ph1);
     return X;
   } else {
-    float IRA = 1 / (RA[p] + RA[T + p]);
-    float IRA1 = IRA - 1;
-    float RB0 = RB[p], RE0 = RE[p], RF0 = RF[p], RC0 = IRA * RF0;
-    float RB1 = RB[T + p], RE1 = RE[T + p], RF1 = RF[T + p], RC1 = IRA * RF1;
-    float Psi = RB0 * (*ph1) + RB1 * (*ph2_order1);
-    float X = IRA1 * dF - IRA * Psi;
+    real IRA = 1 / (RA[p] + RA[T + p]);
+    real IRA1 = IRA - 1;
+    real RB0 = RB[p], RE0 = RE[p], RF0 = RF[p], RC0 = IRA * RF0;
+    real RB1 = RB[T + p], RE1 = RE[T + p], RF1 = RF[T + p], RC1 = IRA * RF1;
+    real Psi = RB0 * (*ph1) + RB1 * (*ph2_order1);
+    real X = IRA1 * dF - IRA * Psi;
     *ph2_order1 = RE1 * (*ph2_order1) + RC1 * (dF - Psi);
     *ph1 = RE0 * (*ph1) + RC0 * (dF - Psi);
     return X;
@@ -231,20 +241,20 @@ static inline float pml_step(int form, int order, float dF, float* ph1, float* p
 }
 
 static void pml_generic(int electric, int form, int order, int direction, int xs, int xf, int ys, int yf,
-                        int zs, int zf, int gnx, int gny, int gnz, const float* coef, const uint32_t* ID,
-                        float* Ex, float* Ey, float* Ez, float* Hx, float* Hy, float* Hz,
-                        float* Phi1, float* Phi2, const int* d1, const int* d2,
-                        const float* RA, const float* RB, const float* RE, const float* RF, float d) {
+                        int zs, int zf, int gnx, int gny, int gnz, const real* coef, const uint32_t* ID,
+                        real* Ex, real* Ey, real* Ez, real* Hx, real* Hy, real* Hz,
+                        real* Phi1, real* Phi2, const int* d1, const int* d2,
+                        const real* RA, const real* RB, const real* RE, const real* RF, real d) {
   const size_t NY = gny + 1, NZ = gnz + 1, NC = (size_t)(gnx + 1) * NY * NZ;
   const int nxs = xf - xs, nys = yf - ys, nzs = zf - zs;
   const int axis = direction % 3, minus = direction < 3;
   const int T = axis == 0 ? nxs : (axis == 1 ? nys : nzs);
   const size_t o1 = (size_t)d1[0] * d1[1] * d1[2], o2 = (size_t)d2[0] * d2[1] * d2[2];
   /* components: first (Phi1) and second (Phi2) tangential fields, their signs and sources */
-  float *F1, *F2;
-  const float *S1, *S2;    /* field differenced for F1 / F2 */
+  real *F1, *F2;
+  const real *S1, *S2;    /* field differenced for F1 / F2 */
   const uint32_t *ID1, *ID2;
-  float sg1, sg2;
+  real sg1, sg2;
   int s1i = 0, s1j = 0, s1k = 0;  /* stencil offset along the axis */
   if (electric) {
     if (axis == 0) { F1 = Ey; S1 = Hz; ID1 = ID + NC; sg1 = -1; F2 = Ez; S2 = Hy; ID2 = ID + 2 * NC; sg2 = 1; s1i = 1; }
@@ -268,15 +278,15 @@ static void pml_generic(int electric, int form, int order, int direction, int xs
         const size_t q = IDX(ii, jj, kk);
         /* E: (F[q] - F[q - 1 along axis]) / d;  H: (F[q + 1 along axis] - F[q]) / d */
         const size_t qa = electric ? IDX(ii - s1i, jj - s1j, kk - s1k) : IDX(ii + s1i, jj + s1j, kk + s1k);
-        float dF1 = electric ? (S1[q] - S1[qa]) / d : (S1[qa] - S1[q]) / d;
-        float* ph = Phi1 + (((size_t)i * d1[1] + j) * d1[2] + k);
-        float X = pml_step(form, order, dF1, ph, ph + o1, RA, RB, RE, RF, T, p);
-        const float c1 = coef[5 * (size_t)ID1[q] + 4];
+        real dF1 = electric ? (S1[q] - S1[qa]) / d : (S1[qa] - S1[q]) / d;
+        real* ph = Phi1 + (((size_t)i * d1[1] + j) * d1[2] + k);
+        real X = pml_step(form, order, dF1, ph, ph + o1, RA, RB, RE, RF, T, p);
+        const real c1 = coef[5 * (size_t)ID1[q] + 4];
         F1[q] = sg1 > 0 ? F1[q] + c1 * X : F1[q] - c1 * X;
-        float dF2 = electric ? (S2[q] - S2[qa]) / d : (S2[qa] - S2[q]) / d;
+        real dF2 = electric ? (S2[q] - S2[qa]) / d : (S2[qa] - S2[q]) / d;
         ph = Phi2 + (((size_t)i * d2[1] + j) * d2[2] + k);
         X = pml_step(form, order, dF2, ph, ph + o2, RA, RB, RE, RF, T, p);
-        const float c2 = coef[5 * (size_t)ID2[q] + 4];
+        const real c2 = coef[5 * (size_t)ID2[q] + 4];
         F2[q] = sg2 > 0 ? F2[q] + c2 * X : F2[q] - c2 * X;
       }
     }
@@ -284,19 +294,19 @@ static void pml_generic(int electric, int form, int order, int direction, int xs
 }
 
 void oracle_pml_electric(int form, int order, int direction, int xs, int xf, int ys, int yf, int zs, int zf,
-                         int nx, int ny, int nz, const float* cE, const uint32_t* ID,
-                         float* Ex, float* Ey, float* Ez, const float* Hx, const float* Hy, const float* Hz,
-                         float* Phi1, float* Phi2, const int* d1, const int* d2,
-                         const float* RA, const float* RB, const float* RE, const float* RF, float d) {
+                         int nx, int ny, int nz, const real* cE, const uint32_t* ID,
+                         real* Ex, real* Ey, real* Ez, const real* Hx, const real* Hy, const real* Hz,
+                         real* Phi1, real* Phi2, const int* d1, const int* d2,
+                         const real* RA, const real* RB, const real* RE, const real* RF, real d) {
   pml_generic(1, form, order, direction, xs, xf, ys, yf, zs, zf, nx, ny, nz, cE, ID, Ex, Ey, Ez,
-              (float*)Hx, (float*)Hy, (float*)Hz, Phi1, Phi2, d1, d2, RA, RB, RE, RF, d);
+              (real*)Hx, (real*)Hy, (real*)Hz, Phi1, Phi2, d1, d2, RA, RB, RE, RF, d);
 }
 
 void oracle_pml_magnetic(int form, int order, int direction, int xs, int xf, int ys, int yf, int zs, int zf,
-                         int nx, int ny, int nz, const float* cH, const uint32_t* ID,
-                         const float* Ex, const float* Ey, const float* Ez, float* Hx, float* Hy, float* Hz,
-                         float* Phi1, float* Phi2, const int* d1, const int* d2,
-                         const float* RA, const float* RB, const float* RE, const float* RF, float d) {
-  pml_generic(0, form, order, direction, xs, xf, ys, yf, zs, zf, nx, ny, nz, cH, ID, (float*)Ex,
-              (float*)Ey, (float*)Ez, Hx, Hy, Hz, Phi1, Phi2, d1, d2, RA, RB, RE, RF, d);
+                         int nx, int ny, int nz, const real* cH, const uint32_t* ID,
+                         const real* Ex, const real* Ey, const real* Ez, real* Hx, real* Hy, real* Hz,
+                         real* Phi1, real* Phi2, const int* d1, const int* d2,
+                         const real* RA, const real* RB, const real* RE, const real* RF, real d) {
+  pml_generic(0, form, order, direction, xs, xf, ys, yf, zs, zf, nx, ny, nz, cH, ID, (real*)Ex,
+              (real*)Ey, (real*)Ez, Hx, Hy, Hz, Phi1, Phi2, d1, d2, RA, RB, RE, RF, d);
 }

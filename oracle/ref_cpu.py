@@ -7,11 +7,7 @@ called with the reference's own signatures exactly as ``solve_cpu`` calls them
 (``gprMax/model_build_run.py:424-470``; PML dispatch by name as ``gprMax/pml.py:276-296``).
 The model arrays come from the front-end, which builds them identically to the reference.
 """
-import importlib
 import os
-import sys
-
-import numpy as np
 
 from oracle import OracleSolver
 
@@ -19,34 +15,57 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BUILD = os.path.join(HERE, '_ref')
 
 
-def available():
-    """True when the compiled reference kernels can be imported."""
+def available(variant=''):
+    """True when the compiled reference kernels (``variant`` '' = the reference's own flags,
+    'nofma' = the same C without floating-point contraction) can be imported."""
     try:
-        _modules()
+        _modules(variant)
         return True
     except Exception:
         return False
 
 
-def _modules():
-    if REF_BUILD not in sys.path:
-        sys.path.insert(0, REF_BUILD)
-    fu = importlib.import_module('gprMax.fields_updates_ext')
+_loaded = {}
+
+
+def _load_ext(variant, mod):
+    """Import one compiled kernel module of a build variant from its file, under a package
+    name of its own, so the two variants can be loaded side by side in one process."""
+    import glob
+    import importlib.util
+    key = (variant, mod)
+    if key not in _loaded:
+        parts = mod.split('.')
+        base = os.path.join(REF_BUILD, variant) if variant else REF_BUILD
+        found = glob.glob(os.path.join(base, *parts[:-1], parts[-1] + '.*.so'))
+        if not found:
+            raise ImportError('reference kernel {} ({}) not built'.format(mod, variant or 'stock'))
+        name = 'gbref_{}.{}'.format(variant or 'stock', parts[-1])
+        spec = importlib.util.spec_from_file_location(name, found[0])
+        m = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        _loaded[key] = m
+    return _loaded[key]
+
+
+def _modules(variant=''):
+    fu = _load_ext(variant, 'gprMax.fields_updates_ext')
     pml = {}
     for kind in ('electric', 'magnetic'):
         for form in ('HORIPML', 'MRIPML'):
-            pml[(kind, form)] = importlib.import_module(
-                'gprMax.pml_updates.pml_updates_{}_{}_ext'.format(kind, form))
+            pml[(kind, form)] = _load_ext(
+                variant, 'gprMax.pml_updates.pml_updates_{}_{}_ext'.format(kind, form))
     return fu, pml
 
 
 class RefCPUSolver(OracleSolver):
-    """``solve_cpu`` over the reference's compiled kernels with ``nthreads`` OpenMP threads."""
+    """``solve_cpu`` over the reference's compiled kernels with ``nthreads`` OpenMP threads
+    (``variant`` 'nofma': the build without floating-point contraction)."""
 
-    def __init__(self, G, nthreads=None):
+    def __init__(self, G, nthreads=None, variant=''):
         super().__init__(G)
         self.nthreads = nthreads or os.cpu_count() or 1
-        self.fu, pml = _modules()
+        self.fu, pml = _modules(variant)
         form = G.pmlformulation
         self.pml_e = [getattr(pml[('electric', form)], 'order{}_{}'.format(self.order, s.pml.direction))
                       for s in self.slabs]

@@ -52,10 +52,13 @@ def _install_shims():
         sys.modules['h5py'] = types.ModuleType('h5py')
 
 
-def load(src='/root/reference', variant=''):
+def load(src=None, variant=''):
     """Import the reference's model driver; returns the ``gprMax.model_build_run`` module.
     ``variant='nofma'`` selects the kernels compiled without floating-point contraction."""
     global REF_BUILD
+    if src is None:
+        import build_ref
+        src = build_ref.SOURCE
     if variant:
         REF_BUILD = os.path.join(HERE, '_ref', variant)
     if not os.path.isdir(os.path.join(REF_BUILD, 'gprMax')):
@@ -86,9 +89,12 @@ class _Args:
         self.opt_taguchi = False
 
 
-def run_reference(inputfile, src='/root/reference', currentmodelrun=1, modelend=1,
+def run_reference(inputfile, src=None, currentmodelrun=1, modelend=1,
                   nthreads=None, quiet=True, variant=''):
     """Run one model through the reference and return its grid object after the solve."""
+    if src is None:
+        import build_ref
+        src = build_ref.SOURCE
     mbr = load(src, variant)
     from gprMax.constants import c, e0, m0, z0
     from gprMax.materials import Material

@@ -1,6 +1,6 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Needs a gprMax v3.1.7 checkout (``--src``, default ``/root/reference``) and its kernels built
+Needs a gprMax v3.1.7 checkout (``--src``, default ``build_ref.SOURCE``) and its kernels built
 by ``oracle/build_ref.py`` (both the default build and ``--variant nofma``). Each model runs
 through the reference's own driver (``oracle/ref_harness.py``: input parsing, grid build,
 ``solve_cpu``), once per build, in a child process. Writes, per model, ``<name>.npz`` with:
@@ -30,7 +30,7 @@ The reference's own test models come from ``tests/models_basic`` (with ``_ref.ou
 
 It also copies one of those ``_ref.out`` files here as a fixture for the HDF5 reader.
 
-Usage: python tests/golden/make_golden.py [--src /root/reference] [--only NAME ...]
+Usage: python tests/golden/make_golden.py [--src PATH_TO_GPRMAX_CHECKOUT] [--only NAME ...]
 """
 import argparse
 import hashlib
@@ -48,6 +48,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, 'tests'))
 sys.path.insert(0, os.path.join(ROOT, 'oracle'))
+import build_ref  # noqa: E402
 
 REFERENCE_MODELS = ['hertzian_dipole_fs', 'hertzian_dipole_dispersive', 'hertzian_dipole_hs',
                     'magnetic_dipole_fs', '2D_ExHyHz', '2D_EyHxHz', '2D_EzHxHy',
@@ -218,7 +219,7 @@ def make(name, text, src, refout=None, run=1, end=1, files=None):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--src', default='/root/reference')
+    ap.add_argument('--src', default=build_ref.SOURCE)
     ap.add_argument('--only', nargs='*')
     a = ap.parse_args()
     from models import MODELS

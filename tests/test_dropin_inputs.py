@@ -14,7 +14,9 @@ import pytest
 
 from models import MODELS
 
-SRC = os.environ.get('GPRMAX_REFERENCE_SRC', '/root/reference')
+import build_ref  # noqa: E402  (oracle/ is on sys.path via conftest)
+
+SRC = build_ref.SOURCE
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BUILD = os.path.join(os.path.dirname(HERE), 'oracle', '_ref', 'nofma', 'gprMax')
 

@@ -15,7 +15,9 @@ from gprmax_gb300.exceptions import CmdInputError
 from gprmax_gb300.fractals import FractalVolume
 from gprmax_gb300.model import build_model_file
 
-SRC = os.environ.get('GPRMAX_REFERENCE_SRC', '/root/reference')
+import build_ref  # noqa: E402  (oracle/ is on sys.path via conftest)
+
+SRC = build_ref.SOURCE
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.join(os.path.dirname(HERE), 'oracle')
 REF_BUILD = os.path.join(ORACLE, '_ref', 'nofma', 'gprMax')

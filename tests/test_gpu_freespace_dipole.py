@@ -3,7 +3,10 @@
 
 * bit-exact against the oracle (the reference's time loop restated in C);
 * the error of the fp32 fields against an fp64 run of the same grid (the pure-torch
-  restatement of the update, tests/adjoint_reference.py, in fp64 on the GPU);
+  restatement of the update, tests/adjoint_reference.py, in fp64 on the GPU, and the oracle's
+  loops in fp64 with fp64 tables);
+* the difference from the reference's kernels as shipped (-O3 -march=native, contracted to
+  fused multiply-adds), which the bit-exact comparison (no contraction) does not show;
 * against the analytical dipole field (tests/analytical_dipole.py), to the level the FDTD
   discretisation allows.
 """
@@ -53,7 +56,28 @@ def test_error_against_fp64_run(native, gpu_run):
     ez = rx[2, :, 0].astype(np.float64)
     err = np.abs(ez - tr[0]).max() / np.abs(tr[0]).max()
     print('\nfp32 GPU against fp64 run: max |Ez error| / peak = {:.3e}'.format(err))
-    assert err <= 1e-4
+    # measured 2.0e-5 on the GB300
+    assert err <= 3e-5
+
+
+def test_error_against_fp64_oracle_and_stock_build(native, gpu_run):
+    import oracle
+    import ref_cpu
+    G, rx = gpu_run
+    r64 = oracle.OracleSolver(G, fp64=True).run().receivers()
+    out = []
+    for name, ref in [('fp64 oracle', r64)] + (
+            [('stock build', ref_cpu.RefCPUSolver(G).run().receivers())]
+            if ref_cpu.available('') else []):
+        errs = []
+        for c, g in ((2, 0), (3, 3), (4, 3)):   # Ez, Hx, Hy: the receiver's outputs
+            peak = np.abs(ref[g:g + 3, :, 0]).max()
+            errs.append(np.abs(rx[c, :, 0].astype(np.float64) - ref[c, :, 0]).max() / peak)
+        out.append((name, max(errs)))
+    print('\n100^3 free-space dipole, GPU against ' + ', '.join(
+        '{}: {:.3e} of peak'.format(n, e) for n, e in out))
+    for name, e in out:
+        assert e <= 1e-3, name
 
 
 def test_against_analytical_dipole(native, gpu_run):
