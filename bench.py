@@ -42,6 +42,9 @@ WORKLOAD = 'dispersive_soil_400x400x200_debye50_pml10'
 # the 400x400x200 workload), else the small capture's `dram_bytes_per_cell:` line scaled by cells
 TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'half_step_traffic_dispersive_soil_400x400x200.md')
 TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'e_half_step_dispersive_soil_256x256x128.md')
+# the same two lines for the fused step kernel
+FUSED_TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'fused_step_traffic_dispersive_soil_400x400x200.md')
+FUSED_TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'fused_step_dispersive_soil_256x256x128.md')
 
 
 def _profile_value(path, key):
@@ -55,13 +58,16 @@ def _profile_value(path, key):
     return None
 
 
-def measured_traffic(cells):
-    """DRAM bytes of one E half-step launch over `cells` cells (ncu), and where they came from."""
-    full = _profile_value(TRAFFIC_FULL, 'dram_bytes_per_launch')
-    full_cells = _profile_value(TRAFFIC_FULL, 'cells')
+def measured_traffic(cells, fused=False):
+    """DRAM bytes of one launch of the dominant kernel (the fused step, or the E half-step) over
+    `cells` cells (ncu), and where they came from."""
+    full_path = FUSED_TRAFFIC_FULL if fused else TRAFFIC_FULL
+    small_path = FUSED_TRAFFIC_PROFILE if fused else TRAFFIC_PROFILE
+    full = _profile_value(full_path, 'dram_bytes_per_launch')
+    full_cells = _profile_value(full_path, 'cells')
     if full is not None and full_cells == cells:
         return int(full), 'ncu, full-size launch'
-    per_cell = _profile_value(TRAFFIC_PROFILE, 'dram_bytes_per_cell')
+    per_cell = _profile_value(small_path, 'dram_bytes_per_cell')
     if per_cell is not None:
         return int(round(per_cell * cells)), 'ncu, 256x256x128 launch scaled by cells'
     return None, None
@@ -114,6 +120,19 @@ def algorithmic_bytes(G):
         from gprmax_gb300.solver import real_dispersive_state
         e += dcells * (24 if real_dispersive_state(G) else 48) * G.maxpoles
     return h, e
+
+
+def fused_bytes(G):
+    """Bytes per launch of the fused step (both half-steps in one pass): E and H read once and
+    written once (48 B per node), the packed E ID word (4 B) and, unless every material has the
+    same H row, the H ID word (4 B); the dispersive state and the E and H PML state as in the
+    half-steps. The halo rows, columns and planes the tiles re-read are not counted (they are
+    meant to be cache hits)."""
+    h, e = algorithmic_bytes(G)
+    cells = G.nx * G.ny * G.nz
+    # h = cells*(36 [+ id]) + pml, e = cells*40 + pml + disp: the fused step drops one read of
+    # E (12 B) and one of H (12 B) per node against their sum
+    return h + e - 24 * cells
 
 
 class ClockSampler:
@@ -279,8 +298,9 @@ def run_gb300(args):
     # --- end to end through the public API: upload from host, K steps, read back traces
     if dist is not None:
         dist.barrier()
+    options = 8 if args.half_steps else 0
     t0 = time.perf_counter()
-    dm = DeviceModel(G)
+    dm = DeviceModel(G, options)
     t1 = time.perf_counter()
     dm.run(K)
     dm.synchronize()
@@ -305,15 +325,30 @@ def run_gb300(args):
     # --- per-kernel launch times for the roofline
     ms_h, ms_e, ms_t = dm.profile(max(args.profile_steps, 1))
     checksum = float(np.abs(dm.receivers()).sum())
+    step = dm.step_info()
     dm.close()
+    fused = step['fused']
     value = replica_rate(world, cells, K, ms / 1e3)
     bytes_h, bytes_e = algorithmic_bytes(G)
+    if fused:
+        bytes_e = fused_bytes(G)
     peak, peak_kind = load_peaks()
     npf = max(args.profile_steps, 1)
     t_e = ms_e / npf / 1e3
     t_h = ms_h / npf / 1e3
     achieved = bytes_e / t_e / 1e9
-    traffic, traffic_src = measured_traffic(cells)
+    traffic, traffic_src = measured_traffic(cells, fused)
+    if fused:
+        kernels = {'fused_step': {'ms': t_e * 1e3, 'bytes': bytes_e, 'GBps': round(achieved, 1),
+                                  'tile_rows': step['tj'], 'chunks': step['nch'],
+                                  'planes_per_chunk': step['planes'], 'blocks': step['blocks']},
+                   'step_ms_profiled': ms_t / npf}
+    else:
+        kernels = {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
+                                   'GBps': round(bytes_h / t_h / 1e9, 1)},
+                   'e_half_step': {'ms': t_e * 1e3, 'bytes': bytes_e,
+                                   'GBps': round(achieved, 1)},
+                   'step_ms_profiled': ms_t / npf}
     if rank != 0:
         return
     out = {
@@ -329,16 +364,14 @@ def run_gb300(args):
                 'h2d_bytes_per_step': int(h2d / K), 'd2h_bytes_per_step': int(d2h / K),
                 'what': 'DeviceModel(G) upload from host + {} steps + receiver read-back'.format(K),
                 'parts': e2e_parts},
-        'gpu_launches': 3 * K,
-        'roofline': {'bound': 'hbm', 'kernel': 'e_half_step', 'achieved': round(achieved, 1),
+        # per step: the fused step and the end-of-step kernel, or H, E and end-of-step
+        'gpu_launches': (2 if fused else 3) * K,
+        'roofline': {'bound': 'hbm', 'kernel': 'fused_step' if fused else 'e_half_step',
+                     'achieved': round(achieved, 1),
                      'peak': peak, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
                      'traffic': traffic, 'traffic_source': traffic_src, 'peak_source': peak_kind,
                      'bytes_per_launch': bytes_e, 'ms_per_launch': t_e * 1e3},
-        'kernels': {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
-                                    'GBps': round(bytes_h / t_h / 1e9, 1)},
-                    'e_half_step': {'ms': t_e * 1e3, 'bytes': bytes_e,
-                                    'GBps': round(achieved, 1)},
-                    'step_ms_profiled': ms_t / npf},
+        'kernels': kernels,
         'clocks': clk.summary(),
         'checksum_rx_abs_sum': checksum,
     }
@@ -782,6 +815,8 @@ def main():
     ap.add_argument('--ref-budget', type=float, default=150.0)
     ap.add_argument('--grid', type=int, nargs=3, default=None,
                     help='smaller soil grid (profiling runs); default 400 400 200')
+    ap.add_argument('--half-steps', action='store_true',
+                    help='soil: step with the two half-step kernels instead of the fused step')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
     ap.add_argument('--workload', choices=['soil', 'bscan', 'bscan2d', 'adjoint', 'sweep', 'build'],

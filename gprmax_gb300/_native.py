@@ -11,8 +11,10 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
-SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'adjoint.cu', 'geom.cu', 'fdtd_kernels.cuh']
-PML_KINDS = 5   # kernels_inst.cu is compiled once per PML kind
+SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fused_inst.cu', 'adjoint.cu', 'geom.cu',
+           'fdtd_kernels.cuh', 'fused_step.cuh']
+PML_KINDS = 5       # kernels_inst.cu is compiled once per PML kind
+FUSED_TJ = (7, 15)  # fused_inst.cu once per PML kind and tile height
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # --fmad=false: every product and sum is rounded as written, which makes the GPU results
@@ -42,8 +44,8 @@ def _stale():
 def build(force=False, verbose=False):
     """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources.
 
-    The main translation unit and one kernel-instantiation unit per PML kind are compiled in
-    parallel, then linked."""
+    The main translation unit, one half-step instantiation unit per PML kind and one fused-step
+    unit per PML kind and tile height are compiled in parallel, then linked."""
     if not force and not _stale():
         return LIBPATH
     from concurrent.futures import ThreadPoolExecutor
@@ -56,6 +58,12 @@ def build(force=False, verbose=False):
     for pk in range(PML_KINDS):
         jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
                      os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
+        for tj in FUSED_TJ:
+            jobs.append((os.path.join(CSRC, 'fused_inst.cu'),
+                         os.path.join(objdir, 'fused_pk{}_tj{}.o'.format(pk, tj)),
+                         ['-DGBF_PK={}'.format(pk), '-DGBF_TJ={}'.format(tj)]))
+    # the longest units first, so the pool ends together
+    jobs.sort(key=lambda j: 'fused_inst' not in j[0])
 
     def compile_one(job):
         src, obj, extra = job
@@ -64,7 +72,7 @@ def build(force=False, verbose=False):
             print(' '.join(cmd))
         subprocess.run(cmd, check=True, cwd=CSRC)
         return obj
-    with ThreadPoolExecutor(len(jobs)) as ex:
+    with ThreadPoolExecutor(min(len(jobs), max(os.cpu_count() or 1, 1))) as ex:
         objs = list(ex.map(compile_one, jobs))
     cmd = [_nvcc()] + ARCH + ['-shared'] + objs + ['-o', LIBPATH + '.tmp']
     if verbose:
@@ -116,6 +124,9 @@ _SIGS = {
     'gbf_upload_fields': (ctypes.c_int, [_P, _P]),
     'gbf_download_dispersive': (ctypes.c_int, [_P, _P]),
     'gbf_download_snapshot': (ctypes.c_int, [_P, ctypes.c_int, _P]),
+    'gbf_step_info': (ctypes.c_int, [_P, _P]),
+    'gbf_set_fused_tiles': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    'gbf_fused_tiles': (ctypes.c_int, [ctypes.c_int32] * 5 + [_P]),
     'gbf_profile': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     'gbf_device_bytes': (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),

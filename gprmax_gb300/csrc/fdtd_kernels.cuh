@@ -48,8 +48,10 @@ struct Slab {
   int ocount;       // Phi elements per CFS order (< 2^30: a slab holds under half the nodes)
   float* phiE1;     // Phi arrays [order][...] of the first/second tangential E component
   float* phiE2;
-  float* phiH1;
+  float* phiH1;     // H Phi read by the H update ...
   float* phiH2;
+  float* phiH1n;    // ... and written (another buffer in the fused step, whose halo nodes read
+  float* phiH2n;    // the H state of nodes other tiles own; the same arrays otherwise)
   const float* eR;  // [4][order][T]: RA, RB, RE, RF for E
   const float* hR;  // same for H
 };
@@ -93,6 +95,8 @@ struct Box {
 struct StepParams {
   float* E[3];
   float* H[3];
+  float* En[3];           // fused step: where the new E and H go (the other field buffer)
+  float* Hn[3];
   const uint32_t* ID[6];  // per component [ncomp]
   const uint32_t* PE;     // packed E IDs per node: x | y << 10 | z << 20 | dispersive << 30
   const uint32_t* PH;     // packed H IDs per node: x | y << 10 | z << 20
@@ -150,39 +154,46 @@ __device__ __forceinline__ PmlRow load_row(const float* __restrict__ R, int T, i
   return c;
 }
 
+// The Phi state is read from `in` and its next value written to `out` (the same array, except
+// for the H state of the fused step), and only when `wr` (a halo node recomputed by a tile
+// that does not own it reads the state but leaves it to its owner).
 template <int PK>
-__device__ __forceinline__ float pml_update(float dF, float* phi, int pidx, int ocount,
-                                            const PmlRow& c) {
-  const float ph0 = phi[pidx];
+__device__ __forceinline__ float pml_update(float dF, const float* in, float* out, int pidx,
+                                            int ocount, const PmlRow& c, bool wr) {
+  const float ph0 = in[pidx];
   if (PK == PML_HORI1) {
     const float RA01 = c.RA0 - 1.0f;
     const float X = RA01 * dF + c.RB0 * ph0;
-    phi[pidx] = c.RE0 * ph0 - c.RF0 * dF;
+    if (wr) out[pidx] = c.RE0 * ph0 - c.RF0 * dF;
     return X;
   } else if (PK == PML_HORI2) {
     const float RA01 = c.RA0 * c.RA1 - 1.0f;
-    const float ph1 = phi[pidx + ocount];
+    const float ph1 = in[pidx + ocount];
     const float X = RA01 * dF + c.RA1 * c.RB0 * ph0 + c.RB1 * ph1;
-    phi[pidx + ocount] = c.RE1 * ph1 - c.RF1 * (c.RA0 * dF + c.RB0 * ph0);
-    phi[pidx] = c.RE0 * ph0 - c.RF0 * dF;
+    if (wr) {
+      out[pidx + ocount] = c.RE1 * ph1 - c.RF1 * (c.RA0 * dF + c.RB0 * ph0);
+      out[pidx] = c.RE0 * ph0 - c.RF0 * dF;
+    }
     return X;
   } else if (PK == PML_MRI1) {
     const float IRA = 1.0f / c.RA0;
     const float IRA1 = IRA - 1.0f;
     const float RC0 = IRA * c.RB0 * c.RF0;
     const float X = IRA1 * dF - IRA * ph0;
-    phi[pidx] = c.RE0 * ph0 + RC0 * dF - RC0 * ph0;
+    if (wr) out[pidx] = c.RE0 * ph0 + RC0 * dF - RC0 * ph0;
     return X;
   } else {  // PML_MRI2
     const float IRA = 1.0f / (c.RA0 + c.RA1);
     const float IRA1 = IRA - 1.0f;
     const float RC0 = IRA * c.RF0;
     const float RC1 = IRA * c.RF1;
-    const float ph1 = phi[pidx + ocount];
+    const float ph1 = in[pidx + ocount];
     const float Psi = c.RB0 * ph0 + c.RB1 * ph1;
     const float X = IRA1 * dF - IRA * Psi;
-    phi[pidx + ocount] = c.RE1 * ph1 + RC1 * (dF - Psi);
-    phi[pidx] = c.RE0 * ph0 + RC0 * (dF - Psi);
+    if (wr) {
+      out[pidx + ocount] = c.RE1 * ph1 + RC1 * (dF - Psi);
+      out[pidx] = c.RE0 * ph0 + RC0 * (dF - Psi);
+    }
     return X;
   }
 }
@@ -232,7 +243,8 @@ __device__ __forceinline__ int axis_member(int c, int n, int Tm, int Tp, int& pr
 // y: x, z; z: x, y) with their Phi arrays 1 and 2. `where` is axis_member's result (1 or 2).
 template <int PK, bool ELECTRIC, int AX>
 __device__ __forceinline__ void pml_axis(const StepParams& p, int where, int pr, int i, int j,
-                                         int k, float dA, float dB, float& XA, float& XB) {
+                                         int k, float dA, float dB, float& XA, float& XB,
+                                         bool wr = true) {
   // the two slabs of the axis are selected field by field, which keeps every parameter read a
   // constant-bank operand (no indexed parameter loads)
   const Slab& m = p.slab[AX];
@@ -247,8 +259,10 @@ __device__ __forceinline__ void pml_axis(const StepParams& p, int where, int pr,
   const int ocount = plus ? q.ocount : m.ocount;
   float* ph1 = ELECTRIC ? (plus ? q.phiE1 : m.phiE1) : (plus ? q.phiH1 : m.phiH1);
   float* ph2 = ELECTRIC ? (plus ? q.phiE2 : m.phiE2) : (plus ? q.phiH2 : m.phiH2);
-  XA = pml_update<PK>(div_cell(dA, d, r, fast), ph1, pidx, ocount, c);
-  XB = pml_update<PK>(div_cell(dB, d, r, fast), ph2, pidx, ocount, c);
+  float* out1 = ELECTRIC ? ph1 : (plus ? q.phiH1n : m.phiH1n);
+  float* out2 = ELECTRIC ? ph2 : (plus ? q.phiH2n : m.phiH2n);
+  XA = pml_update<PK>(div_cell(dA, d, r, fast), ph1, out1, pidx, ocount, c, wr);
+  XB = pml_update<PK>(div_cell(dB, d, r, fast), ph2, out2, pidx, ocount, c, wr);
 }
 
 // Sign with which axis AX's X enters component C: H x-axis Hy +, Hz -; y-axis Hx -, Hz +;
@@ -381,7 +395,8 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
                                        int i, int j, int k, bool src, int it, const int* where,
                                        const int* pr, float dEz_y, float dEy_z, float dEx_z,
                                        float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
-                                       uint32_t my, uint32_t mz, float& hx, float& hy, float& hz) {
+                                       uint32_t my, uint32_t mz, float& hx, float& hy, float& hz,
+                                       bool wphi = true) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const bool iin = CORE || i < nx, jin = CORE || j < ny, kin = k < nz;
   const bool ipos = CORE || i >= 1, jpos = CORE || j >= 1;
@@ -392,9 +407,9 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
   const bool hz2 = !p.two_d || ((nx == 1 || ny == 1) && kin);
   float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
   if (PK != PML_NONE) {
-    if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0]);
-    if (!CORE && where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1]);
-    if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2]);
+    if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0], wphi);
+    if (!CORE && where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1], wphi);
+    if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2], wphi);
   }
   // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
@@ -898,6 +913,7 @@ struct TLine {
 };
 
 struct RxParams {
+  const float* Eold[3];  // E the step read (the other buffer after a fused step; else E itself)
   const int* coords;   // [nrx][3]
   float* out;          // [9][iterations][nrx]
   int nrx;
@@ -913,6 +929,16 @@ struct RxParams {
 __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxParams& r, int* d_it) {
   const int it = *d_it;
   if (threadIdx.x == 0) {
+    // E outside the half-step's range changes only here: after a fused step, which wrote its
+    // E into the other buffer, each source node first takes its value from the buffer the step
+    // read, active or not, so that both buffers keep it
+    for (int s = 0; s < r.nsrcOut; ++s) {
+      const Src& q = r.srcOut[s];
+      if (q.comp < 3 && r.Eold[q.comp] != p.E[q.comp]) {
+        const long long idx = (long long)q.i * p.sx + (long long)q.j * p.sy + q.k;
+        p.E[q.comp][idx] = r.Eold[q.comp][idx];
+      }
+    }
     for (int s = 0; s < r.nsrcOut; ++s) {
       const Src& q = r.srcOut[s];
       if (it < q.first || it > q.last) continue;

@@ -1,7 +1,9 @@
 // gbfdtd.cu — context, device memory, time loop and C ABI of libgbfdtd.so (see include/gbfdtd.h).
 //
 // Device layout (one allocation per array, all C order with k fastest):
-//   fields   6 x fp32 [nx+1][ny+1][nz+1]         E then H
+//   fields   6 x fp32 [nx+1][ny+1][nz+1]         E then H; twice (two buffers) for models that
+//                                                take the fused step, which reads one and writes
+//                                                the other (ctx->cur is the current one)
 //   ID       uint32 [6][nx+1][ny+1][nz+1]
 //   T        float2 [3][P][nx+1][ny+1][nz+1]     dispersive state (P = maxpoles)
 //   Phi      per slab, E and H, first and second tangential component, fp32 [order][...]
@@ -12,14 +14,16 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
 
 #include "../../include/gbfdtd.h"
-#include "fdtd_kernels.cuh"
+#include "fused_step.cuh"
 
 using namespace gbf;
 
@@ -65,10 +69,27 @@ struct gbf_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
+  int graph_cur = 0;           // field buffer current when the graph was captured
   int grid_h = 0, grid_e = 0;  // persistent grid sizes
+  long long phi_floats = 0;    // all PML state (both H buffers for the fused step)
+  // fused step (fused_step.cuh): eligible models get two field buffers and two H PML buffers
+  int fused_ok = 0;            // buffers allocated for it
+  int fused_avail = 0;         // a fused kernel exists for the model (after the tables are known)
+  int fused = 0;               // the step is the fused kernel (else the two half-step kernels)
+  int cur = 0;                 // field / H PML buffer holding the current iteration
+  float* phiH[6][2][2] = {};   // [slab][buffer][first/second component]
+  FusedFn fk = nullptr;
+  FusedTiles ft{};
+  int f_tj = 0, f_blocks = 0;
+  size_t smem_f = 0;
+  int tuned = 0;
+  std::vector<std::pair<int, int>> tune_cand;   // candidate (tile height, chunks) being timed
+  std::vector<cudaEvent_t> tune_ev;             // two events per timed step
+  int tune_next = 0;
 };
 
 static std::string g_create_err;
+static void tune_release(gbf_ctx* ctx);
 
 static void invalidate_graph(gbf_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -196,11 +217,96 @@ static int pml_kind(const gbf_grid_desc& d) {
   return d.pml_order == 1 ? PML_MRI1 : PML_MRI2;
 }
 
+// Point the kernel parameters at buffer `b` (fields and H PML state), which then holds the
+// current iteration. En/Hn and phiH*n name the same arrays: the in-place form that every kernel
+// but the fused step uses (the batch copies these parameters too).
+static void set_current(gbf_ctx* ctx, int b) {
+  ctx->cur = b;
+  const long long n = ctx->ncomp;
+  float* base = ctx->fields + (size_t)b * 6 * n;
+  StepParams& p = ctx->sp;
+  for (int c = 0; c < 3; ++c) {
+    p.E[c] = p.En[c] = base + c * n;
+    p.H[c] = p.Hn[c] = base + (3 + c) * n;
+    ctx->rp.Eold[c] = p.E[c];
+  }
+  for (int s = 0; s < 6; ++s) {
+    Slab& sl = p.slab[s];
+    if (!sl.T) continue;
+    sl.phiH1 = sl.phiH1n = ctx->phiH[s][b][0];
+    sl.phiH2 = sl.phiH2n = ctx->phiH[s][b][1];
+  }
+}
+
+static float* current_fields(const gbf_ctx* ctx) {
+  return ctx->fields + (size_t)ctx->cur * 6 * ctx->ncomp;
+}
+
+// Parameters of a fused step that reads the current buffers and writes the other ones.
+static StepParams fused_params(const gbf_ctx* ctx) {
+  StepParams q = ctx->sp;
+  const int o = ctx->cur ^ 1;
+  const long long n = ctx->ncomp;
+  float* base = ctx->fields + (size_t)o * 6 * n;
+  for (int c = 0; c < 3; ++c) {
+    q.En[c] = base + c * n;
+    q.Hn[c] = base + (3 + c) * n;
+  }
+  for (int s = 0; s < 6; ++s) {
+    Slab& sl = q.slab[s];
+    if (!sl.T) continue;
+    sl.phiH1n = ctx->phiH[s][o][0];
+    sl.phiH2n = ctx->phiH[s][o][1];
+  }
+  return q;
+}
+
+// The launch decomposition for nch >= 1 chunks (clamped to [1, nx + 1]); nblocks < 0 when it
+// does not fit.
+static FusedTiles fused_tiles(int nx, int ny, int nz, int tj, int nch) {
+  FusedTiles t;
+  t.nseg = (nz + 1 + kTileK - 1) / kTileK;
+  t.njt = (ny + 1 + tj - 1) / tj;
+  const int planes = nx + 1;
+  if (nch < 1) nch = 1;
+  if (nch > planes) nch = planes;
+  t.L = (planes + nch - 1) / nch;
+  t.nch = (planes + t.L - 1) / t.L;
+  const long long nw = (long long)t.nseg * t.njt * t.nch;
+  t.nblocks = nw > (1LL << 30) ? -1 : (int)nw;
+  return t;
+}
+
+static FusedFn fused_kernel(int pk, int tj, int np, int uh, int tr) {
+  switch (tj * 10 + pk) {
+    case 70: return fused_kernel_pk0_tj7(np, uh, tr);
+    case 71: return fused_kernel_pk1_tj7(np, uh, tr);
+    case 72: return fused_kernel_pk2_tj7(np, uh, tr);
+    case 73: return fused_kernel_pk3_tj7(np, uh, tr);
+    case 74: return fused_kernel_pk4_tj7(np, uh, tr);
+    case 150: return fused_kernel_pk0_tj15(np, uh, tr);
+    case 151: return fused_kernel_pk1_tj15(np, uh, tr);
+    case 152: return fused_kernel_pk2_tj15(np, uh, tr);
+    case 153: return fused_kernel_pk3_tj15(np, uh, tr);
+    case 154: return fused_kernel_pk4_tj15(np, uh, tr);
+    default: return nullptr;
+  }
+}
+
 extern "C" {
 
 const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
 
 int gbf_check_cell_division(float d) { return reciprocal_division_exact(d) ? 1 : 0; }
+
+int gbf_fused_tiles(int32_t nx, int32_t ny, int32_t nz, int32_t tj, int32_t nch, int32_t* out) {
+  if (nx < 1 || ny < 1 || nz < 1 || tj < 1 || tj > 31 || !out) return GBF_EINVAL;
+  const FusedTiles t = fused_tiles(nx, ny, nz, tj, nch);
+  if (t.nblocks < 0) return GBF_EINVAL;
+  const int32_t v[6] = {t.nseg, t.njt, t.nch, t.L, t.nblocks, kTileK};
+  memcpy(out, v, sizeof v);
+  return GBF_OK;
+}
 
 int gbf_sweep_boxes(int32_t nx, int32_t ny, int32_t nz, const int32_t thickness[6],
                     int32_t electric, int32_t* boxes) {
@@ -228,6 +334,8 @@ int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n) {
 
 void gbf_destroy(gbf_ctx* ctx) {
   if (!ctx) return;
+  for (cudaEvent_t e : ctx->tune_ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   void* ptrs[] = {ctx->fields, ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
@@ -255,7 +363,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~7) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
+  if ((d.options & ~15) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
@@ -278,7 +386,24 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   }
   int rc = GBF_OK;
   auto A = [&](void** p, size_t n) { if (rc == GBF_OK) rc = dev_alloc(ctx, p, n); };
-  A((void**)&ctx->fields, sizeof(float) * 6 * npts);
+  // the fused step (3D, packed IDs, at most kFusedMaxPoles poles, no transmission lines, not
+  // turned off by option bit 3) needs a second field buffer; without room for it the model
+  // takes the two half-step kernels
+  ctx->fused_ok = (ones == 0 && d.ntl == 0 && d.nmat <= 1024 && d.maxpoles <= kFusedMaxPoles &&
+                   !(d.options & 8)) ? 1 : 0;
+  if (ctx->fused_ok) {
+    const size_t fb = sizeof(float) * 12 * npts;
+    if (cudaMalloc((void**)&ctx->fields, fb) == cudaSuccess) {
+      ctx->bytes += fb;
+      if (cudaMemsetAsync(ctx->fields, 0, fb, ctx->stream) != cudaSuccess)
+        rc = fail(ctx, GBF_ECUDA, "gbf_create: clearing the field buffers failed");
+    } else {
+      (void)cudaGetLastError();
+      ctx->fields = nullptr;
+      ctx->fused_ok = 0;
+    }
+  }
+  if (!ctx->fused_ok) A((void**)&ctx->fields, sizeof(float) * 6 * npts);
   A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
   if (d.nmat <= 1024) {
     ctx->idp = 1;
@@ -294,15 +419,17 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
     A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * npts);
   }
-  // PML state: per slab 4 Phi arrays of order * T * nu * nv
+  // PML state: per slab 4 Phi arrays of order * T * nu * nv (6 with the second H buffer)
   long long phi_total = 0;
+  const int nphi = ctx->fused_ok ? 6 : 4;
   for (int s = 0; s < 6; ++s) {
     const int t = d.pml_thickness[s];
     if (!t) continue;
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
-    phi_total += 4LL * d.pml_order * t * nu * nv;
+    phi_total += (long long)nphi * d.pml_order * t * nu * nv;
   }
+  ctx->phi_floats = phi_total;
   A((void**)&ctx->pml_mem, sizeof(float) * phi_total);
   int tmax = 1;
   for (int s = 0; s < 6; ++s) tmax = d.pml_thickness[s] > tmax ? d.pml_thickness[s] : tmax;
@@ -326,8 +453,8 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   // kernel parameters
   StepParams& p = ctx->sp;
   for (int c = 0; c < 3; ++c) {
-    p.E[c] = ctx->fields + c * npts;
-    p.H[c] = ctx->fields + (3 + c) * npts;
+    p.E[c] = p.En[c] = ctx->fields + c * npts;
+    p.H[c] = p.Hn[c] = ctx->fields + (3 + c) * npts;
   }
   for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID + c * npts;
   p.PE = ctx->PE;
@@ -373,12 +500,21 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     sl.phiE2 = phi; phi += per;
     sl.phiH1 = phi; phi += per;
     sl.phiH2 = phi; phi += per;
+    sl.phiH1n = sl.phiH1;
+    sl.phiH2n = sl.phiH2;
+    ctx->phiH[s][0][0] = ctx->phiH[s][1][0] = sl.phiH1;
+    ctx->phiH[s][0][1] = ctx->phiH[s][1][1] = sl.phiH2;
+    if (ctx->fused_ok) {
+      ctx->phiH[s][1][0] = phi; phi += per;
+      ctx->phiH[s][1][1] = phi; phi += per;
+    }
     sl.eR = ctx->pml_coef + (size_t)(s * 2 + 0) * 4 * d.pml_order * tmax;
     sl.hR = ctx->pml_coef + (size_t)(s * 2 + 1) * 4 * d.pml_order * tmax;
   }
   p.nsrcE = p.nsrcH = 0;
   p.srcE = p.srcH = ctx->srcs;
   RxParams& r = ctx->rp;
+  for (int c = 0; c < 3; ++c) r.Eold[c] = p.E[c];
   r.coords = ctx->rx_coords;
   r.out = ctx->rxs;
   r.nrx = d.nrx;
@@ -400,6 +536,39 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
 }
 
 }  // extern "C"
+
+// Tiles of the fused step: k segments of kTileK nodes, j tiles of `tj` rows and `nch` chunks of
+// planes along x (nch <= 0: as many chunks as give one wave of resident warps). Returns 0 when
+// no fused kernel exists for the model or the tiling does not fit.
+static int configure_fused(gbf_ctx* ctx, int tj, int nch) {
+  const gbf_grid_desc& d = ctx->d;
+  FusedFn f = fused_kernel(pml_kind(d), tj, d.maxpoles, ctx->uniform_h, ctx->treal);
+  if (!f) return 0;
+  size_t sm = 0;
+  if (ctx->sp.smem) sm = ctx->smem_e + 16 + (ctx->uniform_h ? 0 : ctx->smem_h);
+  if (sm > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  if (nch <= 0) {   // one wave of resident warps
+    const FusedTiles one = fused_tiles(d.nx, d.ny, d.nz, tj, 1);
+    int dev = 0, sms = 1, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)f, (tj + 1) * 32, sm);
+    const long long resident = (long long)sms * (per > 0 ? per : 1);
+    nch = (int)(resident / ((long long)one.nseg * one.njt));
+  }
+  const FusedTiles t = fused_tiles(d.nx, d.ny, d.nz, tj, nch);
+  if (t.nblocks < 0) return 0;
+  ctx->fk = f;
+  ctx->ft = t;
+  ctx->f_tj = tj;
+  ctx->smem_f = sm;
+  ctx->f_blocks = t.nblocks;
+  return 1;
+}
 
 // Coefficient tables, dispersive flags and packed IDs, once ctx->ID holds the ID array.
 static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
@@ -433,6 +602,11 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   ctx->grid_h = 0;
   ctx->grid_e = 0;
   invalidate_graph(ctx);
+  // one fused kernel per step where the model allows it (tiles tuned at the first run)
+  tune_release(ctx);
+  ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
+  ctx->fused = ctx->fused_avail;
+  ctx->tuned = 0;
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -681,12 +855,10 @@ int gbf_set_snapshots(gbf_ctx* ctx, const int32_t* defs) {
 int gbf_reset(gbf_ctx* ctx) {
   if (!ctx) return GBF_EINVAL;
   const gbf_grid_desc& d = ctx->d;
-  CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * 6 * ctx->ncomp, ctx->stream));
+  CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * (ctx->fused_ok ? 12 : 6) * ctx->ncomp, ctx->stream));
   if (ctx->T) CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)d.maxpoles * ctx->ncomp, ctx->stream));
-  long long phi_total = 0;
-  for (int s = 0; s < 6; ++s)
-    if (ctx->sp.slab[s].T) phi_total += 4LL * d.pml_order * ctx->sp.slab[s].ocount;
-  if (phi_total) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * phi_total, ctx->stream));
+  if (ctx->phi_floats) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * ctx->phi_floats, ctx->stream));
+  set_current(ctx, 0);
   CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
   CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
   if (d.ntl && (int)ctx->tls_init.size() == d.ntl) {
@@ -811,7 +983,32 @@ static void launch_tl(gbf_ctx* ctx) {
                                                            ctx->d.dx, ctx->d.dy, ctx->d.dz);
 }
 
+// The fused step kernel from the current buffers into the other ones; the other buffers then
+// hold the current iteration. Returns the E arrays the step read.
+struct EPtrs {
+  const float* e[3];
+};
+static EPtrs launch_fused_kernel(gbf_ctx* ctx) {
+  const StepParams q = fused_params(ctx);
+  ctx->fk<<<ctx->f_blocks, (ctx->f_tj + 1) * 32, ctx->smem_f, ctx->stream>>>(q, ctx->ft);
+  EPtrs prev;
+  for (int c = 0; c < 3; ++c) prev.e[c] = q.E[c];
+  set_current(ctx, ctx->cur ^ 1);
+  return prev;
+}
+
+static void launch_fused_end(gbf_ctx* ctx, const EPtrs& prev) {
+  RxParams r = ctx->rp;
+  for (int c = 0; c < 3; ++c) r.Eold[c] = prev.e[c];
+  end_of_step<<<1, 256, 0, ctx->stream>>>(ctx->sp, r, ctx->d_it);
+}
+
 static void launch_step(gbf_ctx* ctx) {
+  if (ctx->fused) {
+    const EPtrs prev = launch_fused_kernel(ctx);
+    launch_fused_end(ctx, prev);
+    return;
+  }
   launch_h(ctx);
   launch_tl(ctx);
   launch_e(ctx);
@@ -834,8 +1031,145 @@ static int launch_snapshot(gbf_ctx* ctx, int s) {
 
 static const int kGraphSteps = 16;
 
+// ---- step tuner ------------------------------------------------------------------------
+// The candidates are the fused step with each tiling and the two half-step kernels. Every one
+// gives the same result bit for bit (a node's arithmetic depends on neither), so the tuner times
+// real steps: the first steps of a model's run go through the candidates in turn (kTuneReps
+// rounds), the step's update kernels between two events, and once all have run the fastest is
+// kept (the smallest time over the rounds; the first round also carries the first-launch cost).
+// The model advances as usual meanwhile. The choice is kept per model shape for the process.
+// GBF_FUSED_TILE="tj,nch" forces a fused tiling; GBF_FUSED_TUNE=0 keeps the default (the fused
+// step with as many chunks as give one wave of resident blocks, tile height 7).
+static const int kTuneReps = 2;
+struct TuneKey {
+  int v[9];
+  bool operator<(const TuneKey& o) const { return memcmp(v, o.v, sizeof v) < 0; }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, std::pair<int, int>> g_tune;
+
+static TuneKey tune_key(const gbf_ctx* ctx) {
+  const gbf_grid_desc& d = ctx->d;
+  return TuneKey{{d.nx, d.ny, d.nz, pml_kind(d), d.maxpoles, ctx->uniform_h, ctx->treal,
+                  (int)ctx->smem_f, ctx->device}};
+}
+
+static void tune_release(gbf_ctx* ctx) {
+  for (cudaEvent_t e : ctx->tune_ev)
+    if (e) cudaEventDestroy(e);
+  ctx->tune_ev.clear();
+  ctx->tune_cand.clear();
+  ctx->tune_next = 0;
+}
+
+// Decide whether the model needs tuning steps and set up the candidates (once).
+static int tune_begin(gbf_ctx* ctx) {
+  if (ctx->tuned || !ctx->tune_cand.empty()) return GBF_OK;
+  invalidate_graph(ctx);
+  const char* force = getenv("GBF_FUSED_TILE");
+  int ftj = 0, fnch = 0;
+  if (force && sscanf(force, "%d,%d", &ftj, &fnch) == 2 && configure_fused(ctx, ftj, fnch)) {
+    ctx->fused = 1;
+    ctx->tuned = 1;
+    return GBF_OK;
+  }
+  const char* tune = getenv("GBF_FUSED_TUNE");
+  if (tune && tune[0] == '0') {
+    configure_fused(ctx, 7, 0);
+    ctx->fused = 1;
+    ctx->tuned = 1;
+    return GBF_OK;
+  }
+  const TuneKey key = tune_key(ctx);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto f = g_tune.find(key);
+    if (f != g_tune.end()) {
+      const bool use = f->second.first && configure_fused(ctx, f->second.first, f->second.second);
+      ctx->fused = use ? 1 : 0;
+      ctx->tuned = 1;
+      return GBF_OK;
+    }
+  }
+  std::vector<std::pair<int, int>> cand;
+  for (int tj : {7, 15}) {
+    if (!configure_fused(ctx, tj, 0)) continue;
+    const int base = ctx->ft.nch;
+    for (int nch : {base, 2 * base, 4 * base}) {
+      if (!configure_fused(ctx, tj, nch)) continue;
+      const std::pair<int, int> c(tj, ctx->ft.nch);
+      bool seen = false;
+      for (auto& x : cand) seen |= x == c;
+      if (!seen) cand.push_back(c);
+    }
+  }
+  cand.emplace_back(0, 0);   // the two half-step kernels
+  ctx->tune_ev.assign(2 * cand.size() * kTuneReps, nullptr);
+  for (auto& e : ctx->tune_ev) {
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      (void)cudaGetLastError();
+      tune_release(ctx);
+      configure_fused(ctx, 7, 0);
+      ctx->tuned = 1;
+      return GBF_OK;
+    }
+  }
+  ctx->tune_cand = cand;
+  ctx->tune_next = 0;
+  return GBF_OK;
+}
+
+// One step of the run with the next candidate tiling, timed; after the last one, pick.
+static int tune_step(gbf_ctx* ctx) {
+  const int nc = (int)ctx->tune_cand.size();
+  const int q = ctx->tune_next;
+  const std::pair<int, int> c = ctx->tune_cand[q % nc];
+  if (c.first) {
+    configure_fused(ctx, c.first, c.second);
+    ctx->fused = 1;
+    CK(cudaEventRecord(ctx->tune_ev[2 * q], ctx->stream));
+    const EPtrs prev = launch_fused_kernel(ctx);
+    CK(cudaEventRecord(ctx->tune_ev[2 * q + 1], ctx->stream));
+    launch_fused_end(ctx, prev);
+  } else {
+    ctx->fused = 0;
+    CK(cudaEventRecord(ctx->tune_ev[2 * q], ctx->stream));
+    launch_h(ctx);
+    launch_tl(ctx);
+    launch_e(ctx);
+    CK(cudaEventRecord(ctx->tune_ev[2 * q + 1], ctx->stream));
+    launch_end(ctx);
+  }
+  CK(cudaGetLastError());
+  ctx->tune_next = q + 1;
+  if (ctx->tune_next < nc * kTuneReps) return GBF_OK;
+  CK(cudaEventSynchronize(ctx->tune_ev.back()));
+  std::vector<float> best(nc, 1e30f);
+  for (int r = 0; r < nc * kTuneReps; ++r) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->tune_ev[2 * r], ctx->tune_ev[2 * r + 1]));
+    if (ms < best[r % nc]) best[r % nc] = ms;
+  }
+  int pick = 0;
+  for (int k = 1; k < nc; ++k)
+    if (best[k] < best[pick]) pick = k;
+  const std::pair<int, int> win = ctx->tune_cand[pick];
+  if (win.first) configure_fused(ctx, win.first, win.second);
+  ctx->fused = win.first ? 1 : 0;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[tune_key(ctx)] = win;
+  }
+  tune_release(ctx);
+  ctx->tuned = 1;
+  return GBF_OK;
+}
+
 static int ensure_graph(gbf_ctx* ctx) {
   if (ctx->gexec) return GBF_OK;
+  // an even number of steps: a fused graph ends on the buffer it started from
+  static_assert(kGraphSteps % 2 == 0, "graph steps");
+  ctx->graph_cur = ctx->cur;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < kGraphSteps; ++s) launch_step(ctx);
   cudaGraph_t g = nullptr;
@@ -854,8 +1188,8 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
   if (!ctx->materials) return fail(ctx, GBF_ESTATE, "gbf_run: materials not uploaded");
   if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
     return fail(ctx, GBF_EINVAL, "gbf_run: %d steps from iteration %d exceed %d iterations", nsteps, ctx->it, ctx->d.iterations);
-  if (flags & GBF_RUN_GRAPH) {
-    int rc = ensure_graph(ctx);
+  if (ctx->fused_avail && !ctx->tuned && nsteps > 0) {
+    int rc = tune_begin(ctx);
     if (rc) return rc;
   }
   int done = 0;
@@ -874,8 +1208,23 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
       if (t > it && t - it < span) span = t - it;
     }
     int n = span;
+    // while the fused step's tiles are being chosen: one timed candidate step at a time
+    while (n > 0 && ctx->fused_avail && !ctx->tuned) {
+      int rc = tune_step(ctx);
+      if (rc) return rc;
+      --n;
+    }
+    if ((flags & GBF_RUN_GRAPH) && !ctx->gexec && n >= kGraphSteps) {
+      int rc = ensure_graph(ctx);
+      if (rc) return rc;
+    }
     if ((flags & GBF_RUN_GRAPH) && ctx->gexec) {
-      while (n >= ctx->graph_steps) {
+      // the graph starts from the buffer it was captured on: one plain step realigns
+      if (n > ctx->graph_steps && ctx->cur != ctx->graph_cur) {
+        launch_step(ctx);
+        --n;
+      }
+      while (n >= ctx->graph_steps && ctx->cur == ctx->graph_cur) {
         CK(cudaGraphLaunch(ctx->gexec, ctx->stream));
         n -= ctx->graph_steps;
       }
@@ -929,14 +1278,17 @@ int gbf_download_rx(gbf_ctx* ctx, float* rxs) {
 
 int gbf_download_fields(gbf_ctx* ctx, float* fields) {
   if (!ctx || !fields) return GBF_EINVAL;
-  CK(cudaMemcpyAsync(fields, ctx->fields, sizeof(float) * 6 * ctx->ncomp, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(fields, current_fields(ctx), sizeof(float) * 6 * ctx->ncomp, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
 
 int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
   if (!ctx || !fields) return GBF_EINVAL;
-  CK(cudaMemcpyAsync(ctx->fields, fields, sizeof(float) * 6 * ctx->ncomp, cudaMemcpyHostToDevice, ctx->stream));
+  // both buffers of a fused model: E outside the half-step's range is read from either
+  for (int b = 0; b < (ctx->fused_ok ? 2 : 1); ++b)
+    CK(cudaMemcpyAsync(ctx->fields + (size_t)b * 6 * ctx->ncomp, fields, sizeof(float) * 6 * ctx->ncomp,
+                       cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
@@ -974,12 +1326,22 @@ int gbf_download_snapshot(gbf_ctx* ctx, int s, float* out) {
 int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_total) {
   if (!ctx || !ms_h || !ms_e || !ms_total) return GBF_EINVAL;
   if (!ctx->materials) return fail(ctx, GBF_ESTATE, "gbf_profile: materials not uploaded");
+
   if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
     return fail(ctx, GBF_EINVAL, "gbf_profile: too many steps");
   std::vector<cudaEvent_t> ev(3 * nsteps + 1);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], ctx->stream));
   for (int s = 0; s < nsteps; ++s) {
+    if (ctx->fused) {
+      // one kernel for the whole step: reported in the E column, the H column stays 0
+      CK(cudaEventRecord(ev[3 * s + 1], ctx->stream));
+      const EPtrs prev = launch_fused_kernel(ctx);
+      CK(cudaEventRecord(ev[3 * s + 2], ctx->stream));
+      launch_fused_end(ctx, prev);
+      CK(cudaEventRecord(ev[3 * s + 3], ctx->stream));
+      continue;
+    }
     launch_h(ctx);
     launch_tl(ctx);
     CK(cudaEventRecord(ev[3 * s + 1], ctx->stream));
@@ -999,6 +1361,32 @@ int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_to
   for (auto& e : ev) cudaEventDestroy(e);
   ctx->it += nsteps;
   *ms_h += th; *ms_e += te; *ms_total += tt;
+  return GBF_OK;
+}
+
+int gbf_set_fused_tiles(gbf_ctx* ctx, int32_t tj, int32_t nch) {
+  if (!ctx) return GBF_EINVAL;
+  if (!ctx->fused_avail) return fail(ctx, GBF_ESTATE, "gbf_set_fused_tiles: the model does not take the fused step");
+  if (tj != 7 && tj != 15) return fail(ctx, GBF_EINVAL, "gbf_set_fused_tiles: tile height %d (7 or 15)", tj);
+  tune_release(ctx);
+  if (!configure_fused(ctx, tj, nch))
+    return fail(ctx, GBF_EINVAL, "gbf_set_fused_tiles: no fused kernel for tile height %d and %d chunks", tj, nch);
+  ctx->fused = 1;
+  ctx->tuned = 1;
+  invalidate_graph(ctx);
+  return GBF_OK;
+}
+
+int gbf_step_info(gbf_ctx* ctx, int32_t info[8]) {
+  if (!ctx || !info) return GBF_EINVAL;
+  info[0] = ctx->fused;
+  info[1] = ctx->fused ? ctx->f_tj : 0;
+  info[2] = ctx->fused ? ctx->ft.nch : 0;
+  info[3] = ctx->fused ? ctx->ft.L : 0;
+  info[4] = ctx->fused ? ctx->f_blocks : 0;
+  info[5] = ctx->tuned;
+  info[6] = ctx->cur;
+  info[7] = ctx->fused_ok | (ctx->fused_avail << 1);
   return GBF_OK;
 }
 

@@ -270,6 +270,22 @@ class DeviceModel:
                                          ctypes.byref(t)))
         return h.value, e.value, t.value
 
+    def step_info(self):
+        """How the model steps: {'fused': bool, 'tj', 'nch', 'planes', 'blocks', 'tuned',
+        'buffer', 'two_buffers', 'fused_available'} (``gbf_step_info``)."""
+        info = np.zeros(8, dtype=np.int32)
+        self._check(self.lib.gbf_step_info(self.ctx, _ptr(info)))
+        keys = ('fused', 'tj', 'nch', 'planes', 'blocks', 'tuned', 'buffer', 'two_buffers')
+        out = {k: int(v) for k, v in zip(keys, info)}
+        out['fused'] = bool(out['fused'])
+        out['fused_available'] = bool(out['two_buffers'] & 2)
+        out['two_buffers'] = bool(out['two_buffers'] & 1)
+        return out
+
+    def set_fused_tiles(self, tj, nch):
+        """Fix the fused step's tiling (tile height ``tj`` rows, ``nch`` chunks along x)."""
+        self._check(self.lib.gbf_set_fused_tiles(self.ctx, int(tj), int(nch)))
+
     def device_bytes(self):
         b = ctypes.c_size_t(0)
         self._check(self.lib.gbf_device_bytes(self.ctx, ctypes.byref(b)))

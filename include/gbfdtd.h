@@ -71,7 +71,9 @@ typedef struct gbf_grid_desc {
                                     dispersive state complex even when every pole is Debye
                                     (otherwise only its real parts are stored then, the
                                     imaginary parts being +0 throughout; needed to batch such a
-                                    model with others whose state is complex); other bits 0 */
+                                    model with others whose state is complex); bit 3: advance
+                                    every iteration with the two half-step kernels even where
+                                    the fused step applies (see gbf_run); other bits 0 */
     int32_t ntl;                 /* transmission lines among the nsrc sources */
     int32_t reserved[2];         /* must be zero */
 } gbf_grid_desc;
@@ -126,7 +128,13 @@ int gbf_reset(gbf_ctx* ctx);
  * the H half-step (update, PML, magnetic sources), the E half-step (update or dispersive
  * update, PML, E sources, dispersive second part) and stores receiver samples, in the order of
  * solve_cpu (model_build_run.py:424-470). Asynchronous on the context stream unless
- * GBF_RUN_CHECK is set. */
+ * GBF_RUN_CHECK is set.
+ * 3D models with at most 1024 materials, at most 2 poles and no transmission lines can also
+ * advance with one fused kernel per iteration (both half-steps in one pass over the grid; the
+ * same results bit for bit), unless options bit 3 is set. Which form runs, and the fused
+ * kernel's tiles, are chosen by timing: the first steps of the first run of each model shape in
+ * the process each use one candidate (twice round; the model advances as usual, the choice
+ * changing no result) and the fastest is kept from then on. */
 int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
 
 /* Iteration the next gbf_run call starts at. */
@@ -153,8 +161,30 @@ int gbf_download_dispersive(gbf_ctx* ctx, float* T);
 int gbf_download_snapshot(gbf_ctx* ctx, int s, float* out);
 
 /* Time `nsteps` iterations on the context stream with CUDA events around every launch; adds
- * the summed device milliseconds of the H and E half-step kernels and of the whole sequence. */
+ * the summed device milliseconds of the H and E half-step kernels and of the whole sequence.
+ * With the fused step the whole update is one kernel: its time goes to *ms_e, *ms_h gets 0. */
 int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_total);
+
+/* Fix the fused step's tiles instead of letting the first run time candidates: tile height tj
+ * (7 or 15 rows) and nch chunks along x (<= 0: one wave of resident blocks). Results do not depend
+ * on the tiling. GBF_ESTATE when the model does not take the fused step. No counterpart in the
+ * reference. */
+int gbf_set_fused_tiles(gbf_ctx* ctx, int32_t tj, int32_t nch);
+
+/* The fused step's launch decomposition for a grid of nx x ny x nz cells, tile height tj rows
+ * and nch chunks along x (host arithmetic only, no device call): out[0] k segments, [1] j
+ * tiles, [2] chunks, [3] planes per chunk, [4] blocks, [5] k nodes owned per tile. Block b works
+ * on segment b % out[0], tile (b / out[0]) % out[1], chunk b / (out[0] * out[1]) with tj + 1
+ * warps, warp w on row tile * tj - 1 + w. No counterpart in the reference; exported so the tiling
+ * can be checked without a GPU. */
+int gbf_fused_tiles(int32_t nx, int32_t ny, int32_t nz, int32_t tj, int32_t nch, int32_t* out);
+
+/* How the context steps: info[0] 1 for the fused step (0: two half-step kernels), [1] its tile
+ * height in j, [2] chunks along x, [3] planes per chunk, [4] blocks per launch, [5] 1 once the
+ * step form and tiles are chosen, [6] the field buffer holding the current iteration, [7] bit 0
+ * the second buffer exists, bit 1 a fused kernel exists for the model. No counterpart in the reference (its GPU solver has one fixed launch shape,
+ * grid.py:103). */
+int gbf_step_info(gbf_ctx* ctx, int32_t info[8]);
 
 /* Run `nsteps` iterations like gbf_run, bracketed by CUDA events recorded on the context
  * stream; blocks until done and returns the elapsed device milliseconds in *ms. */

@@ -22,7 +22,11 @@ REF_BUILD = os.path.join(os.path.dirname(HERE), 'oracle', '_ref', 'nofma', 'gprM
 
 
 def _reference_available():
-    return os.path.isdir(os.path.join(SRC, 'gprMax')) and os.path.isdir(REF_BUILD)
+    """The checkout and the no-contraction build of every reference module ``run_model``
+    imports (``oracle/build_ref.py --variant nofma``; the kernels alone are not enough)."""
+    import glob
+    return (os.path.isdir(os.path.join(SRC, 'gprMax')) and
+            bool(glob.glob(os.path.join(REF_BUILD, 'geometry_outputs_ext.*.so'))))
 
 
 pytestmark = pytest.mark.skipif(not _reference_available(),

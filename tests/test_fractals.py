@@ -3,6 +3,7 @@ materials and the command checks against the reference (``gprMax/fractals.py:141
 ``gprMax/materials.py:268-330``, ``input_cmds_geometry.py:808-888``,
 ``input_cmds_multiuse.py:694-722``). Whole-model agreement (ID array and coefficients) is
 covered by the ``fractal`` golden fixture."""
+import glob
 import os
 import subprocess
 import sys
@@ -113,7 +114,8 @@ np.savez({dest!r}, **out)
 '''
 
 
-@pytest.mark.skipif(not (os.path.isdir(os.path.join(SRC, 'gprMax')) and os.path.isdir(REF_BUILD)),
+@pytest.mark.skipif(not (os.path.isdir(os.path.join(SRC, 'gprMax')) and
+                         bool(glob.glob(os.path.join(REF_BUILD, 'fractals_generate_ext.*.so')))),
                     reason='reference sources or compiled reference kernels absent')
 def test_fractal_volume_matches_reference_bit_for_bit():
     with tempfile.TemporaryDirectory() as tmp:
@@ -183,7 +185,8 @@ np.savez({dest!r}, **out)
 '''
 
 
-@pytest.mark.skipif(not (os.path.isdir(os.path.join(SRC, 'gprMax')) and os.path.isdir(REF_BUILD)),
+@pytest.mark.skipif(not (os.path.isdir(os.path.join(SRC, 'gprMax')) and
+                         bool(glob.glob(os.path.join(REF_BUILD, 'fractals_generate_ext.*.so')))),
                     reason='reference sources or compiled reference kernels absent')
 def test_fractal_surface_matches_reference_bit_for_bit():
     from gprmax_gb300.fractals import FractalSurface

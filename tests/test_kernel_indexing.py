@@ -167,3 +167,74 @@ def test_sweep_boxes_cover_the_domain_once(native_lib, n3, thick, electric):
                 assert idx.min() >= 1 and idx.max() <= n3[axis] - 1
     assert start == np.prod(ext)
     assert (seen == 1).all()
+
+
+def _fused_tiles(lib, n3, tj, nch):
+    import ctypes
+    out = np.zeros(6, dtype=np.int32)
+    rc = lib.gbf_fused_tiles(n3[0], n3[1], n3[2], tj, nch, out.ctypes.data_as(ctypes.c_void_p))
+    assert rc == 0
+    return [int(v) for v in out]
+
+
+@pytest.mark.parametrize('n3', [(7, 9, 5), (23, 19, 40), (12, 30, 62), (31, 8, 31)])
+@pytest.mark.parametrize('tj', [7, 15])
+@pytest.mark.parametrize('nch', [1, 3, 7, 1000])
+def test_fused_tiles_cover_the_grid_once(native_lib, n3, tj, nch):
+    """The fused step's tiling (fused_step.cuh, decomposition from the library's own
+    ``gbf_fused_tiles``), restated: block b has tj + 1 warps; warp w, lane l works on row
+    j = tile * tj - 1 + w and column k = seg * K - 1 + l over planes [i0 - 1 or 0, i1); warp 0
+    and lane 0 are halo. Checks that every H node of [0,nx]x[0,ny]x[0,nz] and every E node of
+    [0,nx)x[0,ny)x[0,nz) is stored by exactly one thread, that every guarded load lies inside
+    the arrays, and that each E update finds the H values it needs (j-1 from the warp below,
+    k-1 from the lane below, i-1 from the same thread's previous plane)."""
+    nx, ny, nz = n3
+    nseg, njt, nchunks, L, nblocks, K = _fused_tiles(native_lib, n3, tj, nch)
+    assert K == 31 and nblocks == nseg * njt * nchunks
+    assert nseg * K >= nz + 1 and njt * tj >= ny + 1 and nchunks * L >= nx + 1
+    assert (nchunks - 1) * L < nx + 1
+    hcount = np.zeros((nx + 1, ny + 1, nz + 1), dtype=np.int32)
+    ecount = np.zeros((nx, ny, nz), dtype=np.int32)
+    lane = np.arange(32)
+    for b in range(nblocks):
+        seg, rest = b % nseg, b // nseg
+        jt, ch = rest % njt, rest // njt
+        k = seg * K - 1 + lane
+        kv = (k >= 0) & (k <= nz)
+        assert ((k >= 0) | (lane == 0)).all()        # only the halo lane can fall below 0
+        i0 = ch * L
+        i1 = min(i0 + L, nx + 1)
+        assert i0 <= nx
+        ib = i0 - 1 if i0 > 0 else 0
+        for w in range(tj + 1):
+            j = jt * tj - 1 + w
+            jv = 0 <= j <= ny
+            own = (lane > 0) & (w > 0) & kv & jv
+            eown = (lane > 0) & (w > 0) & (k < nz) & (j < ny)
+            assert j >= 0 or w == 0                  # only the halo warp can fall below 0
+            for i in range(ib, i1):
+                # loads at planes i .. i + 2 are guarded by pl <= nx and the node's validity;
+                # the last lane's k + 1 and the top warp's j + 1 by k + 1 <= nz, j + 1 <= ny
+                if jv:
+                    assert k[kv].min() >= 0 and k[kv].max() <= nz
+                halo = i < i0
+                if not halo and jv:
+                    hcount[i, j, k[own]] += 1
+                if not halo and i < nx and eown.any():
+                    ecount[i, j, k[eown]] += 1
+                    # H(j - 1) from warp w - 1 >= 0 of the same block; H(k - 1) from lane - 1 >= 0;
+                    # H(i - 1) formed by this thread at the previous plane i - 1 >= ib
+                    assert w - 1 >= 0 and (lane[eown] >= 1).all()
+                    assert i == 0 or i - 1 >= ib
+    assert (hcount == 1).all(), 'H nodes stored {}..{} times'.format(hcount.min(), hcount.max())
+    assert (ecount == 1).all(), 'E nodes stored {}..{} times'.format(ecount.min(), ecount.max())
+
+
+def test_fused_tiles_at_the_benchmark_size(native_lib):
+    """The decomposition of the 400 x 400 x 200 soil covers it with whole tiles and stays far
+    inside int32 node indices."""
+    nseg, njt, nchunks, L, nblocks, K = _fused_tiles(native_lib, (400, 400, 200), 7, 2)
+    assert (nseg, njt) == (7, 58)
+    assert nchunks * L >= 401 and (nchunks - 1) * L < 401
+    assert nblocks == 7 * 58 * nchunks
+    assert 401 * 401 * 201 < 2 ** 31
