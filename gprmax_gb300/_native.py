@@ -111,6 +111,10 @@ _SIGS = {
     'gbf_destroy': (None, [_P]),
     'gbf_upload_materials': (ctypes.c_int, [_P, _P, _P, _P, _P]),
     'gbf_upload_pml': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
+    'gbf_upload_materials_packed': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
+    'gbf_pack_ids': (ctypes.c_int, [_P, ctypes.c_int64, _P, _P, _P]),
+    'gbf_host_alloc': (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
+    'gbf_host_free': (None, [_P]),
     'gbf_upload_sources': (ctypes.c_int, [_P, _P, _P, _P]),
     'gbf_set_receivers': (ctypes.c_int, [_P, _P]),
     'gbf_set_snapshots': (ctypes.c_int, [_P, _P]),

@@ -948,7 +948,8 @@ __device__ __forceinline__ void end_of_step_body(const StepParams& p, const RxPa
         E[idx] = *q.w;
         continue;
       }
-      const uint32_t m = p.ID[q.comp][idx];
+      // the edge's material: from the packed E word, or the ID array when IDs are not packed
+      const uint32_t m = p.PE ? (p.PE[idx] >> (kPackBits * q.comp)) & kPackMask : p.ID[q.comp][idx];
       const float c4 = p.cEs[m];
       const float w = q.w[it];
       float F = E[idx];
@@ -1085,18 +1086,5 @@ __global__ void snapshot_store(const __grid_constant__ StepParams p, const SnapP
   }
 }
 
-// Packed per-node material words for the half-step kernels (IDs < 1024): E word holds the Ex,
-// Ey, Ez IDs and a flag that one of them has dispersive poles; H word the Hx, Hy, Hz IDs.
-__global__ void pack_ids(const __grid_constant__ StepParams p, const unsigned char* dispersive,
-                         uint32_t* pe, uint32_t* ph) {
-  const int n = p.ncomp;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const uint32_t ex = p.ID[0][q], ey = p.ID[1][q], ez = p.ID[2][q];
-    uint32_t w = ex | (ey << kPackBits) | (ez << (2 * kPackBits));
-    if (dispersive && (dispersive[ex] | dispersive[ey] | dispersive[ez])) w |= kDispersiveBit;
-    pe[q] = w;
-    ph[q] = p.ID[3][q] | (p.ID[4][q] << kPackBits) | (p.ID[5][q] << (2 * kPackBits));
-  }
-}
 #endif  // GBF_KERNELS_ONLY
 }  // namespace gbf

@@ -404,11 +404,14 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     }
   }
   if (!ctx->fused_ok) A((void**)&ctx->fields, sizeof(float) * 6 * npts);
-  A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
+  // packed IDs (at most 1024 materials): two words per node, built straight from the caller's
+  // array; otherwise the six ID arrays themselves
   if (d.nmat <= 1024) {
     ctx->idp = 1;
     A((void**)&ctx->PE, sizeof(uint32_t) * npts);
     A((void**)&ctx->PH, sizeof(uint32_t) * npts);
+  } else {
+    A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
   }
   A((void**)&ctx->disp, (size_t)d.nmat);
   A((void**)&ctx->cE4, sizeof(float4) * d.nmat);
@@ -456,7 +459,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     p.E[c] = p.En[c] = ctx->fields + c * npts;
     p.H[c] = p.Hn[c] = ctx->fields + (3 + c) * npts;
   }
-  for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID + c * npts;
+  for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID ? ctx->ID + c * npts : nullptr;
   p.PE = ctx->PE;
   p.PH = ctx->PH;
   for (int q = 0; q < kSrcInline; ++q) p.srcqE[q] = p.srcqH[q] = -1;
@@ -570,9 +573,55 @@ static int configure_fused(gbf_ctx* ctx, int tj, int nch) {
   return 1;
 }
 
-// Coefficient tables, dispersive flags and packed IDs, once ctx->ID holds the ID array.
+// Packed per-node material words (IDs < 1024) from an ID array [6][n] that the device can read
+// (device memory, or host memory the device reaches directly or through a mapping): E word the
+// Ex, Ey, Ez IDs and bit 30 when one of them has dispersive poles, H word the Hx, Hy, Hz IDs.
+// The largest ID goes to *mx, so that one pass both packs and checks the array.
+__global__ void pack_ids_from(const uint32_t* __restrict__ ID, long long n, int nmat,
+                              const unsigned char* __restrict__ disp, uint32_t* __restrict__ pe,
+                              uint32_t* __restrict__ ph, unsigned int* mx) {
+  unsigned int m = 0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const uint32_t ex = ID[q], ey = ID[n + q], ez = ID[2 * n + q];
+    const uint32_t hx = ID[3 * n + q], hy = ID[4 * n + q], hz = ID[5 * n + q];
+    const uint32_t a = max(max(ex, ey), ez), b = max(max(hx, hy), hz);
+    m = max(m, max(a, b));
+    uint32_t w = (ex & kPackMask) | ((ey & kPackMask) << kPackBits) | ((ez & kPackMask) << (2 * kPackBits));
+    if (disp && a < (uint32_t)nmat && (disp[ex] | disp[ey] | disp[ez])) w |= kDispersiveBit;
+    pe[q] = w;
+    ph[q] = (hx & kPackMask) | ((hy & kPackMask) << kPackBits) | ((hz & kPackMask) << (2 * kPackBits));
+  }
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+// Packed words copied in as the caller packed them (gbf_pack_ids: no dispersive flag): add the
+// flag to the E words and put the largest ID in *mx.
+__global__ void finish_packed_ids(uint32_t* __restrict__ pe, const uint32_t* __restrict__ ph,
+                                  long long n, int nmat, const unsigned char* __restrict__ disp,
+                                  unsigned int* mx) {
+  unsigned int m = 0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    uint32_t w = pe[q];
+    const uint32_t h = ph[q];
+    const uint32_t ex = w & kPackMask, ey = (w >> kPackBits) & kPackMask, ez = (w >> (2 * kPackBits)) & kPackMask;
+    const uint32_t a = max(max(ex, ey), ez);
+    const uint32_t b = max(max(h & kPackMask, (h >> kPackBits) & kPackMask), (h >> (2 * kPackBits)) & kPackMask);
+    m = max(m, max(a, b));
+    if (w >> (3 * kPackBits)) m = 0xffffffffu;   // bits above the three IDs must be clear
+    if (disp && a < (uint32_t)nmat && (disp[ex] | disp[ey] | disp[ez])) pe[q] = w | kDispersiveBit;
+  }
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+// Coefficient tables, dispersive flags and, with packed IDs, the packed words: from `ids` (an ID
+// array [6][ncomp] the device can read), or, with `ids` NULL, from the words already copied into
+// ctx->PE/PH by the caller's packing. Plain IDs are already in ctx->ID.
 static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
-                         const float* coeffD) {
+                         const float* coeffD, const uint32_t* ids) {
   const int nmat = ctx->d.nmat;
   // one H row for every material (no magnetic materials): the H half-step then needs no IDs
   int uni = 1;
@@ -605,8 +654,12 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   // one fused kernel per step where the model allows it (tiles tuned at the first run)
   tune_release(ctx);
   ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
-  ctx->fused = ctx->fused_avail;
-  ctx->tuned = 0;
+  // measured on the GB300: with PML slabs the fused step runs slower than the two half-step
+  // kernels (its slab nodes wait on their PML state within each plane), so such models take the
+  // half-step kernels without timing the fused one (gbf_set_fused_tiles still selects it)
+  const bool timed = ctx->fused_avail && pml_kind(ctx->d) == PML_NONE;
+  ctx->fused = timed ? 1 : 0;
+  ctx->tuned = timed ? 0 : 1;
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -645,9 +698,31 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   }
   CK(cudaMemcpyAsync(ctx->disp, disp.data(), nmat, cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->idp == 1) {
-    pack_ids<<<1024, 256, 0, ctx->stream>>>(ctx->sp, ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
-                                           ctx->PE, ctx->PH);
+    unsigned int* dmax = nullptr;
+    CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
+    CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ids)
+      pack_ids_from<<<sms * 8, 256, 0, ctx->stream>>>(ids, ctx->ncomp, nmat,
+                                                     ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
+                                                     ctx->PE, ctx->PH, dmax);
+    else
+      finish_packed_ids<<<sms * 8, 256, 0, ctx->stream>>>(ctx->PE, ctx->PH, ctx->ncomp, nmat,
+                                                         ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
+                                                         dmax);
     CK(cudaGetLastError());
+    unsigned int mx = 0;
+    CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(dmax, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (mx >= (unsigned)nmat) {
+      ctx->materials = false;
+      if (mx == 0xffffffffu)
+        return fail(ctx, GBF_EINVAL, "packed material words have bits set above the three IDs");
+      return fail(ctx, GBF_EINVAL, "material ID %u >= nmat %d", mx, nmat);
+    }
   }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->materials = true;
@@ -695,9 +770,53 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
   const size_t n = 6 * (size_t)ctx->ncomp;
-  // a large array is page-locked for the copy (registration is cheap next to the first copy of
-  // pageable memory); where that is refused the copy goes from pageable memory
   const size_t bytes = sizeof(uint32_t) * n;
+  if (ctx->idp == 1) {
+    // packed IDs: one kernel reads the caller's array where it lies and writes the two words
+    // per node, checking every ID on the way. Where the device reads pageable host memory
+    // through the host's page tables (NVLink-C2C systems) it reads the array directly; else the
+    // array is page-locked and mapped for the kernel, or, where that is refused, copied to a
+    // device buffer first. The array is not kept on the device.
+    int pageable = 0, host_tables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, ctx->device);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, ctx->device);
+    const uint32_t* src = nullptr;
+    bool mapped = false;
+    uint32_t* tmp = nullptr;
+    if (pageable && host_tables) {
+      src = ID;
+    } else if (cudaHostRegister(const_cast<uint32_t*>(ID), bytes,
+                                cudaHostRegisterMapped | cudaHostRegisterReadOnly) == cudaSuccess) {
+      mapped = true;
+      void* dp = nullptr;
+      if (cudaHostGetDevicePointer(&dp, const_cast<uint32_t*>(ID), 0) == cudaSuccess) {
+        src = static_cast<const uint32_t*>(dp);
+      } else {
+        (void)cudaGetLastError();
+      }
+    } else {
+      (void)cudaGetLastError();
+    }
+    if (!src) {
+      if (cudaMalloc((void**)&tmp, bytes) != cudaSuccess) {
+        if (mapped) cudaHostUnregister(const_cast<uint32_t*>(ID));
+        return fail(ctx, GBF_ENOMEM, "gbf_upload_materials: no room for the ID array");
+      }
+      cudaError_t ce = cudaMemcpyAsync(tmp, ID, bytes, cudaMemcpyHostToDevice, ctx->stream);
+      if (ce != cudaSuccess) {
+        cudaFree(tmp);
+        if (mapped) cudaHostUnregister(const_cast<uint32_t*>(ID));
+        return fail(ctx, GBF_ECUDA, "gbf_upload_materials: ID copy: %s", cudaGetErrorString(ce));
+      }
+      src = tmp;
+    }
+    const int rc = upload_tables(ctx, coeffE, coeffH, coeffD, src);   // synchronises the stream
+    if (tmp) cudaFree(tmp);
+    if (mapped) cudaHostUnregister(const_cast<uint32_t*>(ID));
+    return rc;
+  }
+  // plain IDs: a large array is page-locked for the copy (registration is cheap next to the
+  // first copy of pageable memory); where that is refused the copy goes from pageable memory
   bool locked = false;
   if (bytes >= ((size_t)64 << 20)) {
     locked = cudaHostRegister(const_cast<uint32_t*>(ID), bytes, cudaHostRegisterReadOnly) == cudaSuccess;
@@ -714,7 +833,70 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   // every ID must index the tables (checked on the device)
   const int rc = check_ids(ctx, "gbf_upload_materials");
   if (rc != GBF_OK) return rc;
-  return upload_tables(ctx, coeffE, coeffH, coeffD);
+  return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
+}
+
+int gbf_upload_materials_packed(gbf_ctx* ctx, const uint32_t* PE, const uint32_t* PH,
+                                const float* coeffE, const float* coeffH, const float* coeffD) {
+  if (!ctx) return GBF_EINVAL;
+  if (!PE || !PH || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: NULL array");
+  if (ctx->idp != 1)
+    return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: %d materials do not pack (at most 1024)", ctx->d.nmat);
+  const size_t bytes = sizeof(uint32_t) * (size_t)ctx->ncomp;
+  CK(cudaMemcpyAsync(ctx->PE, PE, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->PH, PH, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
+}
+
+int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint32_t* maxid) {
+  if (!ID || !PE || !PH || n < 1) return fail(nullptr, GBF_EINVAL, "gbf_pack_ids: bad arguments");
+  // contiguous ranges over the host's cores; each range packs and keeps its largest ID
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = nt < 1 ? 1 : (nt > 64 ? 64 : nt);
+  if ((int64_t)nt > n / 65536 + 1) nt = (unsigned)(n / 65536 + 1);
+  std::vector<uint32_t> mx(nt, 0);
+  auto work = [&](unsigned t) {
+    const int64_t lo = n * (int64_t)t / nt, hi = n * (int64_t)(t + 1) / nt;
+    uint32_t m = 0;
+    for (int64_t q = lo; q < hi; ++q) {
+      const uint32_t ex = ID[q], ey = ID[n + q], ez = ID[2 * n + q];
+      const uint32_t hx = ID[3 * n + q], hy = ID[4 * n + q], hz = ID[5 * n + q];
+      const uint32_t a = ex > ey ? ex : ey, b = hx > hy ? hx : hy;
+      const uint32_t c = ez > hz ? ez : hz;
+      const uint32_t ab = a > b ? a : b;
+      m = m > ab ? m : ab;
+      m = m > c ? m : c;
+      PE[q] = (ex & kPackMask) | ((ey & kPackMask) << kPackBits) | ((ez & kPackMask) << (2 * kPackBits));
+      PH[q] = (hx & kPackMask) | ((hy & kPackMask) << kPackBits) | ((hz & kPackMask) << (2 * kPackBits));
+    }
+    mx[t] = m;
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  uint32_t m = 0;
+  for (uint32_t v : mx) m = m > v ? m : v;
+  if (maxid) *maxid = m;
+  if (m > kPackMask) return fail(nullptr, GBF_EINVAL, "gbf_pack_ids: material ID %u does not fit 10 bits", m);
+  return GBF_OK;
+}
+
+int gbf_host_alloc(size_t bytes, void** out) {
+  if (!out) return GBF_EINVAL;
+  *out = nullptr;
+  cudaError_t e = cudaHostAlloc(out, bytes ? bytes : 16, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    *out = nullptr;
+    return fail(nullptr, e == cudaErrorMemoryAllocation ? GBF_ENOMEM : GBF_ECUDA,
+                "gbf_host_alloc: %s", cudaGetErrorString(e));
+  }
+  return GBF_OK;
+}
+
+void gbf_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
@@ -731,10 +913,12 @@ int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
                 dims[2], gdev, ctx->d.nx, ctx->d.ny, ctx->d.nz, ctx->device);
   const size_t n = 6 * (size_t)ctx->ncomp;
   CK(cudaStreamSynchronize(gstream));
+  if (ctx->idp == 1)   // packed straight from the geometry's IDs
+    return upload_tables(ctx, coeffE, coeffH, coeffD, gid);
   CK(cudaMemcpyAsync(ctx->ID, gid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   const int rc = check_ids(ctx, "gbf_upload_materials_geom");
   if (rc != GBF_OK) return rc;
-  return upload_tables(ctx, coeffE, coeffH, coeffD);
+  return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
 }
 
 int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]) {

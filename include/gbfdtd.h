@@ -98,6 +98,26 @@ void gbf_destroy(gbf_ctx* ctx);
 int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
                          const float* coeffH, const float* coeffD);
 
+/* The material IDs as two packed words per node (models with at most 1024 materials), made
+ * by gbf_pack_ids: PE uint32 [nx+1][ny+1][nz+1] = IDx | IDy << 10 | IDz << 20 of the E
+ * components, PH the same for H; coefficient tables as for gbf_upload_materials. Copies a third
+ * of the bytes of the ID array (from page-locked memory, see gbf_host_alloc, at the full copy
+ * rate). GBF_EINVAL when an ID does not index the tables or the model has more than 1024
+ * materials. No counterpart in the reference: the same upload as gbf_upload_materials
+ * (model_build_run.py:512-529) from a compact form of the ID array. */
+int gbf_upload_materials_packed(gbf_ctx* ctx, const uint32_t* PE, const uint32_t* PH,
+                                const float* coeffE, const float* coeffH, const float* coeffD);
+
+/* Pack an ID array [6][n] (n nodes per component, the layout of gbf_upload_materials) into
+ * PE and PH [n] on the host's cores; *maxid gets the largest ID (GBF_EINVAL above 1023). Host
+ * arithmetic only. No counterpart in the reference. */
+int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint32_t* maxid);
+
+/* Page-locked host memory (cudaHostAlloc) for the inputs of gbf_upload_materials_packed, and
+ * its release. No counterpart in the reference. */
+int gbf_host_alloc(size_t bytes, void** out);
+void gbf_host_free(void* p);
+
 /* Copy one PML slab's coefficient rows, each fp32 [pml_order][thickness], E then H:
  * ERA, ERB, ERE, ERF, HRA, HRB, HRE, HRF (pml.py:221-274). `slab` indexes x0, y0, z0, xmax,
  * ymax, zmax; slabs with zero thickness take no call. Replaces: PML.gpu_initialise_arrays
@@ -131,10 +151,12 @@ int gbf_reset(gbf_ctx* ctx);
  * GBF_RUN_CHECK is set.
  * 3D models with at most 1024 materials, at most 2 poles and no transmission lines can also
  * advance with one fused kernel per iteration (both half-steps in one pass over the grid; the
- * same results bit for bit), unless options bit 3 is set. Which form runs, and the fused
- * kernel's tiles, are chosen by timing: the first steps of the first run of each model shape in
- * the process each use one candidate (twice round; the model advances as usual, the choice
- * changing no result) and the fastest is kept from then on. */
+ * same results bit for bit), unless options bit 3 is set. For models without PML slabs, which
+ * form runs, and the fused kernel's tiles, are chosen by timing: the first steps of the first
+ * run of each model shape in the process each use one candidate (twice round; the model
+ * advances as usual, the choice changing no result) and the fastest is kept from then on.
+ * Models with PML slabs take the half-step kernels (measured faster there) unless
+ * gbf_set_fused_tiles selects the fused step. */
 int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
 
 /* Iteration the next gbf_run call starts at. */

@@ -238,3 +238,23 @@ def test_fused_tiles_at_the_benchmark_size(native_lib):
     assert nchunks * L >= 401 and (nchunks - 1) * L < 401
     assert nblocks == 7 * 58 * nchunks
     assert 401 * 401 * 201 < 2 ** 31
+
+
+def test_pack_ids_on_the_host(native_lib):
+    """``gbf_pack_ids`` (host arithmetic): the E and H words are the three 10-bit IDs of each
+    node, the largest ID is reported, and IDs above 1023 are refused."""
+    import ctypes
+    rng = np.random.default_rng(3)
+    n = 100003
+    ID = rng.integers(0, 1024, size=(6, n), dtype=np.uint32)
+    pe = np.zeros(n, np.uint32)
+    ph = np.zeros(n, np.uint32)
+    mx = ctypes.c_uint32(0)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert native_lib.gbf_pack_ids(p(ID), n, p(pe), p(ph), ctypes.byref(mx)) == 0
+    np.testing.assert_array_equal(pe, ID[0] | (ID[1] << 10) | (ID[2] << 20))
+    np.testing.assert_array_equal(ph, ID[3] | (ID[4] << 10) | (ID[5] << 20))
+    assert mx.value == ID.max()
+    ID[4, 777] = 1024
+    assert native_lib.gbf_pack_ids(p(ID), n, p(pe), p(ph), ctypes.byref(mx)) == -1
+    assert mx.value == 1024
