@@ -48,9 +48,11 @@ def build(force=False, verbose=False):
     unit per PML kind and tile height are compiled in parallel, then linked."""
     if not force and not _stale():
         return LIBPATH
+    import shutil
+    import tempfile
     from concurrent.futures import ThreadPoolExecutor
-    objdir = os.path.join(CSRC, '_build')
-    os.makedirs(objdir, exist_ok=True)
+    # objects in a scratch folder, removed once the library is linked
+    objdir = tempfile.mkdtemp(prefix='gbfdtd_build_')
     compile_flags = [f for f in NVCC_FLAGS if f != '-shared']
     jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), []),
             (os.path.join(CSRC, 'adjoint.cu'), os.path.join(objdir, 'adjoint.o'), []),
@@ -77,7 +79,10 @@ def build(force=False, verbose=False):
     cmd = [_nvcc()] + ARCH + ['-shared'] + objs + ['-o', LIBPATH + '.tmp']
     if verbose:
         print(' '.join(cmd))
-    subprocess.run(cmd, check=True, cwd=CSRC)
+    try:
+        subprocess.run(cmd, check=True, cwd=CSRC)
+    finally:
+        shutil.rmtree(objdir, ignore_errors=True)
     os.replace(LIBPATH + '.tmp', LIBPATH)
     return LIBPATH
 

@@ -18,7 +18,8 @@
 //                  gradient partials dL/dCA += lamE E_n, dL/dCB += lamE (curl/d, PML X, source)
 //   adj_h_step(n)  per H node: lamH += transposed E curl of u_E and transposed E-PML
 //                  differences, then undo the H half-step n: u_H = DB/d lamH, PML adjoints
-// The gradient partials are fp32 within a segment and folded into fp64 at its end.
+// The gradient partials are fp32 over at most ceil(sqrt(T)) steps and then folded into fp64
+// (every that many steps and at the end of each segment).
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -469,10 +470,13 @@ adj_h_step(const __grid_constant__ AdjParams p, const __grid_constant__ AdjStep 
   }
 }
 
-__global__ void adj_fold(const float* __restrict__ a, double* __restrict__ g, long long n) {
+// Add the fp32 partial sums to the fp64 gradient and clear them for the next span.
+__global__ void adj_fold(float* __restrict__ a, double* __restrict__ g, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x)
+       q += (long long)gridDim.x * blockDim.x) {
     g[q] += (double)a[q];
+    a[q] = 0.f;
+  }
 }
 
 }  // namespace
@@ -823,6 +827,10 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
   b.gtr = gtraces;
   const PhiSet recPH = phiset(a, a->recPhiH);
   const int fold_blocks = a->grid;
+  // the fp32 partials add up at most `span` steps (ceil(sqrt(T))) before they go into fp64,
+  // however long a segment is
+  int span = 1;
+  while ((long long)span * span < T) ++span;
   for (int c = a->nck - 1; c >= 0; --c) {
     const int n0 = a->seg[c];
     const int n1 = a->seg[c + 1];
@@ -848,6 +856,7 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
     AK(cudaMemsetAsync(a->gCA, 0, sizeof(float) * 3 * N, a->stream));
     AK(cudaMemsetAsync(a->gCB, 0, sizeof(float) * 3 * N, a->stream));
     // undo the segment's steps in reverse
+    int since = 0;
     for (int it = n1 - 1; it >= n0; --it) {
       const int m = it - n0;
       b.En = a->segE + (size_t)m * 3 * N;
@@ -857,9 +866,12 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
       b.finish = it + 1 < T ? 1 : 0;
       adj_e_step<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
       adj_h_step<<<a->grid, kAdjThreads, 0, a->stream>>>(a->p, b);
+      if (++since == span || it == n0) {
+        adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCA, gCA, 3 * (long long)N);
+        adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCB, gCB, 3 * (long long)N);
+        since = 0;
+      }
     }
-    adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCA, gCA, 3 * (long long)N);
-    adj_fold<<<fold_blocks, kAdjThreads, 0, a->stream>>>(a->gCB, gCB, 3 * (long long)N);
     AK(cudaGetLastError());
   }
   AK(cudaStreamSynchronize(a->stream));
@@ -867,8 +879,10 @@ int gbf_adj_backward(gbf_adj* a, const float* CA, const float* CB, const float* 
 }
 
 // Fixed device scratch of gbf_adj_backward_static: the fp32 per-segment partial sums of the
-// two gradients (3N floats each), which gbf_adj_backward keeps in buffers of the context.
-// 16 MiB, enough for grids of up to kStaticScratchFloats / 6 = 699,050 nodes per component.
+// two gradients (3N floats each), which gbf_adj_backward keeps in buffers of the context (those
+// are still allocated by gbf_adj_create; the static call only keeps its partials here instead).
+// 16 MiB, enough for grids of up to kStaticScratchFloats / 6 = 699,050 nodes per component;
+// every device that loads the library holds it, whether or not the call is used.
 constexpr size_t kStaticScratchFloats = (size_t)4 << 20;
 static __device__ __align__(256) float g_static_scratch[kStaticScratchFloats];
 constexpr int kStaticMaxDevices = 64;
@@ -895,6 +909,17 @@ int gbf_adj_backward_static(gbf_adj* a, const float* CA, const float* CB, const 
   {
     std::lock_guard<std::mutex> g(g_static_scratch_lock);
     base = g_static_scratch_addr[a->device];
+    if (base) {
+      // a device reset since the address was taken unloads the module and the array with it:
+      // the cached address must still name device memory of this device, else it is taken anew
+      cudaPointerAttributes at;
+      if (cudaPointerGetAttributes(&at, base) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+          at.device != a->device) {
+        (void)cudaGetLastError();
+        base = nullptr;
+        g_static_scratch_addr[a->device] = nullptr;
+      }
+    }
     if (!base) {
       // once per device: the address of the array in this device's copy of the module
       void* addr = nullptr;
@@ -913,6 +938,9 @@ int gbf_adj_backward_static(gbf_adj* a, const float* CA, const float* CB, const 
   a->gCA = base;
   a->gCB = base + 3 * (size_t)a->N;
   const int rc = gbf_adj_backward(a, CA, CB, gtraces, gCA, gCB);
+  // on failure, work already queued may still use the array: wait for it, so that a return
+  // means the call is done with the array on every path
+  if (rc != GBF_OK) (void)cudaStreamSynchronize(a->stream);
   a->gCA = keepA;
   a->gCB = keepB;
   return rc;

@@ -305,12 +305,16 @@ int gbf_adj_forward(gbf_adj* adj, const float* CA, const float* CB, float* trace
 int gbf_adj_backward(gbf_adj* adj, const float* CA, const float* CB, const float* gtraces,
                      double* gCA, double* gCB);
 /* gbf_adj_backward with its fp32 per-segment partial sums in a fixed 16 MiB device array of
- * the library instead of buffers of the context; allocates nothing. Same arguments and
- * results. Grids of more than 699,050 nodes per component ((nx+1)(ny+1)(nz+1)) are rejected
- * with GBF_EINVAL. The first call on a device looks up the array's address (setup); make it
- * before any stream capture. All contexts on a device share the array: overlapping calls, from
- * two threads or two contexts, race on it and must be serialised by the caller. No counterpart
- * in the reference. */
+ * the library instead of the context's two buffers (which gbf_adj_create still allocates);
+ * the call itself allocates no memory, for callers that must not allocate while they run (a
+ * caller whose own allocator owns all device memory, or a time-critical loop). Same arguments
+ * and results. Grids of more than 699,050 nodes per component ((nx+1)(ny+1)(nz+1)) are rejected
+ * with GBF_EINVAL. The array exists on every device that loads the library, used or not. The
+ * first call on a device looks up the array's address (setup; again after a device reset);
+ * make it before any stream capture. All contexts on a device share the array: overlapping
+ * calls, from two threads or two contexts, race on it and must be serialised by the caller; a
+ * call returns only when it no longer uses the array, on failure too. No counterpart in the
+ * reference. */
 int gbf_adj_backward_static(gbf_adj* adj, const float* CA, const float* CB, const float* gtraces,
                             double* gCA, double* gCB);
 

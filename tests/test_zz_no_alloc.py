@@ -1,6 +1,8 @@
 """GPU: gbf_adj_backward_static, the adjoint backward whose fp32 segment partials live in a
-fixed device array of the library, gives the same gradients as gbf_adj_backward, bit for bit,
-on two consecutive calls; grids too large for that array are rejected with GBF_EINVAL."""
+fixed device array of the library (for callers that may not allocate device memory during the
+call), gives the same gradients as gbf_adj_backward, bit for bit, on two consecutive calls, and
+after its first call takes no device memory; grids too large for that array are rejected with
+GBF_EINVAL."""
 import ctypes
 
 import numpy as np
@@ -15,11 +17,17 @@ pytestmark = pytest.mark.gpu
 GBF_EINVAL = -1
 
 
-def _call(solver, fn, CA, CB, gtr):
+def _call(solver, fn, CA, CB, gtr, free=None):
+    """One backward call into fresh NaN-filled outputs; with `free`, the device's free bytes
+    (cudaMemGetInfo) just before and after the call are appended to it."""
     gCA = torch.full((3,) + solver.model.shape, float('nan'), dtype=torch.float64, device='cuda')
     gCB = torch.full_like(gCA, float('nan'))
     torch.cuda.synchronize()
+    before = torch.cuda.mem_get_info()[0]
     rc = fn(solver.h, CA.data_ptr(), CB.data_ptr(), gtr.data_ptr(), gCA.data_ptr(), gCB.data_ptr())
+    torch.cuda.synchronize()
+    if free is not None:
+        free.append((before, torch.cuda.mem_get_info()[0]))
     solver._check(rc)
     return gCA.cpu(), gCB.cpu()
 
@@ -37,10 +45,14 @@ def test_static_scratch_backward_matches_backward(native):
         gtr = (0.25 * tr).contiguous()
         want = _call(solver, native.gbf_adj_backward, CA, CB, gtr)
         assert float(want[0].abs().max()) > 0
+        free = []
         for _ in range(2):
-            got = _call(solver, native.gbf_adj_backward_static, CA, CB, gtr)
+            got = _call(solver, native.gbf_adj_backward_static, CA, CB, gtr, free)
             for g, w in zip(got, want):
                 np.testing.assert_array_equal(g.numpy(), w.numpy())
+        # after the first call (which looks the array up) the call takes no device memory
+        assert free[1][0] == free[1][1], 'the second call changed free device memory'
+        assert free[0][1] == free[1][1]
         # the context's own buffers are untouched: the plain call still agrees afterwards
         again = _call(solver, native.gbf_adj_backward, CA, CB, gtr)
         for g, w in zip(again, want):
