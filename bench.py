@@ -189,13 +189,14 @@ class ClockSampler:
                 'reasons': sorted(reasons), 'samples': len(self.rows)}
 
 
-def build_workload(iterations, grid=None):
+def build_workload(iterations, grid=None, snapshot_at=0):
     from gprmax_gb300 import workloads
     if grid:
         nx, ny, nz = grid
-        G = workloads.dispersive_soil(nx=nx, ny=ny, nz=nz, surface=int(nz * 0.75))
+        G = workloads.dispersive_soil(nx=nx, ny=ny, nz=nz, surface=int(nz * 0.75),
+                                      snapshot_at=snapshot_at)
     else:
-        G = workloads.dispersive_soil()
+        G = workloads.dispersive_soil(snapshot_at=snapshot_at)
     if iterations > G.iterations:
         # longer time window; per-step work is unchanged
         G.iterations = iterations
@@ -294,7 +295,7 @@ def run_gb300(args):
     from gprmax_gb300.solver import DeviceModel
     _native.lib()
     K, W = args.steps, args.warmup
-    G = build_workload(max(3117, K + W + args.profile_steps + 1), args.grid)
+    G = build_workload(max(3117, K + W + args.profile_steps + 1), args.grid, args.snapshot_at)
     cells = G.nx * G.ny * G.nz
     # warm the CUDA context with a tiny model (not timed)
     from gprmax_gb300.workloads import freespace_dipole
@@ -668,7 +669,7 @@ def run_adjoint(args):
     flat = g.abs().flatten()
     top = torch.topk(flat, max(20, flat.numel() // 100)).indices.cpu().numpy()
     rng = np.random.default_rng(5)
-    cells = rng.choice(top, 20, replace=False)
+    cells = rng.choice(top, min(args.fd_cells, top.size), replace=False)
     errs = []
     for c in cells:
         # fourth-order central difference, step 5 % of eps_r (the fp32 forward's rounding noise
@@ -721,9 +722,9 @@ def run_adjoint(args):
                                   'max_rel_diff_vs_default': rich_dev},
            'forward_runs_s': [round(t, 4) for t in fwd_times],
            'forward_Mcells_per_s': round(cells_n * m.iterations / t_fwd / 1e6, 1),
-           'fd_check': {'cells': 20, 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',
-                        'median_rel_err': float(np.median(errs)),
-                        'max_rel_err': float(np.max(errs))},
+           'fd_check': {'cells': len(errs), 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',
+                        'median_rel_err': float(np.median(errs)) if errs else None,
+                        'max_rel_err': float(np.max(errs)) if errs else None},
            'misfit': float(L.detach())}
     print(json.dumps(out), flush=True)
 
@@ -831,6 +832,10 @@ def main():
     ap.add_argument('--ref-budget', type=float, default=150.0)
     ap.add_argument('--grid', type=int, nargs=3, default=None,
                     help='smaller soil grid (profiling runs); default 400 400 200')
+    ap.add_argument('--snapshot-at', type=int, default=0,
+                    help='soil: add a snapshot of the whole domain at this iteration (profiling)')
+    ap.add_argument('--fd-cells', type=int, default=20,
+                    help='adjoint: cells of the finite-difference check (0: none)')
     ap.add_argument('--half-steps', action='store_true',
                     help='soil: step with the two half-step kernels instead of the fused step')
     ap.add_argument('--no-warm-context', action='store_true',

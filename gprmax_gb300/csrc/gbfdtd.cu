@@ -660,6 +660,14 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   const bool timed = ctx->fused_avail && pml_kind(ctx->d) == PML_NONE;
   ctx->fused = timed ? 1 : 0;
   ctx->tuned = timed ? 0 : 1;
+  // GBF_FUSED_TILE="tj,nch" selects the fused step with that tiling for every model that has one
+  const char* force = getenv("GBF_FUSED_TILE");
+  int ftj = 0, fnch = 0;
+  if (ctx->fused_avail && force && sscanf(force, "%d,%d", &ftj, &fnch) == 2 &&
+      configure_fused(ctx, ftj, fnch)) {
+    ctx->fused = 1;
+    ctx->tuned = 1;
+  }
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {

@@ -52,12 +52,14 @@ def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
 
 
 def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
-                    timewindow='12e-9', cylinder=True, pml=10, messages=False, device_build=False):
+                    timewindow='12e-9', cylinder=True, pml=10, messages=False, device_build=False,
+                    snapshot_at=0):
     """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
 
     Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
     sigma ~ logU[1e-4,1e-2] S/m. A PEC cylinder of radius 20 mm runs along y at depth 60 mm;
     an x-polarised dipole and a receiver 40 mm apart sit 10 mm above the surface.
+    ``snapshot_at`` > 0 adds a snapshot of the whole domain (every cell) at that iteration.
     """
     rng = np.random.default_rng(seed)
     es = rng.uniform(5, 20, nmat)
@@ -79,6 +81,9 @@ def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed
     if cylinder:
         lines.append('#cylinder: {0:g} 0 {1:g} {0:g} {2:g} {1:g} 0.02 pec'.format(
             xc, zsurf - 0.06, ny * dx))
+    if snapshot_at:
+        lines.append('#snapshot: 0 0 0 {:g} {:g} {:g} {d:g} {d:g} {d:g} {} soil_snapshot'.format(
+            nx * dx, ny * dx, nz * dx, int(snapshot_at), d=dx))
     first_soil = 2
 
     def soil(G):
