@@ -9,11 +9,13 @@ default settings (``gprMax/fields_outputs.py:111-161``):
   group nodes and a local heap of link names, symbol-table nodes (SNOD) holding the entries;
 * datasets with contiguous storage (Dataspace v1, Datatype v1, Data Layout v3 messages);
 * attributes (Attribute message v1) with scalar or 1-D data of fixed-point, IEEE float or
-  fixed-length string type.
+  fixed-length string type, and text attributes as h5py stores a Python ``str``: a scalar
+  variable-length UTF-8 string (Datatype class 9 over unsigned bytes) whose characters lie in a
+  global heap collection (GCOL), one collection per file.
 
 The reader also follows object header continuation messages and skips messages it does not
-use (fill value, modification time, ...), so it reads files produced by h5py. Variable-length
-strings (stored in the global heap) are returned as None.
+use (fill value, modification time, ...), so it reads files produced by h5py, variable-length
+strings included.
 """
 import struct
 
@@ -51,6 +53,13 @@ def _dtype_message(dt):
         # fixed-length string, null-terminated, ASCII
         return bytes([0x10 | 3, 0x00, 0, 0]) + struct.pack('<I', dt.itemsize)
     raise TypeError('unsupported dtype {}'.format(dt))
+
+
+# a scalar variable-length UTF-8 string: class 9 (string, null padding, UTF-8), 16-byte element
+# (length, global heap collection address, object index), base type one unsigned byte
+_VLSTR_MESSAGE = (bytes([0x10 | 9, 0x01, 0x01, 0x00]) + struct.pack('<I', 16)
+                  + bytes([0x10 | 0, 0, 0, 0]) + struct.pack('<IHH', 1, 0, 8))
+GCOL_MIN = 4096   # smallest global heap collection
 
 
 def _dataspace_message(shape):
@@ -155,6 +164,8 @@ class _Writer:
     def __init__(self, root):
         self.root = root
         self.buf = bytearray()
+        self.gcol = UNDEF      # the file's global heap collection (text attributes)
+        self.gindex = {}       # text -> object index in it
 
     def alloc(self, n):
         off = len(self.buf)
@@ -169,11 +180,45 @@ class _Writer:
         body = body + b'\x00' * (_pad8(len(body)) - len(body))
         return struct.pack('<HHB3x', mtype, len(body), 0) + body
 
+    def _texts(self, node, out):
+        for v in node.attrs.values():
+            if isinstance(v, str) and v not in out:
+                out.append(v)
+        for c in getattr(node, 'children', {}).values():
+            self._texts(c, out)
+        return out
+
+    def write_gheap(self):
+        """One global heap collection with every text attribute of the file (objects numbered
+        from 1, each padded to 8 bytes, then the free-space object filling the rest)."""
+        texts = self._texts(self.root, [])
+        if not texts:
+            return
+        objs = b''
+        for n, t in enumerate(texts, 1):
+            b = t.encode('utf-8')
+            self.gindex[t] = n
+            objs += struct.pack('<HHIQ', n, 0, 0, len(b)) + b + b'\x00' * (_pad8(len(b)) - len(b))
+        size = max(GCOL_MIN, 16 + len(objs) + 16)
+        body = b'GCOL' + struct.pack('<B3xQ', 1, size) + objs
+        body += struct.pack('<HHIQ', 0, 0, 0, size - len(body))
+        self.gcol = self.alloc(size)
+        self.put(self.gcol, body)
+
     def _attr_messages(self, attrs):
         out = []
         for name, value in attrs.items():
-            a = _as_array(value)
             nm = name.encode('utf-8') + b'\x00'
+            if isinstance(value, str):
+                dtm, dsm = _VLSTR_MESSAGE, _dataspace_message(())
+                data = struct.pack('<IQI', len(value.encode('utf-8')), self.gcol, self.gindex[value])
+                body = struct.pack('<BxHHH', 1, len(nm), len(dtm), len(dsm))
+                body += nm + b'\x00' * (_pad8(len(nm)) - len(nm))
+                body += dtm + b'\x00' * (_pad8(len(dtm)) - len(dtm))
+                body += dsm + b'\x00' * (_pad8(len(dsm)) - len(dsm))
+                out.append(self._message(0x000C, body + data))
+                continue
+            a = _as_array(value)
             dtm = _dtype_message(a.dtype)
             dsm = _dataspace_message(a.shape)
             body = struct.pack('<BxHHH', 1, len(nm), len(dtm), len(dsm))
@@ -257,6 +302,7 @@ class _Writer:
 
     def write(self, path):
         sb = self.alloc(96)
+        self.write_gheap()
         root_addr, btree, heap = self.write_group(self.root)
         eof = len(self.buf)
         hdr = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack('<HHI', LEAF_K, INTERNAL_K, 0)
@@ -358,14 +404,33 @@ class _Reader:
         off += _pad8(tlen)
         shape = self.dataspace(body[off:off + slen])
         off += _pad8(slen)
-        if dt is None:
-            return name, None
+        if dt is None:   # variable-length string: (length, collection address, index)
+            if shape != ():
+                return name, None
+            length, addr, index = struct.unpack_from('<IQI', body, off)
+            text = self.gheap_object(addr, index)
+            return name, None if text is None else text[:length].decode('utf-8')
         n = int(np.prod(shape)) if shape else 1
         a = np.frombuffer(bytes(body[off:off + n * dt.itemsize]), dtype=dt).reshape(shape)
         if dt.kind == 'S':
             v = a[()] if shape == () else a
             return name, (v.split(b'\x00')[0].decode('utf-8') if shape == () else v)
         return name, (a[()] if shape == () else a.copy())
+
+    def gheap_object(self, addr, index):
+        """Object ``index`` of the global heap collection at ``addr`` (None if absent)."""
+        if self.b[addr:addr + 4] != b'GCOL':
+            return None
+        size = self.u('Q', addr + 8)[0]
+        off = addr + 16
+        while off + 16 <= addr + size:
+            idx, _, _, osize = self.u('HHIQ', off)
+            if idx == 0:
+                return None
+            if idx == index:
+                return bytes(self.b[off + 16:off + 16 + osize])
+            off += 16 + _pad8(osize)
+        return None
 
     def obj(self, name, addr):
         node = Node(name)
