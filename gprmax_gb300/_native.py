@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
 SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fused_inst.cu', 'adjoint.cu', 'geom.cu',
-           'fdtd_kernels.cuh', 'fused_step.cuh']
+           'fractal.cu', 'fdtd_kernels.cuh', 'fused_step.cuh']
 PML_KINDS = 5       # kernels_inst.cu is compiled once per PML kind
 FUSED_TJ = (7, 15)  # fused_inst.cu once per PML kind and tile height
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
@@ -56,7 +56,8 @@ def build(force=False, verbose=False):
     compile_flags = [f for f in NVCC_FLAGS if f != '-shared']
     jobs = [(os.path.join(CSRC, 'gbfdtd.cu'), os.path.join(objdir, 'gbfdtd.o'), []),
             (os.path.join(CSRC, 'adjoint.cu'), os.path.join(objdir, 'adjoint.o'), []),
-            (os.path.join(CSRC, 'geom.cu'), os.path.join(objdir, 'geom.o'), [])]
+            (os.path.join(CSRC, 'geom.cu'), os.path.join(objdir, 'geom.o'), []),
+            (os.path.join(CSRC, 'fractal.cu'), os.path.join(objdir, 'fractal.o'), [])]
     for pk in range(PML_KINDS):
         jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
                      os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
@@ -76,7 +77,8 @@ def build(force=False, verbose=False):
         return obj
     with ThreadPoolExecutor(min(len(jobs), max(os.cpu_count() or 1, 1))) as ex:
         objs = list(ex.map(compile_one, jobs))
-    cmd = [_nvcc()] + ARCH + ['-shared'] + objs + ['-o', LIBPATH + '.tmp']
+    # cuFFT for the fractal fields' transforms (fractal.cu)
+    cmd = [_nvcc()] + ARCH + ['-shared'] + objs + ['-lcufft', '-o', LIBPATH + '.tmp']
     if verbose:
         print(' '.join(cmd))
     try:
@@ -134,6 +136,7 @@ _SIGS = {
     'gbf_download_dispersive': (ctypes.c_int, [_P, _P]),
     'gbf_download_snapshot': (ctypes.c_int, [_P, ctypes.c_int, _P]),
     'gbf_step_info': (ctypes.c_int, [_P, _P]),
+    'gbf_fractal_field': (ctypes.c_int, [ctypes.c_int32, _P, _P, ctypes.c_float, _P, _P]),
     'gbf_set_fused_tiles': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     'gbf_fused_tiles': (ctypes.c_int, [ctypes.c_int32] * 5 + [_P]),
     'gbf_profile': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float),

@@ -873,7 +873,7 @@ def _fractal_box(G, tmp, geometry):
         else:
             if not mixingmodel:
                 raise CmdInputError("'" + ' '.join(tmp) + "'" + ' needs a mixing model to bin {} materials from; {} is a single material'.format(nbins, tmp[12]))
-            vol = volume.generate_fractal_volume()
+            vol = volume.generate_fractal_volume(device=getattr(G, "device_fractals", False))
             vol += mixingmodel.startmaterialnum
         mask = volume.generate_volume_mask()
         waternumID = next((x.numID for x in G.materials if x.ID == 'water'), 0)
@@ -886,7 +886,7 @@ def _fractal_box(G, tmp, geometry):
         raise CmdInputError("'" + ' '.join(tmp) + "'" + ' is being used with a single material and no modifications, therefore please use a #box command instead.')
     if not mixingmodel:
         raise CmdInputError("'" + ' '.join(tmp) + "'" + ' needs a mixing model to bin {} materials from; {} is a single material'.format(nbins, tmp[12]))
-    vol = volume.generate_fractal_volume()
+    vol = volume.generate_fractal_volume(device=getattr(G, "device_fractals", False))
     vol += mixingmodel.startmaterialnum
     geo.build_voxels_array(G, (xs, ys, zs), vol.astype('int16', order='C'), averaging)
 
@@ -969,7 +969,7 @@ def _surface_roughness(G, tmp, volume):
     surface.weighting = np.array([float(tmp[8]), float(tmp[9])])
     if surface.surfaceID in [x.surfaceID for x in volume.fractalsurfaces]:
         raise CmdInputError("'" + ' '.join(tmp) + "'" + ' has already been used on the {} surface'.format(surface.surfaceID))
-    surface.generate_fractal_surface()
+    surface.generate_fractal_surface(device=getattr(G, "device_fractals", False))
     volume.fractalsurfaces.append(surface)
     _log(G, 'Fractal surface from {:g}m, {:g}m, {:g}m, to {:g}m, {:g}m, {:g}m with fractal '
             'dimension {:g}, fractal weightings {:g}, {:g}, fractal seeding {}, and range {:g}m '

@@ -10,6 +10,11 @@ extension's ``float D`` argument, B = 0.9 where it is zero, the complex value di
 real B component-wise), the DC term
 zeroed, the real part of the inverse FFT in float32, and ``numpy.digitize`` into ``nbins``
 bins row by row.
+
+With ``device=True`` (an opt-in for building many realisations) the same seeded noise goes
+through the transforms and the filter on the GPU (``gbf_fractal_field``, double precision); the
+field then agrees with the reference's to rounding, so a cell whose value lies at a bin edge can
+land in the neighbouring bin.
 """
 import math
 
@@ -43,6 +48,25 @@ def _fractal_filter(A, w, v1, dimension):
     return out
 
 
+def device_field(noise, weights, dimension):
+    """The fp32 fractal field of ``noise`` (float64, 2D or 3D) computed on the GPU: the filtered
+    inverse FFT's real part, ``dimension`` taken as float32 as the reference's filter takes it."""
+    import ctypes
+    from . import _native
+    from .exceptions import SolverError
+    lib = _native.lib()
+    noise = np.ascontiguousarray(noise, dtype=np.float64)
+    dims = np.array(noise.shape, dtype=np.int32)
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    out = np.empty(noise.shape, dtype=np.float32)
+    p = lambda a: ctypes.c_void_p(a.ctypes.data)
+    rc = lib.gbf_fractal_field(noise.ndim, p(dims), p(w), ctypes.c_float(float(np.float32(dimension))),
+                               p(noise), p(out))
+    if rc != 0:
+        raise SolverError('gbf_fractal_field failed ({})'.format(rc))
+    return out
+
+
 class FractalSurface:
     """A fractal surface on one face of a fractal box (``#add_surface_roughness``,
     ``gprMax/fractals.py:29-111``): heights in cells, scaled into ``fractalrange``."""
@@ -63,8 +87,8 @@ class FractalSurface:
         self.filldepth = 0
         self.operatingonID = None
 
-    def generate_fractal_surface(self):
-        """Heights (float32 [n1][n2]) of the surface."""
+    def generate_fractal_surface(self, device=False):
+        """Heights (float32 [n1][n2]) of the surface (``device``: transforms on the GPU)."""
         if self.xs == self.xf:
             dims = (self.ny, self.nz)
         elif self.ys == self.yf:
@@ -75,10 +99,13 @@ class FractalSurface:
         v1 = np.array([w[0] * dims[0] / 2, w[1] * dims[1] / 2])
         rng = np.random.default_rng(seed=self.seed)
         A = rng.standard_normal(size=(dims[0], dims[1]))
-        A = fftpack.fftshift(fftpack.fftn(A))
-        surf = fftpack.ifftshift(_fractal_filter(A, w, v1, self.dimension))
-        surf[0, 0] = 0
-        surf = np.real(fftpack.ifftn(surf)).astype(floattype, copy=False)
+        if device:
+            surf = device_field(A, w, self.dimension)
+        else:
+            A = fftpack.fftshift(fftpack.fftn(A))
+            surf = fftpack.ifftshift(_fractal_filter(A, w, v1, self.dimension))
+            surf[0, 0] = 0
+            surf = np.real(fftpack.ifftn(surf)).astype(floattype, copy=False)
         # scaled to the requested range (the reference's expression, types as numpy gives them)
         fmin = np.amin(surf)
         fmax = np.amax(surf)
@@ -173,8 +200,9 @@ class FractalVolume:
         self.mask = mask
         return mask
 
-    def generate_fractal_volume(self):
-        """Bin numbers (float32 array [nx][ny][nz], values 0..nbins-1) of the fractal field."""
+    def generate_fractal_volume(self, device=False):
+        """Bin numbers (float32 array [nx][ny][nz], values 0..nbins-1) of the fractal field
+        (``device``: transforms on the GPU, binned in one pass)."""
         n = np.array([self.nx, self.ny, self.nz])
         if self.nx == 1:
             scaling = np.insert(np.amin(n[1:]) / n[1:], 0, 1)
@@ -189,6 +217,13 @@ class FractalVolume:
         v1 = np.array([w[0] * self.nx / 2, w[1] * self.ny / 2, w[2] * self.nz / 2])
         rng = np.random.default_rng(seed=self.seed)
         A = rng.standard_normal(size=(self.nx, self.ny, self.nz))
+        if device:
+            vol = device_field(A, w, self.dimension)
+            bins = np.linspace(np.amin(vol), np.amax(vol), self.nbins)
+            # the same rule as the row-by-row loop below, applied to every cell at once
+            vol = np.digitize(vol, bins, right=True).astype(floattype)
+            self.fractalvolume = vol
+            return vol
         A = fftpack.fftshift(fftpack.fftn(A))
         vol = fftpack.ifftshift(_fractal_filter(A, w, v1, self.dimension))
         vol[0, 0, 0] = 0

@@ -18,15 +18,18 @@ from .yee_build import build_electric_components, build_magnetic_components
 
 
 def build_grid(lines, G=None, usernamespace=None, inputfilename='', messages=None,
-               geometry_hook=None, device_build=False):
+               geometry_hook=None, device_build=False, device_fractals=False):
     """Build a model from input-file lines up to the coefficient tables (before solving).
 
     Follows the build sequence of ``run_model`` (``model_build_run.py:110-292``).
     ``geometry_hook(G)``, when given, runs before the geometry commands (used to place
     programmatic voxel blocks, as ``#fractal_box`` would). ``device_build``: the geometry
     arrays are built in GPU memory (:mod:`gprmax_gb300.devgeom`) and handed to the solver there.
+    ``device_fractals``: fractal volumes and surfaces are transformed on the GPU (equal to the
+    host's to rounding; cells at a bin edge can change bin), an opt-in for realisations.
     """
     G = G or FDTDGrid()
+    G.device_fractals = device_fractals
     if usernamespace is None:
         usernamespace = {'c': c, 'e0': e0, 'm0': m0, 'z0': z0, 'number_model_runs': 1,
                          'inputfile': os.path.abspath(inputfilename) if inputfilename else '',

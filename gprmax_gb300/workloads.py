@@ -17,13 +17,19 @@ from .materials import Material
 from .model import build_grid, finish_build
 
 
-def fractal_volume(shape, dimension, seed, nbins):
-    """Bin indices 0..nbins-1 of a seeded fractal field of the given shape."""
+def fractal_volume(shape, dimension, seed, nbins, device=False):
+    """Bin indices 0..nbins-1 of a seeded fractal field of the given shape (``device``: the
+    transforms and filter on the GPU, equal to the host's field to rounding)."""
     nx, ny, nz = shape
     weighting = np.array([1.0, 1.0, 1.0]) * (np.amin(np.array(shape)) / np.array(shape, dtype=np.float64))
     v1 = np.array([weighting[0] * nx / 2, weighting[1] * ny / 2, weighting[2] * nz / 2])
     rng = np.random.default_rng(seed=seed)
     A = rng.standard_normal(size=shape)
+    if device:
+        from .fractals import device_field
+        vol = device_field(A, weighting, float(np.float32(dimension)))
+        bins = np.linspace(np.amin(vol), np.amax(vol), nbins)
+        return np.digitize(vol, bins, right=True).astype(np.int64)
     A = np.fft.fftshift(np.fft.fftn(A))
     i = (weighting[0] * np.arange(nx) - v1[0])[:, None, None]
     j = (weighting[1] * np.arange(ny) - v1[1])[None, :, None]
@@ -53,7 +59,7 @@ def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
 
 def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
                     timewindow='12e-9', cylinder=True, pml=10, messages=False, device_build=False,
-                    snapshot_at=0):
+                    snapshot_at=0, device_fractals=False):
     """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
 
     Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
@@ -87,7 +93,7 @@ def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed
     first_soil = 2
 
     def soil(G):
-        bins = fractal_volume((nx, ny, surface), 1.5, seed, nmat)
+        bins = fractal_volume((nx, ny, surface), 1.5, seed, nmat, device=device_fractals)
         build_voxels_array(G, (0, 0, 0), bins + first_soil, averaging=False)
     return build_grid([l + '\n' for l in lines], messages=messages, geometry_hook=soil,
                       device_build=device_build)

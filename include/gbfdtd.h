@@ -193,6 +193,16 @@ int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_to
  * reference. */
 int gbf_set_fused_tiles(gbf_ctx* ctx, int32_t tj, int32_t nch);
 
+/* A fractal field on the device (#fractal_box, #add_surface_roughness): the fp32 real part of
+ * the inverse FFT of FFT(noise) / r^D, r the distance of each frequency from the spectrum's
+ * centre with per-axis weights, r^D = 0.9 where it is 0, the DC term zeroed
+ * (gprMax/fractals.py:141-194 and :29-111, filter fractals_generate_ext.pyx:24-86). rank 2 or 3,
+ * dims [rank], weights [rank], noise float64 [dims] (host, the seeded Gaussian noise), field
+ * float32 [dims] (host). Double-precision transforms (cuFFT): equal to the reference's field to
+ * rounding, not bit for bit; the reference's binning of it is left to the caller. */
+int gbf_fractal_field(int32_t rank, const int32_t* dims, const double* weights, float dimension,
+                      const double* noise, float* field);
+
 /* The fused step's launch decomposition for a grid of nx x ny x nz cells, tile height tj rows
  * and nch chunks along x (host arithmetic only, no device call): out[0] k segments, [1] j
  * tiles, [2] chunks, [3] planes per chunk, [4] blocks, [5] k nodes owned per tile. Block b works
