@@ -564,12 +564,15 @@ def run_bscan2d(args):
             dm.close()
         return time.perf_counter() - t0, dev, traces, setup
 
+    grid_info = {}
+
     def batched():
         t0 = time.perf_counter()
         bm = BatchModel(grids)
         setup = time.perf_counter() - t0
         dev = bm.run_timed(iters)
         traces = bm.receivers()
+        grid_info.update(bm.info())
         bm.close()
         return time.perf_counter() - t0, dev, traces, setup
 
@@ -599,7 +602,7 @@ def run_bscan2d(args):
                                 'device_ms_all_traces': round(dev_p, 3),
                                 'model_setup_s': round(setup_p, 4)},
            'batched': {'device_ms_all_traces': round(dev_b, 3),
-                       'model_setup_s': round(setup_b, 4),
+                       'model_setup_s': round(setup_b, 4), 'grid': dict(grid_info),
                        'Mcells_per_s': round(cells * n * iters / (dev_b / 1e3) / 1e6, 1)},
            'speedup_vs_plain': round(wall_p / wall_b, 3),
            'traces_identical': bool(identical),

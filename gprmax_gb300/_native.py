@@ -136,6 +136,7 @@ _SIGS = {
     'gbf_download_dispersive': (ctypes.c_int, [_P, _P]),
     'gbf_download_snapshot': (ctypes.c_int, [_P, ctypes.c_int, _P]),
     'gbf_step_info': (ctypes.c_int, [_P, _P]),
+    'gbf_batch_info': (ctypes.c_int, [_P, _P]),
     'gbf_fractal_field': (ctypes.c_int, [ctypes.c_int32, _P, _P, ctypes.c_float, _P, _P]),
     'gbf_set_fused_tiles': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     'gbf_fused_tiles': (ctypes.c_int, [ctypes.c_int32] * 5 + [_P]),

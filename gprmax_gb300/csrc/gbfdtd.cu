@@ -1619,6 +1619,7 @@ struct gbf_batch {
   int it = 0;
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
+  int tuned = 0;               // grid sizes chosen (batch_tune)
 };
 
 static int bfail(gbf_batch* b, int code, const char* fmt, ...) {
@@ -1659,6 +1660,107 @@ static void batch_step(gbf_batch* b) {
   b->hk<<<b->grid_h, kThreads, b->smem_h, b->stream>>>(bp);
   b->ek<<<b->grid_e, kThreads, b->smem_e, b->stream>>>(bp);
   end_of_step_batch<<<bp.n, 256, 0, b->stream>>>(b->d_models, b->d_rx);
+}
+
+// ---- batch grid tuner ----------------------------------------------------------------------
+// The batched half-steps are persistent grid-stride launches: any grid size gives the same
+// results, but how many blocks share the models (each block sets up every model it reaches)
+// decides the time. The first steps of a batch's first run each use one candidate, k blocks
+// per SM for k = 1..4 (up to what fits), twice round, timed with events; the fastest is kept
+// for the batch and, per set of model shapes, for the process.
+static std::mutex g_btune_mu;
+static std::map<std::vector<long long>, std::pair<int, int>> g_btune;
+
+static std::vector<long long> batch_key(const gbf_batch* b) {
+  const gbf_ctx* m0 = b->models[0];
+  std::vector<long long> k = {(long long)b->models.size(), pml_kind(m0->d), m0->d.maxpoles,
+                              m0->idp, m0->treal, b->device};
+  for (const gbf_ctx* c : b->models) {
+    k.push_back(c->d.nx);
+    k.push_back(c->d.ny);
+    k.push_back(c->d.nz);
+  }
+  return k;
+}
+
+static const int kBatchTuneReps = 2;
+
+// Returns the steps it ran (0 when the batch needs no tuning or nsteps is too short), or a
+// negative status.
+static int batch_tune(gbf_batch* b, int nsteps) {
+  if (b->tuned) return 0;
+  const std::vector<long long> key = batch_key(b);
+  {
+    std::lock_guard<std::mutex> lock(g_btune_mu);
+    auto f = g_btune.find(key);
+    if (f != g_btune.end()) {
+      b->grid_h = f->second.first;
+      b->grid_e = f->second.second;
+      b->tuned = 1;
+      return 0;
+    }
+  }
+  int dev = 0, sms = 1, ph = 0, pe = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ph, (const void*)b->hk, kThreads, b->smem_h);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pe, (const void*)b->ek, kThreads, b->smem_e);
+  ph = ph > 0 ? ph : 1;
+  pe = pe > 0 ? pe : 1;
+  std::vector<std::pair<int, int>> cand;
+  for (int k = 1; k <= 4; ++k) {
+    const std::pair<int, int> c(sms * (k < ph ? k : ph), sms * (k < pe ? k : pe));
+    bool seen = false;
+    for (auto& x : cand) seen |= x == c;
+    if (!seen) cand.push_back(c);
+  }
+  const int nc = (int)cand.size();
+  if (nc < 2) {
+    b->tuned = 1;
+    return 0;
+  }
+  if (nsteps < nc * kBatchTuneReps) return 0;   // too short a run to time them; try next time
+  std::vector<cudaEvent_t> ev(2 * nc * kBatchTuneReps, nullptr);
+  int rc = GBF_OK;
+  for (auto& e : ev)
+    if (rc == GBF_OK && cudaEventCreate(&e) != cudaSuccess) rc = GBF_ECUDA;
+  BatchParams bp;
+  bp.models = b->d_models;
+  bp.rangeH = b->d_rangeH;
+  bp.rangeE = b->d_rangeE;
+  bp.n = (int)b->models.size();
+  for (int r = 0; r < nc * kBatchTuneReps && rc == GBF_OK; ++r) {
+    const std::pair<int, int>& c = cand[r % nc];
+    cudaEventRecord(ev[2 * r], b->stream);
+    b->hk<<<c.first, kThreads, b->smem_h, b->stream>>>(bp);
+    b->ek<<<c.second, kThreads, b->smem_e, b->stream>>>(bp);
+    cudaEventRecord(ev[2 * r + 1], b->stream);
+    end_of_step_batch<<<bp.n, 256, 0, b->stream>>>(b->d_models, b->d_rx);
+    if (cudaGetLastError() != cudaSuccess) rc = GBF_ECUDA;
+  }
+  std::vector<float> best(nc, 1e30f);
+  if (rc == GBF_OK && cudaEventSynchronize(ev.back()) != cudaSuccess) rc = GBF_ECUDA;
+  for (int r = 0; r < nc * kBatchTuneReps && rc == GBF_OK; ++r) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]) != cudaSuccess) rc = GBF_ECUDA;
+    if (ms < best[r % nc]) best[r % nc] = ms;
+  }
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  if (rc != GBF_OK) return bfail(b, rc, "batch tuning: %s", cudaGetErrorString(cudaGetLastError()));
+  int pick = 0;
+  for (int k = 1; k < nc; ++k)
+    if (best[k] < best[pick]) pick = k;
+  b->grid_h = cand[pick].first;
+  b->grid_e = cand[pick].second;
+  b->tuned = 1;
+  if (b->gexec) {
+    cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+  }
+  std::lock_guard<std::mutex> lock(g_btune_mu);
+  g_btune[key] = cand[pick];
+  return nc * kBatchTuneReps;
 }
 
 // The whole requested time loop as one CUDA graph (re-captured when the length changes).
@@ -1781,12 +1883,16 @@ int gbf_batch_run(gbf_batch* b, int32_t nsteps, uint32_t flags) {
   int rc = check_batch_steps(b, nsteps);
   if (rc) return rc;
   if (nsteps == 0) return GBF_OK;
-  if (flags & GBF_RUN_GRAPH) {
-    rc = ensure_batch_graph(b, nsteps);
+  // the first steps of the first run time the candidate grid sizes (real steps)
+  const int tuning = batch_tune(b, nsteps);
+  if (tuning < 0) return tuning;
+  const int rest = nsteps - tuning;
+  if (rest > 0 && (flags & GBF_RUN_GRAPH)) {
+    rc = ensure_batch_graph(b, rest);
     if (rc) return rc;
     BK(cudaGraphLaunch(b->gexec, b->stream));
   } else {
-    for (int s = 0; s < nsteps; ++s) batch_step(b);
+    for (int s = 0; s < rest; ++s) batch_step(b);
   }
   BK(cudaGetLastError());
   b->it += nsteps;
@@ -1798,7 +1904,7 @@ int gbf_batch_run_timed(gbf_batch* b, int32_t nsteps, uint32_t flags, float* ms)
   if (!b || !ms) return GBF_EINVAL;
   int rc0 = check_batch_steps(b, nsteps);
   if (rc0) return rc0;
-  if ((flags & GBF_RUN_GRAPH) && nsteps > 0) {   // capture before the timed region
+  if ((flags & GBF_RUN_GRAPH) && nsteps > 0 && b->tuned) {   // capture before the timed region
     rc0 = ensure_batch_graph(b, nsteps);
     if (rc0) return rc0;
   }
@@ -1813,6 +1919,14 @@ int gbf_batch_run_timed(gbf_batch* b, int32_t nsteps, uint32_t flags, float* ms)
   BK(cudaEventElapsedTime(ms, a, z));
   cudaEventDestroy(a);
   cudaEventDestroy(z);
+  return GBF_OK;
+}
+
+int gbf_batch_info(gbf_batch* b, int32_t info[3]) {
+  if (!b || !info) return GBF_EINVAL;
+  info[0] = b->tuned;
+  info[1] = b->grid_h;
+  info[2] = b->grid_e;
   return GBF_OK;
 }
 

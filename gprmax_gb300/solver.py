@@ -439,6 +439,12 @@ class BatchModel:
     def synchronize(self):
         self._check(self.lib.gbf_batch_synchronize(self.b))
 
+    def info(self):
+        """{'tuned': bool, 'blocks_h', 'blocks_e'}: the grid sizes of the batched launches."""
+        info = np.zeros(3, dtype=np.int32)
+        self._check(self.lib.gbf_batch_info(self.b, _ptr(info)))
+        return {'tuned': bool(info[0]), 'blocks_h': int(info[1]), 'blocks_e': int(info[2])}
+
     def receivers(self):
         """Per model, fp32 [9][iterations][nrx] receiver samples."""
         self.synchronize()

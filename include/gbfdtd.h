@@ -263,10 +263,17 @@ int gbf_download_tls(gbf_ctx* ctx, float* out);
 typedef struct gbf_batch gbf_batch;
 int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out);
 void gbf_batch_destroy(gbf_batch* batch);
-/* Advance every model nsteps iterations (flags: GBF_RUN_GRAPH). */
+/* Advance every model nsteps iterations (flags: GBF_RUN_GRAPH). The first run of a batch
+ * chooses the grid size of its persistent launches by timing: its first steps each use one
+ * candidate (1 to 4 blocks per SM, twice round; real steps, the grid size changing no result),
+ * and the fastest is kept for the batch and, per set of model shapes, for the process. */
 int gbf_batch_run(gbf_batch* batch, int32_t nsteps, uint32_t flags);
-/* The same, timed with CUDA events on the batch's stream (graph capture outside the timing). */
+/* The same, timed with CUDA events on the batch's stream (graph capture outside the timing
+ * once the grid size is chosen). */
 int gbf_batch_run_timed(gbf_batch* batch, int32_t nsteps, uint32_t flags, float* ms);
+/* info[0] 1 once the grid size is chosen, [1] blocks of the H launch, [2] of the E launch. No
+ * counterpart in the reference. */
+int gbf_batch_info(gbf_batch* batch, int32_t info[3]);
 int gbf_batch_synchronize(gbf_batch* batch);
 int gbf_batch_last_error(gbf_batch* batch, char* buf, size_t n);
 

@@ -54,6 +54,9 @@ def test_batch_matches_plain_runs(native, template, pml):
     grids = _grids(template, 4, 80, pml)
     bm = BatchModel(grids)
     bm.run()
+    # the first steps timed the candidate grid sizes; every later run uses the fastest
+    info = bm.info()
+    assert info['tuned'] and info['blocks_h'] > 0 and info['blocks_e'] > 0
     rx = bm.receivers()
     fields = [m.fields() for m in bm.models]
     bm.close()
