@@ -308,7 +308,7 @@ def run_gb300(args):
     # --- end to end through the public API: upload from host, K steps, read back traces
     if dist is not None:
         dist.barrier()
-    options = 8 if args.half_steps else 0
+    options = (8 if args.half_steps else 0) | (16 if args.plain_e else 0)
     # the model's inputs in page-locked host memory before the timed region: the material IDs
     # packed two words per node (a third of the ID array's bytes); the copy itself is timed
     from gprmax_gb300.solver import pack_materials
@@ -363,7 +363,7 @@ def run_gb300(args):
         kernels = {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
                                    'GBps': round(bytes_h / t_h / 1e9, 1)},
                    'e_half_step': {'ms': t_e * 1e3, 'bytes': bytes_e,
-                                   'GBps': round(achieved, 1)},
+                                   'GBps': round(achieved, 1), 'staged': step['staged']},
                    'step_ms_profiled': ms_t / npf}
     if rank != 0:
         return
@@ -381,7 +381,9 @@ def run_gb300(args):
                 'parts': e2e_parts},
         # per step: the fused step and the end-of-step kernel, or H, E and end-of-step
         'gpu_launches': (2 if fused else 3) * K,
-        'roofline': {'bound': 'hbm', 'kernel': 'fused_step' if fused else 'e_half_step',
+        'roofline': {'bound': 'hbm',
+                     'kernel': ('fused_step' if fused else
+                                'e_half_step_staged' if step['staged'] else 'e_half_step'),
                      'achieved': round(achieved, 1),
                      'peak': peak, 'unit': 'GB/s', 'frac': round(achieved / peak, 4),
                      'traffic': traffic, 'traffic_source': traffic_src, 'peak_source': peak_kind,
@@ -841,6 +843,8 @@ def main():
                     help='adjoint: cells of the finite-difference check (0: none)')
     ap.add_argument('--half-steps', action='store_true',
                     help='soil: step with the two half-step kernels instead of the fused step')
+    ap.add_argument('--plain-e', action='store_true',
+                    help='soil: the plain E half-step kernel instead of the staged sweep')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
     ap.add_argument('--workload', choices=['soil', 'bscan', 'bscan2d', 'adjoint', 'sweep', 'build'],

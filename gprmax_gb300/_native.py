@@ -11,9 +11,9 @@ import threading
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
-SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fused_inst.cu', 'adjoint.cu', 'geom.cu',
-           'fractal.cu', 'fdtd_kernels.cuh', 'fused_step.cuh']
-PML_KINDS = 5       # kernels_inst.cu is compiled once per PML kind
+SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fused_inst.cu', 'staged_inst.cu', 'adjoint.cu',
+           'geom.cu', 'fractal.cu', 'fdtd_kernels.cuh', 'fused_step.cuh', 'staged_e.cuh']
+PML_KINDS = 5       # kernels_inst.cu and staged_inst.cu are compiled once per PML kind
 FUSED_TJ = (7, 15)  # fused_inst.cu once per PML kind and tile height
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -44,8 +44,9 @@ def _stale():
 def build(force=False, verbose=False):
     """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources.
 
-    The main translation unit, one half-step instantiation unit per PML kind and one fused-step
-    unit per PML kind and tile height are compiled in parallel, then linked."""
+    The main translation unit, one half-step and one staged-E instantiation unit per PML kind
+    and one fused-step unit per PML kind and tile height are compiled in parallel, then
+    linked."""
     if not force and not _stale():
         return LIBPATH
     import shutil
@@ -61,6 +62,8 @@ def build(force=False, verbose=False):
     for pk in range(PML_KINDS):
         jobs.append((os.path.join(CSRC, 'kernels_inst.cu'),
                      os.path.join(objdir, 'kernels_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
+        jobs.append((os.path.join(CSRC, 'staged_inst.cu'),
+                     os.path.join(objdir, 'staged_pk{}.o'.format(pk)), ['-DGBF_PK={}'.format(pk)]))
         for tj in FUSED_TJ:
             jobs.append((os.path.join(CSRC, 'fused_inst.cu'),
                          os.path.join(objdir, 'fused_pk{}_tj{}.o'.format(pk, tj)),

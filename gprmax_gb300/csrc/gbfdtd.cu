@@ -24,6 +24,7 @@
 
 #include "../../include/gbfdtd.h"
 #include "fused_step.cuh"
+#include "staged_e.cuh"
 
 using namespace gbf;
 
@@ -32,9 +33,13 @@ struct gbf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  long long ncomp = 0;
-  float* fields = nullptr;     // 6 * ncomp
-  uint32_t* ID = nullptr;      // 6 * ncomp
+  long long npts = 0;          // nodes per component, (nx+1)(ny+1)(nz+1)
+  long long ncomp = 0;         // device stride of one component array: npts rounded up to 64
+                               // nodes, so every field, packed-ID and pole-state array starts
+                               // on a 256-byte boundary (the staged E sweep copies them in
+                               // 16-byte-aligned bulk copies)
+  float* fields = nullptr;     // 6 * ncomp (12 * ncomp with the fused step's second buffer)
+  uint32_t* ID = nullptr;      // 6 * npts, the caller's layout
   uint32_t* PE = nullptr;      // packed E IDs (ncomp), when nmat <= 1024
   uint32_t* PH = nullptr;      // packed H IDs
   unsigned char* disp = nullptr;   // per material: has dispersive poles
@@ -86,10 +91,18 @@ struct gbf_ctx {
   std::vector<std::pair<int, int>> tune_cand;   // candidate (tile height, chunks) being timed
   std::vector<cudaEvent_t> tune_ev;             // two events per timed step
   int tune_next = 0;
+  // staged E half-step (staged_e.cuh): used where it applies unless option bit 4 is set
+  int staged = 0;
+  SKernFn sk = nullptr;
+  StagedGeom sg{};
+  size_t smem_st = 0;
+  int staged_threads = 0;
+  int* d_err = nullptr;        // device error word of the staged sweep (a wait ran out)
 };
 
 static std::string g_create_err;
 static void tune_release(gbf_ctx* ctx);
+static void configure_staged(gbf_ctx* ctx);
 
 static void invalidate_graph(gbf_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -339,7 +352,8 @@ void gbf_destroy(gbf_ctx* ctx) {
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   void* ptrs[] = {ctx->fields, ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
-                  ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it};
+                  ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it,
+                  ctx->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (float* p : ctx->snaps)
@@ -363,11 +377,11 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~15) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
+  if ((d.options & ~31) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
-  if ((long long)(d.ny + 1) * (d.nz + 1) * (d.nx + 1) > (1LL << 31) - 1)
-    return fail(nullptr, GBF_EINVAL, "gbf_create: more than 2^31 nodes per component");
+  if (npts + 63 > (1LL << 31) - 1)
+    return fail(nullptr, GBF_EINVAL, "gbf_create: more than 2^31 - 64 nodes per component");
   const int n3[3] = {d.nx, d.ny, d.nz};
   for (int s = 0; s < 6; ++s) {
     const int t = d.pml_thickness[s];
@@ -376,7 +390,9 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   }
   gbf_ctx* ctx = new gbf_ctx();
   ctx->d = d;
-  ctx->ncomp = npts;
+  ctx->npts = npts;
+  ctx->ncomp = (npts + 63) & ~63LL;
+  const long long ncomp = ctx->ncomp;
   cudaError_t e = cudaGetDevice(&ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -392,7 +408,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   ctx->fused_ok = (ones == 0 && d.ntl == 0 && d.nmat <= 1024 && d.maxpoles <= kFusedMaxPoles &&
                    !(d.options & 8)) ? 1 : 0;
   if (ctx->fused_ok) {
-    const size_t fb = sizeof(float) * 12 * npts;
+    const size_t fb = sizeof(float) * 12 * ncomp;
     if (cudaMalloc((void**)&ctx->fields, fb) == cudaSuccess) {
       ctx->bytes += fb;
       if (cudaMemsetAsync(ctx->fields, 0, fb, ctx->stream) != cudaSuccess)
@@ -403,13 +419,13 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
       ctx->fused_ok = 0;
     }
   }
-  if (!ctx->fused_ok) A((void**)&ctx->fields, sizeof(float) * 6 * npts);
+  if (!ctx->fused_ok) A((void**)&ctx->fields, sizeof(float) * 6 * ncomp);
   // packed IDs (at most 1024 materials): two words per node, built straight from the caller's
   // array; otherwise the six ID arrays themselves
   if (d.nmat <= 1024) {
     ctx->idp = 1;
-    A((void**)&ctx->PE, sizeof(uint32_t) * npts);
-    A((void**)&ctx->PH, sizeof(uint32_t) * npts);
+    A((void**)&ctx->PE, sizeof(uint32_t) * ncomp);
+    A((void**)&ctx->PH, sizeof(uint32_t) * ncomp);
   } else {
     A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
   }
@@ -420,7 +436,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   A((void**)&ctx->cHs, sizeof(float) * d.nmat);
   if (d.maxpoles > 0) {
     A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
-    A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * npts);
+    A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * ncomp);
   }
   // PML state: per slab 4 Phi arrays of order * T * nu * nv (6 with the second H buffer)
   long long phi_total = 0;
@@ -442,6 +458,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   A((void**)&ctx->rx_coords, sizeof(int) * 3 * (d.nrx + 1));
   A((void**)&ctx->rxs, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
   A((void**)&ctx->d_it, sizeof(int));
+  A((void**)&ctx->d_err, sizeof(int));
   if (d.ntl) {
     A((void**)&ctx->tls, sizeof(TLine) * d.ntl);
     A((void**)&ctx->tl_waves, sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
@@ -456,14 +473,14 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   // kernel parameters
   StepParams& p = ctx->sp;
   for (int c = 0; c < 3; ++c) {
-    p.E[c] = p.En[c] = ctx->fields + c * npts;
-    p.H[c] = p.Hn[c] = ctx->fields + (3 + c) * npts;
+    p.E[c] = p.En[c] = ctx->fields + c * ncomp;
+    p.H[c] = p.Hn[c] = ctx->fields + (3 + c) * ncomp;
   }
   for (int c = 0; c < 6; ++c) p.ID[c] = ctx->ID ? ctx->ID + c * npts : nullptr;
   p.PE = ctx->PE;
   p.PH = ctx->PH;
   for (int q = 0; q < kSrcInline; ++q) p.srcqE[q] = p.srcqH[q] = -1;
-  p.ncomp = (int)npts;
+  p.ncomp = (int)ncomp;
   p.nx = d.nx; p.ny = d.ny; p.nz = d.nz;
   p.two_d = (d.nx == 1 || d.ny == 1 || d.nz == 1) ? 1 : 0;
   p.sy = d.nz + 1;
@@ -651,6 +668,7 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   ctx->grid_h = 0;
   ctx->grid_e = 0;
   invalidate_graph(ctx);
+  configure_staged(ctx);
   // one fused kernel per step where the model allows it (tiles tuned at the first run)
   tune_release(ctx);
   ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
@@ -713,11 +731,11 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (ids)
-      pack_ids_from<<<sms * 8, 256, 0, ctx->stream>>>(ids, ctx->ncomp, nmat,
+      pack_ids_from<<<sms * 8, 256, 0, ctx->stream>>>(ids, ctx->npts, nmat,
                                                      ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
                                                      ctx->PE, ctx->PH, dmax);
     else
-      finish_packed_ids<<<sms * 8, 256, 0, ctx->stream>>>(ctx->PE, ctx->PH, ctx->ncomp, nmat,
+      finish_packed_ids<<<sms * 8, 256, 0, ctx->stream>>>(ctx->PE, ctx->PH, ctx->npts, nmat,
                                                          ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
                                                          dmax);
     CK(cudaGetLastError());
@@ -755,7 +773,7 @@ __global__ void id_max_kernel(const uint32_t* a, long long n, unsigned int* mx) 
 
 // The largest ID in ctx->ID (on the device) must index the coefficient tables.
 static int check_ids(gbf_ctx* ctx, const char* who) {
-  const size_t n = 6 * (size_t)ctx->ncomp;
+  const size_t n = 6 * (size_t)ctx->npts;
   unsigned int* dmax = nullptr;
   CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
   CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
@@ -777,7 +795,7 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
   if (!ctx) return GBF_EINVAL;
   if (!ID || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials: NULL array");
-  const size_t n = 6 * (size_t)ctx->ncomp;
+  const size_t n = 6 * (size_t)ctx->npts;
   const size_t bytes = sizeof(uint32_t) * n;
   if (ctx->idp == 1) {
     // packed IDs: one kernel reads the caller's array where it lies and writes the two words
@@ -851,7 +869,7 @@ int gbf_upload_materials_packed(gbf_ctx* ctx, const uint32_t* PE, const uint32_t
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: NULL array");
   if (ctx->idp != 1)
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: %d materials do not pack (at most 1024)", ctx->d.nmat);
-  const size_t bytes = sizeof(uint32_t) * (size_t)ctx->ncomp;
+  const size_t bytes = sizeof(uint32_t) * (size_t)ctx->npts;
   CK(cudaMemcpyAsync(ctx->PE, PE, bytes, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->PH, PH, bytes, cudaMemcpyHostToDevice, ctx->stream));
   return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
@@ -919,7 +937,7 @@ int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials_geom: geometry %d x %d x %d on device %d "
                 "does not match the context's grid %d x %d x %d on device %d", dims[0], dims[1],
                 dims[2], gdev, ctx->d.nx, ctx->d.ny, ctx->d.nz, ctx->device);
-  const size_t n = 6 * (size_t)ctx->ncomp;
+  const size_t n = 6 * (size_t)ctx->npts;
   CK(cudaStreamSynchronize(gstream));
   if (ctx->idp == 1)   // packed straight from the geometry's IDs
     return upload_tables(ctx, coeffE, coeffH, coeffD, gid);
@@ -1154,8 +1172,99 @@ static void launch_h(gbf_ctx* ctx) {
   kern<<<grid, block, ctx->smem_h, ctx->stream>>>(p);
 }
 
+// The division constants of FastDiv for divisor d >= 2 (staged_e.cuh).
+static FastDiv fast_div(int d) {
+  int l = 0;
+  while ((1LL << l) < d) ++l;
+  FastDiv f;
+  f.m = (uint32_t)(((1ULL << (31 + l)) + (uint64_t)d - 1) / (uint64_t)d);
+  f.sh = l - 1;
+  return f;
+}
+
+// The staged E half-step (staged_e.cuh) where it applies: 3D grids with packed IDs, coefficient
+// tables in shared memory, no poles or at most two with real state, arrays of at least two
+// chunk spans, and a ring of at least two stages that fits in shared memory beside the tables;
+// option bit 4 keeps the plain kernel.
+static void configure_staged(gbf_ctx* ctx) {
+  ctx->staged = 0;
+  ctx->sk = nullptr;
+  const gbf_grid_desc& d = ctx->d;
+  const StepParams& p = ctx->sp;
+  const int np = d.maxpoles;
+  if ((d.options & 16) || p.two_d || ctx->idp != 1 || !p.smem || np > 2 || (np > 0 && !ctx->treal))
+    return;
+  const int L = kStageL, W = kStageSpan;
+  if (ctx->ncomp < 2 * (long long)W || p.sy < 2 || p.sx < 2) return;
+  SKernFn k = nullptr;
+  switch (pml_kind(d)) {
+    case PML_HORI1: staged_pk1(np, ctx->treal, &k); break;
+    case PML_HORI2: staged_pk2(np, ctx->treal, &k); break;
+    case PML_MRI1: staged_pk3(np, ctx->treal, &k); break;
+    case PML_MRI2: staged_pk4(np, ctx->treal, &k); break;
+    default: staged_pk0(np, ctx->treal, &k); break;
+  }
+  if (!k) return;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  StagedGeom& g = ctx->sg;
+  g.nstream = 11 + 3 * np;
+  g.ring_off = (int)((ctx->smem_e + 127) & ~(size_t)127);
+  const size_t stage = sizeof(float) * (size_t)W * g.nstream;
+  // room for the kernel's static shared memory (the barriers and the abort flag)
+  const size_t fixed = 1024;
+  int ns = kStageMax;
+  while (ns >= 2 && g.ring_off + ns * stage + fixed > (size_t)optin) --ns;
+  if (ns < 2) return;
+  g.nstages = ns;
+  g.cpp = (int)(((long long)p.ny * p.sy + 3 + L - 1) / L);
+  if ((long long)g.cpp * p.nx > (1LL << 31) - 1) return;
+  g.nchunks = g.cpp * p.nx;
+  g.ilo = p.boxE[0].i0;
+  g.ihi = p.boxE[0].i0 + (p.boxE[0].count ? p.boxE[0].bi : 0);
+  g.jlo = p.boxE[0].j0;
+  g.jhi = p.boxE[0].j0 + (p.boxE[0].count ? p.boxE[0].bj : 0);
+  g.amax = (int)(ctx->ncomp - W);   // a multiple of 4: ncomp is one of 64, W one of 8
+  g.by_sy = fast_div(p.sy);
+  g.by_cpp = fast_div(g.cpp < 2 ? 2 : g.cpp);
+  g.err = ctx->d_err;
+  g.limit_ns = 2000000000LL;
+  const size_t smem = g.ring_off + ns * stage;
+  if (cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return;
+  }
+  ctx->smem_st = smem;
+  ctx->sk = k;
+  ctx->staged_threads = kStagedThreads;
+  ctx->staged = 1;
+}
+
+// A staged sweep that gave up waiting for a stage leaves the error word set (read and cleared
+// here, after the context's work so far has finished).
+static int staged_status(gbf_ctx* ctx) {
+  if (!ctx->d_err) return GBF_OK;
+  int v = 0;
+  CK(cudaMemcpyAsync(&v, ctx->d_err, sizeof v, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (v) {
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return fail(ctx, GBF_ECUDA, "E half-step: a shared-memory stage was not filled within the "
+                "wait limit; the fields of this run are not valid");
+  }
+  return GBF_OK;
+}
+
 static void launch_e(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
+  if (ctx->staged) {
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    ctx->sk<<<sms, ctx->staged_threads, ctx->smem_st, ctx->stream>>>(p, ctx->sg);
+    return;
+  }
   HKern hk;
   EKern kern;
   pick_kernels(ctx, &hk, &kern);
@@ -1428,6 +1537,7 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
   }
   if (flags & GBF_RUN_CHECK) {
     CK(cudaStreamSynchronize(ctx->stream));
+    return staged_status(ctx);
   }
   return GBF_OK;
 }
@@ -1465,22 +1575,26 @@ int gbf_download_rx(gbf_ctx* ctx, float* rxs) {
   const size_t n = 9 * (size_t)ctx->d.iterations * ctx->d.nrx;
   if (n) CK(cudaMemcpyAsync(rxs, ctx->rxs, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  return GBF_OK;
+  return staged_status(ctx);
 }
 
 int gbf_download_fields(gbf_ctx* ctx, float* fields) {
   if (!ctx || !fields) return GBF_EINVAL;
-  CK(cudaMemcpyAsync(fields, current_fields(ctx), sizeof(float) * 6 * ctx->ncomp, cudaMemcpyDeviceToHost, ctx->stream));
+  // device arrays [6][ncomp] -> the caller's [6][npts]
+  CK(cudaMemcpy2DAsync(fields, sizeof(float) * ctx->npts, current_fields(ctx),
+                       sizeof(float) * ctx->ncomp, sizeof(float) * ctx->npts, 6,
+                       cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  return GBF_OK;
+  return staged_status(ctx);
 }
 
 int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
   if (!ctx || !fields) return GBF_EINVAL;
   // both buffers of a fused model: E outside the half-step's range is read from either
   for (int b = 0; b < (ctx->fused_ok ? 2 : 1); ++b)
-    CK(cudaMemcpyAsync(ctx->fields + (size_t)b * 6 * ctx->ncomp, fields, sizeof(float) * 6 * ctx->ncomp,
-                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpy2DAsync(ctx->fields + (size_t)b * 6 * ctx->ncomp, sizeof(float) * ctx->ncomp,
+                         fields, sizeof(float) * ctx->npts, sizeof(float) * ctx->npts, 6,
+                         cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
@@ -1488,15 +1602,19 @@ int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
 int gbf_download_dispersive(gbf_ctx* ctx, float* T) {
   if (!ctx || !T) return GBF_EINVAL;
   if (!ctx->T) return fail(ctx, GBF_ESTATE, "gbf_download_dispersive: model has no dispersive state");
-  const size_t n = 3 * (size_t)ctx->d.maxpoles * ctx->ncomp;
+  // device arrays [3P][ncomp] -> the caller's [3P][npts]
+  const int rows = 3 * ctx->d.maxpoles;
+  const size_t n = (size_t)rows * ctx->npts;
   if (!ctx->treal) {
-    CK(cudaMemcpyAsync(T, ctx->T, sizeof(float2) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpy2DAsync(T, sizeof(float2) * ctx->npts, ctx->T, sizeof(float2) * ctx->ncomp,
+                         sizeof(float2) * ctx->npts, rows, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return GBF_OK;
   }
   // real parts on the device: copy them into the first half, then spread them out in place
   // from the end, each with its imaginary part +0
-  CK(cudaMemcpyAsync(T, ctx->T, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpy2DAsync(T, sizeof(float) * ctx->npts, ctx->T, sizeof(float) * ctx->ncomp,
+                       sizeof(float) * ctx->npts, rows, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   for (size_t q = n; q-- > 0;) {
     T[2 * q] = T[q];
@@ -1578,7 +1696,7 @@ int gbf_step_info(gbf_ctx* ctx, int32_t info[8]) {
   info[4] = ctx->fused ? ctx->f_blocks : 0;
   info[5] = ctx->tuned;
   info[6] = ctx->cur;
-  info[7] = ctx->fused_ok | (ctx->fused_avail << 1);
+  info[7] = ctx->fused_ok | (ctx->fused_avail << 1) | (ctx->staged << 2);
   return GBF_OK;
 }
 

@@ -332,13 +332,15 @@ class DeviceModel:
 
     def step_info(self):
         """How the model steps: {'fused': bool, 'tj', 'nch', 'planes', 'blocks', 'tuned',
-        'buffer', 'two_buffers', 'fused_available'} (``gbf_step_info``)."""
+        'buffer', 'two_buffers', 'fused_available', 'staged'} (``gbf_step_info``; 'staged': the
+        E half-step is the staged sweep)."""
         info = np.zeros(8, dtype=np.int32)
         self._check(self.lib.gbf_step_info(self.ctx, _ptr(info)))
         keys = ('fused', 'tj', 'nch', 'planes', 'blocks', 'tuned', 'buffer', 'two_buffers')
         out = {k: int(v) for k, v in zip(keys, info)}
         out['fused'] = bool(out['fused'])
         out['fused_available'] = bool(out['two_buffers'] & 2)
+        out['staged'] = bool(out['two_buffers'] & 4)
         out['two_buffers'] = bool(out['two_buffers'] & 1)
         return out
 

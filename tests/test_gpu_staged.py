@@ -1,0 +1,88 @@
+"""GPU: the staged E half-step (gprmax_gb300/csrc/staged_e.cuh) against the plain E half-step
+kernel (options bit 4), bit for bit.
+
+The staged sweep copies each chunk's E, H and H-neighbour rows, packed material words and pole
+state into shared memory with bulk copies and updates the nodes from there, with e_node's
+arithmetic; so receivers, all six fields and the dispersive state must equal the plain kernel's
+exactly. The models cover every PML kind, no poles and one real pole, magnetic materials,
+sources on the domain's upper faces, a transmission line, receiver arrays, fractal soil and
+rough surfaces; grids from 20 x 18 x 16 cells (copies clamped at both ends of the arrays) up.
+Both runs use the two half-step kernels (options bit 3), so the staged sweep runs every step.
+"""
+import numpy as np
+import pytest
+
+from models import MODELS
+
+pytestmark = pytest.mark.gpu
+
+STAGED_MODELS = ['fs_hori1', 'pml_off', 'hori2', 'mri1', 'mri2', 'debye1', 'faces', 'smoothed',
+                 'fractal', 'rough', 'rxarray', 'tline', 'triangles']
+
+
+def _run(G, options, nsteps=None):
+    from gprmax_gb300.solver import DeviceModel
+    dm = DeviceModel(G, options)
+    try:
+        dm.run(nsteps)
+        out = {'rx': dm.receivers(), 'f': dm.fields(), 'info': dm.step_info()}
+        if G.maxpoles:
+            out['T'] = dm.dispersive()
+    finally:
+        dm.close()
+    return out
+
+
+def _equal(a, b):
+    np.testing.assert_array_equal(a['rx'], b['rx'])
+    np.testing.assert_array_equal(a['f'], b['f'])
+    if 'T' in a:
+        np.testing.assert_array_equal(a['T'], b['T'])
+
+
+@pytest.mark.parametrize('name', STAGED_MODELS)
+def test_staged_e_half_step_equals_plain(native, name):
+    from gprmax_gb300.model import build_grid
+    G = build_grid(MODELS[name].splitlines(True), messages=False)
+    got = _run(G, 8)
+    ref = _run(G, 8 | 16)
+    assert got['info']['staged'], 'model {} should take the staged E half-step'.format(name)
+    assert not ref['info']['staged']
+    _equal(got, ref)
+
+
+def test_staged_against_oracle(native):
+    import oracle
+    from gprmax_gb300.model import build_grid
+    G = build_grid(MODELS['debye1'].splitlines(True), messages=False)
+    got = _run(G, 8)
+    assert got['info']['staged']
+    ref = oracle.OracleSolver(G).run()
+    np.testing.assert_array_equal(got['rx'], ref.receivers())
+    np.testing.assert_array_equal(got['f'], ref.fields())
+
+
+def test_complex_poles_keep_the_plain_kernel(native):
+    """Complex pole state (option bit 2) is not staged: the plain kernel runs, and the results
+    are the staged run's."""
+    from gprmax_gb300.model import build_grid
+    G = build_grid(MODELS['debye1'].splitlines(True), messages=False)
+    cplx = _run(G, 8 | 4)
+    assert not cplx['info']['staged']
+    real = _run(G, 8)
+    np.testing.assert_array_equal(cplx['rx'], real['rx'])
+    np.testing.assert_array_equal(cplx['f'], real['f'])
+
+
+def test_staged_soil(native):
+    """A 160 x 160 x 80 cut of the benchmark soil (50 Debye materials, 10-cell PML, dipole and
+    receiver), 300 iterations, staged against plain; the default run (whatever step the tuner
+    keeps) equals both."""
+    from gprmax_gb300 import workloads
+    G = workloads.dispersive_soil(nx=160, ny=160, nz=80, surface=60, timewindow='3e-9')
+    got = _run(G, 8, 300)
+    ref = _run(G, 8 | 16, 300)
+    assert got['info']['staged']
+    _equal(got, ref)
+    dflt = _run(G, 0, 300)
+    _equal(dflt, ref)

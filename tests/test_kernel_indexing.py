@@ -258,3 +258,146 @@ def test_pack_ids_on_the_host(native_lib):
     ID[4, 777] = 1024
     assert native_lib.gbf_pack_ids(p(ID), n, p(pe), p(ph), ctypes.byref(mx)) == -1
     assert mx.value == 1024
+
+
+def _staged_consumers():
+    """kStagedC of staged_e.cuh: consumer warps per block, one node per consumer thread per
+    chunk (chunks of L = 32 kStagedC nodes, copies of L + 8 floats)."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), '..', 'gprmax_gb300',
+                            'csrc', 'staged_e.cuh')).read()
+    assert re.search(r'kStageL = 32 \* kStagedC;', src)
+    assert re.search(r'kStageSpan = kStageL \+ 8;', src)
+    return int(re.search(r'kStagedC = (\d+);', src).group(1))
+
+
+def _fast_div(d):
+    """FastDiv's constants for divisor d (gbfdtd.cu fast_div) and its quotient function."""
+    l = 0
+    while (1 << l) < d:
+        l += 1
+    m = ((1 << (31 + l)) + d - 1) // d
+    assert m < 2 ** 32
+    return lambda n: ((np.asarray(n, dtype=np.uint64) * np.uint64(m)) >> np.uint64(32)) >> np.uint64(l - 1)
+
+
+def test_fast_division():
+    """The multiply-high division the staged sweep uses for n / sy and n / cpp is exact for
+    every n in [0, 2^31) (theorem 4.2 of Granlund and Montgomery, PLDI 1994): checked on every
+    divisor up to 1200 and on the divisors of large grids, at the multiples of d and their
+    neighbours and at random n."""
+    rng = np.random.default_rng(5)
+    top = 2 ** 31 - 1
+    for d in list(range(2, 1201)) + [4095, 4097, 8191, 8192, 32769, 65535, 65536, 80601, 80602]:
+        q = _fast_div(d)
+        mult = np.arange(0, top, d * max(1, top // d // 2000), dtype=np.int64)
+        n = np.concatenate([mult, mult + 1, mult + d - 1, rng.integers(0, top, 2000), [top]])
+        n = n[(n >= 0) & (n <= top)]
+        np.testing.assert_array_equal(q(n).astype(np.int64), n // d)
+
+
+def _staged_sweep(lib, n3, thick, planes=None):
+    """The staged E sweep's chunks, restated: host geometry (gbfdtd.cu configure_staged) and
+    device arithmetic (staged_e.cuh stage_chunk's header, the consumer loop). Checks every copy
+    and every shared-memory read a node makes, and returns the flat indices of the updated
+    nodes and each chunk's core flag."""
+    nx, ny, nz = n3
+    T = 32 * _staged_consumers()
+    L = T
+    W = L + 8
+    sy, sx = nz + 1, (ny + 1) * (nz + 1)
+    npts = (nx + 1) * sx
+    ncomp = (npts + 63) & ~63
+    assert ncomp >= 2 * W, 'grid too small for the staged sweep'
+    i0, j0, _, bi, bj, _, _, _, _, count = _boxes(lib, n3, thick, True)[0]
+    ilo, ihi = i0, i0 + (bi if count else 0)
+    jlo, jhi = j0, j0 + (bj if count else 0)
+    cpp = (ny * sy + 3 + L - 1) // L
+    amax = ncomp - W
+    c = np.arange(nx * cpp, dtype=np.int64)
+    if planes is not None:
+        c = np.concatenate([np.arange(p * cpp, (p + 1) * cpp) for p in planes])
+    i = c if cpp == 1 else _fast_div(cpp)(c).astype(np.int64)
+    np.testing.assert_array_equal(i, c // cpp)
+    s = ((i * sx) & ~3) + (c - i * cpp) * L
+    clamp = lambda a: np.clip(a, 0, amax)
+    aE, aH = clamp(s), clamp(s - 4)
+    aJ, aI = clamp((s - sy) & ~3), clamp((s - sx) & ~3)
+    for a in (aE, aH, aJ, aI):      # 16-byte aligned starts, copies inside their arrays
+        assert (a % 4 == 0).all() and (a >= 0).all() and (a + W <= ncomp).all()
+    shE, shH = s - aE, s - aH
+    shJ, shI = s - sy - aJ, s - sx - aI
+    # the header's row and column of node s, and each consumer thread's offsets from it
+    by_sy = _fast_div(sy)
+    f = s - i * sx
+    jf = np.where(f >= 0, by_sy(np.maximum(f, 0)).astype(np.int64), -1)
+    kf = f - jf * sy
+    assert ((kf >= 0) & (kf < sy)).all()
+    t = np.arange(T)
+    tq = by_sy(t).astype(np.int64)
+    tr = t - tq * sy
+    J = jf[:, None] + tq[None, :]
+    K = kf[:, None] + tr[None, :]
+    wrap = K >= sy
+    K = np.where(wrap, K - sy, K)
+    J = np.where(wrap, J + 1, J)
+    r = t[None, :]
+    assert (J * sy + K == f[:, None] + r).all() and (K >= 0).all() and (K < sy).all()
+    valid = (J >= 0) & (J < ny) & (K < nz)
+    I = np.broadcast_to(i[:, None], J.shape)
+    # every shared-memory read a node makes lies inside its stream's span
+    inspan = lambda x, m: ((x >= 0) & (x < W))[m].all()
+    assert inspan(shE[:, None] + r, valid)                        # E, packed word, pole state
+    assert inspan(shH[:, None] + r, valid)                        # own H
+    assert inspan(shH[:, None] + r - 1, valid & (K >= 1))         # H at k - 1
+    assert inspan(shJ[:, None] + r, valid & (J >= 1))             # H at j - 1
+    assert inspan(shI[:, None] + r, valid & (I >= 1))             # H at i - 1
+    # the core test: a core chunk's nodes lie in the core box, so its node code may skip the x
+    # and y tests
+    jl = by_sy(np.minimum(f + L - 1, ny * sy - 1)).astype(np.int64)
+    core = (i >= ilo) & (i < ihi) & (jf >= jlo) & (jl < jhi)
+    m = valid & core[:, None]
+    assert ((I[m] >= ilo) & (I[m] < ihi) & (J[m] >= jlo) & (J[m] < jhi)).all()
+    assert (I[m] >= 1).all() and (J[m] >= 1).all()
+    idx = (s[:, None] + r)[valid]
+    assert (idx == (I * sx + J * sy + K)[valid]).all()
+    return idx, core
+
+
+@pytest.mark.parametrize('n3,thick', [((13, 11, 14), (4, 0, 3, 2, 3, 0)),
+                                      ((30, 28, 26), (6, 6, 6, 6, 6, 6)),
+                                      ((41, 7, 9), (0, 0, 0, 0, 0, 0)),
+                                      ((20, 18, 16), (0, 0, 0, 0, 0, 0)),
+                                      ((20, 37, 64), (3, 5, 10, 2, 4, 10)),
+                                      ((60, 50, 40), (10, 0, 5, 10, 7, 0))])
+def test_staged_sweep_covers_the_e_domain_once(native_lib, n3, thick):
+    """The staged E half-step (staged_e.cuh) updates every node of the E domain exactly once,
+    reads only inside the spans its bulk copies filled (copies aligned, inside their arrays),
+    and runs the core node code only on chunks inside the core box."""
+    nx, ny, nz = n3
+    W = 32 * _staged_consumers() + 8
+    if ((nx + 1) * (ny + 1) * (nz + 1) + 63) & ~63 < 2 * W:
+        pytest.skip('grid below the staged sweep\'s minimum')
+    idx, core = _staged_sweep(native_lib, n3, thick)
+    sy, sx = nz + 1, (ny + 1) * (nz + 1)
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing='ij')
+    want = np.sort((ii * sx + jj * sy + kk).ravel())
+    np.testing.assert_array_equal(np.sort(idx), want)
+
+
+def test_staged_sweep_at_the_benchmark_size(native_lib):
+    """The 400 x 400 x 200 soil: the first, second, a middle, the second-last and the last
+    plane, checked as above; most chunks of a middle plane take the core code."""
+    n3, thick = (400, 400, 200), (10,) * 6
+    planes = (0, 1, 11, 200, 389, 390, 398, 399)
+    idx, core = _staged_sweep(native_lib, n3, thick, planes)
+    sy, sx = 201, 401 * 201
+    for p in planes:
+        got = np.sort(idx[(idx >= p * sx) & (idx < (p + 1) * sx)])
+        jj, kk = np.meshgrid(np.arange(400), np.arange(200), indexing='ij')
+        np.testing.assert_array_equal(got, np.sort((p * sx + jj * sy + kk).ravel()))
+    L = 32 * _staged_consumers()
+    cpp = (400 * 201 + 3 + L - 1) // L
+    mid = core[planes.index(200) * cpp:(planes.index(200) + 1) * cpp]
+    assert mid.mean() > 0.85 and not core[:cpp].any()
