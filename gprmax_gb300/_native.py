@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 LIBPATH = os.path.join(CSRC, 'libgbfdtd.so')
 SOURCES = ['gbfdtd.cu', 'kernels_inst.cu', 'fused_inst.cu', 'staged_inst.cu', 'adjoint.cu',
-           'geom.cu', 'fractal.cu', 'fdtd_kernels.cuh', 'fused_step.cuh', 'staged_e.cuh']
+           'geom.cu', 'fractal.cu', 'fdtd_kernels.cuh', 'fused_step.cuh', 'staged.cuh']
 PML_KINDS = 5       # kernels_inst.cu and staged_inst.cu are compiled once per PML kind
 FUSED_TJ = (7, 15)  # fused_inst.cu once per PML kind and tile height
 HEADER = os.path.join(os.path.dirname(HERE), 'include', 'gbfdtd.h')
@@ -44,8 +44,8 @@ def _stale():
 def build(force=False, verbose=False):
     """Compile ``libgbfdtd.so`` for sm_103a if it is missing or older than its sources.
 
-    The main translation unit, one half-step and one staged-E instantiation unit per PML kind
-    and one fused-step unit per PML kind and tile height are compiled in parallel, then
+    The main translation unit, one half-step and one staged half-step instantiation unit per
+    PML kind and one fused-step unit per PML kind and tile height are compiled in parallel, then
     linked."""
     if not force and not _stale():
         return LIBPATH

@@ -154,13 +154,13 @@ __device__ __forceinline__ PmlRow load_row(const float* __restrict__ R, int T, i
   return c;
 }
 
-// The Phi state is read from `in` and its next value written to `out` (the same array, except
-// for the H state of the fused step), and only when `wr` (a halo node recomputed by a tile
-// that does not own it reads the state but leaves it to its owner).
+// The Phi state's present values are ph0 (and ph1, the second CFS order, at pidx + ocount); its
+// next value is written to `out` (the array read, except for the H state of the fused step),
+// and only when `wr` (a halo node recomputed by a tile that does not own it reads the state but
+// leaves it to its owner).
 template <int PK>
-__device__ __forceinline__ float pml_update(float dF, const float* in, float* out, int pidx,
-                                            int ocount, const PmlRow& c, bool wr) {
-  const float ph0 = in[pidx];
+__device__ __forceinline__ float pml_update_v(float dF, float ph0, float ph1, float* out, int pidx,
+                                              int ocount, const PmlRow& c, bool wr) {
   if (PK == PML_HORI1) {
     const float RA01 = c.RA0 - 1.0f;
     const float X = RA01 * dF + c.RB0 * ph0;
@@ -168,7 +168,6 @@ __device__ __forceinline__ float pml_update(float dF, const float* in, float* ou
     return X;
   } else if (PK == PML_HORI2) {
     const float RA01 = c.RA0 * c.RA1 - 1.0f;
-    const float ph1 = in[pidx + ocount];
     const float X = RA01 * dF + c.RA1 * c.RB0 * ph0 + c.RB1 * ph1;
     if (wr) {
       out[pidx + ocount] = c.RE1 * ph1 - c.RF1 * (c.RA0 * dF + c.RB0 * ph0);
@@ -187,7 +186,6 @@ __device__ __forceinline__ float pml_update(float dF, const float* in, float* ou
     const float IRA1 = IRA - 1.0f;
     const float RC0 = IRA * c.RF0;
     const float RC1 = IRA * c.RF1;
-    const float ph1 = in[pidx + ocount];
     const float Psi = c.RB0 * ph0 + c.RB1 * ph1;
     const float X = IRA1 * dF - IRA * Psi;
     if (wr) {
@@ -196,6 +194,16 @@ __device__ __forceinline__ float pml_update(float dF, const float* in, float* ou
     }
     return X;
   }
+}
+
+// The same with the state read from `in`.
+template <int PK>
+__device__ __forceinline__ float pml_update(float dF, const float* in, float* out, int pidx,
+                                            int ocount, const PmlRow& c, bool wr) {
+  constexpr bool two = PK == PML_HORI2 || PK == PML_MRI2;
+  const float ph0 = in[pidx];
+  const float ph1 = two ? in[pidx + ocount] : 0.f;
+  return pml_update_v<PK>(dF, ph0, ph1, out, pidx, ocount, c, wr);
 }
 
 // x / d rounded to nearest, as IEEE division gives it. When the host has verified d
@@ -390,13 +398,14 @@ __device__ __forceinline__ float hsrcm(const StepParams& p, const HCoef& c, uint
 // the PML). The X values of the node's slabs are formed first (they depend only on the E
 // differences and the Phi state), then each component takes its main update and its
 // corrections in the reference's order.
+// h_node_x takes the slab X values already formed (XA, XB per axis; zero off the slabs).
 template <int PK, int IDP, bool CORE>
-__device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
-                                       int i, int j, int k, bool src, int it, const int* where,
-                                       const int* pr, float dEz_y, float dEy_z, float dEx_z,
-                                       float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
-                                       uint32_t my, uint32_t mz, float& hx, float& hy, float& hz,
-                                       bool wphi = true) {
+__device__ __forceinline__ void h_node_x(const StepParams& p, const HCoef& hc,
+                                         int i, int j, int k, bool src, int it, const int* where,
+                                         const float* XA, const float* XB, float dEz_y,
+                                         float dEy_z, float dEx_z, float dEz_x, float dEy_x,
+                                         float dEx_y, uint32_t mx, uint32_t my, uint32_t mz,
+                                         float& hx, float& hy, float& hz) {
   const int nx = p.nx, ny = p.ny, nz = p.nz;
   const bool iin = CORE || i < nx, jin = CORE || j < ny, kin = k < nz;
   const bool ipos = CORE || i >= 1, jpos = CORE || j >= 1;
@@ -405,12 +414,6 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
   const bool hx2 = !p.two_d || ((ny == 1 || nz == 1) && iin);
   const bool hy2 = !p.two_d || ((nx == 1 || nz == 1) && jin);
   const bool hz2 = !p.two_d || ((nx == 1 || ny == 1) && kin);
-  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
-  if (PK != PML_NONE) {
-    if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0], wphi);
-    if (!CORE && where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1], wphi);
-    if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2], wphi);
-  }
   // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
     const bool mainu = ipos && jin && kin && hx2;
@@ -450,6 +453,23 @@ __device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
     if (src) F = apply_h_sources(F, 5, i, j, k, it, hsrcm<IDP>(p, hc, mz), p);
     hz = F;
   }
+}
+
+template <int PK, int IDP, bool CORE>
+__device__ __forceinline__ void h_node(const StepParams& p, const HCoef& hc,
+                                       int i, int j, int k, bool src, int it, const int* where,
+                                       const int* pr, float dEz_y, float dEy_z, float dEx_z,
+                                       float dEz_x, float dEy_x, float dEx_y, uint32_t mx,
+                                       uint32_t my, uint32_t mz, float& hx, float& hy, float& hz,
+                                       bool wphi = true) {
+  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
+  if (PK != PML_NONE) {
+    if (!CORE && where[0]) pml_axis<PK, false, 0>(p, where[0], pr[0], i, j, k, dEz_x, dEy_x, XA[0], XB[0], wphi);
+    if (!CORE && where[1]) pml_axis<PK, false, 1>(p, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1], wphi);
+    if (where[2]) pml_axis<PK, false, 2>(p, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2], wphi);
+  }
+  h_node_x<PK, IDP, CORE>(p, hc, i, j, k, src, it, where, XA, XB, dEz_y, dEy_z, dEx_z, dEz_x,
+                          dEy_x, dEx_y, mx, my, mz, hx, hy, hz);
 }
 
 // One H node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j
@@ -627,18 +647,14 @@ __device__ __forceinline__ float apply_e_sources(float F, int comp, int i, int j
 // E update of one node for all three components: main update (update_electric, or part A of
 // the dispersive update), slab corrections in slab order, sources, dispersive part B.
 // where[a] / pr[a]: slab membership and profile index along each axis (0 outside the PML).
+// e_node_x takes the slab X values already formed (XA, XB per axis; zero off the slabs).
 template <int PK, int NP, bool CORE, bool TR>
-__device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
-                                       const float2* CD, int i, int j, int k, bool src, int it,
-                                       const int* where, const int* pr, float dHz_y,
-                                       float dHy_z, float dHx_z, float dHz_x, float dHy_x,
-                                       float dHx_y, const uint32_t* m, float* e, float2 (*t)[NP > 0 ? NP : 1]) {
-  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
-  if (PK != PML_NONE) {
-    if (!CORE && where[0]) pml_axis<PK, true, 0>(p, where[0], pr[0], i, j, k, dHz_x, dHy_x, XA[0], XB[0]);
-    if (!CORE && where[1]) pml_axis<PK, true, 1>(p, where[1], pr[1], i, j, k, dHz_y, dHx_y, XA[1], XB[1]);
-    if (where[2]) pml_axis<PK, true, 2>(p, where[2], pr[2], i, j, k, dHy_z, dHx_z, XA[2], XB[2]);
-  }
+__device__ __forceinline__ void e_node_x(const StepParams& p, const float4* C4, const float* Cs,
+                                         const float2* CD, int i, int j, int k, bool src, int it,
+                                         const int* where, const float* XA, const float* XB,
+                                         const uint32_t* m, float* e,
+                                         float2 (*t)[NP > 0 ? NP : 1], float dHz_y, float dHy_z,
+                                         float dHx_z, float dHz_x, float dHy_x, float dHx_y) {
 #pragma unroll
   for (int comp = 0; comp < 3; ++comp) {
     bool mainu, pml;
@@ -723,6 +739,22 @@ __device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, co
       }
     }
   }
+}
+
+template <int PK, int NP, bool CORE, bool TR>
+__device__ __forceinline__ void e_node(const StepParams& p, const float4* C4, const float* Cs,
+                                       const float2* CD, int i, int j, int k, bool src, int it,
+                                       const int* where, const int* pr, float dHz_y,
+                                       float dHy_z, float dHx_z, float dHz_x, float dHy_x,
+                                       float dHx_y, const uint32_t* m, float* e, float2 (*t)[NP > 0 ? NP : 1]) {
+  float XA[3] = {0.f, 0.f, 0.f}, XB[3] = {0.f, 0.f, 0.f};
+  if (PK != PML_NONE) {
+    if (!CORE && where[0]) pml_axis<PK, true, 0>(p, where[0], pr[0], i, j, k, dHz_x, dHy_x, XA[0], XB[0]);
+    if (!CORE && where[1]) pml_axis<PK, true, 1>(p, where[1], pr[1], i, j, k, dHz_y, dHx_y, XA[1], XB[1]);
+    if (where[2]) pml_axis<PK, true, 2>(p, where[2], pr[2], i, j, k, dHy_z, dHx_z, XA[2], XB[2]);
+  }
+  e_node_x<PK, NP, CORE, TR>(p, C4, Cs, CD, i, j, k, src, it, where, XA, XB, m, e, t, dHz_y, dHy_z,
+                             dHx_z, dHz_x, dHy_x, dHx_y);
 }
 
 // One E node at (i, j, k): loads, update, stores. CORE: the node lies in the core box (i and j

@@ -24,7 +24,7 @@
 
 #include "../../include/gbfdtd.h"
 #include "fused_step.cuh"
-#include "staged_e.cuh"
+#include "staged.cuh"
 
 using namespace gbf;
 
@@ -76,7 +76,8 @@ struct gbf_ctx {
   int graph_steps = 0;
   int graph_cur = 0;           // field buffer current when the graph was captured
   int grid_h = 0, grid_e = 0;  // persistent grid sizes
-  long long phi_floats = 0;    // all PML state (both H buffers for the fused step)
+  long long phi_floats = 0;    // all PML state (both H buffers for the fused step) and padding
+  int zspan = 0;               // floats per z-slab Phi copy of the staged sweeps (0: no z slab)
   // fused step (fused_step.cuh): eligible models get two field buffers and two H PML buffers
   int fused_ok = 0;            // buffers allocated for it
   int fused_avail = 0;         // a fused kernel exists for the model (after the tables are known)
@@ -91,13 +92,12 @@ struct gbf_ctx {
   std::vector<std::pair<int, int>> tune_cand;   // candidate (tile height, chunks) being timed
   std::vector<cudaEvent_t> tune_ev;             // two events per timed step
   int tune_next = 0;
-  // staged E half-step (staged_e.cuh): used where it applies unless option bit 4 is set
-  int staged = 0;
-  SKernFn sk = nullptr;
-  StagedGeom sg{};
-  size_t smem_st = 0;
-  int staged_threads = 0;
-  int* d_err = nullptr;        // device error word of the staged sweep (a wait ran out)
+  // staged half-steps (staged.cuh): used where they apply unless option bit 4 is set
+  int staged = 0, staged_h = 0;
+  SKernFn sk = nullptr, skh = nullptr;
+  StagedGeom sg{}, sgh{};
+  size_t smem_st = 0, smem_sth = 0;
+  int* d_err = nullptr;        // device error word of the staged sweeps (a wait ran out)
 };
 
 static std::string g_create_err;
@@ -438,7 +438,9 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
     A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * ncomp);
   }
-  // PML state: per slab 4 Phi arrays of order * T * nu * nv (6 with the second H buffer)
+  // PML state: per slab 4 Phi arrays of order * T * nu * nv (6 with the second H buffer), each
+  // starting on a 256-byte boundary; after them room for the staged sweeps' last z-slab copy,
+  // which may read up to zpad floats past the end of an array
   long long phi_total = 0;
   const int nphi = ctx->fused_ok ? 6 : 4;
   for (int s = 0; s < 6; ++s) {
@@ -446,10 +448,12 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     if (!t) continue;
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
-    phi_total += (long long)nphi * d.pml_order * t * nu * nv;
+    phi_total += (long long)nphi * ((d.pml_order * t * nu * nv + 63) & ~63LL);
   }
-  ctx->phi_floats = phi_total;
-  A((void**)&ctx->pml_mem, sizeof(float) * phi_total);
+  const int tz = d.pml_thickness[2] > d.pml_thickness[5] ? d.pml_thickness[2] : d.pml_thickness[5];
+  ctx->zspan = tz ? (int)((((kStageL + 2) / (d.nz + 1) + 2) * (long long)tz + 3 + 3) & ~3LL) : 0;
+  ctx->phi_floats = phi_total + ctx->zspan + 64;
+  A((void**)&ctx->pml_mem, sizeof(float) * ctx->phi_floats);
   int tmax = 1;
   for (int s = 0; s < 6; ++s) tmax = d.pml_thickness[s] > tmax ? d.pml_thickness[s] : tmax;
   A((void**)&ctx->pml_coef, sizeof(float) * 6 * 2 * 4 * d.pml_order * tmax);
@@ -515,7 +519,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
     sl.ocount = (int)(t * nu * nv);
-    const long long per = (long long)d.pml_order * sl.ocount;
+    const long long per = ((long long)d.pml_order * sl.ocount + 63) & ~63LL;
     sl.phiE1 = phi; phi += per;
     sl.phiE2 = phi; phi += per;
     sl.phiH1 = phi; phi += per;
@@ -1163,6 +1167,12 @@ static int persistent_blocks(const void* kern, size_t smem) {
 
 static void launch_h(gbf_ctx* ctx) {
   const StepParams& p = ctx->sp;
+  if (ctx->staged_h) {
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    ctx->skh<<<sms, kStagedThreads, ctx->smem_sth, ctx->stream>>>(p, ctx->sgh);
+    return;
+  }
   HKern kern;
   EKern ek;
   pick_kernels(ctx, &kern, &ek);
@@ -1182,63 +1192,89 @@ static FastDiv fast_div(int d) {
   return f;
 }
 
-// The staged E half-step (staged_e.cuh) where it applies: 3D grids with packed IDs, coefficient
-// tables in shared memory, no poles or at most two with real state, arrays of at least two
-// chunk spans, and a ring of at least two stages that fits in shared memory beside the tables;
-// option bit 4 keeps the plain kernel.
-static void configure_staged(gbf_ctx* ctx) {
-  ctx->staged = 0;
-  ctx->sk = nullptr;
-  const gbf_grid_desc& d = ctx->d;
+// Geometry of a staged sweep (ELECTRIC: E, else H) with `nstream` streams per chunk behind
+// `tables` bytes of coefficient tables, and the kernel's shared-memory limit; false when no ring
+// of two stages fits.
+static bool staged_geom(gbf_ctx* ctx, bool electric, int nstream, size_t tables, SKernFn k,
+                        StagedGeom& g, size_t& smem) {
   const StepParams& p = ctx->sp;
-  const int np = d.maxpoles;
-  if ((d.options & 16) || p.two_d || ctx->idp != 1 || !p.smem || np > 2 || (np > 0 && !ctx->treal))
-    return;
+  const gbf_grid_desc& d = ctx->d;
   const int L = kStageL, W = kStageSpan;
-  if (ctx->ncomp < 2 * (long long)W || p.sy < 2 || p.sx < 2) return;
-  SKernFn k = nullptr;
-  switch (pml_kind(d)) {
-    case PML_HORI1: staged_pk1(np, ctx->treal, &k); break;
-    case PML_HORI2: staged_pk2(np, ctx->treal, &k); break;
-    case PML_MRI1: staged_pk3(np, ctx->treal, &k); break;
-    case PML_MRI2: staged_pk4(np, ctx->treal, &k); break;
-    default: staged_pk0(np, ctx->treal, &k); break;
-  }
-  if (!k) return;
   int optin = 0;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
-  StagedGeom& g = ctx->sg;
-  g.nstream = 11 + 3 * np;
-  g.ring_off = (int)((ctx->smem_e + 127) & ~(size_t)127);
-  const size_t stage = sizeof(float) * (size_t)W * g.nstream;
-  // room for the kernel's static shared memory (the barriers and the abort flag)
+  g.nstream = nstream;
+  // the PML profile rows of the kernel's field type after the tables, then the ring
+  g.rows_off = (int)((tables + 15) & ~(size_t)15);
+  int rows = 0;
+  for (int s = 0; s < 6; ++s) {
+    g.roff[s] = rows;
+    rows += 4 * d.pml_order * d.pml_thickness[s];
+  }
+  g.ring_off = (int)((g.rows_off + sizeof(float) * rows + 127) & ~(size_t)127);
+  g.zspan = ctx->zspan;
+  g.zslots = ctx->zspan ? 4 * d.pml_order : 0;
+  g.stage_floats = W * nstream + g.zslots * g.zspan;
+  const size_t stage = sizeof(float) * (size_t)g.stage_floats;
+  // room for the kernel's static shared memory (barriers, headers, the abort flag)
   const size_t fixed = 1024;
   int ns = kStageMax;
   while (ns >= 2 && g.ring_off + ns * stage + fixed > (size_t)optin) --ns;
-  if (ns < 2) return;
+  if (ns < 2) return false;
   g.nstages = ns;
-  g.cpp = (int)(((long long)p.ny * p.sy + 3 + L - 1) / L);
-  if ((long long)g.cpp * p.nx > (1LL << 31) - 1) return;
-  g.nchunks = g.cpp * p.nx;
-  g.ilo = p.boxE[0].i0;
-  g.ihi = p.boxE[0].i0 + (p.boxE[0].count ? p.boxE[0].bi : 0);
-  g.jlo = p.boxE[0].j0;
-  g.jhi = p.boxE[0].j0 + (p.boxE[0].count ? p.boxE[0].bj : 0);
+  const long long plen = electric ? (long long)p.ny * p.sy : p.sx;
+  const int planes = electric ? p.nx : p.nx + 1;
+  g.cpp = (int)((plen + 3 + L - 1) / L);
+  if ((long long)g.cpp * planes > (1LL << 31) - 1) return false;
+  g.nchunks = g.cpp * planes;
+  const Box& core = electric ? p.boxE[0] : p.boxH[0];
+  g.ilo = core.i0;
+  g.ihi = core.i0 + (core.count ? core.bi : 0);
+  g.jlo = core.j0;
+  g.jhi = core.j0 + (core.count ? core.bj : 0);
   g.amax = (int)(ctx->ncomp - W);   // a multiple of 4: ncomp is one of 64, W one of 8
   g.by_sy = fast_div(p.sy);
   g.by_cpp = fast_div(g.cpp < 2 ? 2 : g.cpp);
   g.err = ctx->d_err;
   g.limit_ns = 2000000000LL;
-  const size_t smem = g.ring_off + ns * stage;
+  smem = g.ring_off + ns * stage;
   if (cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess) {
     (void)cudaGetLastError();
-    return;
+    return false;
   }
-  ctx->smem_st = smem;
-  ctx->sk = k;
-  ctx->staged_threads = kStagedThreads;
-  ctx->staged = 1;
+  return true;
+}
+
+// The staged half-steps (staged.cuh) where they apply: 3D grids with packed IDs and coefficient
+// tables in shared memory whose arrays span at least two chunks; for E no poles or at most two
+// with real state; a ring of at least two stages that fits in shared memory beside the tables.
+// Option bit 4 keeps the plain kernels.
+static void configure_staged(gbf_ctx* ctx) {
+  ctx->staged = ctx->staged_h = 0;
+  ctx->sk = ctx->skh = nullptr;
+  const gbf_grid_desc& d = ctx->d;
+  const StepParams& p = ctx->sp;
+  const int np = d.maxpoles;
+  if ((d.options & 16) || p.two_d || ctx->idp != 1 || !p.smem) return;
+  if (ctx->ncomp < 2 * (long long)kStageSpan || p.sy < 2 || p.sx < 2) return;
+  SKernFn ke = nullptr, kh = nullptr;
+  const int idp_h = ctx->uniform_h ? 0 : 1;
+  switch (pml_kind(d)) {
+    case PML_HORI1: staged_pk1(np, ctx->treal, idp_h, &ke, &kh); break;
+    case PML_HORI2: staged_pk2(np, ctx->treal, idp_h, &ke, &kh); break;
+    case PML_MRI1: staged_pk3(np, ctx->treal, idp_h, &ke, &kh); break;
+    case PML_MRI2: staged_pk4(np, ctx->treal, idp_h, &ke, &kh); break;
+    default: staged_pk0(np, ctx->treal, idp_h, &ke, &kh); break;
+  }
+  if (ke && np <= 2 && (np == 0 || ctx->treal) &&
+      staged_geom(ctx, true, 11 + 3 * np, ctx->smem_e, ke, ctx->sg, ctx->smem_st)) {
+    ctx->sk = ke;
+    ctx->staged = 1;
+  }
+  if (kh && staged_geom(ctx, false, 10 + idp_h, ctx->smem_h, kh, ctx->sgh, ctx->smem_sth)) {
+    ctx->skh = kh;
+    ctx->staged_h = 1;
+  }
 }
 
 // A staged sweep that gave up waiting for a stage leaves the error word set (read and cleared
@@ -1251,8 +1287,8 @@ static int staged_status(gbf_ctx* ctx) {
   if (v) {
     CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return fail(ctx, GBF_ECUDA, "E half-step: a shared-memory stage was not filled within the "
-                "wait limit; the fields of this run are not valid");
+    return fail(ctx, GBF_ECUDA, "staged half-step: a shared-memory stage was not filled within "
+                "the wait limit; the fields of this run are not valid");
   }
   return GBF_OK;
 }
@@ -1262,7 +1298,7 @@ static void launch_e(gbf_ctx* ctx) {
   if (ctx->staged) {
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    ctx->sk<<<sms, ctx->staged_threads, ctx->smem_st, ctx->stream>>>(p, ctx->sg);
+    ctx->sk<<<sms, kStagedThreads, ctx->smem_st, ctx->stream>>>(p, ctx->sg);
     return;
   }
   HKern hk;
@@ -1696,7 +1732,7 @@ int gbf_step_info(gbf_ctx* ctx, int32_t info[8]) {
   info[4] = ctx->fused ? ctx->f_blocks : 0;
   info[5] = ctx->tuned;
   info[6] = ctx->cur;
-  info[7] = ctx->fused_ok | (ctx->fused_avail << 1) | (ctx->staged << 2);
+  info[7] = ctx->fused_ok | (ctx->fused_avail << 1) | (ctx->staged << 2) | (ctx->staged_h << 3);
   return GBF_OK;
 }
 

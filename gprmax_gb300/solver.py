@@ -332,8 +332,8 @@ class DeviceModel:
 
     def step_info(self):
         """How the model steps: {'fused': bool, 'tj', 'nch', 'planes', 'blocks', 'tuned',
-        'buffer', 'two_buffers', 'fused_available', 'staged'} (``gbf_step_info``; 'staged': the
-        E half-step is the staged sweep)."""
+        'buffer', 'two_buffers', 'fused_available', 'staged', 'staged_h'} (``gbf_step_info``;
+        'staged', 'staged_h': the E, H half-step is the staged sweep)."""
         info = np.zeros(8, dtype=np.int32)
         self._check(self.lib.gbf_step_info(self.ctx, _ptr(info)))
         keys = ('fused', 'tj', 'nch', 'planes', 'blocks', 'tuned', 'buffer', 'two_buffers')
@@ -341,6 +341,7 @@ class DeviceModel:
         out['fused'] = bool(out['fused'])
         out['fused_available'] = bool(out['two_buffers'] & 2)
         out['staged'] = bool(out['two_buffers'] & 4)
+        out['staged_h'] = bool(out['two_buffers'] & 8)
         out['two_buffers'] = bool(out['two_buffers'] & 1)
         return out
 

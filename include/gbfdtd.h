@@ -74,9 +74,9 @@ typedef struct gbf_grid_desc {
                                     model with others whose state is complex); bit 3: advance
                                     every iteration with the two half-step kernels even where
                                     the fused step applies (see gbf_run); bit 4: take the plain
-                                    E half-step kernel even where the staged one applies (3D
-                                    grids with at most 1024 materials and no poles or at most
-                                    two Debye-like poles: its inputs are copied chunk by chunk
+                                    half-step kernels even where the staged ones apply (3D
+                                    grids with at most 1024 materials, for E no poles or at most
+                                    two Debye-like poles: their inputs are copied chunk by chunk
                                     into shared memory ahead of the threads that update them;
                                     the same results bit for bit); other bits 0 */
     int32_t ntl;                 /* transmission lines among the nsrc sources */
@@ -161,8 +161,8 @@ int gbf_reset(gbf_ctx* ctx);
  * run of each model shape in the process each use one candidate (twice round; the model
  * advances as usual, the choice changing no result) and the fastest is kept from then on.
  * Models with PML slabs take the half-step kernels (measured faster there) unless
- * gbf_set_fused_tiles selects the fused step. The E half-step is the staged sweep where it
- * applies (options bit 4); its waits for shared-memory stages are bounded, and one that ran out
+ * gbf_set_fused_tiles selects the fused step. The half-steps are staged sweeps where they
+ * apply (options bit 4); their waits for shared-memory stages are bounded, and one that ran out
  * makes GBF_RUN_CHECK, gbf_download_rx and gbf_download_fields return GBF_ECUDA. */
 int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
 
@@ -221,9 +221,10 @@ int gbf_fused_tiles(int32_t nx, int32_t ny, int32_t nz, int32_t tj, int32_t nch,
 /* How the context steps: info[0] 1 for the fused step (0: two half-step kernels), [1] its tile
  * height in j, [2] chunks along x, [3] planes per chunk, [4] blocks per launch, [5] 1 once the
  * step form and tiles are chosen, [6] the field buffer holding the current iteration, [7] bit 0
- * the second buffer exists, bit 1 a fused kernel exists for the model, bit 2 the E half-step is
- * the staged sweep (its inputs copied into shared memory by bulk copies; options bit 4). No
- * counterpart in the reference (its GPU solver has one fixed launch shape, grid.py:103). */
+ * the second buffer exists, bit 1 a fused kernel exists for the model, bits 2 and 3 the E and
+ * the H half-step are staged sweeps (their inputs copied into shared memory by bulk copies;
+ * options bit 4). No counterpart in the reference (its GPU solver has one fixed launch shape,
+ * grid.py:103). */
 int gbf_step_info(gbf_ctx* ctx, int32_t info[8]);
 
 /* Run `nsteps` iterations like gbf_run, bracketed by CUDA events recorded on the context

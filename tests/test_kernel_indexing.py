@@ -261,12 +261,12 @@ def test_pack_ids_on_the_host(native_lib):
 
 
 def _staged_consumers():
-    """kStagedC of staged_e.cuh: consumer warps per block, one node per consumer thread per
+    """kStagedC of staged.cuh: consumer warps per block, one node per consumer thread per
     chunk (chunks of L = 32 kStagedC nodes, copies of L + 8 floats)."""
     import os
     import re
     src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), '..', 'gprmax_gb300',
-                            'csrc', 'staged_e.cuh')).read()
+                            'csrc', 'staged.cuh')).read()
     assert re.search(r'kStageL = 32 \* kStagedC;', src)
     assert re.search(r'kStageSpan = kStageL \+ 8;', src)
     return int(re.search(r'kStagedC = (\d+);', src).group(1))
@@ -297,9 +297,9 @@ def test_fast_division():
         np.testing.assert_array_equal(q(n).astype(np.int64), n // d)
 
 
-def _staged_sweep(lib, n3, thick, planes=None):
-    """The staged E sweep's chunks, restated: host geometry (gbfdtd.cu configure_staged) and
-    device arithmetic (staged_e.cuh stage_chunk's header, the consumer loop). Checks every copy
+def _staged_sweep(lib, n3, thick, electric=True, planes=None):
+    """The staged sweep's chunks (E, or H), restated: host geometry (gbfdtd.cu staged_geom) and
+    device arithmetic (staged.cuh stage_chunk's header, the consumer loop). Checks every copy
     and every shared-memory read a node makes, and returns the flat indices of the updated
     nodes and each chunk's core flag."""
     nx, ny, nz = n3
@@ -310,24 +310,27 @@ def _staged_sweep(lib, n3, thick, planes=None):
     npts = (nx + 1) * sx
     ncomp = (npts + 63) & ~63
     assert ncomp >= 2 * W, 'grid too small for the staged sweep'
-    i0, j0, _, bi, bj, _, _, _, _, count = _boxes(lib, n3, thick, True)[0]
+    i0, j0, _, bi, bj, _, _, _, _, count = _boxes(lib, n3, thick, electric)[0]
     ilo, ihi = i0, i0 + (bi if count else 0)
     jlo, jhi = j0, j0 + (bj if count else 0)
-    cpp = (ny * sy + 3 + L - 1) // L
+    plen = ny * sy if electric else sx
+    nplanes = nx if electric else nx + 1
+    cpp = (plen + 3 + L - 1) // L
     amax = ncomp - W
-    c = np.arange(nx * cpp, dtype=np.int64)
+    c = np.arange(nplanes * cpp, dtype=np.int64)
     if planes is not None:
         c = np.concatenate([np.arange(p * cpp, (p + 1) * cpp) for p in planes])
     i = c if cpp == 1 else _fast_div(cpp)(c).astype(np.int64)
     np.testing.assert_array_equal(i, c // cpp)
     s = ((i * sx) & ~3) + (c - i * cpp) * L
+    dj, di = (-sy, -sx) if electric else (sy, sx)
     clamp = lambda a: np.clip(a, 0, amax)
-    aE, aH = clamp(s), clamp(s - 4)
-    aJ, aI = clamp((s - sy) & ~3), clamp((s - sx) & ~3)
+    aE, aH = clamp(s), clamp(s - 4 if electric else s)
+    aJ, aI = clamp((s + dj) & ~3), clamp((s + di) & ~3)
     for a in (aE, aH, aJ, aI):      # 16-byte aligned starts, copies inside their arrays
         assert (a % 4 == 0).all() and (a >= 0).all() and (a + W <= ncomp).all()
     shE, shH = s - aE, s - aH
-    shJ, shI = s - sy - aJ, s - sx - aI
+    shJ, shI = s + dj - aJ, s + di - aI
     # the header's row and column of node s, and each consumer thread's offsets from it
     by_sy = _fast_div(sy)
     f = s - i * sx
@@ -344,22 +347,54 @@ def _staged_sweep(lib, n3, thick, planes=None):
     J = np.where(wrap, J + 1, J)
     r = t[None, :]
     assert (J * sy + K == f[:, None] + r).all() and (K >= 0).all() and (K < sy).all()
-    valid = (J >= 0) & (J < ny) & (K < nz)
     I = np.broadcast_to(i[:, None], J.shape)
     # every shared-memory read a node makes lies inside its stream's span
     inspan = lambda x, m: ((x >= 0) & (x < W))[m].all()
-    assert inspan(shE[:, None] + r, valid)                        # E, packed word, pole state
-    assert inspan(shH[:, None] + r, valid)                        # own H
-    assert inspan(shH[:, None] + r - 1, valid & (K >= 1))         # H at k - 1
-    assert inspan(shJ[:, None] + r, valid & (J >= 1))             # H at j - 1
-    assert inspan(shI[:, None] + r, valid & (I >= 1))             # H at i - 1
+    if electric:
+        valid = (J >= 0) & (J < ny) & (K < nz)
+        assert inspan(shE[:, None] + r, valid)                    # E, packed word, pole state
+        assert inspan(shH[:, None] + r, valid)                    # own H
+        assert inspan(shH[:, None] + r - 1, valid & (K >= 1))     # H at k - 1
+        assert inspan(shJ[:, None] + r, valid & (J >= 1))         # H at j - 1
+        assert inspan(shI[:, None] + r, valid & (I >= 1))         # H at i - 1
+    else:
+        valid = (J >= 0) & (J <= ny)
+        assert (shH == shE).all()
+        assert inspan(shE[:, None] + r, valid)                    # own E, H, packed word
+        assert inspan(shE[:, None] + r + 1, valid & (K < nz))     # E at k + 1
+        assert inspan(shJ[:, None] + r, valid & (J < ny))         # E at j + 1
+        assert inspan(shI[:, None] + r, valid & (I < nx))         # E at i + 1
     # the core test: a core chunk's nodes lie in the core box, so its node code may skip the x
     # and y tests
-    jl = by_sy(np.minimum(f + L - 1, ny * sy - 1)).astype(np.int64)
+    jl = by_sy(np.minimum(f + L - 1, plen - 1)).astype(np.int64)
     core = (i >= ilo) & (i < ihi) & (jf >= jlo) & (jl < jhi)
     m = valid & core[:, None]
     assert ((I[m] >= ilo) & (I[m] < ihi) & (J[m] >= jlo) & (J[m] < jhi)).all()
-    assert (I[m] >= 1).all() and (J[m] >= 1).all()
+    assert (I[m] >= 1).all() and (J[m] >= 1).all() and (I[m] < nx).all() and (J[m] < ny).all()
+    # the z slabs' Phi state: the copies of the chunk's rows hold every element its slab nodes
+    # read, for each CFS order (the second order's elements ocount further on)
+    Tz = (thick[2], thick[5])
+    if max(Tz):
+        zspan = ((((L + 2) // sy + 2) * max(Tz) + 3 + 3) // 4) * 4
+        j0 = np.maximum(jf, 0)
+        j1 = np.minimum(jl, ny - 1)
+        zrows = (j0 <= j1) & (True if electric else (i < nx))
+        for side in (0, 1):
+            T = Tz[side]
+            if not T:
+                continue
+            where, pr = axis_member(K, nz, Tz[0], Tz[1], electric)
+            node = valid & (where == side + 1)
+            if not electric:
+                node &= (I < nx) & (J < ny) & (K < nz)
+            assert not (node & ~zrows[:, None]).any()
+            ocount = T * nx * ny
+            pidx = (I * ny + J) * T + pr
+            lo = (i * ny + j0) * T
+            for o in range(2):
+                a = (lo + o * ocount) & ~3
+                off = pidx + o * ocount - a[:, None]
+                assert ((off >= 0) & (off < zspan))[node].all()
     idx = (s[:, None] + r)[valid]
     assert (idx == (I * sx + J * sy + K)[valid]).all()
     return idx, core
@@ -371,33 +406,37 @@ def _staged_sweep(lib, n3, thick, planes=None):
                                       ((20, 18, 16), (0, 0, 0, 0, 0, 0)),
                                       ((20, 37, 64), (3, 5, 10, 2, 4, 10)),
                                       ((60, 50, 40), (10, 0, 5, 10, 7, 0))])
-def test_staged_sweep_covers_the_e_domain_once(native_lib, n3, thick):
-    """The staged E half-step (staged_e.cuh) updates every node of the E domain exactly once,
-    reads only inside the spans its bulk copies filled (copies aligned, inside their arrays),
-    and runs the core node code only on chunks inside the core box."""
+@pytest.mark.parametrize('electric', [True, False])
+def test_staged_sweep_covers_the_domain_once(native_lib, n3, thick, electric):
+    """The staged half-steps (staged.cuh) update every node of their domain exactly once, read
+    only inside the spans their bulk copies filled (copies aligned, inside their arrays), and
+    run the core node code only on chunks inside the core box."""
     nx, ny, nz = n3
     W = 32 * _staged_consumers() + 8
     if ((nx + 1) * (ny + 1) * (nz + 1) + 63) & ~63 < 2 * W:
         pytest.skip('grid below the staged sweep\'s minimum')
-    idx, core = _staged_sweep(native_lib, n3, thick)
+    idx, core = _staged_sweep(native_lib, n3, thick, electric)
     sy, sx = nz + 1, (ny + 1) * (nz + 1)
-    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing='ij')
+    ext = (nx, ny, nz) if electric else (nx + 1, ny + 1, nz + 1)
+    ii, jj, kk = np.meshgrid(*(np.arange(e) for e in ext), indexing='ij')
     want = np.sort((ii * sx + jj * sy + kk).ravel())
     np.testing.assert_array_equal(np.sort(idx), want)
 
 
-def test_staged_sweep_at_the_benchmark_size(native_lib):
+@pytest.mark.parametrize('electric', [True, False])
+def test_staged_sweep_at_the_benchmark_size(native_lib, electric):
     """The 400 x 400 x 200 soil: the first, second, a middle, the second-last and the last
-    plane, checked as above; most chunks of a middle plane take the core code."""
+    planes, checked as above; most chunks of a middle plane take the core code."""
     n3, thick = (400, 400, 200), (10,) * 6
-    planes = (0, 1, 11, 200, 389, 390, 398, 399)
-    idx, core = _staged_sweep(native_lib, n3, thick, planes)
+    planes = (0, 1, 11, 200, 389, 390, 398, 399) + (() if electric else (400,))
+    idx, core = _staged_sweep(native_lib, n3, thick, electric, planes)
     sy, sx = 201, 401 * 201
     for p in planes:
         got = np.sort(idx[(idx >= p * sx) & (idx < (p + 1) * sx)])
-        jj, kk = np.meshgrid(np.arange(400), np.arange(200), indexing='ij')
+        ext = (400, 200) if electric else (401, 201)
+        jj, kk = np.meshgrid(np.arange(ext[0]), np.arange(ext[1]), indexing='ij')
         np.testing.assert_array_equal(got, np.sort((p * sx + jj * sy + kk).ravel()))
     L = 32 * _staged_consumers()
-    cpp = (400 * 201 + 3 + L - 1) // L
+    cpp = ((400 * 201 if electric else sx) + 3 + L - 1) // L
     mid = core[planes.index(200) * cpp:(planes.index(200) + 1) * cpp]
     assert mid.mean() > 0.85 and not core[:cpp].any()
