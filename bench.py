@@ -361,7 +361,7 @@ def run_gb300(args):
                    'step_ms_profiled': ms_t / npf}
     else:
         kernels = {'h_half_step': {'ms': t_h * 1e3, 'bytes': bytes_h,
-                                   'GBps': round(bytes_h / t_h / 1e9, 1)},
+                                   'GBps': round(bytes_h / t_h / 1e9, 1), 'staged': step['staged_h']},
                    'e_half_step': {'ms': t_e * 1e3, 'bytes': bytes_e,
                                    'GBps': round(achieved, 1), 'staged': step['staged']},
                    'step_ms_profiled': ms_t / npf}

@@ -93,7 +93,12 @@ struct gbf_ctx {
   std::vector<cudaEvent_t> tune_ev;             // two events per timed step
   int tune_next = 0;
   // staged half-steps (staged.cuh): used where they apply unless option bit 4 is set
-  int staged = 0, staged_h = 0;
+  int staged = 0, staged_h = 0;       // the step's E / H half-step is the staged sweep
+  int staged_av = 0;                  // where a staged sweep applies: bit 0 E, bit 1 H
+  int forms_tuned = 1;                // staged or plain chosen (by the form tuner or the caller)
+  std::vector<int> form_cand;         // combinations being timed (bit 0 staged E, bit 1 staged H)
+  std::vector<cudaEvent_t> form_ev;   // two events per timed step
+  int form_next = 0;
   SKernFn sk = nullptr, skh = nullptr;
   StagedGeom sg{}, sgh{};
   size_t smem_st = 0, smem_sth = 0;
@@ -103,6 +108,8 @@ struct gbf_ctx {
 static std::string g_create_err;
 static void tune_release(gbf_ctx* ctx);
 static void configure_staged(gbf_ctx* ctx);
+static void form_release(gbf_ctx* ctx);
+static bool form_cached(gbf_ctx* ctx);
 
 static void invalidate_graph(gbf_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -348,6 +355,8 @@ int gbf_last_error(gbf_ctx* ctx, char* buf, size_t n) {
 void gbf_destroy(gbf_ctx* ctx) {
   if (!ctx) return;
   for (cudaEvent_t e : ctx->tune_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->form_ev)
     if (e) cudaEventDestroy(e);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -672,7 +681,6 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   ctx->grid_h = 0;
   ctx->grid_e = 0;
   invalidate_graph(ctx);
-  configure_staged(ctx);
   // one fused kernel per step where the model allows it (tiles tuned at the first run)
   tune_release(ctx);
   ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
@@ -690,6 +698,8 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
     ctx->fused = 1;
     ctx->tuned = 1;
   }
+  // the staged half-steps and whether their form is still to be chosen
+  configure_staged(ctx);
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -1250,8 +1260,10 @@ static bool staged_geom(gbf_ctx* ctx, bool electric, int nstream, size_t tables,
 // with real state; a ring of at least two stages that fits in shared memory beside the tables.
 // Option bit 4 keeps the plain kernels.
 static void configure_staged(gbf_ctx* ctx) {
-  ctx->staged = ctx->staged_h = 0;
+  ctx->staged = ctx->staged_h = ctx->staged_av = 0;
   ctx->sk = ctx->skh = nullptr;
+  form_release(ctx);
+  ctx->forms_tuned = 1;
   const gbf_grid_desc& d = ctx->d;
   const StepParams& p = ctx->sp;
   const int np = d.maxpoles;
@@ -1275,6 +1287,9 @@ static void configure_staged(gbf_ctx* ctx) {
     ctx->skh = kh;
     ctx->staged_h = 1;
   }
+  ctx->staged_av = ctx->staged | (ctx->staged_h << 1);
+  // staged where available until the form tuner (or an earlier model of this shape) decides
+  ctx->forms_tuned = ctx->staged_av == 0 || form_cached(ctx);
 }
 
 // A staged sweep that gave up waiting for a stage leaves the error word set (read and cleared
@@ -1397,6 +1412,84 @@ static void tune_release(gbf_ctx* ctx) {
   ctx->tune_ev.clear();
   ctx->tune_cand.clear();
   ctx->tune_next = 0;
+}
+
+// ---- half-step form tuner ---------------------------------------------------------------
+// Where a staged sweep applies, each half-step can run staged or plain, with the same results
+// bit for bit; which is faster depends on the model (how much its nodes wait on memory against
+// the staging's own work per chunk). The first steps of the first run of each model shape time
+// every combination (kTuneReps rounds; the H and E kernels of a real step between two events)
+// and keep the fastest, for the model and, per shape, for the process.
+static std::map<TuneKey, int> g_form;
+
+static void form_release(gbf_ctx* ctx) {
+  for (cudaEvent_t e : ctx->form_ev)
+    if (e) cudaEventDestroy(e);
+  ctx->form_ev.clear();
+  ctx->form_cand.clear();
+  ctx->form_next = 0;
+}
+
+static void set_forms(gbf_ctx* ctx, int f) {
+  ctx->staged = f & 1;
+  ctx->staged_h = (f >> 1) & 1;
+}
+
+static bool form_cached(gbf_ctx* ctx) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto f = g_form.find(tune_key(ctx));
+  if (f == g_form.end()) return false;
+  set_forms(ctx, f->second & ctx->staged_av);
+  return true;
+}
+
+// One timed step with the next combination; after the last one, pick.
+static int form_step(gbf_ctx* ctx) {
+  if (ctx->form_cand.empty()) {
+    for (int f = 0; f < 4; ++f)
+      if (!(f & ~ctx->staged_av)) ctx->form_cand.push_back(f);
+    ctx->form_ev.assign(2 * ctx->form_cand.size() * kTuneReps, nullptr);
+    for (auto& e : ctx->form_ev)
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        (void)cudaGetLastError();
+        form_release(ctx);
+        set_forms(ctx, ctx->staged_av);
+        ctx->forms_tuned = 1;
+        return GBF_OK;
+      }
+    ctx->form_next = 0;
+    invalidate_graph(ctx);
+  }
+  const int nc = (int)ctx->form_cand.size();
+  const int q = ctx->form_next;
+  set_forms(ctx, ctx->form_cand[q % nc]);
+  CK(cudaEventRecord(ctx->form_ev[2 * q], ctx->stream));
+  launch_h(ctx);
+  launch_tl(ctx);
+  launch_e(ctx);
+  CK(cudaEventRecord(ctx->form_ev[2 * q + 1], ctx->stream));
+  launch_end(ctx);
+  CK(cudaGetLastError());
+  ctx->form_next = q + 1;
+  if (ctx->form_next < nc * kTuneReps) return GBF_OK;
+  CK(cudaEventSynchronize(ctx->form_ev.back()));
+  std::vector<float> best(nc, 1e30f);
+  for (int r = 0; r < nc * kTuneReps; ++r) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ctx->form_ev[2 * r], ctx->form_ev[2 * r + 1]));
+    if (ms < best[r % nc]) best[r % nc] = ms;
+  }
+  int pick = 0;
+  for (int k = 1; k < nc; ++k)
+    if (best[k] < best[pick]) pick = k;
+  set_forms(ctx, ctx->form_cand[pick]);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_form[tune_key(ctx)] = ctx->form_cand[pick];
+  }
+  form_release(ctx);
+  ctx->forms_tuned = 1;
+  return GBF_OK;
 }
 
 // Decide whether the model needs tuning steps and set up the candidates (once).
@@ -1545,7 +1638,13 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
       if (t > it && t - it < span) span = t - it;
     }
     int n = span;
-    // while the fused step's tiles are being chosen: one timed candidate step at a time
+    // while the half-step forms, then the fused step's tiles are being chosen: one timed
+    // candidate step at a time
+    while (n > 0 && !ctx->forms_tuned) {
+      int rc = form_step(ctx);
+      if (rc) return rc;
+      --n;
+    }
     while (n > 0 && ctx->fused_avail && !ctx->tuned) {
       int rc = tune_step(ctx);
       if (rc) return rc;
@@ -1723,6 +1822,19 @@ int gbf_set_fused_tiles(gbf_ctx* ctx, int32_t tj, int32_t nch) {
   return GBF_OK;
 }
 
+int gbf_set_step_forms(gbf_ctx* ctx, int32_t forms) {
+  if (!ctx) return GBF_EINVAL;
+  if (forms < 0 || forms > 3) return fail(ctx, GBF_EINVAL, "gbf_set_step_forms: forms %d (0..3)", forms);
+  if (forms & ~ctx->staged_av)
+    return fail(ctx, GBF_EINVAL, "gbf_set_step_forms: a staged sweep asked for (%d) does not apply "
+                "to the model (available: %d)", forms, ctx->staged_av);
+  form_release(ctx);
+  set_forms(ctx, forms);
+  ctx->forms_tuned = 1;
+  invalidate_graph(ctx);
+  return GBF_OK;
+}
+
 int gbf_step_info(gbf_ctx* ctx, int32_t info[8]) {
   if (!ctx || !info) return GBF_EINVAL;
   info[0] = ctx->fused;
@@ -1732,7 +1844,8 @@ int gbf_step_info(gbf_ctx* ctx, int32_t info[8]) {
   info[4] = ctx->fused ? ctx->f_blocks : 0;
   info[5] = ctx->tuned;
   info[6] = ctx->cur;
-  info[7] = ctx->fused_ok | (ctx->fused_avail << 1) | (ctx->staged << 2) | (ctx->staged_h << 3);
+  info[7] = ctx->fused_ok | (ctx->fused_avail << 1) | (ctx->staged << 2) | (ctx->staged_h << 3) |
+            (ctx->forms_tuned << 4) | (ctx->staged_av << 5);
   return GBF_OK;
 }
 

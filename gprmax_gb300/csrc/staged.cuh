@@ -196,6 +196,16 @@ __device__ __forceinline__ void stage_chunk(const StepParams& p, const StagedGeo
   int zcopies = 0;
   if (zrows)
     for (int side = 0; side < 2; ++side) zcopies += p.slab[2 + 3 * side].T ? 2 * order : 0;
+  // the z copies' first elements, written to the header before the arrival below releases it
+  if (zrows) {
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const Slab& sl = p.slab[2 + 3 * side];
+#pragma unroll
+      for (int o = 0; o < order; ++o)
+        h[kHdrZ + 2 * side + o] = ((i * p.ny + j0) * sl.T + o * sl.ocount) & ~3;
+    }
+  }
   constexpr uint32_t bytes = W * sizeof(float);
   float* d = ring + (size_t)st * g.stage_floats;
   // the arrival releases the header to the consumers that wait on this phase
@@ -206,11 +216,9 @@ __device__ __forceinline__ void stage_chunk(const StepParams& p, const StagedGeo
     for (int side = 0; side < 2; ++side) {
       const Slab& sl = p.slab[2 + 3 * side];
       if (!sl.T) continue;
-      const int lo = (i * p.ny + j0) * sl.T;
 #pragma unroll
       for (int o = 0; o < order; ++o) {
-        const int a = (lo + o * sl.ocount) & ~3;
-        h[kHdrZ + 2 * side + o] = a;
+        const int a = h[kHdrZ + 2 * side + o];
         const float* src1 = ELECTRIC ? sl.phiE1 : sl.phiH1;
         const float* src2 = ELECTRIC ? sl.phiE2 : sl.phiH2;
         bulk_copy(z + ((side * 2 + 0) * order + o) * g.zspan, src1 + a, g.zspan * 4u, bar);

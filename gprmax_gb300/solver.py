@@ -332,8 +332,9 @@ class DeviceModel:
 
     def step_info(self):
         """How the model steps: {'fused': bool, 'tj', 'nch', 'planes', 'blocks', 'tuned',
-        'buffer', 'two_buffers', 'fused_available', 'staged', 'staged_h'} (``gbf_step_info``;
-        'staged', 'staged_h': the E, H half-step is the staged sweep)."""
+        'buffer', 'two_buffers', 'fused_available', 'staged', 'staged_h', 'forms_tuned',
+        'staged_available', 'staged_h_available'} (``gbf_step_info``; 'staged', 'staged_h': the
+        E, H half-step is the staged sweep)."""
         info = np.zeros(8, dtype=np.int32)
         self._check(self.lib.gbf_step_info(self.ctx, _ptr(info)))
         keys = ('fused', 'tj', 'nch', 'planes', 'blocks', 'tuned', 'buffer', 'two_buffers')
@@ -342,8 +343,16 @@ class DeviceModel:
         out['fused_available'] = bool(out['two_buffers'] & 2)
         out['staged'] = bool(out['two_buffers'] & 4)
         out['staged_h'] = bool(out['two_buffers'] & 8)
+        out['forms_tuned'] = bool(out['two_buffers'] & 16)
+        out['staged_available'] = bool(out['two_buffers'] & 32)
+        out['staged_h_available'] = bool(out['two_buffers'] & 64)
         out['two_buffers'] = bool(out['two_buffers'] & 1)
         return out
+
+    def set_step_forms(self, e_staged, h_staged):
+        """Fix each half-step's form: the staged sweep or the plain kernel
+        (``gbf_set_step_forms``; the results are the same bit for bit)."""
+        self._check(self.lib.gbf_set_step_forms(self.ctx, int(bool(e_staged)) | 2 * int(bool(h_staged))))
 
     def set_fused_tiles(self, tj, nch):
         """Fix the fused step's tiling (tile height ``tj`` rows, ``nch`` chunks along x)."""

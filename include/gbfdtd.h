@@ -161,9 +161,11 @@ int gbf_reset(gbf_ctx* ctx);
  * run of each model shape in the process each use one candidate (twice round; the model
  * advances as usual, the choice changing no result) and the fastest is kept from then on.
  * Models with PML slabs take the half-step kernels (measured faster there) unless
- * gbf_set_fused_tiles selects the fused step. The half-steps are staged sweeps where they
- * apply (options bit 4); their waits for shared-memory stages are bounded, and one that ran out
- * makes GBF_RUN_CHECK, gbf_download_rx and gbf_download_fields return GBF_ECUDA. */
+ * gbf_set_fused_tiles selects the fused step. Where a staged sweep applies to a half-step
+ * (options bit 4), staged or plain is chosen the same way (every combination timed on the first
+ * steps of the first run of each model shape; gbf_set_step_forms fixes it); the staged sweeps'
+ * waits for shared-memory stages are bounded, and one that ran out makes GBF_RUN_CHECK,
+ * gbf_download_rx and gbf_download_fields return GBF_ECUDA. */
 int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
 
 /* Iteration the next gbf_run call starts at. */
@@ -223,9 +225,16 @@ int gbf_fused_tiles(int32_t nx, int32_t ny, int32_t nz, int32_t tj, int32_t nch,
  * step form and tiles are chosen, [6] the field buffer holding the current iteration, [7] bit 0
  * the second buffer exists, bit 1 a fused kernel exists for the model, bits 2 and 3 the E and
  * the H half-step are staged sweeps (their inputs copied into shared memory by bulk copies;
- * options bit 4). No counterpart in the reference (its GPU solver has one fixed launch shape,
- * grid.py:103). */
+ * options bit 4), bit 4 set once staged or plain is chosen for each, bits 5 and 6 a staged
+ * sweep applies to E, to H. No counterpart in the reference (its GPU solver has one fixed launch
+ * shape, grid.py:103). */
 int gbf_step_info(gbf_ctx* ctx, int32_t info[8]);
+
+/* Fix the form of the half-steps: bit 0 the staged E sweep, bit 1 the staged H sweep (clear:
+ * the plain kernel), instead of choosing by timing at the first run. GBF_EINVAL when a staged
+ * sweep asked for does not apply to the model. The results are the same bit for bit. No
+ * counterpart in the reference. */
+int gbf_set_step_forms(gbf_ctx* ctx, int32_t forms);
 
 /* Run `nsteps` iterations like gbf_run, bracketed by CUDA events recorded on the context
  * stream; blocks until done and returns the elapsed device milliseconds in *ms. */

@@ -21,10 +21,12 @@ STAGED_MODELS = ['fs_hori1', 'pml_off', 'hori2', 'mri1', 'mri2', 'debye1', 'face
                  'fractal', 'rough', 'rxarray', 'tline', 'triangles', 'mixed']
 
 
-def _run(G, options, nsteps=None):
+def _run(G, options, nsteps=None, forms=None):
     from gprmax_gb300.solver import DeviceModel
     dm = DeviceModel(G, options)
     try:
+        if forms is not None:
+            dm.set_step_forms(*forms)
         dm.run(nsteps)
         out = {'rx': dm.receivers(), 'f': dm.fields(), 'info': dm.step_info()}
         if G.maxpoles:
@@ -45,21 +47,28 @@ def _equal(a, b):
 def test_staged_e_half_step_equals_plain(native, name):
     from gprmax_gb300.model import build_grid
     G = build_grid(MODELS[name].splitlines(True), messages=False)
-    got = _run(G, 8)
+    cplx = name == 'mixed'      # complex poles: E keeps the plain kernel
+    got = _run(G, 8, forms=(not cplx, True))
     ref = _run(G, 8 | 16)
     assert got['info']['staged_h'], 'model {} should take the staged H half-step'.format(name)
-    if name != 'mixed':     # complex poles: E keeps the plain kernel
-        assert got['info']['staged'], 'model {} should take the staged E half-step'.format(name)
+    assert got['info']['staged'] == (not cplx)
     assert not ref['info']['staged'] and not ref['info']['staged_h']
     _equal(got, ref)
+    # each staged sweep alone, and the forms the tuner keeps
+    _equal(_run(G, 8, forms=(False, True)), ref)
+    if not cplx:
+        _equal(_run(G, 8, forms=(True, False)), ref)
+    tuned = _run(G, 8)
+    assert tuned['info']['forms_tuned']
+    _equal(tuned, ref)
 
 
 def test_staged_against_oracle(native):
     import oracle
     from gprmax_gb300.model import build_grid
     G = build_grid(MODELS['debye1'].splitlines(True), messages=False)
-    got = _run(G, 8)
-    assert got['info']['staged']
+    got = _run(G, 8, forms=(True, True))
+    assert got['info']['staged'] and got['info']['staged_h']
     ref = oracle.OracleSolver(G).run()
     np.testing.assert_array_equal(got['rx'], ref.receivers())
     np.testing.assert_array_equal(got['f'], ref.fields())
@@ -67,11 +76,19 @@ def test_staged_against_oracle(native):
 
 def test_complex_poles_keep_the_plain_kernel(native):
     """Complex pole state (option bit 2) is not staged: the plain kernel runs, and the results
-    are the staged run's."""
+    are the staged run's; asking for the staged E sweep there is refused."""
     from gprmax_gb300.model import build_grid
     G = build_grid(MODELS['debye1'].splitlines(True), messages=False)
     cplx = _run(G, 8 | 4)
-    assert not cplx['info']['staged']
+    assert not cplx['info']['staged'] and not cplx['info']['staged_available']
+    from gprmax_gb300.exceptions import SolverError
+    from gprmax_gb300.solver import DeviceModel
+    dm = DeviceModel(G, 8 | 4)
+    try:
+        with pytest.raises(SolverError):
+            dm.set_step_forms(True, True)
+    finally:
+        dm.close()
     real = _run(G, 8)
     np.testing.assert_array_equal(cplx['rx'], real['rx'])
     np.testing.assert_array_equal(cplx['f'], real['f'])
@@ -83,7 +100,7 @@ def test_staged_soil(native):
     keeps) equals both."""
     from gprmax_gb300 import workloads
     G = workloads.dispersive_soil(nx=160, ny=160, nz=80, surface=60, timewindow='3e-9')
-    got = _run(G, 8, 300)
+    got = _run(G, 8, 300, forms=(True, True))
     ref = _run(G, 8 | 16, 300)
     assert got['info']['staged'] and got['info']['staged_h']
     _equal(got, ref)
