@@ -42,6 +42,8 @@ WORKLOAD = 'dispersive_soil_400x400x200_debye50_pml10'
 # the 400x400x200 workload), else the small capture's `dram_bytes_per_cell:` line scaled by cells
 TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'half_step_traffic_dispersive_soil_400x400x200.md')
 TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'e_half_step_dispersive_soil_256x256x128.md')
+STAGED_TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'e_half_step_staged_traffic_dispersive_soil_400x400x200.md')
+STAGED_TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'e_half_step_staged_dispersive_soil_256x256x128.md')
 # the same two lines for the fused step kernel
 FUSED_TRAFFIC_FULL = os.path.join(ROOT, 'profiles', 'fused_step_traffic_dispersive_soil_400x400x200.md')
 FUSED_TRAFFIC_PROFILE = os.path.join(ROOT, 'profiles', 'fused_step_dispersive_soil_256x256x128.md')
@@ -58,11 +60,12 @@ def _profile_value(path, key):
     return None
 
 
-def measured_traffic(cells, fused=False):
-    """DRAM bytes of one launch of the dominant kernel (the fused step, or the E half-step) over
-    `cells` cells (ncu), and where they came from."""
-    full_path = FUSED_TRAFFIC_FULL if fused else TRAFFIC_FULL
-    small_path = FUSED_TRAFFIC_PROFILE if fused else TRAFFIC_PROFILE
+def measured_traffic(cells, fused=False, staged=False):
+    """DRAM bytes of one launch of the dominant kernel (the fused step, or the E half-step,
+    staged or plain) over `cells` cells (ncu), and where they came from."""
+    full_path = FUSED_TRAFFIC_FULL if fused else (STAGED_TRAFFIC_FULL if staged else TRAFFIC_FULL)
+    small_path = (FUSED_TRAFFIC_PROFILE if fused else
+                  (STAGED_TRAFFIC_PROFILE if staged else TRAFFIC_PROFILE))
     full = _profile_value(full_path, 'dram_bytes_per_launch')
     full_cells = _profile_value(full_path, 'cells')
     if full is not None and full_cells == cells:
@@ -353,7 +356,7 @@ def run_gb300(args):
     t_e = ms_e / npf / 1e3
     t_h = ms_h / npf / 1e3
     achieved = bytes_e / t_e / 1e9
-    traffic, traffic_src = measured_traffic(cells, fused)
+    traffic, traffic_src = measured_traffic(cells, fused, step['staged'])
     if fused:
         kernels = {'fused_step': {'ms': t_e * 1e3, 'bytes': bytes_e, 'GBps': round(achieved, 1),
                                   'tile_rows': step['tj'], 'chunks': step['nch'],
