@@ -404,13 +404,14 @@ def dm_bytes(G):
     return G.memory_estimate()
 
 
-def upload_bytes(G, packed=None):
+def upload_bytes(G, packed=None, materials=True):
     """Host bytes a model's upload copies to the device: material IDs (two packed words per node
-    when ``packed``, else the ID array), coefficient tables, PML profiles and the sources'
-    waveform tables."""
+    when ``packed``, else the ID array) and coefficient tables (unless ``materials`` is false:
+    a model sharing another's), PML profiles and the sources' waveform tables."""
     ids = sum(w.array.nbytes for w in packed) if packed else G.ID.nbytes
-    return (ids + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
-            + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)
+    mats = (ids + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
+            + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)) if materials else 0
+    return (mats
             + sum(8 * getattr(p, 'ERA').nbytes for p in G.pmls)
             + len(G.hertziandipoles + G.voltagesources + G.magneticdipoles) * G.iterations * 4)
 
@@ -571,25 +572,34 @@ def run_bscan2d(args):
 
     grid_info = {}
 
-    def batched():
+    shared_models = []
+
+    def batched(share=True):
         t0 = time.perf_counter()
-        bm = BatchModel(grids)
+        bm = BatchModel(grids, share_geometry=share)
         setup = time.perf_counter() - t0
         dev = bm.run_timed(iters)
         traces = bm.receivers()
-        grid_info.update(bm.info())
+        if share:
+            grid_info.update(bm.info())
+            shared_models[:] = [m.shared_from is not None for m in bm.models]
         bm.close()
         return time.perf_counter() - t0, dev, traces, setup
 
     runs_p = [plain() for _ in range(3)]
+    runs_u = [batched(False) for _ in range(3)]
     runs_b = [batched() for _ in range(3)]
-    identical = all(np.array_equal(a, b) for a, b in zip(runs_p[0][2], runs_b[0][2]))
+    identical = all(np.array_equal(a, b) and np.array_equal(a, c)
+                    for a, b, c in zip(runs_p[0][2], runs_b[0][2], runs_u[0][2]))
     wall_p = float(np.median([r[0] for r in runs_p]))
     dev_p = float(np.median([r[1] for r in runs_p]))
     wall_b = float(np.median([r[0] for r in runs_b]))
     dev_b = float(np.median([r[1] for r in runs_b]))
     setup_p = float(np.median([r[3] for r in runs_p]))
     setup_b = float(np.median([r[3] for r in runs_b]))
+    wall_u = float(np.median([r[0] for r in runs_u]))
+    setup_u = float(np.median([r[3] for r in runs_u]))
+    h2d_b = sum(upload_bytes(G, materials=not sh) for G, sh in zip(grids, shared_models))
     rx_bytes = sum(int(np.asarray(t).nbytes) for t in runs_b[0][2])
     out = {'metric': 'traces/s', 'value': round(n / wall_b, 2), 'unit': 'traces/s',
            'n_gpus': 1, 'steps': iters, 'warmup': W, 'ms_per_step': dev_b / iters,
@@ -600,7 +610,7 @@ def run_bscan2d(args):
                       'cells_per_trace': cells,
                       'l2': 'no flush: the B-scan state fits in L2 in any run of this model'},
            'e2e': {'value': round(n / wall_b, 2), 'unit': 'traces/s',
-                   'h2d_bytes_per_step': round(sum(upload_bytes(G) for G in grids) / iters, 1),
+                   'h2d_bytes_per_step': round(h2d_b / iters, 1),
                    'd2h_bytes_per_step': round(rx_bytes / iters, 1),
                    'note': 'whole B-scan per timed run: every model uploaded, run and read back'},
            'plain_sequential': {'value': round(n / wall_p, 2), 'unit': 'traces/s',
@@ -608,12 +618,16 @@ def run_bscan2d(args):
                                 'model_setup_s': round(setup_p, 4)},
            'batched': {'device_ms_all_traces': round(dev_b, 3),
                        'model_setup_s': round(setup_b, 4), 'grid': dict(grid_info),
-                       'Mcells_per_s': round(cells * n * iters / (dev_b / 1e3) / 1e6, 1)},
+                       'Mcells_per_s': round(cells * n * iters / (dev_b / 1e3) / 1e6, 1),
+                       'models_sharing_geometry': int(sum(shared_models))},
+           'batched_unshared': {'value': round(n / wall_u, 2), 'unit': 'traces/s',
+                                'model_setup_s': round(setup_u, 4),
+                                'h2d_bytes_per_step': round(sum(upload_bytes(G) for G in grids) / iters, 1)},
            'speedup_vs_plain': round(wall_p / wall_b, 3),
            'traces_identical': bool(identical),
-           # per batched B-scan: H, E and end-of-step kernels per iteration, and per model
-           # upload one kernel that packs and checks its IDs
-           'gpu_launches': 3 * iters + n,
+           # per batched B-scan: H, E and end-of-step kernels per iteration, and per uploaded
+           # geometry one kernel that packs and checks its IDs
+           'gpu_launches': 3 * iters + n - int(sum(shared_models)),
            'host_build_s': round(t_build, 3)}
     if args.cpu_baseline:
         cb = cpu_baseline(grids[0], budget_s=min(args.cpu_budget, 20.0), max_steps=iters - 1)

@@ -143,6 +143,7 @@ _SIGS = {
     'gbf_fractal_field': (ctypes.c_int, [ctypes.c_int32, _P, _P, ctypes.c_float, _P, _P]),
     'gbf_set_fused_tiles': (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     'gbf_set_step_forms': (ctypes.c_int, [_P, ctypes.c_int32]),
+    'gbf_share_materials': (ctypes.c_int, [_P, _P]),
     'gbf_fused_tiles': (ctypes.c_int, [ctypes.c_int32] * 5 + [_P]),
     'gbf_profile': (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -27,6 +28,17 @@
 #include "staged.cuh"
 
 using namespace gbf;
+
+// The device arrays that describe a model's materials (IDs, packed words, coefficient tables):
+// owned by the context that uploaded them and shared by contexts that adopt them
+// (gbf_share_materials); freed with the last context that holds them.
+struct MatSet {
+  std::vector<void*> ptrs;
+  ~MatSet() {
+    for (void* q : ptrs)
+      if (q) cudaFree(q);
+  }
+};
 
 struct gbf_ctx {
   gbf_grid_desc d;
@@ -103,6 +115,9 @@ struct gbf_ctx {
   StagedGeom sg{}, sgh{};
   size_t smem_st = 0, smem_sth = 0;
   int* d_err = nullptr;        // device error word of the staged sweeps (a wait ran out)
+  std::shared_ptr<MatSet> mats;   // holds ID, PE, PH, disp and the tables (see MatSet)
+  size_t mat_bytes = 0;        // their size
+  bool shared_mats = false;    // adopted from another context
 };
 
 static std::string g_create_err;
@@ -360,11 +375,18 @@ void gbf_destroy(gbf_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  void* ptrs[] = {ctx->fields, ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD, ctx->T, ctx->pml_mem,
-                  ctx->pml_coef, ctx->srcs, ctx->waves, ctx->rx_coords, ctx->rxs, ctx->d_it,
-                  ctx->d_err};
+  void* ptrs[] = {ctx->fields, ctx->T, ctx->pml_mem, ctx->pml_coef, ctx->srcs, ctx->waves,
+                  ctx->rx_coords, ctx->rxs, ctx->d_it, ctx->d_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  // the material arrays go with the last context holding them (freed here if never handed to
+  // a MatSet, when creation failed first)
+  if (!ctx->mats) {
+    void* mp[] = {ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD};
+    for (void* p : mp)
+      if (p) cudaFree(p);
+  }
+  ctx->mats.reset();
   for (float* p : ctx->snaps)
     if (p) cudaFree(p);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -482,6 +504,11 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     gbf_destroy(ctx);
     return rc;
   }
+  ctx->mats = std::make_shared<MatSet>();
+  ctx->mats->ptrs = {ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD};
+  ctx->mat_bytes = (ctx->idp == 1 ? 2 * sizeof(uint32_t) * ncomp : 6 * sizeof(uint32_t) * npts) +
+                   (size_t)d.nmat * (1 + 2 * sizeof(float4) + 2 * sizeof(float)) +
+                   (d.maxpoles > 0 ? sizeof(float2) * 3 * d.maxpoles * d.nmat : 0);
 
   // kernel parameters
   StepParams& p = ctx->sp;
@@ -647,6 +674,33 @@ __global__ void finish_packed_ids(uint32_t* __restrict__ pe, const uint32_t* __r
   if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
 }
 
+// Once the model's material tables are known: how it steps (fused step, staged half-steps) and
+// whether those choices are still to be timed.
+static void configure_steps(gbf_ctx* ctx) {
+  ctx->grid_h = 0;
+  ctx->grid_e = 0;
+  invalidate_graph(ctx);
+  // one fused kernel per step where the model allows it (tiles tuned at the first run)
+  tune_release(ctx);
+  ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
+  // measured on the GB300: with PML slabs the fused step runs slower than the two half-step
+  // kernels (its slab nodes wait on their PML state within each plane), so such models take the
+  // half-step kernels without timing the fused one (gbf_set_fused_tiles still selects it)
+  const bool timed = ctx->fused_avail && pml_kind(ctx->d) == PML_NONE;
+  ctx->fused = timed ? 1 : 0;
+  ctx->tuned = timed ? 0 : 1;
+  // GBF_FUSED_TILE="tj,nch" selects the fused step with that tiling for every model that has one
+  const char* force = getenv("GBF_FUSED_TILE");
+  int ftj = 0, fnch = 0;
+  if (ctx->fused_avail && force && sscanf(force, "%d,%d", &ftj, &fnch) == 2 &&
+      configure_fused(ctx, ftj, fnch)) {
+    ctx->fused = 1;
+    ctx->tuned = 1;
+  }
+  // the staged half-steps and whether their form is still to be chosen
+  configure_staged(ctx);
+}
+
 // Coefficient tables, dispersive flags and, with packed IDs, the packed words: from `ids` (an ID
 // array [6][ncomp] the device can read), or, with `ids` NULL, from the words already copied into
 // ctx->PE/PH by the caller's packing. Plain IDs are already in ctx->ID.
@@ -678,28 +732,7 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
     CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)ctx->d.maxpoles * ctx->ncomp, ctx->stream));
   }
   ctx->treal = tr;
-  ctx->grid_h = 0;
-  ctx->grid_e = 0;
-  invalidate_graph(ctx);
-  // one fused kernel per step where the model allows it (tiles tuned at the first run)
-  tune_release(ctx);
-  ctx->fused_avail = ctx->fused_ok ? configure_fused(ctx, 7, 0) : 0;
-  // measured on the GB300: with PML slabs the fused step runs slower than the two half-step
-  // kernels (its slab nodes wait on their PML state within each plane), so such models take the
-  // half-step kernels without timing the fused one (gbf_set_fused_tiles still selects it)
-  const bool timed = ctx->fused_avail && pml_kind(ctx->d) == PML_NONE;
-  ctx->fused = timed ? 1 : 0;
-  ctx->tuned = timed ? 0 : 1;
-  // GBF_FUSED_TILE="tj,nch" selects the fused step with that tiling for every model that has one
-  const char* force = getenv("GBF_FUSED_TILE");
-  int ftj = 0, fnch = 0;
-  if (ctx->fused_avail && force && sscanf(force, "%d,%d", &ftj, &fnch) == 2 &&
-      configure_fused(ctx, ftj, fnch)) {
-    ctx->fused = 1;
-    ctx->tuned = 1;
-  }
-  // the staged half-steps and whether their form is still to be chosen
-  configure_staged(ctx);
+  configure_steps(ctx);
   std::vector<float4> e4(nmat), h4(nmat);
   std::vector<float> es(nmat), hs(nmat);
   for (int m = 0; m < nmat; ++m) {
@@ -959,6 +992,53 @@ int gbf_upload_materials_geom(gbf_ctx* ctx, gbf_geom* geom, const float* coeffE,
   const int rc = check_ids(ctx, "gbf_upload_materials_geom");
   if (rc != GBF_OK) return rc;
   return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
+}
+
+int gbf_share_materials(gbf_ctx* ctx, gbf_ctx* owner) {
+  if (!ctx) return GBF_EINVAL;
+  if (!owner || owner == ctx) return fail(ctx, GBF_EINVAL, "gbf_share_materials: no other context given");
+  if (!owner->materials)
+    return fail(ctx, GBF_ESTATE, "gbf_share_materials: the other context has no materials uploaded");
+  const gbf_grid_desc& a = ctx->d;
+  const gbf_grid_desc& b = owner->d;
+  if (a.nx != b.nx || a.ny != b.ny || a.nz != b.nz || a.nmat != b.nmat ||
+      a.maxpoles != b.maxpoles || (a.options & 4) != (b.options & 4) || ctx->device != owner->device)
+    return fail(ctx, GBF_EINVAL, "gbf_share_materials: grids, material counts, pole counts, the "
+                "dispersive-state layout (options bit 2) and devices must be the same");
+  CK(cudaStreamSynchronize(owner->stream));
+  // this context's own material arrays go (with the last context that holds them)
+  if (!ctx->shared_mats) ctx->bytes -= ctx->mat_bytes;
+  ctx->mats = owner->mats;
+  ctx->shared_mats = true;
+  ctx->ID = owner->ID;
+  ctx->PE = owner->PE;
+  ctx->PH = owner->PH;
+  ctx->disp = owner->disp;
+  ctx->cE4 = owner->cE4;
+  ctx->cEs = owner->cEs;
+  ctx->cH4 = owner->cH4;
+  ctx->cHs = owner->cHs;
+  ctx->cD = owner->cD;
+  ctx->idp = owner->idp;
+  ctx->uniform_h = owner->uniform_h;
+  if (owner->treal != ctx->treal && ctx->T)
+    CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)a.maxpoles * ctx->ncomp, ctx->stream));
+  ctx->treal = owner->treal;
+  StepParams& p = ctx->sp;
+  const StepParams& q = owner->sp;
+  for (int c = 0; c < 6; ++c) p.ID[c] = q.ID[c];
+  p.PE = q.PE;
+  p.PH = q.PH;
+  p.cE4 = q.cE4;
+  p.cEs = q.cEs;
+  p.cH4 = q.cH4;
+  p.cHs = q.cHs;
+  p.cD = q.cD;
+  for (int k = 0; k < 6; ++k) p.hrow[k] = q.hrow[k];
+  configure_steps(ctx);
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->materials = true;
+  return GBF_OK;
 }
 
 int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]) {

@@ -106,10 +106,11 @@ def real_dispersive_state(G):
     return bool((bits[:, :, 1, 1] == 0).all() and ((bits[:, :, 2, 1] & 0x7fffffff) == 0).all())
 
 
-def model_inputs(G, options=0):
+def model_inputs(G, options=0, ids=True):
     """Everything the C ABI receives for grid ``G``: the descriptor and the host arrays, in
-    the reference's layouts. Reads only attributes that the reference's own grid object also
-    carries, so a grid built by the reference's ``run_model`` can be handed over unchanged."""
+    the reference's layouts (without the ID array when ``ids`` is false). Reads only attributes
+    that the reference's own grid object also carries, so a grid built by the reference's
+    ``run_model`` can be handed over unchanged."""
     d = _native.GridDesc()
     d.nx, d.ny, d.nz = G.nx, G.ny, G.nz
     d.iterations = G.iterations
@@ -128,7 +129,7 @@ def model_inputs(G, options=0):
     d.options = options
     inp = {'desc': d,
            'ID': (np.ascontiguousarray(G.ID, dtype=np.uint32)
-                  if getattr(G, 'geom', None) is None else None),
+                  if ids and getattr(G, 'geom', None) is None else None),
            'coeffE': np.ascontiguousarray(G.updatecoeffsE, dtype=np.float32),
            'coeffH': np.ascontiguousarray(G.updatecoeffsH, dtype=np.float32),
            'coeffD': None, 'pml': [], 'sources': None, 'rx': None, 'snapshots': None}
@@ -196,15 +197,17 @@ def pack_materials(G):
 class DeviceModel:
     """One model resident on the GPU (fields, IDs, coefficients, PML and dispersive state).
     ``packed``: the material IDs as ``pack_materials(G)`` returns them, uploaded instead of
-    ``G.ID``."""
+    ``G.ID``. ``share``: another DeviceModel of the same geometry whose material IDs and
+    coefficient tables this one uses instead of uploading its own (``gbf_share_materials``)."""
 
-    def __init__(self, G, options=0, packed=None):
+    def __init__(self, G, options=0, packed=None, share=None):
         self.G = G
         self.lib = _native.lib()
         self.ctx = ctypes.c_void_p(0)
         self.packed = packed
+        self.shared_from = share
         t0 = time.perf_counter()
-        self.inputs = model_inputs(G, options)
+        self.inputs = model_inputs(G, options, ids=share is None)
         d = self.desc = self.inputs['desc']
         self.maxpoles = d.maxpoles
         t1 = time.perf_counter()
@@ -228,7 +231,9 @@ class DeviceModel:
     def _upload(self):
         inp = self.inputs
         t0 = time.perf_counter()
-        if self.packed is not None:
+        if self.shared_from is not None:
+            self._check(self.lib.gbf_share_materials(self.ctx, self.shared_from.ctx))
+        elif self.packed is not None:
             pe, ph = self.packed
             self._check(self.lib.gbf_upload_materials_packed(
                 self.ctx, pe.ptr, ph.ptr, _ptr(inp['coeffE']), _ptr(inp['coeffH']),
@@ -400,13 +405,36 @@ class DeviceModel:
                 G.Tx, G.Ty, G.Tz = T[0], T[1], T[2]
 
 
+def same_geometry(G, H):
+    """Whether grids ``G`` and ``H`` have the same material IDs and coefficient tables (so one
+    device copy serves both): the same object, or equal sizes and tables and then equal IDs
+    (the tables, compared first, tell most different geometries apart cheaply)."""
+    if G is H or G.ID is H.ID:
+        return True
+    if getattr(G, 'geom', None) is not None or getattr(H, 'geom', None) is not None:
+        return False
+    if (G.nx, G.ny, G.nz) != (H.nx, H.ny, H.nz) or len(G.materials) != len(H.materials):
+        return False
+    for a in ('updatecoeffsE', 'updatecoeffsH'):
+        if not np.array_equal(getattr(G, a), getattr(H, a)):
+            return False
+    if pole_count(G) != pole_count(H):
+        return False
+    if pole_count(G) and not np.array_equal(G.updatecoeffsdispersive, H.updatecoeffsdispersive):
+        return False
+    return np.array_equal(G.ID, H.ID)
+
+
 class BatchModel:
     """Many models advanced together: one persistent launch per half-step walks every model
     (``gbf_batch_*`` in the C ABI), and the requested time loop is replayed from one CUDA graph.
     The models may differ in size, geometry, sources and receivers; they must share the PML
-    formulation and order, the pole count and the material-ID layout, and have no snapshots."""
+    formulation and order, the pole count and the material-ID layout, and have no snapshots.
+    Models of one geometry (a B-scan over a fixed model, the traces differing only in source
+    and receiver positions) share one device copy of their material IDs and coefficient tables
+    (``share_geometry``; found with :func:`same_geometry`)."""
 
-    def __init__(self, grids, options=0):
+    def __init__(self, grids, options=0, share_geometry=True):
         self.lib = _native.lib()
         self.models = []
         self.b = ctypes.c_void_p(0)
@@ -415,8 +443,15 @@ class BatchModel:
         if any(pole_count(G) for G in grids) and not all(real_dispersive_state(G) for G in grids):
             options |= 4
         try:
+            owners = []
             for G in grids:
-                self.models.append(DeviceModel(G, options))
+                owner = None
+                if share_geometry:
+                    owner = next((m for m in owners if same_geometry(G, m.G)), None)
+                m = DeviceModel(G, options, share=owner)
+                if owner is None:
+                    owners.append(m)
+                self.models.append(m)
             arr = (ctypes.c_void_p * len(self.models))(*[m.ctx.value for m in self.models])
             rc = self.lib.gbf_batch_create(arr, len(self.models), ctypes.byref(self.b))
             self._check(rc, created=False)

@@ -123,6 +123,15 @@ int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint
 int gbf_host_alloc(size_t bytes, void** out);
 void gbf_host_free(void* p);
 
+/* Use another context's material IDs and coefficient tables instead of uploading them: the
+ * traces of a B-scan over one fixed geometry then share one copy of the IDs and tables on the
+ * device (the reference's --geometry-fixed model runs build the grid once and reuse it,
+ * model_build_run.py:104-106 and :400-403). The contexts must have the same grid, material
+ * and pole counts, dispersive-state layout (options bit 2) and device; the shared arrays live
+ * until the last context holding them is destroyed. Replaces: nothing in the reference, whose
+ * GPU solver uploads every model run's arrays. */
+int gbf_share_materials(gbf_ctx* ctx, gbf_ctx* owner);
+
 /* Copy one PML slab's coefficient rows, each fp32 [pml_order][thickness], E then H:
  * ERA, ERB, ERE, ERF, HRA, HRB, HRE, HRF (pml.py:221-274). `slab` indexes x0, y0, z0, xmax,
  * ymax, zmax; slabs with zero thickness take no call. Replaces: PML.gpu_initialise_arrays

@@ -132,6 +132,9 @@ def test_batch_of_2d_bscan_traces(native, tmp_path):
     assert grids[0].nz == 1 and grids[0].mode == '2D TMz'
     assert grids[-1].rxs[0].xcoord == grids[0].rxs[0].xcoord + 7
     bm = BatchModel(grids)
+    # one geometry: every trace uses the first trace's device IDs and tables
+    assert all(m.shared_from is bm.models[0] for m in bm.models[1:])
+    assert bm.models[1].device_bytes() < bm.models[0].device_bytes()
     bm.run()
     rx = bm.receivers()
     fields = [m.fields() for m in bm.models]
@@ -151,3 +154,49 @@ def test_batch_of_2d_bscan_traces(native, tmp_path):
     assert ez.shape == (grids[0].iterations, len(grids))
     for n in range(len(grids)):
         np.testing.assert_array_equal(ez[:, n], rx[n][OUTPUT_INDEX['Ez'], :, 0])
+
+
+def test_shared_geometry_3d_soil(native):
+    """Traces of one 3D dispersive soil with PML, the dipole and receiver moved per trace: the
+    batch shares one copy of the IDs and tables and its results equal the same batch without
+    sharing and the plain runs bit for bit; models sharing another's arrays keep them after
+    that model is destroyed."""
+    from gprmax_gb300.model import build_grid
+    from gprmax_gb300.solver import BatchModel, DeviceModel
+    grids = []
+    for m in range(4):
+        text = SOIL.format(x=0.034, y=0.030, z=0.032, steps=160, pml='6', sx=(14 + m) / 1000,
+                           sy=0.015, sz=0.022, rx=(18 + m) / 1000, ry=0.011, surf=0.016,
+                           bx=0.017, by=0.015, bz=0.008)
+        grids.append(build_grid(text.splitlines(True), messages=False))
+    runs = {}
+    for share in (True, False):
+        bm = BatchModel(grids, share_geometry=share)
+        assert all((m.shared_from is bm.models[0]) == share for m in bm.models[1:])
+        bm.run()
+        runs[share] = bm.receivers()
+        bm.close()
+    owner = DeviceModel(grids[0])
+    others = [DeviceModel(G, share=owner) for G in grids[1:]]
+    owner.close()
+    for n, m in enumerate(others, start=1):
+        m.run()
+        got = m.receivers()
+        m.close()
+        prx, _ = _plain(grids[n])
+        np.testing.assert_array_equal(got, prx)
+        np.testing.assert_array_equal(runs[True][n], prx)
+        np.testing.assert_array_equal(runs[False][n], prx)
+
+
+def test_share_materials_refuses_other_grids(native):
+    from gprmax_gb300.exceptions import SolverError
+    from gprmax_gb300.solver import DeviceModel
+    a, b = _grids(FREE, 2, 20)
+    assert (a.nx, a.ny, a.nz) != (b.nx, b.ny, b.nz)
+    owner = DeviceModel(a)
+    try:
+        with pytest.raises(SolverError):
+            DeviceModel(b, share=owner)
+    finally:
+        owner.close()
