@@ -597,6 +597,29 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
 
 }  // extern "C"
 
+// Let kernel k take `need` bytes of dynamic shared memory. The limit belongs to the kernel, not
+// to a context, and every launch states its own size; so the limit is raised once to all the
+// device allows beside the kernel's static shared memory, and never lowered by a context that
+// needs less (contexts of different sizes may launch the same kernel in any order, as a batch
+// does).
+static bool allow_dynamic_smem(const void* k, size_t need, int device) {
+  cudaFuncAttributes a{};
+  if (cudaFuncGetAttributes(&a, k) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if ((size_t)a.maxDynamicSharedSizeBytes >= need) return true;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  const long long most = (long long)optin - (long long)a.sharedSizeBytes;
+  if ((long long)need > most ||
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return true;
+}
+
 // Tiles of the fused step: k segments of kTileK nodes, j tiles of `tj` rows and `nch` chunks of
 // planes along x (nch <= 0: as many chunks as give one wave of resident warps). Returns 0 when
 // no fused kernel exists for the model or the tiling does not fit.
@@ -606,11 +629,7 @@ static int configure_fused(gbf_ctx* ctx, int tj, int nch) {
   if (!f) return 0;
   size_t sm = 0;
   if (ctx->sp.smem) sm = ctx->smem_e + 16 + (ctx->uniform_h ? 0 : ctx->smem_h);
-  if (sm > 48 * 1024 &&
-      cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return 0;
-  }
+  if (sm > 48 * 1024 && !allow_dynamic_smem((const void*)f, sm, ctx->device)) return 0;
   if (nch <= 0) {   // one wave of resident warps
     const FusedTiles one = fused_tiles(d.nx, d.ny, d.nz, tj, 1);
     int dev = 0, sms = 1, per = 0;
@@ -1255,12 +1274,14 @@ static int persistent_blocks(const void* kern, size_t smem) {
   return sms * (per > 0 ? per : 1);
 }
 
-static void launch_h(gbf_ctx* ctx) {
+// The step's kernels of one context, on its stream or on `st` (a batch's).
+static void launch_h(gbf_ctx* ctx, cudaStream_t st = nullptr) {
   const StepParams& p = ctx->sp;
+  if (!st) st = ctx->stream;
   if (ctx->staged_h) {
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    ctx->skh<<<sms, kStagedThreads, ctx->smem_sth, ctx->stream>>>(p, ctx->sgh);
+    ctx->skh<<<sms, kStagedThreads, ctx->smem_sth, st>>>(p, ctx->sgh);
     return;
   }
   HKern kern;
@@ -1269,7 +1290,7 @@ static void launch_h(gbf_ctx* ctx) {
   if (!ctx->grid_h) ctx->grid_h = persistent_blocks((const void*)kern, ctx->smem_h);
   dim3 block(kThreads);
   dim3 grid(ctx->grid_h);
-  kern<<<grid, block, ctx->smem_h, ctx->stream>>>(p);
+  kern<<<grid, block, ctx->smem_h, st>>>(p);
 }
 
 // The division constants of FastDiv for divisor d >= 2 (staged_e.cuh).
@@ -1327,12 +1348,7 @@ static bool staged_geom(gbf_ctx* ctx, bool electric, int nstream, size_t tables,
   g.err = ctx->d_err;
   g.limit_ns = 2000000000LL;
   smem = g.ring_off + ns * stage;
-  if (cudaFuncSetAttribute((const void*)k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess) {
-    (void)cudaGetLastError();
-    return false;
-  }
-  return true;
+  return allow_dynamic_smem((const void*)k, smem, ctx->device);
 }
 
 // The staged half-steps (staged.cuh) where they apply: 3D grids with packed IDs and coefficient
@@ -1388,12 +1404,13 @@ static int staged_status(gbf_ctx* ctx) {
   return GBF_OK;
 }
 
-static void launch_e(gbf_ctx* ctx) {
+static void launch_e(gbf_ctx* ctx, cudaStream_t st = nullptr) {
   const StepParams& p = ctx->sp;
+  if (!st) st = ctx->stream;
   if (ctx->staged) {
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    ctx->sk<<<sms, kStagedThreads, ctx->smem_st, ctx->stream>>>(p, ctx->sg);
+    ctx->sk<<<sms, kStagedThreads, ctx->smem_st, st>>>(p, ctx->sg);
     return;
   }
   HKern hk;
@@ -1402,7 +1419,7 @@ static void launch_e(gbf_ctx* ctx) {
   if (!ctx->grid_e) ctx->grid_e = persistent_blocks((const void*)kern, ctx->smem_e);
   dim3 block(kThreads);
   dim3 grid(ctx->grid_e);
-  kern<<<grid, block, ctx->smem_e, ctx->stream>>>(p);
+  kern<<<grid, block, ctx->smem_e, st>>>(p);
 }
 
 static void launch_end(gbf_ctx* ctx) {
@@ -1967,7 +1984,13 @@ struct gbf_batch {
   cudaGraphExec_t gexec = nullptr;
   int graph_steps = 0;
   int tuned = 0;               // grid sizes chosen (batch_tune)
+  std::vector<gbf_ctx*> own;   // models large enough to fill the GPU alone: their own kernels
+  int nbatched = 0;            // models swept by the batched kernels
 };
+
+// A model with at least this many nodes fills the GPU by itself: within a batch it steps with
+// its own half-step kernels (staged where they apply), the smaller ones with the batched kernels.
+static const long long kBatchOwnNodes = 1LL << 21;
 
 static int bfail(gbf_batch* b, int code, const char* fmt, ...) {
   char buf[512];
@@ -2004,8 +2027,11 @@ static void batch_step(gbf_batch* b) {
   bp.rangeH = b->d_rangeH;
   bp.rangeE = b->d_rangeE;
   bp.n = (int)b->models.size();
-  b->hk<<<b->grid_h, kThreads, b->smem_h, b->stream>>>(bp);
-  b->ek<<<b->grid_e, kThreads, b->smem_e, b->stream>>>(bp);
+  if (b->nbatched) b->hk<<<b->grid_h, kThreads, b->smem_h, b->stream>>>(bp);
+  for (gbf_ctx* c : b->own) launch_h(c, b->stream);
+  if (b->nbatched) b->ek<<<b->grid_e, kThreads, b->smem_e, b->stream>>>(bp);
+  for (gbf_ctx* c : b->own) launch_e(c, b->stream);
+  // receivers and the iteration counter of every model, batched or not
   end_of_step_batch<<<bp.n, 256, 0, b->stream>>>(b->d_models, b->d_rx);
 }
 
@@ -2036,6 +2062,10 @@ static const int kBatchTuneReps = 2;
 // negative status.
 static int batch_tune(gbf_batch* b, int nsteps) {
   if (b->tuned) return 0;
+  if (!b->nbatched) {
+    b->tuned = 1;
+    return 0;
+  }
   const std::vector<long long> key = batch_key(b);
   {
     std::lock_guard<std::mutex> lock(g_btune_mu);
@@ -2078,9 +2108,13 @@ static int batch_tune(gbf_batch* b, int nsteps) {
   bp.n = (int)b->models.size();
   for (int r = 0; r < nc * kBatchTuneReps && rc == GBF_OK; ++r) {
     const std::pair<int, int>& c = cand[r % nc];
+    // a whole step: the models with their own kernels advance too (the same in every
+    // candidate's time)
     cudaEventRecord(ev[2 * r], b->stream);
     b->hk<<<c.first, kThreads, b->smem_h, b->stream>>>(bp);
+    for (gbf_ctx* m : b->own) launch_h(m, b->stream);
     b->ek<<<c.second, kThreads, b->smem_e, b->stream>>>(bp);
+    for (gbf_ctx* m : b->own) launch_e(m, b->stream);
     cudaEventRecord(ev[2 * r + 1], b->stream);
     end_of_step_batch<<<bp.n, 256, 0, b->stream>>>(b->d_models, b->d_rx);
     if (cudaGetLastError() != cudaSuccess) rc = GBF_ECUDA;
@@ -2174,6 +2208,12 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
     rp[m] = c->rp;
     rh[m] = (int)h;
     re[m] = (int)ev;
+    // a large model takes no part in the batched half-steps (an empty range there)
+    if (c->npts >= kBatchOwnNodes && !c->sp.two_d) {
+      b->own.push_back(c);
+      continue;
+    }
+    ++b->nbatched;
     const Box& lh = c->sp.boxH[kBoxes - 1];
     const Box& le = c->sp.boxE[kBoxes - 1];
     h += ((long long)(lh.start + lh.count) + kThreads - 1) / kThreads * kThreads;
@@ -2269,11 +2309,12 @@ int gbf_batch_run_timed(gbf_batch* b, int32_t nsteps, uint32_t flags, float* ms)
   return GBF_OK;
 }
 
-int gbf_batch_info(gbf_batch* b, int32_t info[3]) {
+int gbf_batch_info(gbf_batch* b, int32_t info[4]) {
   if (!b || !info) return GBF_EINVAL;
   info[0] = b->tuned;
   info[1] = b->grid_h;
   info[2] = b->grid_e;
+  info[3] = (int32_t)b->own.size();
   return GBF_OK;
 }
 

@@ -487,10 +487,12 @@ class BatchModel:
         self._check(self.lib.gbf_batch_synchronize(self.b))
 
     def info(self):
-        """{'tuned': bool, 'blocks_h', 'blocks_e'}: the grid sizes of the batched launches."""
-        info = np.zeros(3, dtype=np.int32)
+        """{'tuned': bool, 'blocks_h', 'blocks_e', 'own_kernels'}: the grid sizes of the batched
+        launches and how many (large) models step with their own kernels."""
+        info = np.zeros(4, dtype=np.int32)
         self._check(self.lib.gbf_batch_info(self.b, _ptr(info)))
-        return {'tuned': bool(info[0]), 'blocks_h': int(info[1]), 'blocks_e': int(info[2])}
+        return {'tuned': bool(info[0]), 'blocks_h': int(info[1]), 'blocks_e': int(info[2]),
+                'own_kernels': int(info[3])}
 
     def receivers(self):
         """Per model, fp32 [9][iterations][nrx] receiver samples."""

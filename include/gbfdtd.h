@@ -282,7 +282,9 @@ int gbf_download_tls(gbf_ctx* ctx, float* out);
  * A batch borrows contexts that are fully set up (materials, PML rows, sources, receivers
  * uploaded; no snapshots; all at the same iteration, with the same PML kind, pole count and
  * material-ID layout) and advances all of them with one persistent launch per half-step plus
- * one end-of-step launch, replaying the requested time loop from one CUDA graph. Results are
+ * one end-of-step launch, replaying the requested time loop from one CUDA graph; a model of
+ * 2^21 nodes or more, which fills the GPU alone, takes its own half-step kernels (staged where
+ * they apply) within the same graph instead of a share of the batched ones. Results are
  * read from each context as usual (gbf_download_rx ...). While a batch exists, its contexts
  * must not be run or re-uploaded on their own; destroy the batch before the contexts.
  * Replaces: the task farm of independent model runs for B-scans and parameter sweeps
@@ -298,9 +300,9 @@ int gbf_batch_run(gbf_batch* batch, int32_t nsteps, uint32_t flags);
 /* The same, timed with CUDA events on the batch's stream (graph capture outside the timing
  * once the grid size is chosen). */
 int gbf_batch_run_timed(gbf_batch* batch, int32_t nsteps, uint32_t flags, float* ms);
-/* info[0] 1 once the grid size is chosen, [1] blocks of the H launch, [2] of the E launch. No
- * counterpart in the reference. */
-int gbf_batch_info(gbf_batch* batch, int32_t info[3]);
+/* info[0] 1 once the grid size is chosen, [1] blocks of the H launch, [2] of the E launch,
+ * [3] models stepped with their own kernels. No counterpart in the reference. */
+int gbf_batch_info(gbf_batch* batch, int32_t info[4]);
 int gbf_batch_synchronize(gbf_batch* batch);
 int gbf_batch_last_error(gbf_batch* batch, char* buf, size_t n);
 

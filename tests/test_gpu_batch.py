@@ -200,3 +200,30 @@ def test_share_materials_refuses_other_grids(native):
             DeviceModel(b, share=owner)
     finally:
         owner.close()
+
+
+def test_large_models_step_with_their_own_kernels(native):
+    """A model of 2^21 nodes or more takes its own half-step kernels (staged where they apply)
+    inside the batch's graph, the small ones the batched kernels: every trace and field equals
+    the plain run's."""
+    from gprmax_gb300.model import build_grid
+    from gprmax_gb300.solver import BatchModel
+    # two large models of different sizes, their staged kernels' shared-memory rings of
+    # different sizes: each launch states its own size, whichever context was set up last
+    bigs = [build_grid(SOIL.format(x=x, y=0.130, z=z, steps=40, pml='6', sx=0.060, sy=0.065,
+                                   sz=0.090, rx=0.070, ry=0.060, surf=0.064, bx=0.065, by=0.065,
+                                   bz=0.032).splitlines(True), messages=False)
+            for x, z in ((0.136, 0.140), (0.130, 0.128))]
+    for big in bigs:
+        assert (big.nx + 1) * (big.ny + 1) * (big.nz + 1) >= 2 ** 21
+    grids = _grids(SOIL, 2, 40) + bigs
+    bm = BatchModel(grids)
+    assert bm.info()['own_kernels'] == 2
+    bm.run()
+    rx = bm.receivers()
+    fields = [m.fields() for m in bm.models]
+    bm.close()
+    for n, G in enumerate(grids):
+        prx, pf = _plain(G)
+        np.testing.assert_array_equal(rx[n], prx, err_msg='model {}'.format(n))
+        np.testing.assert_array_equal(fields[n], pf, err_msg='model {} fields'.format(n))
