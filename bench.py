@@ -397,6 +397,22 @@ def run_gb300(args):
     }
     if args.cpu_baseline:
         out['cpu_baseline'] = cpu_baseline(G, budget_s=args.cpu_budget)
+    if args.extras and world == 1:
+        # after the timed region: the batched 2D B-scan (section "bscan2d"), so that its figures
+        # come from the same run as the headline
+        try:
+            b = measure_bscan2d(60, 3)
+            out['extras'] = {'bscan2d': {
+                'workload': b['config']['workload'], 'traces_per_s_batched': b['value'],
+                'traces_per_s_batched_unshared': b['batched_unshared']['value'],
+                'traces_per_s_sequential': b['plain_sequential']['value'],
+                'speedup_vs_sequential': b['speedup_vs_plain'],
+                'traces_identical': b['traces_identical'],
+                'models_sharing_geometry': b['batched']['models_sharing_geometry'],
+                'h2d_bytes_per_step': b['e2e']['h2d_bytes_per_step'],
+                'gpu_launches': b['gpu_launches']}}
+        except Exception as e:   # the headline above stands either way
+            out['extras'] = {'bscan2d_error': '{}: {}'.format(type(e).__name__, e)}
     print(json.dumps(out), flush=True)
 
 
@@ -530,6 +546,12 @@ def run_bscan(args):
 
 
 def run_bscan2d(args):
+    """2D B-scan: see measure_bscan2d; prints its JSON line."""
+    print(json.dumps(measure_bscan2d(args.traces, args.warmup, args.cpu_baseline,
+                                     args.cpu_budget)), flush=True)
+
+
+def measure_bscan2d(ntraces, W, with_cpu=False, cpu_budget=20.0):
     """2D B-scan (``workloads.bscan_2d_models``: TMz, 120x105 cells at 2 mm, a dielectric
     half-space with a buried PEC cylinder, 637 iterations, ``--traces`` traces with the antenna
     pair stepped one cell per trace). Every trace runs to its last iteration in both arms, with
@@ -542,9 +564,8 @@ def run_bscan2d(args):
     reference's own kernels on the host cores time one trace."""
     from gprmax_gb300 import workloads
     from gprmax_gb300.solver import BatchModel, DeviceModel
-    W = args.warmup
     t0 = time.perf_counter()
-    grids = workloads.bscan_2d_models(args.traces)
+    grids = workloads.bscan_2d_models(ntraces)
     t_build = time.perf_counter() - t0
     n = len(grids)
     iters = grids[0].iterations
@@ -629,13 +650,13 @@ def run_bscan2d(args):
            # geometry one kernel that packs and checks its IDs
            'gpu_launches': 3 * iters + n - int(sum(shared_models)),
            'host_build_s': round(t_build, 3)}
-    if args.cpu_baseline:
-        cb = cpu_baseline(grids[0], budget_s=min(args.cpu_budget, 20.0), max_steps=iters - 1)
+    if with_cpu:
+        cb = cpu_baseline(grids[0], budget_s=min(cpu_budget, 20.0), max_steps=iters - 1)
         cb['value'] = round(cb['value'] * 1e6 / (cells * iters), 2)
         cb['unit'] = 'traces/s'
         cb['sample'] = 'one trace, ' + cb['sample']
         out['cpu_baseline'] = cb
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def run_adjoint(args):
@@ -862,6 +883,8 @@ def main():
                     help='soil: step with the two half-step kernels instead of the fused step')
     ap.add_argument('--plain-e', action='store_true',
                     help='soil: the plain E half-step kernel instead of the staged sweep')
+    ap.add_argument('--no-extras', dest='extras', action='store_false',
+                    help='soil: skip the 2D B-scan summary added to the line after the timed region')
     ap.add_argument('--no-warm-context', action='store_true',
                     help='skip the small context warm-up model (launch counting for ncu)')
     ap.add_argument('--workload', choices=['soil', 'bscan', 'bscan2d', 'adjoint', 'sweep', 'build'],
