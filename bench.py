@@ -311,7 +311,8 @@ def run_gb300(args):
     # --- end to end through the public API: upload from host, K steps, read back traces
     if dist is not None:
         dist.barrier()
-    options = (8 if args.half_steps else 0) | (16 if args.plain_e else 0)
+    options = ((8 if args.half_steps else 0) | (16 if args.plain_e else 0) |
+               (32 if args.fused_buffers else 0))
     # the model's inputs in page-locked host memory before the timed region: the material IDs
     # packed two words per node (a third of the ID array's bytes); the copy itself is timed
     from gprmax_gb300.solver import pack_materials
@@ -424,7 +425,7 @@ def upload_bytes(G, packed=None, materials=True):
     """Host bytes a model's upload copies to the device: material IDs (two packed words per node
     when ``packed``, else the ID array) and coefficient tables (unless ``materials`` is false:
     a model sharing another's), PML profiles and the sources' waveform tables."""
-    ids = sum(w.array.nbytes for w in packed) if packed else G.ID.nbytes
+    ids = sum(w.array.nbytes for w in packed if w is not None) if packed else G.ID.nbytes
     mats = (ids + G.updatecoeffsE.nbytes + G.updatecoeffsH.nbytes
             + (G.updatecoeffsdispersive.nbytes if G.maxpoles else 0)) if materials else 0
     return (mats
@@ -881,6 +882,9 @@ def main():
                     help='adjoint: cells of the finite-difference check (0: none)')
     ap.add_argument('--half-steps', action='store_true',
                     help='soil: step with the two half-step kernels instead of the fused step')
+    ap.add_argument('--fused-buffers', action='store_true',
+                    help='soil: give the model the fused step\'s second field buffer although it '
+                         'has PML slabs (with GBF_FUSED_TILE, to time the fused step there)')
     ap.add_argument('--plain-e', action='store_true',
                     help='soil: the plain E half-step kernel instead of the staged sweep')
     ap.add_argument('--no-extras', dest='extras', action='store_false',

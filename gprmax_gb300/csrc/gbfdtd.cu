@@ -46,6 +46,8 @@ struct gbf_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   long long npts = 0;          // nodes per component, (nx+1)(ny+1)(nz+1)
+  char* arena = nullptr;       // one allocation holding every array below but the material
+                               // ones (ID, PE, PH, disp, tables: mats) and the snapshots
   long long ncomp = 0;         // device stride of one component array: npts rounded up to 64
                                // nodes, so every field, packed-ID and pole-state array starts
                                // on a 256-byte boundary (the staged E sweep copies them in
@@ -118,6 +120,9 @@ struct gbf_ctx {
   std::shared_ptr<MatSet> mats;   // holds ID, PE, PH, disp and the tables (see MatSet)
   size_t mat_bytes = 0;        // their size
   bool shared_mats = false;    // adopted from another context
+  bool dirty = false;          // the state may differ from the all-zero state it was created in
+  bool ph_uploaded = true;     // the packed H words hold the model's H IDs (else zeros: every
+                               // material has the same H row, and no kernel reads them)
 };
 
 static std::string g_create_err;
@@ -375,17 +380,8 @@ void gbf_destroy(gbf_ctx* ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
-  void* ptrs[] = {ctx->fields, ctx->T, ctx->pml_mem, ctx->pml_coef, ctx->srcs, ctx->waves,
-                  ctx->rx_coords, ctx->rxs, ctx->d_it, ctx->d_err};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
-  // the material arrays go with the last context holding them (freed here if never handed to
-  // a MatSet, when creation failed first)
-  if (!ctx->mats) {
-    void* mp[] = {ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD};
-    for (void* p : mp)
-      if (p) cudaFree(p);
-  }
+  if (ctx->arena) cudaFree(ctx->arena);
+  // the material arrays go with the last context holding them
   ctx->mats.reset();
   for (float* p : ctx->snaps)
     if (p) cudaFree(p);
@@ -408,7 +404,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     return fail(nullptr, GBF_EINVAL, "gbf_create: PML order must be 1 or 2 and formulation 0 or 1");
   if (d.nsrc < 0 || d.nrx < 0 || d.nsnap < 0)
     return fail(nullptr, GBF_EINVAL, "gbf_create: negative counts");
-  if ((d.options & ~31) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
+  if ((d.options & ~63) || d.ntl < 0 || d.ntl > d.nsrc || d.reserved[0] || d.reserved[1])
     return fail(nullptr, GBF_EINVAL, "gbf_create: reserved fields must be zero");
   const long long npts = (long long)(d.nx + 1) * (d.ny + 1) * (d.nz + 1);
   if (npts + 63 > (1LL << 31) - 1)
@@ -431,84 +427,148 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     delete ctx;
     return GBF_ECUDA;
   }
-  int rc = GBF_OK;
-  auto A = [&](void** p, size_t n) { if (rc == GBF_OK) rc = dev_alloc(ctx, p, n); };
   // the fused step (3D, packed IDs, at most kFusedMaxPoles poles, no transmission lines, not
   // turned off by option bit 3) needs a second field buffer; without room for it the model
-  // takes the two half-step kernels
+  // takes the two half-step kernels. With PML slabs the fused step is slower than the
+  // half-step kernels and never chosen by timing, so such models get the second buffer only
+  // when option bit 5 asks for it (to select the fused step with gbf_set_fused_tiles).
+  bool any_pml = false;
+  for (int s = 0; s < 6; ++s) any_pml |= d.pml_thickness[s] > 0;
   ctx->fused_ok = (ones == 0 && d.ntl == 0 && d.nmat <= 1024 && d.maxpoles <= kFusedMaxPoles &&
-                   !(d.options & 8)) ? 1 : 0;
-  if (ctx->fused_ok) {
-    const size_t fb = sizeof(float) * 12 * ncomp;
-    if (cudaMalloc((void**)&ctx->fields, fb) == cudaSuccess) {
-      ctx->bytes += fb;
-      if (cudaMemsetAsync(ctx->fields, 0, fb, ctx->stream) != cudaSuccess)
-        rc = fail(ctx, GBF_ECUDA, "gbf_create: clearing the field buffers failed");
-    } else {
-      (void)cudaGetLastError();
-      ctx->fields = nullptr;
-      ctx->fused_ok = 0;
-    }
-  }
-  if (!ctx->fused_ok) A((void**)&ctx->fields, sizeof(float) * 6 * ncomp);
-  // packed IDs (at most 1024 materials): two words per node, built straight from the caller's
-  // array; otherwise the six ID arrays themselves
-  if (d.nmat <= 1024) {
-    ctx->idp = 1;
-    A((void**)&ctx->PE, sizeof(uint32_t) * ncomp);
-    A((void**)&ctx->PH, sizeof(uint32_t) * ncomp);
-  } else {
-    A((void**)&ctx->ID, sizeof(uint32_t) * 6 * npts);
-  }
-  A((void**)&ctx->disp, (size_t)d.nmat);
-  A((void**)&ctx->cE4, sizeof(float4) * d.nmat);
-  A((void**)&ctx->cEs, sizeof(float) * d.nmat);
-  A((void**)&ctx->cH4, sizeof(float4) * d.nmat);
-  A((void**)&ctx->cHs, sizeof(float) * d.nmat);
-  if (d.maxpoles > 0) {
-    A((void**)&ctx->cD, sizeof(float2) * 3 * d.maxpoles * d.nmat);
-    A((void**)&ctx->T, sizeof(float2) * 3 * (size_t)d.maxpoles * ncomp);
-  }
+                   !(d.options & 8) && (!any_pml || (d.options & 32))) ? 1 : 0;
   // PML state: per slab 4 Phi arrays of order * T * nu * nv (6 with the second H buffer), each
   // starting on a 256-byte boundary; after them room for the staged sweeps' last z-slab copy,
-  // which may read up to zpad floats past the end of an array
-  long long phi_total = 0;
-  const int nphi = ctx->fused_ok ? 6 : 4;
-  for (int s = 0; s < 6; ++s) {
-    const int t = d.pml_thickness[s];
-    if (!t) continue;
-    const int ax = s % 3;
-    const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
-    phi_total += (long long)nphi * ((d.pml_order * t * nu * nv + 63) & ~63LL);
-  }
+  // which may read up to zspan floats past the end of an array
+  auto phi_sum = [&](int nphi) {
+    long long total = 0;
+    for (int s = 0; s < 6; ++s) {
+      const int t = d.pml_thickness[s];
+      if (!t) continue;
+      const int ax = s % 3;
+      const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
+      total += (long long)nphi * ((d.pml_order * t * nu * nv + 63) & ~63LL);
+    }
+    return total;
+  };
   const int tz = d.pml_thickness[2] > d.pml_thickness[5] ? d.pml_thickness[2] : d.pml_thickness[5];
   ctx->zspan = tz ? (int)((((kStageL + 2) / (d.nz + 1) + 2) * (long long)tz + 3 + 3) & ~3LL) : 0;
-  ctx->phi_floats = phi_total + ctx->zspan + 64;
-  A((void**)&ctx->pml_mem, sizeof(float) * ctx->phi_floats);
   int tmax = 1;
   for (int s = 0; s < 6; ++s) tmax = d.pml_thickness[s] > tmax ? d.pml_thickness[s] : tmax;
-  A((void**)&ctx->pml_coef, sizeof(float) * 6 * 2 * 4 * d.pml_order * tmax);
-  A((void**)&ctx->srcs, sizeof(Src) * (d.nsrc + 1));
-  A((void**)&ctx->waves, sizeof(float) * (size_t)(d.nsrc + 1) * d.iterations);
-  A((void**)&ctx->rx_coords, sizeof(int) * 3 * (d.nrx + 1));
-  A((void**)&ctx->rxs, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
-  A((void**)&ctx->d_it, sizeof(int));
-  A((void**)&ctx->d_err, sizeof(int));
-  if (d.ntl) {
-    A((void**)&ctx->tls, sizeof(TLine) * d.ntl);
-    A((void**)&ctx->tl_waves, sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
-    A((void**)&ctx->tl_out, sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
+  // The state arrays in one allocation, cleared once, each on a 256-byte boundary (one
+  // allocation instead of a score of them: creating a context is part of every model's upload)
+  struct Carve {
+    size_t off = 0;
+    size_t take(size_t n) {
+      const size_t o = off;
+      off += (n + 255) & ~(size_t)255;
+      return o;
+    }
+  };
+  size_t o_fields = 0, o_T = 0, o_pml = 0, o_coef = 0, o_srcs = 0, o_waves = 0, o_rxc = 0,
+         o_rxs = 0, o_it = 0, o_err = 0, o_tls = 0, o_tlw = 0, o_tlo = 0;
+  auto layout = [&](bool two) {
+    Carve c;
+    o_fields = c.take(sizeof(float) * (two ? 12 : 6) * ncomp);
+    if (d.maxpoles > 0) o_T = c.take(sizeof(float2) * 3 * (size_t)d.maxpoles * ncomp);
+    ctx->phi_floats = phi_sum(two ? 6 : 4) + ctx->zspan + 64;
+    o_pml = c.take(sizeof(float) * ctx->phi_floats);
+    o_coef = c.take(sizeof(float) * 6 * 2 * 4 * d.pml_order * tmax);
+    o_srcs = c.take(sizeof(Src) * (d.nsrc + 1));
+    o_waves = c.take(sizeof(float) * (size_t)(d.nsrc + 1) * d.iterations);
+    o_rxc = c.take(sizeof(int) * 3 * (d.nrx + 1));
+    o_rxs = c.take(sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
+    o_it = c.take(sizeof(int));
+    o_err = c.take(sizeof(int) * 16);
+    if (d.ntl) {
+      o_tls = c.take(sizeof(TLine) * d.ntl);
+      o_tlw = c.take(sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
+      o_tlo = c.take(sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
+    }
+    return c.off;
+  };
+  size_t total = layout(ctx->fused_ok != 0);
+  cudaError_t me = cudaMalloc((void**)&ctx->arena, total);
+  if (me != cudaSuccess && ctx->fused_ok) {
+    // no room for the fused step's second buffers: the two half-step kernels do without
+    (void)cudaGetLastError();
+    ctx->fused_ok = 0;
+    total = layout(false);
+    me = cudaMalloc((void**)&ctx->arena, total);
+  }
+  int rc = GBF_OK;
+  if (me != cudaSuccess) {
+    (void)cudaGetLastError();
+    ctx->arena = nullptr;
+    rc = fail(ctx, GBF_ENOMEM, "gbf_create: cudaMalloc of %zu bytes failed: %s", total, cudaGetErrorString(me));
+  } else {
+    ctx->bytes += total;
+    if (cudaMemsetAsync(ctx->arena, 0, total, ctx->stream) != cudaSuccess)
+      rc = fail(ctx, GBF_ECUDA, "gbf_create: clearing the state failed");
+    char* a = ctx->arena;
+    ctx->fields = reinterpret_cast<float*>(a + o_fields);
+    if (d.maxpoles > 0) ctx->T = reinterpret_cast<float2*>(a + o_T);
+    ctx->pml_mem = reinterpret_cast<float*>(a + o_pml);
+    ctx->pml_coef = reinterpret_cast<float*>(a + o_coef);
+    ctx->srcs = reinterpret_cast<Src*>(a + o_srcs);
+    ctx->waves = reinterpret_cast<float*>(a + o_waves);
+    ctx->rx_coords = reinterpret_cast<int*>(a + o_rxc);
+    ctx->rxs = reinterpret_cast<float*>(a + o_rxs);
+    ctx->d_it = reinterpret_cast<int*>(a + o_it);
+    ctx->d_err = reinterpret_cast<int*>(a + o_err);
+    if (d.ntl) {
+      ctx->tls = reinterpret_cast<TLine*>(a + o_tls);
+      ctx->tl_waves = reinterpret_cast<float*>(a + o_tlw);
+      ctx->tl_out = reinterpret_cast<float*>(a + o_tlo);
+    }
+  }
+  // The material arrays (packed IDs at most 1024 materials: two words per node, built
+  // straight from the caller's array; otherwise the six ID arrays themselves; the coefficient
+  // tables) in a second allocation, the one gbf_share_materials shares
+  ctx->idp = d.nmat <= 1024 ? 1 : 3;
+  Carve mc;
+  const size_t o_pe = ctx->idp == 1 ? mc.take(sizeof(uint32_t) * ncomp) : 0;
+  const size_t o_ph = ctx->idp == 1 ? mc.take(sizeof(uint32_t) * ncomp) : 0;
+  const size_t o_id = ctx->idp == 1 ? 0 : mc.take(sizeof(uint32_t) * 6 * npts);
+  const size_t o_disp = mc.take((size_t)d.nmat);
+  const size_t o_ce4 = mc.take(sizeof(float4) * d.nmat);
+  const size_t o_ces = mc.take(sizeof(float) * d.nmat);
+  const size_t o_ch4 = mc.take(sizeof(float4) * d.nmat);
+  const size_t o_chs = mc.take(sizeof(float) * d.nmat);
+  const size_t o_cd = d.maxpoles > 0 ? mc.take(sizeof(float2) * 3 * d.maxpoles * d.nmat) : 0;
+  char* m = nullptr;
+  if (rc == GBF_OK) {
+    me = cudaMalloc((void**)&m, mc.off);
+    if (me != cudaSuccess) {
+      (void)cudaGetLastError();
+      m = nullptr;
+      rc = fail(ctx, GBF_ENOMEM, "gbf_create: cudaMalloc of %zu bytes failed: %s", mc.off, cudaGetErrorString(me));
+    } else if (cudaMemsetAsync(m, 0, mc.off, ctx->stream) != cudaSuccess) {
+      rc = fail(ctx, GBF_ECUDA, "gbf_create: clearing the material arrays failed");
+    }
+  }
+  if (m) {
+    ctx->mats = std::make_shared<MatSet>();
+    ctx->mats->ptrs = {m};
+    ctx->mat_bytes = mc.off;
+    ctx->bytes += mc.off;
+    if (ctx->idp == 1) {
+      ctx->PE = reinterpret_cast<uint32_t*>(m + o_pe);
+      ctx->PH = reinterpret_cast<uint32_t*>(m + o_ph);
+    } else {
+      ctx->ID = reinterpret_cast<uint32_t*>(m + o_id);
+    }
+    ctx->disp = reinterpret_cast<unsigned char*>(m + o_disp);
+    ctx->cE4 = reinterpret_cast<float4*>(m + o_ce4);
+    ctx->cEs = reinterpret_cast<float*>(m + o_ces);
+    ctx->cH4 = reinterpret_cast<float4*>(m + o_ch4);
+    ctx->cHs = reinterpret_cast<float*>(m + o_chs);
+    if (d.maxpoles > 0) ctx->cD = reinterpret_cast<float2*>(m + o_cd);
   }
   if (rc != GBF_OK) {
     g_create_err = ctx->err;
     gbf_destroy(ctx);
     return rc;
   }
-  ctx->mats = std::make_shared<MatSet>();
-  ctx->mats->ptrs = {ctx->ID, ctx->PE, ctx->PH, ctx->disp, ctx->cE4, ctx->cEs, ctx->cH4, ctx->cHs, ctx->cD};
-  ctx->mat_bytes = (ctx->idp == 1 ? 2 * sizeof(uint32_t) * ncomp : 6 * sizeof(uint32_t) * npts) +
-                   (size_t)d.nmat * (1 + 2 * sizeof(float4) + 2 * sizeof(float)) +
-                   (d.maxpoles > 0 ? sizeof(float2) * 3 * d.maxpoles * d.nmat : 0);
 
   // kernel parameters
   StepParams& p = ctx->sp;
@@ -681,7 +741,7 @@ __global__ void finish_packed_ids(uint32_t* __restrict__ pe, const uint32_t* __r
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
     uint32_t w = pe[q];
-    const uint32_t h = ph[q];
+    const uint32_t h = ph ? ph[q] : 0u;
     const uint32_t ex = w & kPackMask, ey = (w >> kPackBits) & kPackMask, ez = (w >> (2 * kPackBits)) & kPackMask;
     const uint32_t a = max(max(ex, ey), ez);
     const uint32_t b = max(max(h & kPackMask, (h >> kPackBits) & kPackMask), (h >> (2 * kPackBits)) & kPackMask);
@@ -796,12 +856,14 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ids) ctx->ph_uploaded = true;
     if (ids)
       pack_ids_from<<<sms * 8, 256, 0, ctx->stream>>>(ids, ctx->npts, nmat,
                                                      ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
                                                      ctx->PE, ctx->PH, dmax);
     else
-      finish_packed_ids<<<sms * 8, 256, 0, ctx->stream>>>(ctx->PE, ctx->PH, ctx->npts, nmat,
+      finish_packed_ids<<<sms * 8, 256, 0, ctx->stream>>>(ctx->PE, ctx->ph_uploaded ? ctx->PH : nullptr,
+                                                         ctx->npts, nmat,
                                                          ctx->d.maxpoles > 0 ? ctx->disp : nullptr,
                                                          dmax);
     CK(cudaGetLastError());
@@ -931,18 +993,25 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
 int gbf_upload_materials_packed(gbf_ctx* ctx, const uint32_t* PE, const uint32_t* PH,
                                 const float* coeffE, const float* coeffH, const float* coeffD) {
   if (!ctx) return GBF_EINVAL;
-  if (!PE || !PH || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
+  if (!PE || !coeffE || !coeffH || (ctx->d.maxpoles > 0 && !coeffD))
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: NULL array");
+  // the H words may be left out when every material has the same H row: no kernel reads them
+  if (!PH)
+    for (int m = 1; m < ctx->d.nmat; ++m)
+      if (memcmp(coeffH + 5 * m, coeffH, 5 * sizeof(float)) != 0)
+        return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: the H words may be omitted only "
+                    "when every material has the same H row (material %d differs)", m);
   if (ctx->idp != 1)
     return fail(ctx, GBF_EINVAL, "gbf_upload_materials_packed: %d materials do not pack (at most 1024)", ctx->d.nmat);
   const size_t bytes = sizeof(uint32_t) * (size_t)ctx->npts;
   CK(cudaMemcpyAsync(ctx->PE, PE, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->PH, PH, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  if (PH) CK(cudaMemcpyAsync(ctx->PH, PH, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->ph_uploaded = PH != nullptr;
   return upload_tables(ctx, coeffE, coeffH, coeffD, nullptr);
 }
 
 int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint32_t* maxid) {
-  if (!ID || !PE || !PH || n < 1) return fail(nullptr, GBF_EINVAL, "gbf_pack_ids: bad arguments");
+  if (!ID || !PE || n < 1) return fail(nullptr, GBF_EINVAL, "gbf_pack_ids: bad arguments");
   // contiguous ranges over the host's cores; each range packs and keeps its largest ID
   unsigned nt = std::thread::hardware_concurrency();
   nt = nt < 1 ? 1 : (nt > 64 ? 64 : nt);
@@ -951,16 +1020,27 @@ int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint
   auto work = [&](unsigned t) {
     const int64_t lo = n * (int64_t)t / nt, hi = n * (int64_t)(t + 1) / nt;
     uint32_t m = 0;
-    for (int64_t q = lo; q < hi; ++q) {
-      const uint32_t ex = ID[q], ey = ID[n + q], ez = ID[2 * n + q];
-      const uint32_t hx = ID[3 * n + q], hy = ID[4 * n + q], hz = ID[5 * n + q];
-      const uint32_t a = ex > ey ? ex : ey, b = hx > hy ? hx : hy;
-      const uint32_t c = ez > hz ? ez : hz;
-      const uint32_t ab = a > b ? a : b;
-      m = m > ab ? m : ab;
-      m = m > c ? m : c;
-      PE[q] = (ex & kPackMask) | ((ey & kPackMask) << kPackBits) | ((ez & kPackMask) << (2 * kPackBits));
-      PH[q] = (hx & kPackMask) | ((hy & kPackMask) << kPackBits) | ((hz & kPackMask) << (2 * kPackBits));
+    if (PH) {
+      for (int64_t q = lo; q < hi; ++q) {
+        const uint32_t ex = ID[q], ey = ID[n + q], ez = ID[2 * n + q];
+        const uint32_t hx = ID[3 * n + q], hy = ID[4 * n + q], hz = ID[5 * n + q];
+        const uint32_t a = ex > ey ? ex : ey, b = hx > hy ? hx : hy;
+        const uint32_t c = ez > hz ? ez : hz;
+        const uint32_t ab = a > b ? a : b;
+        m = m > ab ? m : ab;
+        m = m > c ? m : c;
+        PE[q] = (ex & kPackMask) | ((ey & kPackMask) << kPackBits) | ((ez & kPackMask) << (2 * kPackBits));
+        PH[q] = (hx & kPackMask) | ((hy & kPackMask) << kPackBits) | ((hz & kPackMask) << (2 * kPackBits));
+      }
+    } else {
+      // the E words only (a model whose materials share one H row needs no H IDs)
+      for (int64_t q = lo; q < hi; ++q) {
+        const uint32_t ex = ID[q], ey = ID[n + q], ez = ID[2 * n + q];
+        const uint32_t a = ex > ey ? ex : ey;
+        m = m > a ? m : a;
+        m = m > ez ? m : ez;
+        PE[q] = (ex & kPackMask) | ((ey & kPackMask) << kPackBits) | ((ez & kPackMask) << (2 * kPackBits));
+      }
     }
     mx[t] = m;
   };
@@ -1178,12 +1258,17 @@ int gbf_set_snapshots(gbf_ctx* ctx, const int32_t* defs) {
 int gbf_reset(gbf_ctx* ctx) {
   if (!ctx) return GBF_EINVAL;
   const gbf_grid_desc& d = ctx->d;
-  CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * (ctx->fused_ok ? 12 : 6) * ctx->ncomp, ctx->stream));
-  if (ctx->T) CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)d.maxpoles * ctx->ncomp, ctx->stream));
-  if (ctx->phi_floats) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * ctx->phi_floats, ctx->stream));
+  // a context that has not stepped, nor had fields uploaded, still holds the zeros it was
+  // created with (every allocation is cleared then)
+  if (ctx->dirty) {
+    CK(cudaMemsetAsync(ctx->fields, 0, sizeof(float) * (ctx->fused_ok ? 12 : 6) * ctx->ncomp, ctx->stream));
+    if (ctx->T) CK(cudaMemsetAsync(ctx->T, 0, sizeof(float2) * 3 * (size_t)d.maxpoles * ctx->ncomp, ctx->stream));
+    if (ctx->phi_floats) CK(cudaMemsetAsync(ctx->pml_mem, 0, sizeof(float) * ctx->phi_floats, ctx->stream));
+    CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
+    ctx->dirty = false;
+  }
   set_current(ctx, 0);
-  CK(cudaMemsetAsync(ctx->rxs, 0, sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1), ctx->stream));
-  CK(cudaMemsetAsync(ctx->d_it, 0, sizeof(int), ctx->stream));
   if (d.ntl && (int)ctx->tls_init.size() == d.ntl) {
     // line state after the incident-wave run; samples 0 of Vtotal/Itotal are that state
     CK(cudaMemcpyAsync(ctx->tls, ctx->tls_init.data(), sizeof(TLine) * d.ntl,
@@ -1715,6 +1800,7 @@ int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags) {
   if (!ctx->materials) return fail(ctx, GBF_ESTATE, "gbf_run: materials not uploaded");
   if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
     return fail(ctx, GBF_EINVAL, "gbf_run: %d steps from iteration %d exceed %d iterations", nsteps, ctx->it, ctx->d.iterations);
+  if (nsteps > 0) ctx->dirty = true;
   if (ctx->fused_avail && !ctx->tuned && nsteps > 0) {
     int rc = tune_begin(ctx);
     if (rc) return rc;
@@ -1822,6 +1908,7 @@ int gbf_download_fields(gbf_ctx* ctx, float* fields) {
 
 int gbf_upload_fields(gbf_ctx* ctx, const float* fields) {
   if (!ctx || !fields) return GBF_EINVAL;
+  ctx->dirty = true;
   // both buffers of a fused model: E outside the half-step's range is read from either
   for (int b = 0; b < (ctx->fused_ok ? 2 : 1); ++b)
     CK(cudaMemcpy2DAsync(ctx->fields + (size_t)b * 6 * ctx->ncomp, sizeof(float) * ctx->ncomp,
@@ -1871,6 +1958,7 @@ int gbf_profile(gbf_ctx* ctx, int nsteps, float* ms_h, float* ms_e, float* ms_to
 
   if (nsteps < 0 || ctx->it + nsteps > ctx->d.iterations)
     return fail(ctx, GBF_EINVAL, "gbf_profile: too many steps");
+  if (nsteps > 0) ctx->dirty = true;
   std::vector<cudaEvent_t> ev(3 * nsteps + 1);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaEventRecord(ev[0], ctx->stream));
@@ -2270,6 +2358,7 @@ int gbf_batch_run(gbf_batch* b, int32_t nsteps, uint32_t flags) {
   int rc = check_batch_steps(b, nsteps);
   if (rc) return rc;
   if (nsteps == 0) return GBF_OK;
+  for (gbf_ctx* c : b->models) c->dirty = true;
   // the first steps of the first run time the candidate grid sizes (real steps)
   const int tuning = batch_tune(b, nsteps);
   if (tuning < 0) return tuning;

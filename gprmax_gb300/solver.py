@@ -173,10 +173,18 @@ class PinnedWords:
         self.ptr = ctypes.c_void_p(0)
 
 
+def uniform_h(G):
+    """Whether every material of ``G`` has the same H row (DA, DBx, DBy, DBz, srcm): true for
+    any model without magnetic materials, whose H half-step then reads no material IDs."""
+    h = np.asarray(G.updatecoeffsH, dtype=np.float32)
+    return bool((h.view(np.uint32) == h[:1].view(np.uint32)).all())
+
+
 def pack_materials(G):
-    """The material IDs of ``G`` as two packed words per node in page-locked host memory (E:
-    ``IDx | IDy << 10 | IDz << 20``, H likewise), the form ``DeviceModel(G, packed=...)``
-    uploads with a third of the bytes at the full copy rate. Packed on the host's cores
+    """The material IDs of ``G`` as packed words per node in page-locked host memory (E:
+    ``IDx | IDy << 10 | IDz << 20``, H likewise; the H words only when the materials' H rows
+    differ, else None in their place), the form ``DeviceModel(G, packed=...)`` uploads with a
+    third (a sixth) of the bytes at the full copy rate. Packed on the host's cores
     (``gbf_pack_ids``). Returns None for models with more than 1024 materials or IDs built in
     device memory. The words are a copy: pack again after changing ``G.ID``."""
     if len(G.materials) > 1024 or getattr(G, 'geom', None) is not None:
@@ -184,9 +192,11 @@ def pack_materials(G):
     lib = _native.lib()
     ID = np.ascontiguousarray(G.ID, dtype=np.uint32)
     n = ID[0].size
-    pe, ph = PinnedWords(lib, n), PinnedWords(lib, n)
+    pe = PinnedWords(lib, n)
+    ph = None if uniform_h(G) else PinnedWords(lib, n)
     mx = ctypes.c_uint32(0)
-    rc = lib.gbf_pack_ids(_ptr(ID), n, pe.ptr, ph.ptr, ctypes.byref(mx))
+    rc = lib.gbf_pack_ids(_ptr(ID), n, pe.ptr, ph.ptr if ph is not None else None,
+                          ctypes.byref(mx))
     if rc != 0:
         buf = ctypes.create_string_buffer(256)
         lib.gbf_last_error(None, buf, 256)
@@ -236,8 +246,8 @@ class DeviceModel:
         elif self.packed is not None:
             pe, ph = self.packed
             self._check(self.lib.gbf_upload_materials_packed(
-                self.ctx, pe.ptr, ph.ptr, _ptr(inp['coeffE']), _ptr(inp['coeffH']),
-                _ptr(inp['coeffD'])))
+                self.ctx, pe.ptr, ph.ptr if ph is not None else None, _ptr(inp['coeffE']),
+                _ptr(inp['coeffH']), _ptr(inp['coeffD'])))
         elif inp['ID'] is None:
             # IDs built in device memory: copied device to device
             self._check(self.lib.gbf_upload_materials_geom(

@@ -78,7 +78,11 @@ typedef struct gbf_grid_desc {
                                     grids with at most 1024 materials, for E no poles or at most
                                     two Debye-like poles: their inputs are copied chunk by chunk
                                     into shared memory ahead of the threads that update them;
-                                    the same results bit for bit); other bits 0 */
+                                    the same results bit for bit); bit 5: allocate the fused
+                                    step's second field buffer for a model with PML slabs too
+                                    (otherwise such models, for which the fused step is slower,
+                                    do without it and gbf_set_fused_tiles refuses them); other
+                                    bits 0 */
     int32_t ntl;                 /* transmission lines among the nsrc sources */
     int32_t reserved[2];         /* must be zero */
 } gbf_grid_desc;
@@ -107,15 +111,18 @@ int gbf_upload_materials(gbf_ctx* ctx, const uint32_t* ID, const float* coeffE,
  * by gbf_pack_ids: PE uint32 [nx+1][ny+1][nz+1] = IDx | IDy << 10 | IDz << 20 of the E
  * components, PH the same for H; coefficient tables as for gbf_upload_materials. Copies a third
  * of the bytes of the ID array (from page-locked memory, see gbf_host_alloc, at the full copy
- * rate). GBF_EINVAL when an ID does not index the tables or the model has more than 1024
+ * rate). PH may be NULL when every material has the same H row (no magnetic materials: no
+ * kernel then reads H IDs), which halves the copy. GBF_EINVAL when an ID does not index the
+ * tables, PH is NULL for a model whose H rows differ, or the model has more than 1024
  * materials. No counterpart in the reference: the same upload as gbf_upload_materials
  * (model_build_run.py:512-529) from a compact form of the ID array. */
 int gbf_upload_materials_packed(gbf_ctx* ctx, const uint32_t* PE, const uint32_t* PH,
                                 const float* coeffE, const float* coeffH, const float* coeffD);
 
 /* Pack an ID array [6][n] (n nodes per component, the layout of gbf_upload_materials) into
- * PE and PH [n] on the host's cores; *maxid gets the largest ID (GBF_EINVAL above 1023). Host
- * arithmetic only. No counterpart in the reference. */
+ * PE and PH [n] on the host's cores (PH NULL: the E words only, and only the E IDs read);
+ * *maxid gets the largest ID packed (GBF_EINVAL above 1023). Host arithmetic only. No
+ * counterpart in the reference. */
 int gbf_pack_ids(const uint32_t* ID, int64_t n, uint32_t* PE, uint32_t* PH, uint32_t* maxid);
 
 /* Page-locked host memory (cudaHostAlloc) for the inputs of gbf_upload_materials_packed, and

@@ -27,7 +27,8 @@ def _build(name):
 
 def _run(G, options=0, tiles=None, nsteps=None, graph=True):
     from gprmax_gb300.solver import DeviceModel
-    dm = DeviceModel(G, options)
+    # option bit 5: the fused step's buffers for models with PML slabs too
+    dm = DeviceModel(G, options | (32 if tiles is not None else 0))
     try:
         info = dm.step_info()
         if tiles is not None:
@@ -82,7 +83,7 @@ def test_odd_step_counts_and_graph_parity(native):
     G = _build('debye1')
     whole = _run(G, tiles=(7, 3))
     for split in ([1, 33, G.iterations - 34], [17, 16, G.iterations - 33], [5, G.iterations - 5]):
-        dm = DeviceModel(G)
+        dm = DeviceModel(G, 32)
         dm.set_fused_tiles(7, 3)
         try:
             for n, graph in zip(split, [True, False, True]):
@@ -124,9 +125,19 @@ def test_fields_round_trip_and_reset(native):
 
 def test_step_info_reports_the_tuned_tiling(native):
     """A model without PML times its candidates (fused tilings, the half-step kernels) in the
-    first steps of its run; a model with PML takes the half-step kernels from the start."""
+    first steps of its run; a model with PML takes the half-step kernels from the start and has
+    no second field buffer unless option bit 5 asks for one."""
+    from gprmax_gb300.exceptions import SolverError
     from gprmax_gb300.solver import DeviceModel
     dm = DeviceModel(_build('fs_hori1'))
+    try:
+        info = dm.step_info()
+        assert not info['fused_available'] and not info['two_buffers'] and not info['fused']
+        with pytest.raises(SolverError):
+            dm.set_fused_tiles(7, 0)
+    finally:
+        dm.close()
+    dm = DeviceModel(_build('fs_hori1'), 32)
     try:
         info = dm.step_info()
         assert info['fused_available'] and info['tuned'] and not info['fused']

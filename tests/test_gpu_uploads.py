@@ -61,8 +61,11 @@ def test_packed_upload_gives_the_same_run(native, name):
     from gprmax_gb300.model import build_grid
     from gprmax_gb300.solver import DeviceModel, pack_materials
     G = build_grid(MODELS[name].splitlines(True), messages=False)
+    words = pack_materials(G)
+    # the H words only for a model with magnetic materials ('smoothed')
+    assert (words[1] is None) == (name != 'smoothed')
     out = []
-    for packed in (None, pack_materials(G)):
+    for packed in (None, words):
         dm = DeviceModel(G, packed=packed)
         try:
             dm.run()
@@ -95,5 +98,13 @@ def test_packed_upload_rejects_bad_words(native):
         rc = native.gbf_upload_materials_packed(ctx, pe.ptr, ph.ptr, cE.ctypes.data_as(ctypes.c_void_p),
                                                 cH.ctypes.data_as(ctypes.c_void_p), None)
         assert rc == 0
+        # no H words: accepted while every H row is the same, refused otherwise
+        rc = native.gbf_upload_materials_packed(ctx, pe.ptr, None, cE.ctypes.data_as(ctypes.c_void_p),
+                                                cH.ctypes.data_as(ctypes.c_void_p), None)
+        assert rc == 0
+        cH[3, 0] = 0.5
+        rc = native.gbf_upload_materials_packed(ctx, pe.ptr, None, cE.ctypes.data_as(ctypes.c_void_p),
+                                                cH.ctypes.data_as(ctypes.c_void_p), None)
+        assert rc == GBF_EINVAL
     finally:
         native.gbf_destroy(ctx)

@@ -258,6 +258,11 @@ def test_pack_ids_on_the_host(native_lib):
     ID[4, 777] = 1024
     assert native_lib.gbf_pack_ids(p(ID), n, p(pe), p(ph), ctypes.byref(mx)) == -1
     assert mx.value == 1024
+    # the E words only: H IDs are not read
+    pe2 = np.zeros(n, np.uint32)
+    assert native_lib.gbf_pack_ids(p(ID), n, p(pe2), None, ctypes.byref(mx)) == 0
+    np.testing.assert_array_equal(pe2, ID[0] | (ID[1] << 10) | (ID[2] << 20))
+    assert mx.value == ID[:3].max()
 
 
 def _staged_consumers():

@@ -52,7 +52,7 @@ def test_create_rejects_bad_descriptions(lib):
     d.dx = d.dy = d.dz = 1e-3
     ctx = ctypes.c_void_p(0)
     cases = [('pml_thickness', [10, 0, 0, 0, 0, 0]),   # 2 T >= n
-             ('maxpoles', 5), ('pml_order', 3), ('options', 32), ('nz', 0)]
+             ('maxpoles', 5), ('pml_order', 3), ('options', 64), ('nz', 0)]
     for field, value in cases:
         bad = _native.GridDesc.from_buffer_copy(d)
         if field == 'pml_thickness':
