@@ -59,13 +59,14 @@ def freespace_dipole(n=100, timewindow='3e-9', pml=10, messages=False):
 
 def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed=1,
                     timewindow='12e-9', cylinder=True, pml=10, messages=False, device_build=False,
-                    snapshot_at=0, device_fractals=False):
+                    snapshot_at=0, device_fractals=False, extra_lines=()):
     """Heterogeneous single-pole Debye soil below ``surface`` cells, air above.
 
     Per material: eps_s ~ U[5,20], eps_inf ~ U[3,6], tau ~ logU[1e-10,1e-8] s,
     sigma ~ logU[1e-4,1e-2] S/m. A PEC cylinder of radius 20 mm runs along y at depth 60 mm;
     an x-polarised dipole and a receiver 40 mm apart sit 10 mm above the surface.
-    ``snapshot_at`` > 0 adds a snapshot of the whole domain (every cell) at that iteration.
+    ``snapshot_at`` > 0 adds a snapshot of the whole domain (every cell) at that iteration;
+    ``extra_lines`` are further input commands (a PML formulation, CFS parameters).
     """
     rng = np.random.default_rng(seed)
     es = rng.uniform(5, 20, nmat)
@@ -90,6 +91,7 @@ def dispersive_soil(nx=400, ny=400, nz=200, dx=0.002, surface=150, nmat=50, seed
     if snapshot_at:
         lines.append('#snapshot: 0 0 0 {:g} {:g} {:g} {d:g} {d:g} {d:g} {} soil_snapshot'.format(
             nx * dx, ny * dx, nz * dx, int(snapshot_at), d=dx))
+    lines.extend(extra_lines)
     first_soil = 2
 
     def soil(G):

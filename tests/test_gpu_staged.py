@@ -106,3 +106,21 @@ def test_staged_soil(native):
     _equal(got, ref)
     dflt = _run(G, 0, 300)
     _equal(dflt, ref)
+
+
+@pytest.mark.parametrize('formulation,order', [('HORIPML', 2), ('MRIPML', 1), ('MRIPML', 2)])
+def test_staged_soil_other_pml_kinds(native, formulation, order):
+    """A 120 x 110 x 150 cut of the soil (chunks spanning several rows, z slabs on every row)
+    with second-order HORIPML and first- and second-order MRIPML (the CFS parameters of the
+    PML fixtures), 200 iterations: the staged sweeps equal the plain kernels."""
+    from gprmax_gb300 import workloads
+    cfs = ['#pml_cfs: constant forward 0 0 constant forward 1 1 sextic forward 0 0.5836',
+           '#pml_cfs: constant forward 0.05 0.05 cubic forward 1 8 quadratic forward 0 5.8357']
+    extra = ['#pml_formulation: {}'.format(formulation)] + cfs[2 - order:]
+    G = workloads.dispersive_soil(nx=120, ny=110, nz=150, surface=110, timewindow='1.5e-9',
+                                  pml=8, extra_lines=extra)
+    assert len(G.cfs) == order and G.pmlformulation == formulation
+    got = _run(G, 8, 200, forms=(True, True))
+    ref = _run(G, 8 | 16, 200)
+    assert got['info']['staged'] and got['info']['staged_h']
+    _equal(got, ref)
