@@ -154,8 +154,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, long lon
 // node s in the plane (jf = -1 for the up to three nodes before the plane's first), and whether
 // every node of the chunk lies in the core box; zst: the first Phi element of each z-slab copy
 // (z minus, z plus) x (CFS order 1, 2), as an index into the slab's Phi arrays.
+// (rows of 16 ints on 16-byte boundaries, so that a consumer reads its header in four vector
+// loads)
 enum { kHdrI, kHdrS, kHdrShE, kHdrShH, kHdrShJ, kHdrShI, kHdrJ, kHdrK, kHdrCore, kHdrZ,
-       kHdrInts = kHdrZ + 4 };
+       kHdrInts = 16 };
+static_assert(kHdrZ + 4 <= kHdrInts, "header row");
 
 __device__ __forceinline__ int clamp_start(int a, int amax) {
   return a < 0 ? 0 : (a > amax ? amax : a);
@@ -324,9 +327,9 @@ __device__ __forceinline__ void pml_axis_st(const StepParams& p, const StagedGeo
 template <int PK, int IDP, bool CORE>
 __device__ __forceinline__ void h_site_staged(const StepParams& p, const StagedGeom& g,
                                               const HCoef& hc, const float* rows,
-                                              const float* __restrict__ S, const int* h, int r,
-                                              int i, int j, int k, int idx, int it) {
-  const int shE = h[kHdrShE], shJ = h[kHdrShJ], shI = h[kHdrShI];
+                                              const float* __restrict__ S, const int* h, int shE,
+                                              int shJ, int shI, int r, int i, int j, int k,
+                                              int idx, int it) {
   static_assert(IDP == 0 || IDP == 1, "the staged H sweep reads packed IDs or none");
   constexpr int W = kStageSpan;
   const int nx = p.nx, ny = p.ny, nz = p.nz;
@@ -380,9 +383,8 @@ template <int PK, int NP, bool CORE, bool TR>
 __device__ __forceinline__ void e_site_staged(const StepParams& p, const StagedGeom& g,
                                               const float4* C4, const float* Cs, const float2* CD,
                                               const float* rows, const float* __restrict__ S,
-                                              const int* h, int r, int i, int j, int k, int idx,
-                                              int it) {
-  const int shE = h[kHdrShE], shH = h[kHdrShH], shJ = h[kHdrShJ], shI = h[kHdrShI];
+                                              const int* h, int shE, int shH, int shJ, int shI,
+                                              int r, int i, int j, int k, int idx, int it) {
   static_assert(NP == 0 || TR, "the staged sweep keeps real pole state only");
   constexpr int NPV = NP > 0 ? NP : 1;
   constexpr int W = kStageSpan;
@@ -448,7 +450,7 @@ template <bool ELECTRIC, int PK, int NP, bool TR, int IDP>
 __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGeom& g) {
   extern __shared__ __align__(128) float4 smem_st[];
   __shared__ uint64_t full[kStageMax], empty[kStageMax];
-  __shared__ int hdr[kStageMax][kHdrInts];
+  __shared__ __align__(16) int hdr[kStageMax][kHdrInts];
   __shared__ int abort_flag;
   // after a sweep that gave up, the run's fields are void: later launches return at once, until
   // the host has read and cleared the error word
@@ -531,21 +533,31 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
       return;
     }
     const int* h = hdr[st];
-    const int i = h[kHdrI], s = h[kHdrS];
-    int j = h[kHdrJ] + tq, k = h[kHdrK] + tr;
+    // the header's first twelve entries in three vector loads
+    const int4 ha = reinterpret_cast<const int4*>(h)[0];   // i, s, shE, shH
+    const int4 hb = reinterpret_cast<const int4*>(h)[1];   // shJ, shI, jf, kf
+    const int4 hc4 = reinterpret_cast<const int4*>(h)[2];  // core, z starts
+    static_assert(kHdrI == 0 && kHdrS == 1 && kHdrShE == 2 && kHdrShH == 3 && kHdrShJ == 4 &&
+                  kHdrShI == 5 && kHdrJ == 6 && kHdrK == 7 && kHdrCore == 8, "header layout");
+    const int i = ha.x, s = ha.y;
+    int j = hb.z + tq, k = hb.w + tr;
     if (k >= p.sy) { k -= p.sy; ++j; }
     if (j >= 0 && j < jend && k < kend) {
       const float* S = ring + (size_t)st * g.stage_floats;
       if (ELECTRIC) {
-        if (h[kHdrCore])
-          e_site_staged<PK, NP, true, TR>(p, g, C4, Cs, CD, rows, S, h, t, i, j, k, s + t, it);
+        if (hc4.x)
+          e_site_staged<PK, NP, true, TR>(p, g, C4, Cs, CD, rows, S, h, ha.z, ha.w, hb.x, hb.y,
+                                          t, i, j, k, s + t, it);
         else
-          e_site_staged<PK, NP, false, TR>(p, g, C4, Cs, CD, rows, S, h, t, i, j, k, s + t, it);
+          e_site_staged<PK, NP, false, TR>(p, g, C4, Cs, CD, rows, S, h, ha.z, ha.w, hb.x, hb.y,
+                                           t, i, j, k, s + t, it);
       } else {
-        if (h[kHdrCore])
-          h_site_staged<PK, IDP, true>(p, g, hc, rows, S, h, t, i, j, k, s + t, it);
+        if (hc4.x)
+          h_site_staged<PK, IDP, true>(p, g, hc, rows, S, h, ha.z, hb.x, hb.y, t, i, j, k, s + t,
+                                       it);
         else
-          h_site_staged<PK, IDP, false>(p, g, hc, rows, S, h, t, i, j, k, s + t, it);
+          h_site_staged<PK, IDP, false>(p, g, hc, rows, S, h, ha.z, hb.x, hb.y, t, i, j, k,
+                                        s + t, it);
       }
     }
     __syncwarp();
