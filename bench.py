@@ -414,6 +414,17 @@ def run_gb300(args):
                 'gpu_launches': b['gpu_launches']}}
         except Exception as e:   # the headline above stands either way
             out['extras'] = {'bscan2d_error': '{}: {}'.format(type(e).__name__, e)}
+        # the gradient workload's cost (section "adjoint"; the finite-difference check is left
+        # to --workload adjoint)
+        try:
+            c = adjoint_cost()
+            c['solver'].close()
+            out['extras']['adjoint'] = {
+                'workload': 'adjoint_200x200x100_grf', 'iterations': c['m'].iterations,
+                'forward_s': round(c['t_fwd'], 4), 'gradient_s': round(c['t_grad'], 4),
+                'gradient_over_forward': round(c['t_grad'] / c['t_fwd'], 3)}
+        except Exception as e:
+            out['extras']['adjoint_error'] = '{}: {}'.format(type(e).__name__, e)
     print(json.dumps(out), flush=True)
 
 
@@ -660,13 +671,10 @@ def measure_bscan2d(ntraces, W, with_cpu=False, cpu_budget=20.0):
     return out
 
 
-def run_adjoint(args):
-    """Gradient of a trace misfit with respect to per-cell eps_r and sigma on a 200x200x100 grid
-    at 2 mm, 8 ns (2079 iterations): GRF permittivity, random conductivity, 4 dipoles and 8
-    receivers, observed data from a model with a buried 40 mm box 5 % denser. Times the forward
-    (traces) and the checkpointed adjoint (gradient), and checks the gradient against central
-    finite differences of the same GPU forward (fp64 misfit) on 20 seeded cells among the most
-    sensitive 1 %."""
+def adjoint_cost(warmup=3):
+    """The gradient workload (run_adjoint) timed: the forward (traces and misfit) and the
+    gradient (forward with checkpoints, then the adjoint), medians of three after warm-up.
+    Returns the model, solver, parameters, observed traces, gradient and times."""
     import torch
     from gprmax_gb300 import workloads
     from gprmax_gb300.adjoint import AdjointModel, AdjointSolver, fdtd_traces
@@ -683,7 +691,7 @@ def run_adjoint(args):
         CA, CB = m.edge_coefficients(ee, s)
         tr = solver.forward(CA.float().contiguous(), CB.float().contiguous())
         return float(0.5 * ((tr.double() - obs) ** 2).sum())
-    for _ in range(max(args.warmup - 2, 1)):
+    for _ in range(max(warmup - 2, 1)):
         loss_of(e)
     fwd_times = []
     for _ in range(3):
@@ -692,9 +700,7 @@ def run_adjoint(args):
         loss_of(e)
         torch.cuda.synchronize()
         fwd_times.append(time.perf_counter() - t0)
-    t_fwd = float(np.median(fwd_times))
-    # the gradient (forward with checkpoints, then the adjoint), once untimed, then the median
-    # of three
+    # the gradient once untimed, then the median of three
     grad_times = []
     for rep in range(4):
         ee = e.clone().requires_grad_(True)
@@ -707,8 +713,25 @@ def run_adjoint(args):
         L.backward()
         torch.cuda.synchronize()
         grad_times.append(time.perf_counter() - t0)
-    t_grad = float(np.median(grad_times[1:]))
-    g = ee.grad
+    return {'m': m, 'solver': solver, 'e': e, 's': s, 'obs': obs, 'g': ee.grad, 'eps': eps,
+            'loss_of': loss_of, 't_fwd': float(np.median(fwd_times)),
+            't_grad': float(np.median(grad_times[1:])), 'fwd_times': fwd_times,
+            'grad_times': grad_times, 'misfit': float(L.detach())}
+
+
+def run_adjoint(args):
+    """Gradient of a trace misfit with respect to per-cell eps_r and sigma on a 200x200x100 grid
+    at 2 mm, 8 ns (2079 iterations): GRF permittivity, random conductivity, 4 dipoles and 8
+    receivers, observed data from a model with a buried 40 mm box 5 % denser. Times the forward
+    (traces) and the checkpointed adjoint (gradient), and checks the gradient against central
+    finite differences of the same GPU forward (fp64 misfit) on 20 seeded cells among the most
+    sensitive 1 %."""
+    import torch
+    from gprmax_gb300.adjoint import AdjointSolver, fdtd_traces
+    cost = adjoint_cost(args.warmup)
+    m, solver, e, s = cost['m'], cost['solver'], cost['e'], cost['s']
+    obs, g, eps = cost['obs'], cost['g'], cost['eps']
+    loss_of, t_fwd, t_grad = cost['loss_of'], cost['t_fwd'], cost['t_grad']
     # finite differences on 20 cells drawn from the 1 % with the largest |gradient|
     flat = g.abs().flatten()
     top = torch.topk(flat, max(20, flat.numel() // 100)).indices.cpu().numpy()
@@ -756,7 +779,7 @@ def run_adjoint(args):
                       'iterations': m.iterations, 'sources': len(m.sources),
                       'receivers': len(m.receivers)},
            'forward_s': round(t_fwd, 4), 'gradient_s': round(t_grad, 4),
-           'gradient_runs_s': [round(t, 4) for t in grad_times],
+           'gradient_runs_s': [round(t, 4) for t in cost['grad_times']],
            'checkpointing': ('interval -1: the last segment as long as 60 % of the free device '
                              'memory holds (kept from the forward, never recomputed), the steps '
                              'before it in segments of ceil(sqrt(their count))'),
@@ -764,12 +787,12 @@ def run_adjoint(args):
                                   'adjoint_over_forward': round(t_rich / t_fwd, 3),
                                   'gradient_runs_s': [round(t, 4) for t in rich_times],
                                   'max_rel_diff_vs_default': rich_dev},
-           'forward_runs_s': [round(t, 4) for t in fwd_times],
+           'forward_runs_s': [round(t, 4) for t in cost['fwd_times']],
            'forward_Mcells_per_s': round(cells_n * m.iterations / t_fwd / 1e6, 1),
            'fd_check': {'cells': len(errs), 'stencil': '4th-order central, h = 5 % of eps_r, GPU fp32 forward',
                         'median_rel_err': float(np.median(errs)) if errs else None,
                         'max_rel_err': float(np.max(errs)) if errs else None},
-           'misfit': float(L.detach())}
+           'misfit': cost['misfit']}
     print(json.dumps(out), flush=True)
 
 
