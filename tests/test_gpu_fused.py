@@ -167,3 +167,20 @@ def test_models_outside_the_fused_step_keep_two_kernels(native):
         G = _build(name)
         out = _run(G, nsteps=5)
         assert not out['info']['fused_available'] and not out['info']['two_buffers']
+
+
+def test_fused_step_two_debye_poles(native):
+    """The fused step with two Debye poles per material (real pole state, two poles) against the
+    two half-step kernels, on a PML-free soil with a two-pole box."""
+    from gprmax_gb300 import workloads
+    extra = ['#material: 4 0.001 1 0 twopole',
+             '#add_dispersion_debye: 2 3 1e-9 2 1e-10 twopole',
+             '#box: 0.02 0.02 0.02 0.08 0.07 0.06 twopole']
+    G = workloads.dispersive_soil(nx=60, ny=50, nz=70, surface=40, timewindow='3e-10', pml=0,
+                                  extra_lines=extra)
+    assert G.maxpoles == 2
+    ref = _run(G, options=8)
+    for tiles in ((7, 2), (15, 0)):
+        got = _run(G, tiles=tiles)
+        assert got['info_after']['fused']
+        _equal(got, ref)

@@ -124,3 +124,22 @@ def test_staged_soil_other_pml_kinds(native, formulation, order):
     ref = _run(G, 8 | 16, 200)
     assert got['info']['staged'] and got['info']['staged_h']
     _equal(got, ref)
+
+
+def test_staged_two_debye_poles(native):
+    """Two Debye poles per material (the real pole state with two poles, 17 streams a chunk):
+    a 60 x 50 x 70 soil with a two-pole box, staged against plain and against the oracle."""
+    import oracle
+    from gprmax_gb300 import workloads
+    extra = ['#material: 4 0.001 1 0 twopole',
+             '#add_dispersion_debye: 2 3 1e-9 2 1e-10 twopole',
+             '#box: 0.02 0.02 0.02 0.08 0.07 0.06 twopole']
+    G = workloads.dispersive_soil(nx=60, ny=50, nz=70, surface=40, timewindow='3e-10', pml=6,
+                                  extra_lines=extra)
+    assert G.maxpoles == 2
+    got = _run(G, 8, forms=(True, True))
+    assert got['info']['staged'] and got['info']['staged_h']
+    _equal(got, _run(G, 8 | 16))
+    ref = oracle.OracleSolver(G).run()
+    np.testing.assert_array_equal(got['rx'], ref.receivers())
+    np.testing.assert_array_equal(got['f'], ref.fields())
