@@ -152,6 +152,7 @@ _SIGS = {
     'gbf_last_error': (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     'gbf_version': (ctypes.c_char_p, []),
     'gbf_check_cell_division': (ctypes.c_int, [ctypes.c_float]),
+    'gbf_check_cell_division_device': (ctypes.c_int, [ctypes.c_float, ctypes.POINTER(ctypes.c_int32)]),
     'gbf_upload_tls': (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     'gbf_download_tls': (ctypes.c_int, [_P, _P]),
     'gbf_adj_create': (ctypes.c_int, [_P, ctypes.POINTER(_P)]),

@@ -117,6 +117,7 @@ struct gbf_ctx {
   StagedGeom sg{}, sgh{};
   size_t smem_st = 0, smem_sth = 0;
   int* d_err = nullptr;        // device error word of the staged sweeps (a wait ran out)
+  unsigned int* d_scr = nullptr;   // device scratch words: division check [0, 3), largest ID [4]
   std::shared_ptr<MatSet> mats;   // holds ID, PE, PH, disp and the tables (see MatSet)
   size_t mat_bytes = 0;        // their size
   bool shared_mats = false;    // adopted from another context
@@ -333,11 +334,50 @@ static FusedFn fused_kernel(int pk, int tj, int np, int uh, int tr) {
   }
 }
 
+// The same question on the device for a model's three cell sizes at once (what gbf_create
+// uses): bad[a] is set when the corrected product with r[a] differs from the IEEE quotient
+// x / d[a] for some x of the binade [1, 2), computed with the kernels' own operations. The
+// host loop takes about a millisecond per cell size; this takes microseconds.
+__global__ void division_check(float3 d, float3 r, unsigned int* bad) {
+  const int a = blockIdx.y;
+  const float dd = a == 0 ? d.x : (a == 1 ? d.y : d.z);
+  const float rr = a == 0 ? r.x : (a == 1 ? r.y : r.z);
+  unsigned int b = 0;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < (1u << 23);
+       m += gridDim.x * blockDim.x) {
+    const float x = __uint_as_float((127u << 23) | m);
+    const float q = __fmul_rn(x, rr);
+    b |= __fmaf_rn(__fmaf_rn(-q, dd, x), rr, q) != __fdiv_rn(x, dd) ? 1u : 0u;
+  }
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad + a, 1u);
+}
+
 extern "C" {
 
 const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
 
 int gbf_check_cell_division(float d) { return reciprocal_division_exact(d) ? 1 : 0; }
+
+int gbf_check_cell_division_device(float d, int32_t* exact) {
+  if (!exact) return fail(nullptr, GBF_EINVAL, "gbf_check_cell_division_device: NULL argument");
+  *exact = 0;
+  if (!(d >= 0x1p-20f && d <= 0x1p20f)) return GBF_OK;
+  unsigned int* bad = nullptr;
+  cudaError_t e = cudaMalloc((void**)&bad, 3 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(bad, 0, 3 * sizeof(unsigned int));
+  if (e == cudaSuccess) {
+    const float r = 1.0f / d;
+    division_check<<<dim3(2048, 3), 256>>>(make_float3(d, d, d), make_float3(r, r, r), bad);
+    e = cudaGetLastError();
+  }
+  unsigned int h[3] = {1u, 1u, 1u};
+  if (e == cudaSuccess) e = cudaMemcpy(h, bad, sizeof h, cudaMemcpyDeviceToHost);
+  if (bad) cudaFree(bad);
+  if (e != cudaSuccess)
+    return fail(nullptr, GBF_ECUDA, "gbf_check_cell_division_device: %s", cudaGetErrorString(e));
+  *exact = (h[0] | h[1] | h[2]) ? 0 : 1;
+  return GBF_OK;
+}
 
 int gbf_fused_tiles(int32_t nx, int32_t ny, int32_t nz, int32_t tj, int32_t nch, int32_t* out) {
   if (nx < 1 || ny < 1 || nz < 1 || tj < 1 || tj > 31 || !out) return GBF_EINVAL;
@@ -465,7 +505,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     }
   };
   size_t o_fields = 0, o_T = 0, o_pml = 0, o_coef = 0, o_srcs = 0, o_waves = 0, o_rxc = 0,
-         o_rxs = 0, o_it = 0, o_err = 0, o_tls = 0, o_tlw = 0, o_tlo = 0;
+         o_rxs = 0, o_it = 0, o_err = 0, o_scr = 0, o_tls = 0, o_tlw = 0, o_tlo = 0;
   auto layout = [&](bool two) {
     Carve c;
     o_fields = c.take(sizeof(float) * (two ? 12 : 6) * ncomp);
@@ -479,6 +519,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     o_rxs = c.take(sizeof(float) * 9 * (size_t)d.iterations * (d.nrx + 1));
     o_it = c.take(sizeof(int));
     o_err = c.take(sizeof(int) * 16);
+    o_scr = c.take(sizeof(unsigned int) * 16);
     if (d.ntl) {
       o_tls = c.take(sizeof(TLine) * d.ntl);
       o_tlw = c.take(sizeof(float) * 2 * (size_t)d.ntl * d.iterations);
@@ -515,6 +556,7 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     ctx->rxs = reinterpret_cast<float*>(a + o_rxs);
     ctx->d_it = reinterpret_cast<int*>(a + o_it);
     ctx->d_err = reinterpret_cast<int*>(a + o_err);
+    ctx->d_scr = reinterpret_cast<unsigned int*>(a + o_scr);
     if (d.ntl) {
       ctx->tls = reinterpret_cast<TLine*>(a + o_tls);
       ctx->tl_waves = reinterpret_cast<float*>(a + o_tlw);
@@ -610,7 +652,8 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
     sl.rcp = 1.0f / sl.d;
     // per axis (the kernels read it from the minus slab of either side's axis)
     const bool axis_pml = d.pml_thickness[s % 3] || d.pml_thickness[s % 3 + 3];
-    sl.fastdiv = (axis_pml && !(d.options & 2) && reciprocal_division_exact(sl.d)) ? 1 : 0;
+    // a candidate here; division_check below decides
+    sl.fastdiv = (axis_pml && !(d.options & 2) && sl.d >= 0x1p-20f && sl.d <= 0x1p20f) ? 1 : 0;
     if (!t) continue;
     const int ax = s % 3;
     const long long nu = ax == 0 ? d.ny : d.nx, nv = ax == 2 ? d.ny : d.nz;
@@ -645,7 +688,20 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   r.tls = ctx->tls;
   r.ntl = 0;
   r.tl_out = ctx->tl_out;
-  e = cudaStreamSynchronize(ctx->stream);
+  // the corrected-product division per axis, checked on the device (after the arena's clear,
+  // which zeroes the flags)
+  if (p.slab[0].fastdiv || p.slab[1].fastdiv || p.slab[2].fastdiv) {
+    division_check<<<dim3(2048, 3), 256, 0, ctx->stream>>>(
+        make_float3(p.slab[0].d, p.slab[1].d, p.slab[2].d),
+        make_float3(p.slab[0].rcp, p.slab[1].rcp, p.slab[2].rcp), ctx->d_scr);
+    unsigned int bad[3] = {1u, 1u, 1u};
+    e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(bad, ctx->d_scr, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    for (int s = 0; s < 6; ++s) p.slab[s].fastdiv = p.slab[s].fastdiv && !bad[s % 3];
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     fail(nullptr, GBF_ECUDA, "gbf_create: %s", cudaGetErrorString(e));
     gbf_destroy(ctx);
@@ -850,8 +906,7 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
   }
   CK(cudaMemcpyAsync(ctx->disp, disp.data(), nmat, cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->idp == 1) {
-    unsigned int* dmax = nullptr;
-    CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
+    unsigned int* dmax = ctx->d_scr + 4;
     CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
@@ -869,7 +924,6 @@ static int upload_tables(gbf_ctx* ctx, const float* coeffE, const float* coeffH,
     CK(cudaGetLastError());
     unsigned int mx = 0;
     CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(dmax, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (mx >= (unsigned)nmat) {
       ctx->materials = false;
@@ -902,14 +956,12 @@ __global__ void id_max_kernel(const uint32_t* a, long long n, unsigned int* mx) 
 // The largest ID in ctx->ID (on the device) must index the coefficient tables.
 static int check_ids(gbf_ctx* ctx, const char* who) {
   const size_t n = 6 * (size_t)ctx->npts;
-  unsigned int* dmax = nullptr;
-  CK(cudaMallocAsync((void**)&dmax, sizeof(unsigned int), ctx->stream));
+  unsigned int* dmax = ctx->d_scr + 4;
   CK(cudaMemsetAsync(dmax, 0, sizeof(unsigned int), ctx->stream));
   id_max_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->ID, (long long)n, dmax);
   CK(cudaGetLastError());
   unsigned int mx = 0;
   CK(cudaMemcpyAsync(&mx, dmax, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaFreeAsync(dmax, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (mx >= (unsigned)ctx->d.nmat)
     return fail(ctx, GBF_EINVAL, "%s: ID %u >= nmat %d", who, mx, ctx->d.nmat);

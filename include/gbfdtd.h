@@ -374,9 +374,15 @@ int gbf_adj_backward_static(gbf_adj* adj, const float* CA, const float* CB, cons
 /* 1 if, for this cell size, the PML kernels may form dF/d as the product with the rounded
  * reciprocal corrected once by the exact residual, because that equals the IEEE quotient for
  * every dF; 0 otherwise (the kernels then divide). Host only, no device needed; gbf_create
- * checks each slab's cell size this way. No counterpart in the reference, whose PML kernels
+ * asks the same of each axis's cell size on the device (gbf_check_cell_division_device). No
+ * counterpart in the reference, whose PML kernels
  * divide (pml_updates_electric_HORIPML_ext.pyx:80 `dHz = (...) / dx`). */
 int gbf_check_cell_division(float d);
+
+/* The same check on the current CUDA device, with the kernels' own operations (*exact = 1 or
+ * 0); what gbf_create runs for each axis's cell size, in microseconds where the host loop of
+ * gbf_check_cell_division takes about a millisecond. GBF_ECUDA without a device. */
+int gbf_check_cell_division_device(float d, int32_t* exact);
 
 /* The sweep boxes a half-step kernel walks for a grid (electric != 0: E half-step, domain
  * [0,nx) x [0,ny) x [0,nz); else H, domain [0,nx] x [0,ny] x [0,nz]): six rows of ten int32

@@ -108,3 +108,25 @@ def test_packed_upload_rejects_bad_words(native):
         assert rc == GBF_EINVAL
     finally:
         native.gbf_destroy(ctx)
+
+
+def test_device_division_check_agrees_with_the_host_loop():
+    """gbf_create decides the PML kernels' division form per axis on the device; for cell sizes
+    across the range (the soil's 2 mm, round sizes, significands at both ends of the binade,
+    seeded random ones) the device's answer is the host loop's, and sizes outside the window
+    are refused without a launch."""
+    from gprmax_gb300 import _native
+    lib = _native.lib()
+    rng = np.random.default_rng(11)
+    ds = [2e-3, 1e-3, 5e-4, 1e-2, 0.1, 1.0, 1.5]
+    ds += [float(np.float32(1 + 2.0 ** -23)), float(np.float32(2 - 2.0 ** -23))]
+    ds += [float(v) for v in (10 ** rng.uniform(-5, 2, 12)).astype(np.float32)]
+    for d in ds:
+        d = float(np.float32(d))
+        ok = ctypes.c_int32(-1)
+        assert lib.gbf_check_cell_division_device(d, ctypes.byref(ok)) == 0
+        assert ok.value == lib.gbf_check_cell_division(d), d
+    for d in (1e-7, 2e7, 0.0, -1e-3, float('nan')):
+        ok = ctypes.c_int32(-1)
+        assert lib.gbf_check_cell_division_device(d, ctypes.byref(ok)) == 0
+        assert ok.value == 0
