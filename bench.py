@@ -192,14 +192,14 @@ class ClockSampler:
                 'reasons': sorted(reasons), 'samples': len(self.rows)}
 
 
-def build_workload(iterations, grid=None, snapshot_at=0):
+def build_workload(iterations, grid=None, snapshot_at=0, pml='10'):
     from gprmax_gb300 import workloads
     if grid:
         nx, ny, nz = grid
         G = workloads.dispersive_soil(nx=nx, ny=ny, nz=nz, surface=int(nz * 0.75),
-                                      snapshot_at=snapshot_at)
+                                      snapshot_at=snapshot_at, pml=pml)
     else:
-        G = workloads.dispersive_soil(snapshot_at=snapshot_at)
+        G = workloads.dispersive_soil(snapshot_at=snapshot_at, pml=pml)
     if iterations > G.iterations:
         # longer time window; per-step work is unchanged
         G.iterations = iterations
@@ -216,7 +216,9 @@ def workload_config(G, args, world):
     """The ``config`` both arms print for the soil workload (the same dict for the same model)."""
     return {'workload': WORKLOAD if not args.grid else 'dispersive_soil_{}x{}x{}'.format(*args.grid),
             'grid': [G.nx, G.ny, G.nz], 'dx_m': G.dx, 'materials': len(G.materials),
-            'poles': G.maxpoles, 'pml_cells': 10, 'cells': G.nx * G.ny * G.nz,
+            'poles': G.maxpoles,
+            'pml_cells': int(args.pml) if len(args.pml.split()) == 1 else [int(v) for v in args.pml.split()],
+            'cells': G.nx * G.ny * G.nz,
             'l2': 'working set {:.2f} GB > L2 (129 MB), no flush'.format(dm_bytes(G) / 1e9),
             'replicas': world}
 
@@ -298,7 +300,8 @@ def run_gb300(args):
     from gprmax_gb300.solver import DeviceModel
     _native.lib()
     K, W = args.steps, args.warmup
-    G = build_workload(max(3117, K + W + args.profile_steps + 1), args.grid, args.snapshot_at)
+    G = build_workload(max(3117, K + W + args.profile_steps + 1), args.grid, args.snapshot_at,
+                       args.pml)
     cells = G.nx * G.ny * G.nz
     # warm the CUDA context with a tiny model (not timed)
     from gprmax_gb300.workloads import freespace_dipole
@@ -319,6 +322,8 @@ def run_gb300(args):
     packed = pack_materials(G)
     t0 = time.perf_counter()
     dm = DeviceModel(G, options, packed=packed)
+    if args.staged:
+        dm.set_step_forms(True, True)
     t1 = time.perf_counter()
     dm.run(K)
     dm.synchronize()
@@ -451,7 +456,7 @@ def run_reference(args):
         return
     import ref_cpu
     K, W = args.steps, args.warmup
-    G = build_workload(3117, args.grid)
+    G = build_workload(3117, args.grid, pml=args.pml)
     cores = os.cpu_count() or 1
     solver, kind = ref_cpu.make_solver(G, cores)
     t0 = time.perf_counter()
@@ -899,6 +904,8 @@ def main():
     ap.add_argument('--ref-budget', type=float, default=150.0)
     ap.add_argument('--grid', type=int, nargs=3, default=None,
                     help='smaller soil grid (profiling runs); default 400 400 200')
+    ap.add_argument('--pml', default='10',
+                    help="soil: PML cells, one value or six (x0 y0 z0 xmax ymax zmax), as #pml_cells")
     ap.add_argument('--snapshot-at', type=int, default=0,
                     help='soil: add a snapshot of the whole domain at this iteration (profiling)')
     ap.add_argument('--fd-cells', type=int, default=20,
@@ -908,6 +915,9 @@ def main():
     ap.add_argument('--fused-buffers', action='store_true',
                     help='soil: give the model the fused step\'s second field buffer although it '
                          'has PML slabs (with GBF_FUSED_TILE, to time the fused step there)')
+    ap.add_argument('--staged', action='store_true',
+                    help='soil: both half-steps as staged sweeps, without the form tuner (for ncu, '
+                         'under which the tuner\'s own timings are distorted)')
     ap.add_argument('--plain-e', action='store_true',
                     help='soil: the plain E half-step kernel instead of the staged sweep')
     ap.add_argument('--no-extras', dest='extras', action='store_false',
