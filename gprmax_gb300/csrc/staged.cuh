@@ -490,11 +490,12 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
   if (warp == 0) {
     // the producer: lane 0 fills the ring, a stage again once all consumer warps left it
     if (lane != 0) return;
-    int n = 0;
+    // chunk n goes to stage st = n % nstages in round n / nstages; from the second round on it
+    // waits for the phase of the round before (parity of round - 1), counted as it goes
+    int n = 0, st = 0;
+    uint32_t round = 0;
     for (int c = blockIdx.x; c < g.nchunks; c += G, ++n) {
-      const int st = n % g.nstages;
-      if (n >= g.nstages &&
-          !mbar_wait(&empty[st], (uint32_t)(n / g.nstages - 1) & 1u, g.limit_ns, abortp)) {
+      if (round > 0 && !mbar_wait(&empty[st], (round - 1) & 1u, g.limit_ns, abortp)) {
         *abortp = 1;
         atomicOr(g.err, 1);
         break;
@@ -502,6 +503,10 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
       // the consumers' reads of this stage are ordered before the copies that refill it
       proxy_async_fence();
       stage_chunk<ELECTRIC, PK, NP, IDP>(p, g, ring, &full[st], hdr[st], c, st);
+      if (++st == g.nstages) {
+        st = 0;
+        ++round;
+      }
     }
     // on giving up: let the copies in flight (the latest chunk of each stage) land before the
     // block may end
@@ -524,10 +529,11 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
   const float4* C4 = p.smem ? s4 : p.cE4;
   const float* Cs = p.smem ? ss : p.cEs;
   const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
-  int n = 0;
-  for (int c = blockIdx.x; c < g.nchunks; c += G, ++n) {
-    const int st = n % g.nstages;
-    if (!mbar_wait(&full[st], (uint32_t)(n / g.nstages) & 1u, g.limit_ns, abortp)) {
+  // stage and phase parity of the next chunk, counted as it goes (no division per chunk)
+  int st = 0;
+  uint32_t parity = 0;
+  for (int c = blockIdx.x; c < g.nchunks; c += G) {
+    if (!mbar_wait(&full[st], parity, g.limit_ns, abortp)) {
       *abortp = 1;
       atomicOr(g.err, 1);
       return;
@@ -562,6 +568,10 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[st]);
+    if (++st == g.nstages) {
+      st = 0;
+      parity ^= 1u;
+    }
   }
 }
 
