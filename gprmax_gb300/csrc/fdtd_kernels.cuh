@@ -399,7 +399,8 @@ __device__ __forceinline__ float hsrcm(const StepParams& p, const HCoef& c, uint
 // differences and the Phi state), then each component takes its main update and its
 // corrections in the reference's order.
 // h_node_x takes the slab X values already formed (XA, XB per axis; zero off the slabs).
-template <int PK, int IDP, bool CORE>
+// THREE_D: the caller runs only for 3D grids (the 2D gating is then known to pass).
+template <int PK, int IDP, bool CORE, bool THREE_D = false>
 __device__ __forceinline__ void h_node_x(const StepParams& p, const HCoef& hc,
                                          int i, int j, int k, bool src, int it, const int* where,
                                          const float* XA, const float* XB, float dEz_y,
@@ -411,9 +412,9 @@ __device__ __forceinline__ void h_node_x(const StepParams& p, const HCoef& hc,
   const bool ipos = CORE || i >= 1, jpos = CORE || j >= 1;
   // 2D grids (update_magnetic's 2D branch, fields_updates_ext.pyx:377-400): Hx only when ny or
   // nz is one cell and only below i = nx; Hy, Hz likewise along j and k
-  const bool hx2 = !p.two_d || ((ny == 1 || nz == 1) && iin);
-  const bool hy2 = !p.two_d || ((nx == 1 || nz == 1) && jin);
-  const bool hz2 = !p.two_d || ((nx == 1 || ny == 1) && kin);
+  const bool hx2 = THREE_D || !p.two_d || ((ny == 1 || nz == 1) && iin);
+  const bool hy2 = THREE_D || !p.two_d || ((nx == 1 || nz == 1) && jin);
+  const bool hz2 = THREE_D || !p.two_d || ((nx == 1 || ny == 1) && kin);
   // Hx: main i in [1,nx], j in [0,ny), k in [0,nz); slabs along y and z
   {
     const bool mainu = ipos && jin && kin && hx2;

@@ -370,7 +370,7 @@ __device__ __forceinline__ void h_site_staged(const StepParams& p, const StagedG
     if (!CORE && where[1]) pml_axis_st<PK, false, 1>(p, g, rows, z, h + kHdrZ, where[1], pr[1], i, j, k, dEz_y, dEx_y, XA[1], XB[1]);
     if (where[2]) pml_axis_st<PK, false, 2>(p, g, rows, z, h + kHdrZ, where[2], pr[2], i, j, k, dEy_z, dEx_z, XA[2], XB[2]);
   }
-  h_node_x<PK, IDP, CORE>(p, hc, i, j, k, src, it, where, XA, XB, dEz_y, dEy_z, dEx_z, dEz_x,
+  h_node_x<PK, IDP, CORE, true>(p, hc, i, j, k, src, it, where, XA, XB, dEz_y, dEy_z, dEx_z, dEz_x,
                           dEy_x, dEx_y, mx, my, mz, hx, hy, hz);
   p.H[0][idx] = hx;
   p.H[1][idx] = hy;
@@ -532,6 +532,7 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
   // stage and phase parity of the next chunk, counted as it goes (no division per chunk)
   int st = 0;
   uint32_t parity = 0;
+  const float* S = ring;   // stage st
   for (int c = blockIdx.x; c < g.nchunks; c += G) {
     if (!mbar_wait(&full[st], parity, g.limit_ns, abortp)) {
       *abortp = 1;
@@ -549,7 +550,6 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
     int j = hb.z + tq, k = hb.w + tr;
     if (k >= p.sy) { k -= p.sy; ++j; }
     if (j >= 0 && j < jend && k < kend) {
-      const float* S = ring + (size_t)st * g.stage_floats;
       if (ELECTRIC) {
         if (hc4.x)
           e_site_staged<PK, NP, true, TR>(p, g, C4, Cs, CD, rows, S, h, ha.z, ha.w, hb.x, hb.y,
@@ -568,9 +568,11 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
     }
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[st]);
+    S += g.stage_floats;
     if (++st == g.nstages) {
       st = 0;
       parity ^= 1u;
+      S = ring;
     }
   }
 }
