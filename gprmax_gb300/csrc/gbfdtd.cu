@@ -1651,9 +1651,11 @@ static void tune_release(gbf_ctx* ctx) {
 // ---- half-step form tuner ---------------------------------------------------------------
 // Where a staged sweep applies, each half-step can run staged or plain, with the same results
 // bit for bit; which is faster depends on the model (how much its nodes wait on memory against
-// the staging's own work per chunk). The first steps of the first run of each model shape time
-// every combination (kTuneReps rounds; the H and E kernels of a real step between two events)
-// and keep the fastest, for the model and, per shape, for the process.
+// the staging's own work per chunk). The first steps of the first run of each model shape run
+// two candidates in turn, every available staged sweep and the plain kernels (kTuneReps rounds),
+// with three events per step that time the H half-step (with the transmission lines) and the E
+// half-step apart; each half-step keeps its faster form, for the model and, per shape, for the
+// process.
 static std::map<TuneKey, int> g_form;
 
 static void form_release(gbf_ctx* ctx) {
@@ -1680,9 +1682,8 @@ static bool form_cached(gbf_ctx* ctx) {
 // One timed step with the next combination; after the last one, pick.
 static int form_step(gbf_ctx* ctx) {
   if (ctx->form_cand.empty()) {
-    for (int f = 0; f < 4; ++f)
-      if (!(f & ~ctx->staged_av)) ctx->form_cand.push_back(f);
-    ctx->form_ev.assign(2 * ctx->form_cand.size() * kTuneReps, nullptr);
+    ctx->form_cand = {ctx->staged_av, 0};
+    ctx->form_ev.assign(3 * ctx->form_cand.size() * kTuneReps, nullptr);
     for (auto& e : ctx->form_ev)
       if (cudaEventCreate(&e) != cudaSuccess) {
         (void)cudaGetLastError();
@@ -1697,29 +1698,34 @@ static int form_step(gbf_ctx* ctx) {
   const int nc = (int)ctx->form_cand.size();
   const int q = ctx->form_next;
   set_forms(ctx, ctx->form_cand[q % nc]);
-  CK(cudaEventRecord(ctx->form_ev[2 * q], ctx->stream));
+  CK(cudaEventRecord(ctx->form_ev[3 * q], ctx->stream));
   launch_h(ctx);
   launch_tl(ctx);
+  CK(cudaEventRecord(ctx->form_ev[3 * q + 1], ctx->stream));
   launch_e(ctx);
-  CK(cudaEventRecord(ctx->form_ev[2 * q + 1], ctx->stream));
+  CK(cudaEventRecord(ctx->form_ev[3 * q + 2], ctx->stream));
   launch_end(ctx);
   CK(cudaGetLastError());
   ctx->form_next = q + 1;
   if (ctx->form_next < nc * kTuneReps) return GBF_OK;
   CK(cudaEventSynchronize(ctx->form_ev.back()));
-  std::vector<float> best(nc, 1e30f);
+  // the smallest time of each half-step in each candidate over the rounds
+  std::vector<float> bh(nc, 1e30f), be(nc, 1e30f);
   for (int r = 0; r < nc * kTuneReps; ++r) {
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, ctx->form_ev[2 * r], ctx->form_ev[2 * r + 1]));
-    if (ms < best[r % nc]) best[r % nc] = ms;
+    float mh = 0, me = 0;
+    CK(cudaEventElapsedTime(&mh, ctx->form_ev[3 * r], ctx->form_ev[3 * r + 1]));
+    CK(cudaEventElapsedTime(&me, ctx->form_ev[3 * r + 1], ctx->form_ev[3 * r + 2]));
+    bh[r % nc] = mh < bh[r % nc] ? mh : bh[r % nc];
+    be[r % nc] = me < be[r % nc] ? me : be[r % nc];
   }
+  // candidate 0 holds every available staged sweep, candidate 1 none
   int pick = 0;
-  for (int k = 1; k < nc; ++k)
-    if (best[k] < best[pick]) pick = k;
-  set_forms(ctx, ctx->form_cand[pick]);
+  if ((ctx->staged_av & 1) && be[0] < be[1]) pick |= 1;
+  if ((ctx->staged_av & 2) && bh[0] < bh[1]) pick |= 2;
+  set_forms(ctx, pick);
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_form[tune_key(ctx)] = ctx->form_cand[pick];
+    g_form[tune_key(ctx)] = pick;
   }
   form_release(ctx);
   ctx->forms_tuned = 1;

@@ -178,8 +178,9 @@ int gbf_reset(gbf_ctx* ctx);
  * advances as usual, the choice changing no result) and the fastest is kept from then on.
  * Models with PML slabs take the half-step kernels (measured faster there) unless
  * gbf_set_fused_tiles selects the fused step. Where a staged sweep applies to a half-step
- * (options bit 4), staged or plain is chosen the same way (every combination timed on the first
- * steps of the first run of each model shape; gbf_set_step_forms fixes it); the staged sweeps'
+ * (options bit 4), staged or plain is chosen the same way (the first steps of the first run of
+ * each model shape run all staged sweeps and all plain kernels in turn, each half-step timed
+ * apart and keeping its faster form; gbf_set_step_forms fixes it); the staged sweeps'
  * waits for shared-memory stages are bounded, and one that ran out makes GBF_RUN_CHECK,
  * gbf_download_rx and gbf_download_fields return GBF_ECUDA. */
 int gbf_run(gbf_ctx* ctx, int nsteps, uint32_t flags);
