@@ -29,6 +29,9 @@
 namespace gbf {
 
 constexpr int kThreads = 256;   // threads per block of the half-step kernels
+// nodes a block of the batched half-steps sweeps per model visit (four per thread); each
+// model's range of the batch's virtual node index is padded to a multiple of it
+constexpr int kBatchTile = 4 * kThreads;
 constexpr int kSrcInline = 8;   // sources whose node index travels in the kernel parameters
 constexpr int kPackBits = 10;   // bits per material ID in a packed word (IDs < 1024)
 constexpr uint32_t kPackMask = (1u << kPackBits) - 1u;
@@ -529,27 +532,29 @@ __device__ __forceinline__ void h_site(const StepParams& p, const HCoef& hc,
 // swept box by box (core first) by one persistent grid.
 // The H sweep of one model over its boxes. q is the thread's position in the launch's virtual
 // node index and base the position of the model's first node there; returns q after the
-// model's last node.
-template <int PK, int IDP>
+// model's last node. TILE: the sweep also stops at position lim (a batch tile's end).
+template <int PK, int IDP, bool TILE = false>
 __device__ __forceinline__ int h_sweep(const StepParams& p, const HCoef& hc,
-                                       int q, int base, int stride, int it) {
+                                       int q, int base, int stride, int it, int lim = 0) {
   q -= base;
+  lim -= base;   // TILE: positions from lim on belong to another block
   {
     const Box& B = p.boxH[0];
     const int end = B.start + B.count;
-    if (q < end) {
+    if (q < end && (!TILE || q < lim)) {
       BoxWalk w(q - B.start, stride, B);
-      for (; q < end; q += stride, w.advance(B))
+      for (; q < end && (!TILE || q < lim); q += stride, w.advance(B))
         h_site<PK, IDP, true>(p, hc, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
   }
 #pragma unroll 1
   for (int b = 1; b < kBoxes; ++b) {
+    if (TILE && q >= lim) break;
     const Box& B = p.boxH[b];
     const int end = B.start + B.count;
     if (q >= end) continue;
     BoxWalk w(q - B.start, stride, B);
-    for (; q < end; q += stride, w.advance(B))
+    for (; q < end && (!TILE || q < lim); q += stride, w.advance(B))
       h_site<PK, IDP, false>(p, hc, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
   return q + base;
@@ -575,12 +580,15 @@ h_half_step(const __grid_constant__ StepParams p) {
 
 // ---------------------------------------------------------------------------------------
 // Batched half-steps: many models advance in one launch. The launch's virtual node index is
-// the concatenation of the models' sweeps, each padded to whole blocks (range[m] .. range[m+1]),
-// so the threads of a block always work on the same model: on reaching a model a block copies
-// its parameters (and coefficient tables) into shared memory, sweeps it, and moves on.
+// the concatenation of the models' sweeps, each padded to whole tiles of kBatchTile nodes
+// (range[m] .. range[m+1]). Blocks take tiles in turn (tile t = blockIdx.x, + gridDim.x, ...);
+// a tile lies in one model, so on reaching it a block copies that model's parameters (and
+// coefficient tables) into shared memory and sweeps the tile's nodes, four per thread. (A grid
+// stride over the whole index would give a block one node per thread of each small model it
+// passes, and a set-up for each.)
 struct BatchParams {
   const StepParams* models;   // [n] device copies of the models' parameters
-  const int* rangeH;          // [n + 1] starts of the models' H sweeps (multiples of kThreads)
+  const int* rangeH;          // [n + 1] starts of the models' H sweeps (multiples of kBatchTile)
   const int* rangeE;          // [n + 1] same for the E sweeps
   int n;
 };
@@ -597,25 +605,30 @@ __global__ void __launch_bounds__(kThreads, 4)
 h_half_step_batch(const __grid_constant__ BatchParams bp) {
   __shared__ StepParams p;
   extern __shared__ float4 smem_hb[];
-  const int stride = gridDim.x * blockDim.x;
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int total = __ldg(bp.rangeH + bp.n);
+  int m = 0, mend = -1;   // the model whose parameters are loaded (none yet) and its range end
+  int mbeg = 0, it = 0;
+  HCoef hc;
 #pragma unroll 1
-  for (int m = 0; m < bp.n; ++m) {
-    const int end = __ldg(bp.rangeH + m + 1);
-    if (q >= end) continue;   // the same for every thread of the block
-    __syncthreads();
-    load_params(p, bp.models + m);
-    __syncthreads();
-    float4* s4 = smem_hb;
-    float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
-    if (p.smem) stage_tables(p, false, s4, ss, nullptr);
-    __syncthreads();
-    HCoef hc;
-    hc.C4 = p.smem ? s4 : p.cH4;
-    hc.Cs = p.smem ? ss : p.cHs;
-    const int it = p.nsrcH ? *p.d_it : 0;
-    q = h_sweep<PK, IDP>(p, hc, q, __ldg(bp.rangeH + m), stride, it);
-    if (q < end) q += stride;   // past the model's last node, inside its padding
+  for (int t0 = blockIdx.x * kBatchTile; t0 < total; t0 += gridDim.x * kBatchTile) {
+    if (t0 >= mend) {
+      // the tile's model: ranges ascend and are whole tiles (empty for models with their own
+      // kernels), and t0 < total keeps m < n
+      while (__ldg(bp.rangeH + m + 1) <= t0) ++m;
+      mbeg = __ldg(bp.rangeH + m);
+      mend = __ldg(bp.rangeH + m + 1);
+      __syncthreads();
+      load_params(p, bp.models + m);
+      __syncthreads();
+      float4* s4 = smem_hb;
+      float* ss = reinterpret_cast<float*>(s4 + (p.smem ? p.nmat : 0));
+      if (p.smem) stage_tables(p, false, s4, ss, nullptr);
+      __syncthreads();
+      hc.C4 = p.smem ? s4 : p.cH4;
+      hc.Cs = p.smem ? ss : p.cHs;
+      it = p.nsrcH ? *p.d_it : 0;
+    }
+    h_sweep<PK, IDP, true>(p, hc, t0 + threadIdx.x, mbeg, blockDim.x, it, t0 + kBatchTile);
   }
 }
 
@@ -832,26 +845,29 @@ __device__ __forceinline__ void e_site(const StepParams& p, const float4* C4, co
 // E half-step. Domain: i in [0, nx), j in [0, ny), k in [0, nz), swept box by box (core
 // first) by one persistent grid. NP = dispersive poles.
 // The E sweep of one model over its boxes (see h_sweep).
-template <int PK, int NP, int IDP, bool TR>
+template <int PK, int NP, int IDP, bool TR, bool TILE = false>
 __device__ __forceinline__ int e_sweep(const StepParams& p, const float4* C4, const float* Cs,
-                                       const float2* CD, int q, int base, int stride, int it) {
+                                       const float2* CD, int q, int base, int stride, int it,
+                                       int lim = 0) {
   q -= base;
+  lim -= base;   // TILE: positions from lim on belong to another block
   {
     const Box& B = p.boxE[0];
     const int end = B.start + B.count;
-    if (q < end) {
+    if (q < end && (!TILE || q < lim)) {
       BoxWalk w(q - B.start, stride, B);
-      for (; q < end; q += stride, w.advance(B))
+      for (; q < end && (!TILE || q < lim); q += stride, w.advance(B))
         e_site<PK, NP, IDP, true, TR>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
     }
   }
 #pragma unroll 1
   for (int b = 1; b < kBoxes; ++b) {
+    if (TILE && q >= lim) break;
     const Box& B = p.boxE[b];
     const int end = B.start + B.count;
     if (q >= end) continue;
     BoxWalk w(q - B.start, stride, B);
-    for (; q < end; q += stride, w.advance(B))
+    for (; q < end && (!TILE || q < lim); q += stride, w.advance(B))
       e_site<PK, NP, IDP, false, TR>(p, C4, Cs, CD, B.i0 + w.a, B.j0 + w.b, w.k(B), it);
   }
   return q + base;
@@ -897,27 +913,34 @@ __global__ void __launch_bounds__(kThreads, NP >= 3 ? 3 : 4)
 e_half_step_batch(const __grid_constant__ BatchParams bp) {
   __shared__ StepParams p;
   extern __shared__ float4 smem_eb[];
-  const int stride = gridDim.x * blockDim.x;
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int total = __ldg(bp.rangeE + bp.n);
+  int m = 0, mend = -1;   // as h_half_step_batch
+  int mbeg = 0, it = 0;
+  const float4* C4 = nullptr;
+  const float* Cs = nullptr;
+  const float2* CD = nullptr;
 #pragma unroll 1
-  for (int m = 0; m < bp.n; ++m) {
-    const int end = __ldg(bp.rangeE + m + 1);
-    if (q >= end) continue;   // the same for every thread of the block
-    __syncthreads();
-    load_params(p, bp.models + m);
-    __syncthreads();
-    float4* s4;
-    float* ss;
-    float2* sd;
-    e_tables(p, smem_eb, s4, ss, sd);
-    if (p.smem) stage_tables(p, true, s4, ss, NP > 0 ? sd : nullptr);
-    __syncthreads();
-    const float4* C4 = p.smem ? s4 : p.cE4;
-    const float* Cs = p.smem ? ss : p.cEs;
-    const float2* CD = (p.smem && NP > 0) ? sd : p.cD;
-    const int it = p.nsrcE ? *p.d_it : 0;
-    q = e_sweep<PK, NP, IDP, TR>(p, C4, Cs, CD, q, __ldg(bp.rangeE + m), stride, it);
-    if (q < end) q += stride;   // past the model's last node, inside its padding
+  for (int t0 = blockIdx.x * kBatchTile; t0 < total; t0 += gridDim.x * kBatchTile) {
+    if (t0 >= mend) {
+      while (__ldg(bp.rangeE + m + 1) <= t0) ++m;
+      mbeg = __ldg(bp.rangeE + m);
+      mend = __ldg(bp.rangeE + m + 1);
+      __syncthreads();
+      load_params(p, bp.models + m);
+      __syncthreads();
+      float4* s4;
+      float* ss;
+      float2* sd;
+      e_tables(p, smem_eb, s4, ss, sd);
+      if (p.smem) stage_tables(p, true, s4, ss, NP > 0 ? sd : nullptr);
+      __syncthreads();
+      C4 = p.smem ? s4 : p.cE4;
+      Cs = p.smem ? ss : p.cEs;
+      CD = (p.smem && NP > 0) ? sd : p.cD;
+      it = p.nsrcE ? *p.d_it : 0;
+    }
+    e_sweep<PK, NP, IDP, TR, true>(p, C4, Cs, CD, t0 + threadIdx.x, mbeg, blockDim.x, it,
+                                   t0 + kBatchTile);
   }
 }
 

@@ -2362,8 +2362,8 @@ int gbf_batch_create(gbf_ctx* const* models, int32_t nmodels, gbf_batch** out) {
     ++b->nbatched;
     const Box& lh = c->sp.boxH[kBoxes - 1];
     const Box& le = c->sp.boxE[kBoxes - 1];
-    h += ((long long)(lh.start + lh.count) + kThreads - 1) / kThreads * kThreads;
-    ev += ((long long)(le.start + le.count) + kThreads - 1) / kThreads * kThreads;
+    h += ((long long)(lh.start + lh.count) + kBatchTile - 1) / kBatchTile * kBatchTile;
+    ev += ((long long)(le.start + le.count) + kBatchTile - 1) / kBatchTile * kBatchTile;
     if (h > (1LL << 31) - 1 || ev > (1LL << 31) - 1) { bfail(nullptr, GBF_EINVAL, "gbf_batch_create: more than 2^31 nodes in the batch"); return cleanup(GBF_EINVAL); }
     if (c->smem_h > b->smem_h) b->smem_h = c->smem_h;
     if (c->smem_e > b->smem_e) b->smem_e = c->smem_e;

@@ -445,3 +445,93 @@ def test_staged_sweep_at_the_benchmark_size(native_lib, electric):
     cpp = ((400 * 201 if electric else sx) + 3 + L - 1) // L
     mid = core[planes.index(200) * cpp:(planes.index(200) + 1) * cpp]
     assert mid.mean() > 0.85 and not core[:cpp].any()
+
+
+def _batch_tile():
+    """kBatchTile of fdtd_kernels.cuh: nodes a block sweeps per model visit."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), '..', 'gprmax_gb300',
+                            'csrc', 'fdtd_kernels.cuh')).read()
+    threads = int(re.search(r'constexpr int kThreads = (\d+);', src).group(1))
+    per = int(re.search(r'constexpr int kBatchTile = (\d+) \* kThreads;', src).group(1))
+    return per * threads, threads
+
+
+def _box_walk(boxes, q, base, stride, lim):
+    """h_sweep / e_sweep with TILE, restated with BoxWalk's incremental steps: the nodes one
+    thread updates from virtual position q (its model's sweep starting at base) until lim."""
+    out = []
+    q -= base
+    lim -= base
+    for b, (i0, j0, k0, bi, bj, bk, ksplit, kgap, st, count) in enumerate(boxes):
+        end = st + count
+        if b > 0 and q >= lim:
+            break
+        if q >= end or q >= lim:
+            continue
+        plane = bj * bk
+        r = q - st
+        a, r = divmod(r, plane)
+        bb, c = divmod(r, bk)
+        sa, r = divmod(stride, plane)
+        sb, sc = divmod(r, bk)
+        while q < end and q < lim:
+            out.append((i0 + a, j0 + bb, k0 + c + (kgap if c >= ksplit else 0)))
+            q += stride
+            c += sc
+            if c >= bk:
+                c -= bk
+                bb += 1
+            bb += sb
+            if bb >= bj:
+                bb -= bj
+                a += 1
+            a += sa
+    return out
+
+
+@pytest.mark.parametrize('electric', [True, False])
+@pytest.mark.parametrize('grid', [1, 3, 7])
+def test_batch_tiles_cover_every_model_once(native_lib, electric, grid):
+    """The batched half-steps (h_half_step_batch, e_half_step_batch): ranges padded to whole
+    tiles (gbf_batch_create), blocks taking tiles in turn and finding each tile's model, every
+    thread sweeping its tile's nodes with the block's stride. Every node of every batched model
+    is updated exactly once; a model with its own kernels (an empty range) is never entered."""
+    tile, threads = _batch_tile()
+    shapes = [((7, 9, 5), (2, 2, 1, 2, 2, 1)), ((12, 10, 14), (3, 3, 3, 3, 3, 3)),
+              None, ((5, 6, 8), (0, 0, 0, 0, 0, 0)), ((20, 11, 9), (4, 0, 2, 4, 0, 2))]
+    boxes, ranges = [], [0]
+    for s in shapes:
+        if s is None:   # a model with its own kernels
+            boxes.append(None)
+            ranges.append(ranges[-1])
+            continue
+        bx = _boxes(native_lib, s[0], s[1], electric)
+        boxes.append(bx)
+        n = int(bx[-1][8] + bx[-1][9])
+        ranges.append(ranges[-1] + -(-n // tile) * tile)
+    total = ranges[-1]
+    seen = {}
+    for blk in range(grid):
+        m, mend = 0, -1
+        for t0 in range(blk * tile, total, grid * tile):
+            if t0 >= mend:
+                while ranges[m + 1] <= t0:
+                    m += 1
+                mbeg, mend = ranges[m], ranges[m + 1]
+            assert boxes[m] is not None and mbeg <= t0 and t0 + tile <= mend
+            for t in range(threads):
+                for node in _box_walk(boxes[m], t0 + t, mbeg, threads, t0 + tile):
+                    key = (m,) + node
+                    seen[key] = seen.get(key, 0) + 1
+    for m, s in enumerate(shapes):
+        if s is None:
+            assert not any(k[0] == m for k in seen)
+            continue
+        nx, ny, nz = s[0]
+        ext = (nx, ny, nz) if electric else (nx + 1, ny + 1, nz + 1)
+        got = sorted(k[1:] for k in seen if k[0] == m)
+        want = sorted(itertools.product(*(range(e) for e in ext)))
+        assert got == want
+    assert all(v == 1 for v in seen.values())
