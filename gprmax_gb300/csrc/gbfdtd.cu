@@ -352,6 +352,29 @@ __global__ void division_check(float3 d, float3 r, unsigned int* bad) {
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad + a, 1u);
 }
 
+// The device check's answers per cell size (bits of d; bad != 0: the product form is refused).
+static std::mutex g_div_mu;
+static std::vector<std::pair<uint32_t, unsigned int>> g_div;
+static bool division_cached(float d, unsigned int& bad) {
+  uint32_t bits;
+  memcpy(&bits, &d, 4);
+  std::lock_guard<std::mutex> lock(g_div_mu);
+  for (auto& c : g_div)
+    if (c.first == bits) {
+      bad = c.second;
+      return true;
+    }
+  return false;
+}
+static void division_remember(float d, unsigned int bad) {
+  uint32_t bits;
+  memcpy(&bits, &d, 4);
+  std::lock_guard<std::mutex> lock(g_div_mu);
+  for (auto& c : g_div)
+    if (c.first == bits) return;
+  g_div.emplace_back(bits, bad);
+}
+
 extern "C" {
 
 const char* gbf_version(void) { return "gbfdtd 0.1 (sm_103a)"; }
@@ -690,15 +713,24 @@ int gbf_create(const gbf_grid_desc* desc, gbf_ctx** out) {
   r.tl_out = ctx->tl_out;
   // the corrected-product division per axis, checked on the device (after the arena's clear,
   // which zeroes the flags)
+  // (answers kept per cell size for the process: a B-scan's models ask it once)
   if (p.slab[0].fastdiv || p.slab[1].fastdiv || p.slab[2].fastdiv) {
-    division_check<<<dim3(2048, 3), 256, 0, ctx->stream>>>(
-        make_float3(p.slab[0].d, p.slab[1].d, p.slab[2].d),
-        make_float3(p.slab[0].rcp, p.slab[1].rcp, p.slab[2].rcp), ctx->d_scr);
     unsigned int bad[3] = {1u, 1u, 1u};
-    e = cudaGetLastError();
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(bad, ctx->d_scr, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    bool known = true;
+    for (int a = 0; a < 3; ++a)
+      if (p.slab[a].fastdiv) known = known && division_cached(p.slab[a].d, bad[a]);
+    if (!known) {
+      division_check<<<dim3(2048, 3), 256, 0, ctx->stream>>>(
+          make_float3(p.slab[0].d, p.slab[1].d, p.slab[2].d),
+          make_float3(p.slab[0].rcp, p.slab[1].rcp, p.slab[2].rcp), ctx->d_scr);
+      e = cudaGetLastError();
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bad, ctx->d_scr, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+      if (e == cudaSuccess)
+        for (int a = 0; a < 3; ++a)
+          if (p.slab[a].fastdiv) division_remember(p.slab[a].d, bad[a]);
+    }
     for (int s = 0; s < 6; ++s) p.slab[s].fastdiv = p.slab[s].fastdiv && !bad[s % 3];
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1200,17 +1232,21 @@ int gbf_upload_pml(gbf_ctx* ctx, int slab, const float* const rows[8]) {
   int tmax = 1;
   for (int s = 0; s < 6; ++s) tmax = ctx->d.pml_thickness[s] > tmax ? ctx->d.pml_thickness[s] : tmax;
   const int order = ctx->d.pml_order;
+  // rows are [order][thickness]; device rows [q][order][T] with T == thickness: the four rows
+  // of each field type gathered on the host and copied at once
+  std::vector<float> four((size_t)4 * order * t);
   for (int h = 0; h < 2; ++h) {
     float* base = ctx->pml_coef + (size_t)(slab * 2 + h) * 4 * order * tmax;
     for (int q = 0; q < 4; ++q) {
       const float* src = rows[h * 4 + q];
       if (!src) return fail(ctx, GBF_EINVAL, "gbf_upload_pml: NULL row");
-      // rows are [order][thickness]; device rows [q][order][T] with T == thickness
-      CK(cudaMemcpyAsync(base + (size_t)q * order * t, src, sizeof(float) * order * t,
-                         cudaMemcpyHostToDevice, ctx->stream));
+      memcpy(four.data() + (size_t)q * order * t, src, sizeof(float) * order * t);
     }
+    // a copy from pageable memory is staged before the call returns, so `four` may be reused
+    // at once; the stream is synchronised later (gbf_reset, gbf_synchronize, the first run)
+    CK(cudaMemcpyAsync(base, four.data(), sizeof(float) * four.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
   }
-  CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
 
@@ -1253,7 +1289,6 @@ int gbf_upload_sources(gbf_ctx* ctx, const int32_t* info, const float* scale, co
   CK(cudaMemcpyAsync(ctx->srcs, all.data(), sizeof(Src) * all.size(), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->waves, waves, sizeof(float) * (size_t)d.nsrc * d.iterations,
                      cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
   invalidate_graph(ctx);
   for (int q = 0; q < kSrcInline; ++q) ctx->sp.srcqE[q] = ctx->sp.srcqH[q] = -1;
   for (size_t q = 0; q < inE.size() && q < (size_t)kSrcInline; ++q)
@@ -1280,7 +1315,6 @@ int gbf_set_receivers(gbf_ctx* ctx, const int32_t* coords) {
       return fail(ctx, GBF_EINVAL, "gbf_set_receivers: receiver %d at (%d,%d,%d) outside the grid", n, x, y, z);
   }
   CK(cudaMemcpyAsync(ctx->rx_coords, coords, sizeof(int) * 3 * d.nrx, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
   return GBF_OK;
 }
 
