@@ -14,6 +14,9 @@
  *  - Every call returns GBF_OK (0) or a negative GBF_E* status; the message of the last
  *    failure on a context is available from gbf_last_error. Nothing calls exit() or traps.
  *  - Host buffers are owned by the caller and copied; device memory is owned by the context.
+ *    Every call has copied what it needs out of the caller's buffers when it returns; the small
+ *    uploads (PML rows, sources, receivers) complete on the context's stream before its next
+ *    run, and gbf_reset and gbf_synchronize wait for them.
  *  - One context per host thread; calls on one context are not re-entrant. The context owns
  *    one CUDA stream on which all of its work runs.
  *  - Grid sizes nx, ny, nz are cell counts; field and ID arrays have (nx+1)(ny+1)(nz+1) nodes
