@@ -322,7 +322,7 @@ __device__ __forceinline__ float dF_at(const PhiSet& d, int C, int i, int j, int
 }
 
 // Both adjoint kernels wait on memory latency (each node's some forty loads: forward state,
-// coefficients, adjoint state, partials), so they run 5 blocks of 256 per SM at 40 registers
+// coefficients, adjoint state, partials), so they run 5 blocks of 256 per SM at 48 registers
 // rather than 4 at 64: gradient of the 200 x 200 x 100 workload 0.970 s against 1.074 s (6
 // blocks, with spills: 1.008 s).
 __global__ void __launch_bounds__(kAdjThreads, 5)
