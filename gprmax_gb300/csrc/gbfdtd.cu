@@ -1523,8 +1523,9 @@ static bool staged_geom(gbf_ctx* ctx, bool electric, int nstream, size_t tables,
 }
 
 // The staged half-steps (staged.cuh) where they apply: 3D grids with packed IDs and coefficient
-// tables in shared memory whose arrays span at least two chunks; for E no poles or at most two
-// with real state; a ring of at least two stages that fits in shared memory beside the tables.
+// tables in shared memory whose arrays span at least two chunks; for E at most two poles (their
+// state real or complex); a ring of at least two stages that fits in shared memory beside the
+// tables.
 // Option bit 4 keeps the plain kernels.
 static void configure_staged(gbf_ctx* ctx) {
   ctx->staged = ctx->staged_h = ctx->staged_av = 0;
@@ -1545,8 +1546,9 @@ static void configure_staged(gbf_ctx* ctx) {
     case PML_MRI2: staged_pk4(np, ctx->treal, idp_h, &ke, &kh); break;
     default: staged_pk0(np, ctx->treal, idp_h, &ke, &kh); break;
   }
-  if (ke && np <= 2 && (np == 0 || ctx->treal) &&
-      staged_geom(ctx, true, 11 + 3 * np, ctx->smem_e, ke, ctx->sg, ctx->smem_st)) {
+  if (ke && np <= 2 &&
+      staged_geom(ctx, true, 11 + (ctx->treal ? 3 : 6) * np, ctx->smem_e, ke, ctx->sg,
+                  ctx->smem_st)) {
     ctx->sk = ke;
     ctx->staged = 1;
   }

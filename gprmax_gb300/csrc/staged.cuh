@@ -48,7 +48,9 @@ constexpr int kStageL = 32 * kStagedC;
 constexpr int kStageSpan = kStageL + 8;
 constexpr int kStageMax = 4;   // deepest ring
 // streams of an E chunk, each kStageSpan floats in a stage: E own (3), H own from node s - 4
-// (3), Hx, Hz at s - sy (2), Hy, Hz at s - sx (2), the packed E word (1), the pole state (3 NP)
+// (3), Hx, Hz at s - sy (2), Hy, Hz at s - sx (2), the packed E word (1), the pole state (3 NP
+// with its real parts only; 6 NP for complex state: each component and pole's (re, im) pairs
+// take two stream slots)
 constexpr int kStE = 0, kStH = 3, kStJ = 6, kStI = 8, kStPE = 10, kStT = 11;
 // streams of an H chunk: E own (3), H own (3), Ex, Ez at s + sy (2), Ey, Ez at s + sx (2), the
 // packed H word (1, when the H half-step reads IDs)
@@ -70,7 +72,7 @@ struct StagedGeom {
   int cpp;              // chunks per plane
   int nchunks;          // planes * cpp (nx planes for E, nx + 1 for H)
   int nstages;          // stages in the ring (2 .. kStageMax)
-  int nstream;          // streams per chunk: E 11 + 3 NP, H 10 (11 with packed H IDs)
+  int nstream;          // streams per chunk: E 11 + 3 NP (6 NP complex), H 10 (11 with packed H IDs)
   int ilo, ihi;         // core range along x (the plain kernel's core box)
   int jlo, jhi;         // and along y
   int amax;             // largest copy start (nodes) keeping a copy inside its array
@@ -167,7 +169,7 @@ __device__ __forceinline__ int clamp_start(int a, int amax) {
 // The producer: copy chunk c into stage `st` of the ring and describe it in the header h.
 // E chunks take their H neighbours at s - 1, s - sy, s - sx; H chunks their E neighbours at
 // s + 1, s + sy, s + sx.
-template <bool ELECTRIC, int PK, int NP, int IDP>
+template <bool ELECTRIC, int PK, int NP, bool TR, int IDP>
 __device__ __forceinline__ void stage_chunk(const StepParams& p, const StagedGeom& g, float* ring,
                                             uint64_t* bar, int* h, int c, int st) {
   constexpr int W = kStageSpan;
@@ -242,8 +244,15 @@ __device__ __forceinline__ void stage_chunk(const StepParams& p, const StagedGeo
     bulk_copy(d + kStPE * W, p.PE + aE, bytes, bar);
     const float* T = reinterpret_cast<const float*>(p.T);
 #pragma unroll
-    for (int qq = 0; qq < 3 * NP; ++qq)
-      bulk_copy(d + (kStT + qq) * W, T + (long long)qq * p.ncomp + aE, bytes, bar);
+    if (TR) {
+      for (int qq = 0; qq < 3 * NP; ++qq)
+        bulk_copy(d + (kStT + qq) * W, T + (long long)qq * p.ncomp + aE, bytes, bar);
+    } else {
+      // complex state: (re, im) pairs, twice the floats from twice the offset
+#pragma unroll
+      for (int qq = 0; qq < 3 * NP; ++qq)
+        bulk_copy(d + (kStT + 2 * qq) * W, T + 2 * ((long long)qq * p.ncomp + aE), 2 * bytes, bar);
+    }
   } else {
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
@@ -385,7 +394,6 @@ __device__ __forceinline__ void e_site_staged(const StepParams& p, const StagedG
                                               const float* rows, const float* __restrict__ S,
                                               const int* h, int shE, int shH, int shJ, int shI,
                                               int r, int i, int j, int k, int idx, int it) {
-  static_assert(NP == 0 || TR, "the staged sweep keeps real pole state only");
   constexpr int NPV = NP > 0 ? NP : 1;
   constexpr int W = kStageSpan;
   const float* sE = S + kStE * W + shE + r;   // E, the packed word and T share the E start
@@ -412,7 +420,9 @@ __device__ __forceinline__ void e_site_staged(const StepParams& p, const StagedG
     e[comp] = sE[comp * W];
 #pragma unroll
     for (int qq = 0; qq < NP; ++qq)
-      t[comp][qq] = make_float2(sE[(kStT - kStE + comp * NP + qq) * W], 0.f);
+      t[comp][qq] = TR ? make_float2(sE[(kStT - kStE + comp * NP + qq) * W], 0.f)
+                       : *reinterpret_cast<const float2*>(S + (kStT + 2 * (comp * NP + qq)) * W +
+                                                          2 * (shE + r));
   }
   int where[3] = {0, 0, 0}, pr[3] = {0, 0, 0};
   if (PK != PML_NONE) {
@@ -439,8 +449,11 @@ __device__ __forceinline__ void e_site_staged(const StepParams& p, const StagedG
     p.E[comp][idx] = e[comp];
     if (disp) {
 #pragma unroll
-      for (int qq = 0; qq < NP; ++qq)
-        reinterpret_cast<float*>(p.T)[(comp * NP + qq) * (long long)p.ncomp + idx] = t[comp][qq].x;
+      for (int qq = 0; qq < NP; ++qq) {
+        const long long o = (comp * NP + qq) * (long long)p.ncomp + idx;
+        if (TR) reinterpret_cast<float*>(p.T)[o] = t[comp][qq].x;
+        else p.T[o] = t[comp][qq];
+      }
     }
   }
 }
@@ -502,7 +515,7 @@ __device__ __forceinline__ void staged_sweep(const StepParams& p, const StagedGe
       }
       // the consumers' reads of this stage are ordered before the copies that refill it
       proxy_async_fence();
-      stage_chunk<ELECTRIC, PK, NP, IDP>(p, g, ring, &full[st], hdr[st], c, st);
+      stage_chunk<ELECTRIC, PK, NP, TR, IDP>(p, g, ring, &full[st], hdr[st], c, st);
       if (++st == g.nstages) {
         st = 0;
         ++round;

@@ -5,7 +5,8 @@ The staged sweeps copy each chunk's fields, neighbour rows, packed material word
 into shared memory with bulk copies and update the nodes from there, with h_node's and e_node's
 arithmetic; so receivers, all six fields and the dispersive state must equal the plain kernels'
 exactly. The models cover every PML kind, no poles and one real pole, magnetic materials (the
-H sweep reading packed IDs), complex poles (H staged, E plain), sources on the domain's upper
+H sweep reading packed IDs), complex poles (Lorentz, Drude, their state staged as pairs),
+sources on the domain's upper
 faces, a transmission line, receiver arrays, fractal soil and rough surfaces; grids from
 20 x 18 x 16 cells (copies clamped at both ends of the arrays) up. Both runs use the two
 half-step kernels (options bit 3), so the staged sweeps run every step.
@@ -47,17 +48,15 @@ def _equal(a, b):
 def test_staged_e_half_step_equals_plain(native, name):
     from gprmax_gb300.model import build_grid
     G = build_grid(MODELS[name].splitlines(True), messages=False)
-    cplx = name == 'mixed'      # complex poles: E keeps the plain kernel
-    got = _run(G, 8, forms=(not cplx, True))
+    got = _run(G, 8, forms=(True, True))
     ref = _run(G, 8 | 16)
     assert got['info']['staged_h'], 'model {} should take the staged H half-step'.format(name)
-    assert got['info']['staged'] == (not cplx)
+    assert got['info']['staged'], 'model {} should take the staged E half-step'.format(name)
     assert not ref['info']['staged'] and not ref['info']['staged_h']
     _equal(got, ref)
     # each staged sweep alone, and the forms the tuner keeps
     _equal(_run(G, 8, forms=(False, True)), ref)
-    if not cplx:
-        _equal(_run(G, 8, forms=(True, False)), ref)
+    _equal(_run(G, 8, forms=(True, False)), ref)
     tuned = _run(G, 8)
     assert tuned['info']['forms_tuned']
     _equal(tuned, ref)
@@ -74,22 +73,18 @@ def test_staged_against_oracle(native):
     np.testing.assert_array_equal(got['f'], ref.fields())
 
 
-def test_complex_poles_keep_the_plain_kernel(native):
-    """Complex pole state (option bit 2) is not staged: the plain kernel runs, and the results
-    are the staged run's; asking for the staged E sweep there is refused."""
+def test_complex_pole_state_staged(native):
+    """A Debye model with its pole state kept complex (option bit 2) takes the staged E sweep
+    with the (re, im) pairs staged; its results equal the real-state staged run's and the plain
+    kernel's."""
     from gprmax_gb300.model import build_grid
     G = build_grid(MODELS['debye1'].splitlines(True), messages=False)
-    cplx = _run(G, 8 | 4)
-    assert not cplx['info']['staged'] and not cplx['info']['staged_available']
-    from gprmax_gb300.exceptions import SolverError
-    from gprmax_gb300.solver import DeviceModel
-    dm = DeviceModel(G, 8 | 4)
-    try:
-        with pytest.raises(SolverError):
-            dm.set_step_forms(True, True)
-    finally:
-        dm.close()
-    real = _run(G, 8)
+    cplx = _run(G, 8 | 4, forms=(True, True))
+    assert cplx['info']['staged'] and cplx['info']['staged_available']
+    plain = _run(G, 8 | 4 | 16)
+    assert not plain['info']['staged']
+    _equal(cplx, plain)
+    real = _run(G, 8, forms=(True, True))
     np.testing.assert_array_equal(cplx['rx'], real['rx'])
     np.testing.assert_array_equal(cplx['f'], real['f'])
 
