@@ -67,6 +67,13 @@ def test_measured_traffic_takes_the_full_size_capture_only_for_its_grid():
     assert bench.measured_traffic(cells) == (int(full), 'ncu, full-size launch')
     b, src = bench.measured_traffic(1000)
     assert b == int(round(per_cell * 1000)) and 'scaled' in src
+    # the staged E sweep's captures (the kernel the soil runs)
+    full = bench._profile_value(bench.STAGED_TRAFFIC_FULL, 'dram_bytes_per_launch')
+    cells = int(bench._profile_value(bench.STAGED_TRAFFIC_FULL, 'cells'))
+    per_cell = bench._profile_value(bench.STAGED_TRAFFIC_PROFILE, 'dram_bytes_per_cell')
+    assert bench.measured_traffic(cells, staged=True) == (int(full), 'ncu, full-size launch')
+    b, src = bench.measured_traffic(1000, staged=True)
+    assert b == int(round(per_cell * 1000)) and 'scaled' in src
 
 
 def test_reference_arm_prints_the_contract_line():
