@@ -27,8 +27,9 @@
 // whose nodes all lie in the core ranges along x and y (the plain kernels' core box) runs the
 // core node code (only the z slabs to test); the others run the general code.
 //
-// Every copy moves kStageSpan floats from a 16-byte-aligned start: the device arrays start on
-// 256-byte boundaries (their stride is a multiple of 64 nodes) and every start is a multiple of 4
+// Every copy moves kStageSpan floats (twice that, from twice the offset, for a complex pole
+// state's (re, im) pairs) from a 16-byte-aligned start: the device arrays start on 256-byte
+// boundaries (their stride is a multiple of 64 nodes) and every start is a multiple of 4
 // nodes, clamped into [0, amax] so that a copy never leaves its array; a node reads a neighbour
 // only where the plain kernel does, and such values always lie inside the copied span. Waits
 // are bounded: a stage not filled within the limit sets the error word, the block waits (again
