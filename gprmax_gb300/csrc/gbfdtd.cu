@@ -1464,7 +1464,7 @@ static void launch_h(gbf_ctx* ctx, cudaStream_t st = nullptr) {
   kern<<<grid, block, ctx->smem_h, st>>>(p);
 }
 
-// The division constants of FastDiv for divisor d >= 2 (staged_e.cuh).
+// The division constants of FastDiv for divisor d >= 2 (staged.cuh).
 static FastDiv fast_div(int d) {
   int l = 0;
   while ((1LL << l) < d) ++l;
